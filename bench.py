@@ -1,0 +1,341 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 path-tracing core on the 1080p headline workload.
+
+Workload (one step = one frame of the render pass): the two-level scene of 200
+icosphere-3 instances over a 256x256 ground grid (1 directional + 16 sphere
+lights), 1920x1080, 1 sample per pixel, 4 path segments, russian roulette from
+segment 3: plain wavefront path tracing with next-event estimation.  The metric
+is Mrays/s = (camera + extension + shadow rays) / device time.
+
+  value  device-resident inputs, CUDA events on the library's stream around each
+         frame; L2 flushed (256 MiB memset, untimed) between frames
+  e2e    the same frames through the C ABI with host buffers: per frame the
+         instance table goes host->device (instance BVH rebuilt, as the reference's
+         TlasSystem::BuildTlas does every frame) and the HDR radiance image comes
+         back device->host; wall clock around the frames
+  roofline  the dominant kernel's algorithmic bytes per launch / its average
+         launch time (events on the launching stream), against measured HBM peak
+  cpu_baseline  the CPU oracle (multithreaded C++) on this host's cores, one
+         full 1080p frame
+
+--impl reference runs the reference arm: the reference renders through Vulkan
+ray tracing, which cannot run here, so the arm times the CPU oracle (the
+transcription of the reference shaders) on all host cores, each step a
+1/8-row sample of the same frame.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "snake-vk_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mrays/s at 1080p"
+UNIT = "Mrays/s"
+WORKLOAD = ("config 1: 200 icosphere-3 instances (1280 tris) + 256x256 ground (131072 tris), 1 directional + "
+            "16 sphere lights, 1920x1080, 1 spp, max depth 4, russian roulette from 3, plain wavefront path tracing")
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "trace_closest_config1.txt")
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    if not os.path.exists(PROFILE_SUMMARY):
+        return None
+    for line in open(PROFILE_SUMMARY):
+        if line.startswith("dram_bytes_per_launch_full_frame:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(scene, view, settings):
+    import oracle as O
+    osc = O.OracleScene(scene)
+    n = O.threads()
+    ctr = np.zeros(5, np.uint64)
+    t0 = time.perf_counter()
+    osc.render_path(view, settings, nthreads=n, counters=ctr)
+    dt = time.perf_counter() - t0
+    rays = int(ctr[:3].sum())
+    return {"value": rays / dt / 1e6, "unit": UNIT, "cores": n, "kind": "port",
+            "sample": f"one full 1920x1080 frame of the same workload ({rays} rays, {dt:.2f} s wall)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    import oracle as O
+    from snkpt import abi, scenes
+    sc = scenes.config1()
+    view = sc.views[0]
+    osc = O.OracleScene(sc)
+    n = O.threads()
+    W, H = int(view["width"]), int(view["height"])
+    rows = np.arange(H)
+
+    def step(k):
+        sel = rows[(rows % 8) == (k % 8)]
+        px = (sel[:, None] * W + np.arange(W)[None, :]).reshape(-1).astype(np.uint32)
+        ctr = np.zeros(5, np.uint64)
+        st = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=1 + k)
+        t0 = time.perf_counter()
+        osc.render_path(view, st, pixels=px, nthreads=n, counters=ctr)
+        return int(ctr[:3].sum()), time.perf_counter() - t0
+
+    for k in range(args.warmup):
+        step(k)
+    rays, secs = 0, 0.0
+    for k in range(args.steps):
+        r, s = step(args.warmup + k)
+        rays += r
+        secs += s
+    value = rays / secs / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": WORKLOAD, "sample": "every 8th row of the 1080p frame per step"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": n, "kind": "port",
+                             "sample": "every 8th row of the 1080p frame per step (CPU oracle: the reference's "
+                                       "ray-gen/closest-hit/miss logic in multithreaded C++; the reference's own "
+                                       "Vulkan ray-tracing path is unavailable on this box)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import snkpt
+    from snkpt import abi, scenes
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sc = scenes.config1()
+    view = sc.views[0]
+    W, H = int(view["width"]), int(view["height"])
+    stream = torch.cuda.Stream(device=dev)
+    pt = snkpt.PathTracer(local, stream=stream)
+    pt.load_scene(sc)
+    outs = snkpt.alloc_outputs(W, H, device=dev)
+    torch.cuda.synchronize()
+
+    def settings(seed, flags=abi.RENDER_PROFILE):
+        return abi.settings(spp=1, max_depth=4, rr_depth=3, seed=seed, flags=flags)
+
+    # traversal counts for the algorithmic bytes (one untimed instrumented frame)
+    pt.render([view], settings(1, abi.RENDER_COUNT_NODES), [outs])
+    cnt = pt.stats()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for k in range(args.warmup):
+        pt.render([view], settings(100 + k), [outs])
+        pt.stats()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    rays = 0
+    launches = 0
+    stage_ms = {k: 0.0 for k in abi.STAGES}
+    stage_n = {k: 0 for k in abi.STAGES}
+    rays_closest = 0
+    rays_shadow = 0
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ev[k][0].record(stream)
+        pt.render([view], settings(1000 + k), [outs])
+        ev[k][1].record(stream)
+        s = pt.stats()
+        rays += s["rays_camera"] + s["rays_extension"] + s["rays_shadow"]
+        rays_closest += s["rays_camera"] + s["rays_extension"]
+        rays_shadow += s["rays_shadow"]
+        launches += sum(s["stage_launches"].values())
+        for name in abi.STAGES:
+            stage_ms[name] += s["stage_ms"][name]
+            stage_n[name] += s["stage_launches"][name]
+    torch.cuda.synchronize()
+    barrier()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    clk = clocks.stop()
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        r = torch.tensor([rays], device=dev, dtype=torch.float64)
+        dist.all_reduce(r)
+        rays_all = float(r.item())
+    else:
+        rays_all = float(rays)
+    value = rays_all / (total_ms / 1e3) / 1e6
+
+    # roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    dom = max(("trace_closest", "trace_shadow"), key=lambda n: stage_ms[n])
+    if dom == "trace_closest":
+        nrays, nodes, tris, io = rays_closest, cnt["node_visits"], cnt["triangle_tests"], 32 + 24
+        crays = cnt["rays_camera"] + cnt["rays_extension"]
+    else:
+        nrays, nodes, tris, io = rays_shadow, cnt["shadow_node_visits"], cnt["shadow_triangle_tests"], 32 + 16
+        crays = cnt["rays_shadow"]
+    b_ray = io + 80.0 * nodes / max(crays, 1) + 48.0 * tris / max(crays, 1)
+    bytes_per_launch = b_ray * nrays / max(stage_n[dom], 1)
+    avg_launch_s = stage_ms[dom] / max(stage_n[dom], 1) / 1e3
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    traffic = profile_traffic() if dom == "trace_closest" else None
+    roofline = {"bound": "hbm", "kernel": f"k_trace_{dom.split('_')[1]}", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": traffic, "bytes_per_ray": b_ray,
+                "nodes_per_ray": nodes / max(crays, 1), "tris_per_ray": tris / max(crays, 1),
+                "stage_ms_per_frame": {k: v / args.steps for k, v in stage_ms.items() if v > 0}}
+
+    # end to end through the C ABI with host buffers
+    host_rad = torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True).numpy()
+    inst = np.ascontiguousarray(sc.instances)
+    e2e_rays = 0
+    for k in range(max(1, args.warmup)):
+        pt.set_instances(inst)
+        pt.render([view], settings(2000 + k, 0), [{"radiance": host_rad}])
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        pt.set_instances(inst)
+        pt.render([view], settings(3000 + k, 0), [{"radiance": host_rad}])
+        s = pt.stats()
+        e2e_rays += s["rays_camera"] + s["rays_extension"] + s["rays_shadow"]
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_rays * ws / e2e_s / 1e6
+    h2d = inst.nbytes + abi.VIEW_DTYPE.itemsize + abi.SETTINGS_DTYPE.itemsize
+    d2h = host_rad.nbytes
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": 1, "max_depth": 4,
+                       "rays_per_frame": rays / args.steps, "parallelism": f"replicas x{ws}",
+                       "l2": "flushed between steps (256 MiB memset on the same stream, untimed)"},
+            "gpu_launches": launches,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": e2e_s / args.steps * 1e3},
+            "roofline": roofline}
+    if clk:
+        line["clocks"] = clk
+    if rank == 0:
+        if ws == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(sc, view, settings(1, 0))
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,302 @@
+/*
+ * snk_pt.h -- C ABI of the GB300 path-tracing core.
+ *
+ * This library replaces the ray-traced render pass of Snake-VK:
+ *   class RT                         Core/headers/rendering/Raytracing.h:11-31
+ *   RT::Init                         Core/src/rendering/Raytracing.cpp:269-278
+ *   RT::RecordRenderCmdBuf           Core/src/rendering/Raytracing.cpp:227-267
+ *   descriptor table (bindings 0-21) Core/src/rendering/Raytracing.cpp:72-93
+ * together with the scene -> GPU buffer systems that feed that pass
+ * (Core/src/scene/RaytracingBufferSystem.cpp, LightBufferSystem.cpp,
+ * TransformBufferSystem.h, SceneInfoBufferSystem.cpp,
+ * Core/src/assets/ResourceBufferManagers.cpp, Core/src/rendering/MeshBufferManager.cpp)
+ * and the driver's acceleration structures (Core/src/resources/TLAS.cpp).
+ *
+ * Conventions
+ *  - Every entry point returns an int status: SNK_OK (0) or an SNK_ERR_* code.
+ *    snk_pt_get_last_error() returns the message of the last failure on a context.
+ *    (The reference asserts and exits instead, Core/headers/util/util.h:14-31.)
+ *  - Scene data (meshes, instances, materials, lights) is passed in HOST memory
+ *    and copied; the context owns every device copy, the BVHs and the queues.
+ *  - Ray/hit buffers and frame outputs are caller-owned; their memory space is
+ *    given per call (SNK_MEM_DEVICE or SNK_MEM_HOST).  Host outputs are written
+ *    with device->host copies on the context's stream and the call synchronises.
+ *  - One context is used by one host thread at a time.  All GPU work is issued on
+ *    the context's stream (snk_pt_set_stream; default: a stream the context creates).
+ *  - No globals: two contexts never share state.
+ */
+#ifndef SNK_PT_H
+#define SNK_PT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SNK_PT_ABI_VERSION 1u
+
+/* status codes */
+#define SNK_OK                 0
+#define SNK_ERR_INVALID_ARG    1
+#define SNK_ERR_CUDA           2
+#define SNK_ERR_OUT_OF_MEMORY  3
+#define SNK_ERR_STATE          4  /* e.g. render before build */
+#define SNK_ERR_LIMIT          5  /* a device-side bound was hit (stack depth, iteration cap) */
+#define SNK_ERR_UNSUPPORTED    6
+
+/* memory spaces of caller buffers */
+#define SNK_MEM_DEVICE 0u
+#define SNK_MEM_HOST   1u
+
+/* material flags (TexMatBuffers.glsl:3, MAT_FLAG_EMISSIVE) */
+#define SNK_MAT_EMISSIVE 1u
+
+/* invalid index in hits / id outputs (TexMatBuffers.glsl:1, INVALID_GLOBAL_INDEX) */
+#define SNK_INVALID_INDEX 0xFFFFFFFFu
+
+/* render modes */
+#define SNK_MODE_PATH        0u  /* plain unbiased wavefront path tracing with NEE */
+#define SNK_MODE_RESTIR_DI   1u  /* the reference's two-pass ReSTIR DI (RayGen.rgen:411-570) */
+#define SNK_MODE_PATH_CACHE  2u  /* path tracing with the online-trained MLP radiance cache */
+
+/* render flags */
+#define SNK_RENDER_ACCUMULATE_F64  1u  /* add this frame's radiance into the FP64 accumulator */
+#define SNK_RENDER_RESET_ACCUM     2u  /* zero the FP64 accumulator first */
+#define SNK_RENDER_COUNT_NODES     4u  /* count traversal node visits / triangle tests (slower) */
+#define SNK_RENDER_USE_GRAPH       8u  /* replay the frame's kernels from a captured CUDA graph */
+#define SNK_RENDER_PROFILE        16u  /* time every kernel launch with CUDA events (stage_ms) */
+
+/* stages reported in snk_pt_stats.stage_ms / stage_launches */
+#define SNK_STAGE_GENERATE        0
+#define SNK_STAGE_TRACE_CLOSEST   1
+#define SNK_STAGE_SHADE           2
+#define SNK_STAGE_TRACE_SHADOW    3
+#define SNK_STAGE_RESOLVE         4
+#define SNK_STAGE_RESTIR_GBUFFER  5
+#define SNK_STAGE_RESTIR_INITIAL  6
+#define SNK_STAGE_RESTIR_SPATIAL  7
+#define SNK_NUM_STAGES            8
+
+/* trace flags */
+#define SNK_TRACE_ANY_HIT 1u
+
+typedef struct snk_pt_ctx snk_pt_ctx;
+
+typedef struct snk_pt_config {
+    int32_t  device;        /* CUDA device ordinal */
+    uint32_t flags;         /* reserved, 0 */
+    void*    stream;        /* cudaStream_t to issue work on, or NULL to create one */
+    uint64_t reserved[4];
+} snk_pt_config;
+
+/* One mesh (a submesh in the reference: MeshBufferManager.cpp:49-70).
+ * positions/normals: num_vertices x 3 floats; indices: num_triangles x 3 u32.
+ * normals may be NULL (flat geometric normals are used). */
+typedef struct snk_mesh {
+    const float*    positions;
+    const float*    normals;
+    const uint32_t* indices;
+    uint32_t        num_vertices;
+    uint32_t        num_triangles;
+} snk_mesh;
+
+/* One instance of one mesh (InstanceData, RaytracingInstances.glsl:7-13, plus the
+ * current/previous transforms of Transforms.glsl:9-10 and the TLAS instance of
+ * TLAS.cpp:188-200).  transform: row-major 3x4 object->world. 112 bytes. */
+typedef struct snk_instance {
+    float    transform[12];
+    float    prev_transform[12];
+    uint32_t mesh_id;
+    uint32_t material_id;
+    uint32_t flags;         /* reserved, 0 */
+    uint32_t pad;
+} snk_instance;
+
+/* Material (TexMatBuffers.glsl:5-20 without texture indices).  For emissive
+ * materials albedo is the emitted radiance (RayClosestHit.rchit:119-122). 32 bytes. */
+typedef struct snk_material {
+    float    albedo[3];
+    float    roughness;
+    float    metallic;
+    float    ao;
+    uint32_t flags;         /* SNK_MAT_EMISSIVE */
+    uint32_t pad;
+} snk_material;
+
+/* Directional light (LightBuffers.glsl:1-5): dir points towards the light. 32 bytes. */
+typedef struct snk_directional_light {
+    float    dir[3];
+    uint32_t enabled;
+    float    colour[3];
+    float    pad;
+} snk_directional_light;
+
+/* Point light (LightBuffers.glsl:7-15).  colour is the radiant intensity.  With
+ * radius > 0 the path tracer treats it as a sphere light of that radius with
+ * radiance colour / (pi radius^2); ReSTIR DI evaluates it as the reference's
+ * attenuated point light.  48 bytes. */
+typedef struct snk_point_light {
+    float    pos[3];
+    float    radius;
+    float    colour[3];
+    float    atten_constant;
+    float    atten_linear;
+    float    atten_exp;
+    uint32_t pad[2];
+} snk_point_light;
+
+/* Pinhole camera for one view plus its previous-frame pose (for motion vectors).
+ * Replaces CommonUBO / CommonUBO_PrevFrame (CommonUBO.glsl:1-27).  forward, right,
+ * up: orthonormal world-space basis; rows of the image go from +up (row 0) to -up.
+ * 128 bytes. */
+typedef struct snk_view {
+    float    pos[3];
+    float    tan_half_fov_y;
+    float    forward[3];
+    float    aspect;
+    float    right[3];
+    uint32_t width;
+    float    up[3];
+    uint32_t height;
+    float    prev_pos[3];
+    float    prev_tan_half_fov_y;
+    float    prev_forward[3];
+    float    prev_aspect;
+    float    prev_right[3];
+    uint32_t prev_valid;    /* 0: history invalid (CommonUBO.prev_frame_invalid) */
+    float    prev_up[3];
+    uint32_t pad;
+} snk_view;
+
+/* Per-frame settings.  restir_* mirror RtSettings (Raytracing.h:13-16) and the
+ * compile-time LIGHT_RIS_ITERS / M_CAP of RayGen.rgen:95-97.  64 bytes. */
+typedef struct snk_render_settings {
+    uint32_t mode;               /* SNK_MODE_* */
+    uint32_t spp;                /* samples per pixel (path modes) */
+    uint32_t max_depth;          /* path segments per sample */
+    uint32_t rr_depth;           /* russian roulette from this segment on */
+    uint32_t seed;
+    uint32_t frame_index;        /* keys the per-frame random streams */
+    uint32_t flags;              /* SNK_RENDER_* */
+    uint32_t restir_candidates;  /* initial RIS candidates per light kind (32) */
+    uint32_t restir_mcap;        /* temporal M cap (20) */
+    int32_t  restir_temporal;    /* num_temporal_resamples (0 disables temporal reuse) */
+    int32_t  restir_spatial;     /* num_spatial_resamples */
+    float    restir_radius;      /* spatial radius in pixels (30) */
+    uint32_t reserved[4];
+} snk_render_settings;
+
+/* Outputs of one view (RaytracingResources, RenderCommon.h:6-35, plus img_output).
+ * Every pointer may be NULL (not written).  Layouts are row-major width x height:
+ *   radiance  float4 (rgb, 1)        albedo    float4 (rgb, 1)
+ *   normal    float4 (xyz, 0)        position  float4 (world xyz, 1)
+ *   rma       float4 (roughness, metallic, ao, 1)
+ *   motion    float2 (prev uv - current uv, CalcVelocity GBuffer.frag:41-43)
+ *   depth     float  (hit distance along the primary ray, -1 on a miss)
+ *   mat_flags u32, inst_id u32, prim_id u32 (SNK_INVALID_INDEX on a miss) */
+typedef struct snk_view_outputs {
+    float*    radiance;
+    float*    albedo;
+    float*    normal;
+    float*    position;
+    float*    rma;
+    float*    motion;
+    float*    depth;
+    uint32_t* mat_flags;
+    uint32_t* inst_id;
+    uint32_t* prim_id;
+    uint32_t  memory;            /* SNK_MEM_DEVICE or SNK_MEM_HOST */
+    uint32_t  pad;
+} snk_view_outputs;
+
+/* A ray: origin, tmin, direction, tmax (32 bytes). */
+typedef struct snk_ray {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+} snk_ray;
+
+/* A hit (24 bytes): t (-1 on a miss), instance, triangle index within the mesh,
+ * barycentrics of vertices 1 and 2 (hitAttributeEXT, RayClosestHit.rchit:88),
+ * flags bit 0 = hit.  Any-hit queries fill t = 1 / -1 and flags only. */
+typedef struct snk_hit {
+    float    t;
+    uint32_t inst;
+    uint32_t prim;
+    float    u;
+    float    v;
+    uint32_t flags;
+} snk_hit;
+
+typedef struct snk_pt_stats {
+    uint64_t rays_camera;        /* primary rays of the last render */
+    uint64_t rays_extension;     /* closest-hit continuation rays */
+    uint64_t rays_shadow;        /* any-hit rays */
+    uint64_t node_visits;        /* closest-hit rays, only with SNK_RENDER_COUNT_NODES */
+    uint64_t triangle_tests;     /* closest-hit rays, only with SNK_RENDER_COUNT_NODES */
+    uint64_t shadow_node_visits; /* shadow rays, only with SNK_RENDER_COUNT_NODES */
+    uint64_t shadow_triangle_tests;
+    uint64_t wide_nodes;         /* 8-wide BVH nodes (all BLAS + TLAS) */
+    uint64_t triangles;          /* unique triangles stored */
+    uint64_t instances;
+    double   blas_sah_cost;      /* SAH cost of the BLASes (surface-area weighted) */
+    double   last_render_ms;     /* device time of the last render (CUDA events) */
+    uint32_t device_error;       /* last device error word (0 = none) */
+    uint32_t pad;
+    double   stage_ms[8];        /* device time per stage of the last render (SNK_RENDER_PROFILE) */
+    uint64_t stage_launches[8];  /* kernel launches per stage of the last render */
+} snk_pt_stats;
+
+/* ---- lifetime ---------------------------------------------------------------- */
+int snk_pt_abi_version(uint32_t* version);
+/* RT::Init (Raytracing.cpp:269-278) */
+int snk_pt_create(const snk_pt_config* config, snk_pt_ctx** out_ctx);
+int snk_pt_destroy(snk_pt_ctx* ctx);
+int snk_pt_set_stream(snk_pt_ctx* ctx, void* stream);
+int snk_pt_get_last_error(const snk_pt_ctx* ctx, char* buf, size_t len);
+int snk_pt_get_stats(const snk_pt_ctx* ctx, snk_pt_stats* out);
+
+/* ---- scene ------------------------------------------------------------------- */
+/* MeshBufferManager::LoadMeshFromData + BLAS::GenerateFromMeshData
+ * (MeshBufferManager.cpp:22-88, TLAS.cpp:109-186): replaces all meshes. */
+int snk_pt_upload_meshes(snk_pt_ctx* ctx, const snk_mesh* meshes, uint32_t num_meshes);
+/* RaytracingInstanceBufferSystem::UpdateInstanceBuffer / UpdateEmissiveIdxBuffer,
+ * TransformBufferSystem::UpdateTransformBuffer (RaytracingBufferSystem.cpp:69-130,
+ * TransformBufferSystem.h:92-122). */
+int snk_pt_set_instances(snk_pt_ctx* ctx, const snk_instance* instances, uint32_t num_instances);
+/* GlobalMaterialBufferManager::UpdateMaterialUBO (ResourceBufferManagers.cpp:64-101) */
+int snk_pt_set_materials(snk_pt_ctx* ctx, const snk_material* materials, uint32_t num_materials);
+/* LightBufferSystem::UpdateLightSSBO (LightBufferSystem.cpp:65-108) */
+int snk_pt_set_lights(snk_pt_ctx* ctx, const snk_directional_light* dir_light,
+                      const snk_point_light* point_lights, uint32_t num_point_lights);
+/* BLAS builds for new meshes (GPU LBVH -> 8-wide) and the per-frame instance
+ * BVH rebuild of TlasSystem::BuildTlas (TlasSystem.cpp:27-49). */
+int snk_pt_build(snk_pt_ctx* ctx);
+
+/* ---- render ------------------------------------------------------------------ */
+/* RT::RecordRenderCmdBuf (Raytracing.cpp:227-267): renders num_views views in
+ * one batched launch sequence and writes each view's outputs.  Returns after the
+ * work is enqueued (device outputs) or after host outputs are written. */
+int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views,
+                  const snk_render_settings* settings, const snk_view_outputs* outputs);
+
+/* Waits for the context's stream and reports device-side errors (a traversal
+ * bound that was hit) of the work issued so far.  The reference has no
+ * equivalent; its submissions are fenced by the frame loop (VkRenderer.h:49-50). */
+int snk_pt_synchronize(snk_pt_ctx* ctx);
+
+/* Test hook for per-ray parity: closest hit (flags 0) or any hit (SNK_TRACE_ANY_HIT)
+ * of n rays against the built scene (traceRayEXT, RayGen.rgen:101-121,164-176). */
+int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit* hits,
+                      uint32_t flags, uint32_t memory);
+
+/* FP64 converged-image accumulator of view 0: copies the running mean (samples
+ * accumulated so far) as float4 into out (memory space as given). */
+int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SNK_PT_H */

@@ -1,0 +1,904 @@
+// api.cu -- the C ABI of include/snk_pt.h: context, scene upload, acceleration
+// structure builds, frame dispatch and the per-ray test hook.
+//
+// Reference boundary: class RT (Core/headers/rendering/Raytracing.h:11-31),
+// RT::Init / RT::RecordRenderCmdBuf (Core/src/rendering/Raytracing.cpp:227-278)
+// and the scene buffer systems that fill its descriptor table
+// (Core/src/rendering/Raytracing.cpp:72-145).
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/snk_pt.h"
+#include "snk_frame.h"
+#include "snk_host.h"
+
+using namespace snk;
+
+struct HostMesh {
+    std::vector<float> pos, nrm;
+    std::vector<uint32_t> idx;
+    uint32_t nv = 0, nt = 0;
+    bool has_normals = false;
+};
+
+struct RestirState {
+    uint32_t w = 0, h = 0;
+    DBuf<float4> g_pos, g_normal, g_albedo, g_misc, prev_normal;
+    DBuf<float4> res_a, res_b, res_c;   // temporal, history, spatial (48 B = 3 float4 per pixel)
+    uint32_t history_valid = 0;
+    uint32_t hist = 1, spat = 2;        // which of b/c holds history / receives spatial
+};
+
+struct snk_pt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 1;
+    std::string err;
+
+    // host-side scene
+    std::vector<HostMesh> meshes;
+    std::vector<snk_instance> instances;
+    std::vector<snk_material> materials;
+    snk_directional_light dir_light{};
+    std::vector<snk_point_light> point_lights;
+    bool meshes_dirty = true, inst_dirty = true, mats_dirty = true, lights_dirty = true;
+    bool built = false;
+
+    // device scene
+    DBuf<float> d_pos, d_nrm;
+    DBuf<uint32_t> d_idx;
+    std::vector<MeshInfo> h_meshes;
+    DBuf<MeshInfo> d_meshes;
+    DBuf<WideNode> d_blas;
+    DBuf<TriRecord> d_tris;
+    DBuf<WideNode> d_tlas;
+    DBuf<uint32_t> d_tlas_prims;
+    uint32_t tlas_root = INVALID;
+    uint64_t blas_nodes = 0, tlas_nodes = 0, total_tris = 0, tlas_prim_count = 0;
+    double blas_sah = 0.0;
+    DBuf<InstTrace> d_inst_trace;
+    DBuf<InstShade> d_inst_shade;
+    DBuf<MaterialDev> d_mats;
+    DBuf<PointLightDev> d_pls;
+    DBuf<uint32_t> d_emissive;
+    DBuf<LocalLight> d_lights;
+    DBuf<float> d_cdf, d_pmf;
+    uint32_t n_emissive = 0, n_local = 0;
+    DBuf<unsigned> d_err;
+
+    BuildScratch scratch;
+    DBuf<float4> d_box_lo, d_box_hi;
+    DBuf<uint32_t> d_prim_order, d_inst_list;
+
+    // frame buffers
+    DBuf<float4> rays0, rays1, beta, L, srays, scontrib;
+    DBuf<uint32_t> pid0, pid1, counters;
+    DBuf<HitDev> hits;
+    DBuf<unsigned long long> trav;
+    DBuf<ViewDev> d_views;
+    std::map<uint64_t, DBuf<unsigned char>> staging;
+    uint32_t* h_counters = nullptr;          // pinned copy of the last frame's counters
+    unsigned long long* h_trav = nullptr;    // pinned copy of traversal counters
+    bool counters_pending = false;
+    uint32_t last_mode = 0, last_depth = 0, last_count_nodes = 0;
+    uint64_t last_paths = 0, last_pixels = 0;
+
+    std::vector<RestirState> restir;
+    DBuf<double2> accum;
+    uint32_t accum_w = 0, accum_h = 0;
+    uint64_t accum_frames = 0;
+
+    DBuf<float4> tr_rays;
+    DBuf<HitDev> tr_hits;
+    DBuf<uint32_t> tr_work;
+
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timing_pending = false;
+    double last_ms = 0.0;
+
+    // per-launch profiling (SNK_RENDER_PROFILE): event pairs and their stage
+    std::vector<cudaEvent_t> prof_ev;
+    std::vector<int> prof_stage;
+    size_t prof_used = 0;
+    bool prof_pending = false;
+    double stage_ms[SNK_NUM_STAGES] = {0};
+    uint64_t stage_launches[SNK_NUM_STAGES] = {0};
+};
+
+namespace {
+
+int fail(snk_pt_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+int fail(snk_pt_ctx* c, const Status& s) { return fail(c, s.code, s.msg); }
+
+#define API_TRY(expr)                          \
+    do {                                       \
+        Status s__ = (expr);                   \
+        if (!s__.ok()) return fail(ctx, s__);  \
+    } while (0)
+
+Status set_device(snk_pt_ctx* ctx) {
+    SNK_TRY_CUDA(cudaSetDevice(ctx->device));
+    return Status::Ok();
+}
+
+template <class T>
+Status upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s) {
+    SNK_TRY_CUDA(b.reserve(n ? n : 1));
+    if (n) SNK_TRY_CUDA(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    return Status::Ok();
+}
+
+// inverse of a row-major 3x4 affine transform in double rounded to float, the
+// normal matrix transpose(inverse(mat3)) and determinant(mat3).  The CPU oracle
+// evaluates the same expressions in the same order.
+void invert_affine(const float* mf, float* inv_out, float* nmat_out, float* det_out) {
+    double a[3][3], t[3];
+    for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) a[r][c] = mf[4 * r + c]; t[r] = mf[4 * r + 3]; }
+    double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+    double c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+    double c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+    double det = (a[0][0] * c00 + a[0][1] * c01) + a[0][2] * c02;
+    double inv[3][3];
+    inv[0][0] = c00 / det;
+    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+    inv[1][0] = c01 / det;
+    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+    inv[2][0] = c02 / det;
+    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+    for (int r = 0; r < 3; r++) {
+        double it = -((inv[r][0] * t[0] + inv[r][1] * t[1]) + inv[r][2] * t[2]);
+        for (int c = 0; c < 3; c++) inv_out[4 * r + c] = (float)inv[r][c];
+        inv_out[4 * r + 3] = (float)it;
+    }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) nmat_out[3 * r + c] = (float)inv[c][r];
+    *det_out = (float)det;
+}
+
+Status build_meshes(snk_pt_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    size_t nv = 0, ni = 0, nt = 0;
+    ctx->h_meshes.assign(ctx->meshes.size(), MeshInfo{});
+    for (size_t m = 0; m < ctx->meshes.size(); m++) {
+        MeshInfo& mi = ctx->h_meshes[m];
+        mi.vertex_offset = (uint32_t)nv;
+        mi.index_offset = (uint32_t)ni;
+        mi.num_triangles = ctx->meshes[m].nt;
+        mi.has_normals = ctx->meshes[m].has_normals ? 1u : 0u;
+        mi.blas_root = INVALID;
+        nv += ctx->meshes[m].nv;
+        ni += 3ull * ctx->meshes[m].nt;
+        nt += ctx->meshes[m].nt;
+    }
+    if (nv > 0xFFFFFFFFull || ni > 0xFFFFFFFFull) return Status::Err(SNK_ERR_INVALID_ARG, "scene too large");
+    std::vector<float> pos(3 * nv), nrm(3 * nv, 0.0f);
+    std::vector<uint32_t> idx(ni);
+    for (size_t m = 0; m < ctx->meshes.size(); m++) {
+        const HostMesh& H = ctx->meshes[m];
+        const MeshInfo& mi = ctx->h_meshes[m];
+        std::memcpy(&pos[3ull * mi.vertex_offset], H.pos.data(), H.pos.size() * sizeof(float));
+        if (H.has_normals) std::memcpy(&nrm[3ull * mi.vertex_offset], H.nrm.data(), H.nrm.size() * sizeof(float));
+        std::memcpy(&idx[mi.index_offset], H.idx.data(), H.idx.size() * sizeof(uint32_t));
+    }
+    SNK_TRY(upload(ctx->d_pos, pos.data(), pos.size(), st));
+    SNK_TRY(upload(ctx->d_nrm, nrm.data(), nrm.size(), st));
+    SNK_TRY(upload(ctx->d_idx, idx.data(), idx.size(), st));
+    size_t max_nt = 1;
+    for (auto& H : ctx->meshes) max_nt = std::max<size_t>(max_nt, H.nt);
+    SNK_TRY_CUDA(ctx->d_box_lo.reserve(max_nt));
+    SNK_TRY_CUDA(ctx->d_box_hi.reserve(max_nt));
+    SNK_TRY_CUDA(ctx->d_prim_order.reserve(max_nt));
+    SNK_TRY_CUDA(ctx->d_blas.reserve(nt + ctx->meshes.size() + 1));
+    SNK_TRY_CUDA(ctx->d_tris.reserve(nt ? nt : 1));
+    uint32_t node_base = 0, prim_base = 0;
+    double sah_sum = 0.0, sah_w = 0.0;
+    for (size_t m = 0; m < ctx->meshes.size(); m++) {
+        MeshInfo& mi = ctx->h_meshes[m];
+        if (mi.num_triangles == 0) continue;
+        SNK_TRY(launch_triangle_boxes(ctx->d_pos.p, ctx->d_idx.p, mi.vertex_offset, mi.index_offset, mi.num_triangles,
+                                      ctx->d_box_lo.p, ctx->d_box_hi.p, st));
+        BuildResult br;
+        SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, mi.num_triangles, ctx->d_blas.p,
+                               node_base, prim_base, ctx->d_prim_order.p, st, &br));
+        SNK_TRY(launch_fill_triangles(ctx->d_prim_order.p, mi.num_triangles, ctx->d_pos.p, ctx->d_idx.p,
+                                      mi.vertex_offset, mi.index_offset, ctx->d_tris.p + prim_base, st));
+        mi.blas_root = node_base;
+        for (int a = 0; a < 3; a++) { mi.lo[a] = br.lo[a]; mi.hi[a] = br.hi[a]; }
+        node_base += br.num_nodes;
+        prim_base += mi.num_triangles;
+        sah_sum += br.sah * mi.num_triangles;
+        sah_w += mi.num_triangles;
+    }
+    ctx->blas_nodes = node_base;
+    ctx->total_tris = prim_base;
+    ctx->blas_sah = sah_w > 0 ? sah_sum / sah_w : 0.0;
+    SNK_TRY(upload(ctx->d_meshes, ctx->h_meshes.data(), ctx->h_meshes.size(), st));
+    SNK_TRY_CUDA(cudaStreamSynchronize(st));
+    return Status::Ok();
+}
+
+Status build_instances(snk_pt_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    const size_t ni = ctx->instances.size();
+    std::vector<InstTrace> it(ni);
+    std::vector<InstShade> is(ni);
+    std::vector<uint32_t> list;
+    std::vector<uint32_t> emissive;
+    for (size_t i = 0; i < ni; i++) {
+        const snk_instance& in = ctx->instances[i];
+        if (in.mesh_id >= ctx->meshes.size()) return Status::Err(SNK_ERR_INVALID_ARG, "instance mesh_id out of range");
+        if (in.material_id >= ctx->materials.size())
+            return Status::Err(SNK_ERR_INVALID_ARG, "instance material_id out of range");
+        InstShade& S = is[i];
+        std::memcpy(S.m, in.transform, sizeof(S.m));
+        std::memcpy(S.pm, in.prev_transform, sizeof(S.pm));
+        float inv[12];
+        invert_affine(in.transform, inv, S.nmat, &S.det3);
+        S.mesh_id = in.mesh_id;
+        S.material_id = in.material_id;
+        InstTrace& T = it[i];
+        std::memcpy(T.inv, inv, sizeof(inv));
+        T.blas_root = ctx->h_meshes[in.mesh_id].blas_root;
+        T.mesh_id = in.mesh_id;
+        T.material_id = in.material_id;
+        T.pad = 0;
+        if (T.blas_root != INVALID) list.push_back((uint32_t)i);
+        if (ctx->materials[in.material_id].flags & SNK_MAT_EMISSIVE) emissive.push_back((uint32_t)i);
+    }
+    SNK_TRY(upload(ctx->d_inst_trace, it.data(), it.size(), st));
+    SNK_TRY(upload(ctx->d_inst_shade, is.data(), is.size(), st));
+    SNK_TRY(upload(ctx->d_emissive, emissive.data(), emissive.size(), st));
+    ctx->n_emissive = (uint32_t)emissive.size();
+
+    // path-tracer local lights: sphere lights, then every emissive triangle,
+    // selected in proportion to emitted power
+    std::vector<LocalLight> lights;
+    std::vector<double> w;
+    for (size_t k = 0; k < ctx->point_lights.size(); k++) {
+        const snk_point_light& P = ctx->point_lights[k];
+        if (!(P.radius > 0.0f)) continue;
+        LocalLight L{};
+        L.kind = 0;
+        L.index = (uint32_t)k;
+        L.p0[0] = P.pos[0]; L.p0[1] = P.pos[1]; L.p0[2] = P.pos[2];
+        L.p1[0] = P.radius;
+        double inv_area = 1.0 / (M_PI * (double)P.radius * (double)P.radius);
+        L.L[0] = (float)(P.colour[0] * inv_area);
+        L.L[1] = (float)(P.colour[1] * inv_area);
+        L.L[2] = (float)(P.colour[2] * inv_area);
+        lights.push_back(L);
+        w.push_back(4.0 * M_PI * (0.2126 * P.colour[0] + 0.7152 * P.colour[1] + 0.0722 * P.colour[2]));
+    }
+    for (uint32_t ii : emissive) {
+        const snk_instance& in = ctx->instances[ii];
+        const HostMesh& M = ctx->meshes[in.mesh_id];
+        V3 Le = load3(ctx->materials[in.material_id].albedo);
+        for (uint32_t t = 0; t < M.nt; t++) {
+            LocalLight L{};
+            L.kind = 1;
+            L.index = ii;
+            V3 p0 = xform_point(in.transform, load3(&M.pos[3ull * M.idx[3ull * t + 0]]));
+            V3 p1 = xform_point(in.transform, load3(&M.pos[3ull * M.idx[3ull * t + 1]]));
+            V3 p2 = xform_point(in.transform, load3(&M.pos[3ull * M.idx[3ull * t + 2]]));
+            V3 nl = cross(sub(p1, p0), sub(p2, p0));
+            float len = length(nl);
+            float area = 0.5f * len;
+            V3 n = len > 0.0f ? divs(nl, len) : v3(0.0f, 1.0f, 0.0f);
+            L.p0[0] = p0.x; L.p0[1] = p0.y; L.p0[2] = p0.z;
+            L.p1[0] = p1.x; L.p1[1] = p1.y; L.p1[2] = p1.z;
+            L.p2[0] = p2.x; L.p2[1] = p2.y; L.p2[2] = p2.z;
+            L.n[0] = n.x; L.n[1] = n.y; L.n[2] = n.z;
+            L.L[0] = Le.x; L.L[1] = Le.y; L.L[2] = Le.z; L.L[3] = area;
+            lights.push_back(L);
+            w.push_back(2.0 * M_PI * (double)area * (0.2126 * Le.x + 0.7152 * Le.y + 0.0722 * Le.z));
+        }
+    }
+    double total = 0.0;
+    for (double x : w) total += x;
+    std::vector<float> cdf(w.size()), pmf(w.size());
+    double acc = 0.0;
+    for (size_t k = 0; k < w.size(); k++) {
+        acc += w[k];
+        cdf[k] = total > 0 ? (float)(acc / total) : 0.0f;
+        pmf[k] = total > 0 ? (float)(w[k] / total) : 0.0f;
+    }
+    if (!w.empty() && total > 0) cdf.back() = 1.0f;
+    ctx->n_local = total > 0 ? (uint32_t)lights.size() : 0u;
+    SNK_TRY(upload(ctx->d_lights, lights.data(), lights.size(), st));
+    SNK_TRY(upload(ctx->d_cdf, cdf.data(), cdf.size(), st));
+    SNK_TRY(upload(ctx->d_pmf, pmf.data(), pmf.size(), st));
+
+    // instance BVH (rebuilt whenever instances change, as TlasSystem::BuildTlas)
+    ctx->tlas_root = INVALID;
+    ctx->tlas_nodes = 0;
+    ctx->tlas_prim_count = 0;
+    const uint32_t n = (uint32_t)list.size();
+    if (n > 0) {
+        SNK_TRY(upload(ctx->d_inst_list, list.data(), list.size(), st));
+        SNK_TRY_CUDA(ctx->d_box_lo.reserve(n));
+        SNK_TRY_CUDA(ctx->d_box_hi.reserve(n));
+        SNK_TRY_CUDA(ctx->d_prim_order.reserve(n));
+        SNK_TRY_CUDA(ctx->d_tlas.reserve(n + 1));
+        SNK_TRY_CUDA(ctx->d_tlas_prims.reserve(n));
+        SNK_TRY(launch_instance_boxes(ctx->d_inst_list.p, n, ctx->d_inst_shade.p, ctx->d_meshes.p, ctx->d_box_lo.p,
+                                      ctx->d_box_hi.p, st));
+        BuildResult br;
+        SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
+                               ctx->d_prim_order.p, st, &br));
+        SNK_TRY(launch_map_prims(ctx->d_prim_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
+        ctx->tlas_root = 0;
+        ctx->tlas_nodes = br.num_nodes;
+        ctx->tlas_prim_count = n;
+    }
+    SNK_TRY_CUDA(cudaStreamSynchronize(st));
+    return Status::Ok();
+}
+
+Status build_all(snk_pt_ctx* ctx) {
+    SNK_TRY(set_device(ctx));
+    if (ctx->meshes_dirty) {
+        SNK_TRY(build_meshes(ctx));
+        ctx->meshes_dirty = false;
+        ctx->inst_dirty = true;
+    }
+    if (ctx->mats_dirty) {
+        std::vector<MaterialDev> m(ctx->materials.size());
+        static_assert(sizeof(MaterialDev) == sizeof(snk_material), "material layout");
+        std::memcpy(m.data(), ctx->materials.data(), m.size() * sizeof(MaterialDev));
+        SNK_TRY(upload(ctx->d_mats, m.data(), m.size(), ctx->stream));
+        ctx->mats_dirty = false;
+        ctx->inst_dirty = true;
+    }
+    if (ctx->lights_dirty) {
+        static_assert(sizeof(PointLightDev) == sizeof(snk_point_light), "point light layout");
+        SNK_TRY(upload(ctx->d_pls, reinterpret_cast<const PointLightDev*>(ctx->point_lights.data()),
+                       ctx->point_lights.size(), ctx->stream));
+        ctx->lights_dirty = false;
+        ctx->inst_dirty = true;
+    }
+    if (ctx->inst_dirty) {
+        SNK_TRY(build_instances(ctx));
+        ctx->inst_dirty = false;
+    }
+    SNK_TRY_CUDA(ctx->d_err.reserve(1));
+    ctx->built = true;
+    return Status::Ok();
+}
+
+SceneDev scene_dev(snk_pt_ctx* ctx) {
+    SceneDev S;
+    std::memset(&S, 0, sizeof(S));
+    S.blas_nodes = ctx->d_blas.p;
+    S.tris = ctx->d_tris.p;
+    S.tlas_nodes = ctx->d_tlas.p;
+    S.tlas_prims = ctx->d_tlas_prims.p;
+    S.tlas_root = ctx->tlas_root;
+    S.num_instances = (uint32_t)ctx->instances.size();
+    S.inst_trace = ctx->d_inst_trace.p;
+    S.inst_shade = ctx->d_inst_shade.p;
+    S.meshes = ctx->d_meshes.p;
+    S.positions = ctx->d_pos.p;
+    S.normals = ctx->d_nrm.p;
+    S.indices = ctx->d_idx.p;
+    S.materials = ctx->d_mats.p;
+    S.point_lights = ctx->d_pls.p;
+    S.num_point_lights = (uint32_t)ctx->point_lights.size();
+    S.num_emissive_instances = ctx->n_emissive;
+    S.emissive_instances = ctx->d_emissive.p;
+    S.local_lights = ctx->d_lights.p;
+    S.light_cdf = ctx->d_cdf.p;
+    S.light_pmf = ctx->d_pmf.p;
+    S.num_local_lights = ctx->n_local;
+    std::memcpy(&S.dir_light, &ctx->dir_light, sizeof(S.dir_light));
+    S.error_word = ctx->d_err.p;
+    S.num_blas_nodes = (uint32_t)ctx->blas_nodes;
+    S.num_tris = (uint32_t)ctx->total_tris;
+    S.num_tlas_nodes = (uint32_t)ctx->tlas_nodes;
+    S.num_tlas_prims = ctx->tlas_root == INVALID ? 0u : (uint32_t)ctx->tlas_prim_count;
+    return S;
+}
+
+Status ensure_built(snk_pt_ctx* ctx) {
+    if (ctx->meshes_dirty || ctx->inst_dirty || ctx->mats_dirty || ctx->lights_dirty || !ctx->built)
+        return build_all(ctx);
+    return Status::Ok();
+}
+
+Status check_device_error(snk_pt_ctx* ctx) {
+    unsigned e = 0;
+    SNK_TRY_CUDA(cudaMemcpyAsync(&e, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    SNK_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (e) {
+        SNK_TRY_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
+        return Status::Err(SNK_ERR_LIMIT, std::string("device traversal bound hit (error word ") + std::to_string(e) +
+                                              "): bit 1 stack depth, bit 2 step limit, bit 4 bad index");
+    }
+    return Status::Ok();
+}
+
+float* stage(snk_pt_ctx* ctx, uint32_t view, uint32_t kind, size_t bytes, Status* st) {
+    DBuf<unsigned char>& b = ctx->staging[((uint64_t)view << 8) | kind];
+    cudaError_t e = b.reserve(bytes);
+    if (e != cudaSuccess) { *st = Status::Err(SNK_ERR_OUT_OF_MEMORY, "staging allocation failed"); return nullptr; }
+    return reinterpret_cast<float*>(b.p);
+}
+
+constexpr int NUM_OUT = 10;
+// element sizes of the outputs in snk_view_outputs order
+const size_t OUT_BYTES[NUM_OUT] = {16, 16, 16, 16, 16, 8, 4, 4, 4, 4};
+
+void** out_slots(snk_view_outputs& o) { return reinterpret_cast<void**>(&o); }
+void** dev_slots(ViewDev& v) { return reinterpret_cast<void**>(&v.radiance); }
+
+int grid_of(snk_pt_ctx* ctx, int per_sm) { return ctx->num_sms * per_sm; }
+
+// Runs one kernel launch; with profiling on, brackets it with an event pair.
+template <class Fn>
+cudaError_t staged(snk_pt_ctx* ctx, bool profile, int stage, Fn&& fn) {
+    ctx->stage_launches[stage]++;
+    if (!profile) return fn();
+    if (ctx->prof_used + 2 > ctx->prof_ev.size()) {
+        for (int k = 0; k < 16; k++) {
+            cudaEvent_t e;
+            cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess) return r;
+            ctx->prof_ev.push_back(e);
+        }
+        ctx->prof_stage.resize(ctx->prof_ev.size() / 2);
+    }
+    cudaEventRecord(ctx->prof_ev[ctx->prof_used], ctx->stream);
+    cudaError_t r = fn();
+    cudaEventRecord(ctx->prof_ev[ctx->prof_used + 1], ctx->stream);
+    ctx->prof_stage[ctx->prof_used / 2] = stage;
+    ctx->prof_used += 2;
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int snk_pt_abi_version(uint32_t* version) {
+    if (!version) return SNK_ERR_INVALID_ARG;
+    *version = SNK_PT_ABI_VERSION;
+    return SNK_OK;
+}
+
+int snk_pt_create(const snk_pt_config* config, snk_pt_ctx** out_ctx) {
+    if (!out_ctx) return SNK_ERR_INVALID_ARG;
+    *out_ctx = nullptr;
+    snk_pt_ctx* ctx = new snk_pt_ctx();
+    ctx->device = config ? config->device : 0;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        delete ctx;
+        return SNK_ERR_CUDA;
+    }
+    if (ctx->device < 0 || ctx->device >= ndev) { delete ctx; return SNK_ERR_INVALID_ARG; }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) { delete ctx; return SNK_ERR_CUDA; }
+    if (config && config->stream) {
+        ctx->stream = (cudaStream_t)config->stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return SNK_ERR_CUDA; }
+        ctx->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (cudaMallocHost(&ctx->h_counters, CNT_TOTAL * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_trav, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        ctx->d_err.reserve(1) != cudaSuccess || cudaMemset(ctx->d_err.p, 0, sizeof(unsigned)) != cudaSuccess) {
+        snk_pt_destroy(ctx);
+        return SNK_ERR_CUDA;
+    }
+    std::memset(ctx->h_counters, 0, CNT_TOTAL * sizeof(uint32_t));
+    std::memset(ctx->h_trav, 0, 4 * sizeof(unsigned long long));
+    *out_ctx = ctx;
+    return SNK_OK;
+}
+
+int snk_pt_destroy(snk_pt_ctx* ctx) {
+    if (!ctx) return SNK_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->h_trav) cudaFreeHost(ctx->h_trav);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+    cudaStream_t s = ctx->own_stream ? ctx->stream : nullptr;
+    delete ctx;
+    if (s) cudaStreamDestroy(s);
+    return SNK_OK;
+}
+
+int snk_pt_set_stream(snk_pt_ctx* ctx, void* stream) {
+    if (!ctx) return SNK_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, "stream");
+        ctx->own_stream = true;
+    }
+    return SNK_OK;
+}
+
+int snk_pt_get_last_error(const snk_pt_ctx* ctx, char* buf, size_t len) {
+    if (!ctx || !buf || len == 0) return SNK_ERR_INVALID_ARG;
+    size_t n = std::min(len - 1, ctx->err.size());
+    std::memcpy(buf, ctx->err.data(), n);
+    buf[n] = 0;
+    return SNK_OK;
+}
+
+int snk_pt_upload_meshes(snk_pt_ctx* ctx, const snk_mesh* meshes, uint32_t num_meshes) {
+    if (!ctx || (num_meshes && !meshes)) return fail(ctx, SNK_ERR_INVALID_ARG, "upload_meshes: null argument");
+    std::vector<HostMesh> hm(num_meshes);
+    for (uint32_t m = 0; m < num_meshes; m++) {
+        const snk_mesh& M = meshes[m];
+        if ((M.num_vertices && !M.positions) || (M.num_triangles && !M.indices))
+            return fail(ctx, SNK_ERR_INVALID_ARG, "upload_meshes: null mesh array");
+        HostMesh& H = hm[m];
+        H.nv = M.num_vertices;
+        H.nt = M.num_triangles;
+        H.pos.assign(M.positions, M.positions + 3ull * M.num_vertices);
+        H.idx.assign(M.indices, M.indices + 3ull * M.num_triangles);
+        for (uint32_t x : H.idx)
+            if (x >= M.num_vertices) return fail(ctx, SNK_ERR_INVALID_ARG, "upload_meshes: index out of range");
+        for (float f : H.pos)
+            if (!std::isfinite(f)) return fail(ctx, SNK_ERR_INVALID_ARG, "upload_meshes: non-finite vertex position");
+        if (M.normals) {
+            H.has_normals = true;
+            H.nrm.assign(M.normals, M.normals + 3ull * M.num_vertices);
+        }
+    }
+    ctx->meshes.swap(hm);
+    ctx->meshes_dirty = true;
+    ctx->built = false;
+    return SNK_OK;
+}
+
+int snk_pt_set_instances(snk_pt_ctx* ctx, const snk_instance* instances, uint32_t n) {
+    if (!ctx || (n && !instances)) return fail(ctx, SNK_ERR_INVALID_ARG, "set_instances: null argument");
+    for (uint32_t i = 0; i < n; i++)
+        for (int k = 0; k < 12; k++)
+            if (!std::isfinite(instances[i].transform[k]) || !std::isfinite(instances[i].prev_transform[k]))
+                return fail(ctx, SNK_ERR_INVALID_ARG, "set_instances: non-finite transform");
+    ctx->instances.assign(instances, instances + n);
+    ctx->inst_dirty = true;
+    return SNK_OK;
+}
+
+int snk_pt_set_materials(snk_pt_ctx* ctx, const snk_material* materials, uint32_t n) {
+    if (!ctx || (n && !materials)) return fail(ctx, SNK_ERR_INVALID_ARG, "set_materials: null argument");
+    ctx->materials.assign(materials, materials + n);
+    ctx->mats_dirty = true;
+    return SNK_OK;
+}
+
+int snk_pt_set_lights(snk_pt_ctx* ctx, const snk_directional_light* dl, const snk_point_light* pl, uint32_t n) {
+    if (!ctx || (n && !pl)) return fail(ctx, SNK_ERR_INVALID_ARG, "set_lights: null argument");
+    if (dl) ctx->dir_light = *dl;
+    else std::memset(&ctx->dir_light, 0, sizeof(ctx->dir_light));
+    ctx->point_lights.assign(pl, pl + n);
+    ctx->lights_dirty = true;
+    return SNK_OK;
+}
+
+int snk_pt_build(snk_pt_ctx* ctx) {
+    if (!ctx) return SNK_ERR_INVALID_ARG;
+    API_TRY(build_all(ctx));
+    return SNK_OK;
+}
+
+int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, const snk_render_settings* settings,
+                  const snk_view_outputs* outputs) {
+    if (!ctx) return SNK_ERR_INVALID_ARG;
+    if (!views || !settings || !outputs || num_views == 0 || num_views > MAX_VIEWS)
+        return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad views/settings/outputs");
+    const snk_render_settings& rs = *settings;
+    if (rs.mode != SNK_MODE_PATH && rs.mode != SNK_MODE_RESTIR_DI)
+        return fail(ctx, SNK_ERR_UNSUPPORTED, "render: mode not supported by this entry point");
+    if (rs.mode == SNK_MODE_PATH && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
+        return fail(ctx, SNK_ERR_INVALID_ARG, "render: spp must be >= 1 and 1 <= max_depth <= 16");
+    uint64_t n_pixels = 0;
+    for (uint32_t v = 0; v < num_views; v++) {
+        if (views[v].width == 0 || views[v].height == 0) return fail(ctx, SNK_ERR_INVALID_ARG, "render: empty view");
+        if (outputs[v].memory > SNK_MEM_HOST) return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad memory space");
+        n_pixels += (uint64_t)views[v].width * views[v].height;
+    }
+    const uint32_t spp = rs.mode == SNK_MODE_PATH ? rs.spp : 1u;
+    if (n_pixels * spp >= (1ull << 31)) return fail(ctx, SNK_ERR_INVALID_ARG, "render: too many paths");
+    API_TRY(set_device(ctx));
+    API_TRY(ensure_built(ctx));
+    cudaStream_t st = ctx->stream;
+    const uint32_t n_paths = (uint32_t)(n_pixels * spp);
+
+    // per-view device descriptors (host outputs go through staging buffers)
+    std::vector<ViewDev> vd(num_views);
+    uint64_t off = 0;
+    Status sst = Status::Ok();
+    for (uint32_t v = 0; v < num_views; v++) {
+        ViewDev& D = vd[v];
+        std::memset(&D, 0, sizeof(D));
+        std::memcpy(&D.v, &views[v], sizeof(ViewParams));
+        D.pixel_offset = (uint32_t)off;
+        snk_view_outputs o = outputs[v];
+        void** src = out_slots(o);
+        void** dst = dev_slots(D);
+        size_t np = (size_t)views[v].width * views[v].height;
+        for (int k = 0; k < NUM_OUT; k++) {
+            if (!src[k]) continue;
+            if (o.memory == SNK_MEM_HOST) {
+                dst[k] = stage(ctx, v, (uint32_t)k, np * OUT_BYTES[k], &sst);
+                if (!sst.ok()) return fail(ctx, sst);
+            } else {
+                dst[k] = src[k];
+            }
+        }
+        off += np;
+    }
+    API_TRY(upload(ctx->d_views, vd.data(), vd.size(), st));
+
+    FrameParams F;
+    std::memset(&F, 0, sizeof(F));
+    F.S = scene_dev(ctx);
+    F.views = ctx->d_views.p;
+    F.nviews = num_views;
+    F.spp = spp;
+    F.max_depth = rs.max_depth;
+    F.rr_depth = rs.rr_depth;
+    F.seed = rs.seed;
+    F.n_paths = n_paths;
+    F.n_pixels = (uint32_t)n_pixels;
+    const bool count_nodes = (rs.flags & SNK_RENDER_COUNT_NODES) != 0;
+    const bool profile = (rs.flags & SNK_RENDER_PROFILE) != 0;
+    if (ctx->prof_pending) cudaStreamSynchronize(st);   // events of the previous frame are reused
+    ctx->prof_used = 0;
+    ctx->prof_pending = profile;
+    for (int k = 0; k < SNK_NUM_STAGES; k++) ctx->stage_launches[k] = 0;
+
+    // FP64 accumulator of view 0
+    if (rs.flags & SNK_RENDER_ACCUMULATE_F64) {
+        uint32_t w = views[0].width, h = views[0].height;
+        if (ctx->accum_w != w || ctx->accum_h != h || (rs.flags & SNK_RENDER_RESET_ACCUM) || !ctx->accum.p) {
+            if (ctx->accum.reserve(2ull * w * h) != cudaSuccess) return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "accumulator");
+            if (cudaMemsetAsync(ctx->accum.p, 0, 2ull * w * h * sizeof(double2), st) != cudaSuccess)
+                return fail(ctx, SNK_ERR_CUDA, "accumulator reset");
+            ctx->accum_w = w;
+            ctx->accum_h = h;
+            ctx->accum_frames = 0;
+        }
+        F.accumulate = 1;
+        F.accum = ctx->accum.p;
+        ctx->accum_frames++;
+    }
+
+    if (ctx->counters.reserve(CNT_TOTAL) != cudaSuccess || ctx->trav.reserve(4) != cudaSuccess)
+        return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "counters");
+    F.counters = ctx->counters.p;
+    F.trav_counters = count_nodes ? ctx->trav.p : nullptr;
+    if (cudaMemsetAsync(ctx->counters.p, 0, CNT_TOTAL * sizeof(uint32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(ctx->trav.p, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess)
+        return fail(ctx, SNK_ERR_CUDA, "counter reset");
+
+    if (rs.mode == SNK_MODE_PATH) {
+        if (ctx->rays0.reserve(2ull * n_paths) || ctx->rays1.reserve(2ull * n_paths) || ctx->pid0.reserve(n_paths) ||
+            ctx->pid1.reserve(n_paths) || ctx->hits.reserve(n_paths) || ctx->beta.reserve(n_paths) ||
+            ctx->L.reserve(n_paths) || ctx->srays.reserve(4ull * n_paths) || ctx->scontrib.reserve(2ull * n_paths))
+            return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "frame buffers");
+        F.rays[0] = ctx->rays0.p; F.rays[1] = ctx->rays1.p;
+        F.path_ids[0] = ctx->pid0.p; F.path_ids[1] = ctx->pid1.p;
+        F.hits = ctx->hits.p; F.beta = ctx->beta.p; F.L = ctx->L.p;
+        F.shadow_rays = ctx->srays.p; F.shadow_contrib = ctx->scontrib.p;
+        cudaEventRecord(ctx->ev0, st);
+        const int g8 = grid_of(ctx, 8), g16 = grid_of(ctx, 16);
+        cudaError_t e = staged(ctx, profile, SNK_STAGE_GENERATE, [&] { return launch_generate(F, g8, st); });
+        for (uint32_t d = 0; d < rs.max_depth && e == cudaSuccess; d++) {
+            e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
+                       [&] { return launch_trace_closest(F, d, g16, count_nodes, st); });
+            if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_SHADE, [&] { return launch_shade(F, d, g8, st); });
+            if (e == cudaSuccess)
+                e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
+                           [&] { return launch_trace_shadow(F, d, g16, count_nodes, st); });
+        }
+        if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_RESOLVE, [&] { return launch_resolve(F, g8, st); });
+        cudaEventRecord(ctx->ev1, st);
+        if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
+    } else {
+        if (ctx->restir.size() < num_views) ctx->restir.resize(num_views);
+        cudaEventRecord(ctx->ev0, st);
+        for (uint32_t v = 0; v < num_views; v++) {
+            RestirState& R = ctx->restir[v];
+            uint32_t w = views[v].width, h = views[v].height;
+            size_t np = (size_t)w * h;
+            if (R.w != w || R.h != h) {
+                if (R.g_pos.reserve(np) || R.g_normal.reserve(np) || R.g_albedo.reserve(np) || R.g_misc.reserve(np) ||
+                    R.prev_normal.reserve(np) || R.res_a.reserve(3 * np) || R.res_b.reserve(3 * np) ||
+                    R.res_c.reserve(3 * np))
+                    return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir buffers");
+                R.w = w; R.h = h; R.history_valid = 0; R.hist = 1; R.spat = 2;
+            }
+            RestirView RV;
+            RV.g_pos = R.g_pos.p; RV.g_normal = R.g_normal.p; RV.g_albedo = R.g_albedo.p; RV.g_misc = R.g_misc.p;
+            RV.prev_normal = R.prev_normal.p;
+            RV.temporal = R.res_a.p;
+            RV.history = R.hist == 1 ? R.res_b.p : R.res_c.p;
+            RV.spatial = R.spat == 1 ? R.res_b.p : R.res_c.p;
+            RV.history_valid = R.history_valid;
+            RestirSettings s;
+            s.frame_index = rs.frame_index; s.seed = rs.seed; s.candidates = rs.restir_candidates;
+            s.mcap = rs.restir_mcap; s.temporal = rs.restir_temporal; s.spatial = rs.restir_spatial;
+            s.radius = rs.restir_radius; s.pad = 0;
+            cudaError_t e = cudaSuccess;
+            for (int k = 0; k < 3 && e == cudaSuccess; k++)
+                e = staged(ctx, profile, SNK_STAGE_RESTIR_GBUFFER + k,
+                           [&] { return launch_restir_stage(k, F, v, RV, s, grid_of(ctx, 16), st); });
+            if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("restir launch: ") + cudaGetErrorString(e));
+            std::swap(R.hist, R.spat);
+            R.history_valid = 1;
+        }
+        cudaEventRecord(ctx->ev1, st);
+    }
+    ctx->timing_pending = true;
+    cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, CNT_TOTAL * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(ctx->h_trav, ctx->trav.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    ctx->counters_pending = true;
+    ctx->last_mode = rs.mode;
+    ctx->last_depth = rs.max_depth;
+    ctx->last_paths = n_paths;
+    ctx->last_pixels = n_pixels;
+    ctx->last_count_nodes = count_nodes;
+
+    // host outputs: copy back and synchronise
+    bool any_host = false;
+    for (uint32_t v = 0; v < num_views; v++) {
+        if (outputs[v].memory != SNK_MEM_HOST) continue;
+        any_host = true;
+        snk_view_outputs o = outputs[v];
+        void** src = out_slots(o);
+        void** dst = dev_slots(vd[v]);
+        size_t np = (size_t)views[v].width * views[v].height;
+        for (int k = 0; k < NUM_OUT; k++) {
+            if (!src[k]) continue;
+            if (cudaMemcpyAsync(src[k], dst[k], np * OUT_BYTES[k], cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                return fail(ctx, SNK_ERR_CUDA, "render: output copy");
+        }
+    }
+    if (any_host) API_TRY(check_device_error(ctx));
+    return SNK_OK;
+}
+
+int snk_pt_synchronize(snk_pt_ctx* ctx) {
+    if (!ctx) return SNK_ERR_INVALID_ARG;
+    API_TRY(set_device(ctx));
+    if (!ctx->d_err.p) return SNK_OK;
+    API_TRY(check_device_error(ctx));
+    return SNK_OK;
+}
+
+int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit* hits, uint32_t flags,
+                      uint32_t memory) {
+    if (!ctx || (n && (!rays || !hits)) || memory > SNK_MEM_HOST)
+        return fail(ctx, SNK_ERR_INVALID_ARG, "trace_rays: bad arguments");
+    API_TRY(set_device(ctx));
+    API_TRY(ensure_built(ctx));
+    if (n == 0) return SNK_OK;
+    cudaStream_t st = ctx->stream;
+    const float4* d_rays;
+    HitDev* d_hits;
+    if (memory == SNK_MEM_HOST) {
+        if (ctx->tr_rays.reserve(2ull * n) || ctx->tr_hits.reserve(n)) return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "trace buffers");
+        if (cudaMemcpyAsync(ctx->tr_rays.p, rays, sizeof(snk_ray) * (size_t)n, cudaMemcpyHostToDevice, st))
+            return fail(ctx, SNK_ERR_CUDA, "trace_rays: ray upload");
+        d_rays = ctx->tr_rays.p;
+        d_hits = ctx->tr_hits.p;
+    } else {
+        d_rays = reinterpret_cast<const float4*>(rays);
+        d_hits = reinterpret_cast<HitDev*>(hits);
+    }
+    if (ctx->tr_work.reserve(1) || cudaMemsetAsync(ctx->tr_work.p, 0, sizeof(uint32_t), st))
+        return fail(ctx, SNK_ERR_CUDA, "trace_rays: work counter");
+    cudaError_t e = launch_trace_rays(scene_dev(ctx), d_rays, n, d_hits, (flags & SNK_TRACE_ANY_HIT) != 0,
+                                      ctx->tr_work.p, grid_of(ctx, 16), st);
+    if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("trace_rays: ") + cudaGetErrorString(e));
+    if (memory == SNK_MEM_HOST &&
+        cudaMemcpyAsync(hits, d_hits, sizeof(snk_hit) * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return fail(ctx, SNK_ERR_CUDA, "trace_rays: hit download");
+    API_TRY(check_device_error(ctx));
+    return SNK_OK;
+}
+
+int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
+    snk_pt_ctx* ctx = const_cast<snk_pt_ctx*>(cctx);
+    if (!ctx || !out) return SNK_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    cudaSetDevice(ctx->device);
+    if (ctx->counters_pending || ctx->timing_pending) {
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, "get_stats: sync");
+        if (ctx->timing_pending) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+            ctx->last_ms = ms;
+            ctx->timing_pending = false;
+        }
+        ctx->counters_pending = false;
+    }
+    const uint32_t* c = ctx->h_counters;
+    if (ctx->last_mode == SNK_MODE_PATH) {
+        out->rays_camera = ctx->last_paths;
+        uint64_t ext = 0;
+        for (uint32_t d = 1; d < ctx->last_depth; d++) ext += c[CNT_QUEUE + d];
+        out->rays_extension = ext;
+    } else {
+        out->rays_camera = ctx->last_pixels;
+    }
+    out->rays_shadow = c[CNT_SHADOW_RAYS];
+    out->node_visits = ctx->last_count_nodes ? ctx->h_trav[0] : 0;
+    out->triangle_tests = ctx->last_count_nodes ? ctx->h_trav[1] : 0;
+    out->shadow_node_visits = ctx->last_count_nodes ? ctx->h_trav[2] : 0;
+    out->shadow_triangle_tests = ctx->last_count_nodes ? ctx->h_trav[3] : 0;
+    if (ctx->prof_pending) {
+        for (int k = 0; k < SNK_NUM_STAGES; k++) ctx->stage_ms[k] = 0.0;
+        for (size_t i = 0; i + 1 < ctx->prof_used; i += 2) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ctx->prof_ev[i], ctx->prof_ev[i + 1]);
+            ctx->stage_ms[ctx->prof_stage[i / 2]] += ms;
+        }
+        ctx->prof_pending = false;
+    }
+    for (int k = 0; k < SNK_NUM_STAGES; k++) {
+        out->stage_ms[k] = ctx->stage_ms[k];
+        out->stage_launches[k] = ctx->stage_launches[k];
+    }
+    out->wide_nodes = ctx->blas_nodes + ctx->tlas_nodes;
+    out->triangles = ctx->total_tris;
+    out->instances = ctx->instances.size();
+    out->blas_sah_cost = ctx->blas_sah;
+    out->last_render_ms = ctx->last_ms;
+    unsigned e = 0;
+    if (ctx->d_err.p) cudaMemcpy(&e, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    out->device_error = e;
+    return SNK_OK;
+}
+
+int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames) {
+    if (!ctx || !out || memory > SNK_MEM_HOST) return fail(ctx, SNK_ERR_INVALID_ARG, "read_accumulator: bad arguments");
+    if (!ctx->accum.p || ctx->accum_w == 0) return fail(ctx, SNK_ERR_STATE, "read_accumulator: nothing accumulated");
+    API_TRY(set_device(ctx));
+    size_t np = (size_t)ctx->accum_w * ctx->accum_h;
+    std::vector<double2> h(2 * np);
+    if (cudaMemcpyAsync(h.data(), ctx->accum.p, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream) ||
+        cudaStreamSynchronize(ctx->stream))
+        return fail(ctx, SNK_ERR_CUDA, "read_accumulator: copy");
+    std::vector<float> f(4 * np);
+    for (size_t i = 0; i < np; i++) {
+        double cnt = h[2 * i + 1].y > 0 ? h[2 * i + 1].y : 1.0;
+        f[4 * i + 0] = (float)(h[2 * i].x / cnt);
+        f[4 * i + 1] = (float)(h[2 * i].y / cnt);
+        f[4 * i + 2] = (float)(h[2 * i + 1].x / cnt);
+        f[4 * i + 3] = 1.0f;
+    }
+    if (memory == SNK_MEM_HOST) {
+        std::memcpy(out, f.data(), f.size() * sizeof(float));
+    } else if (cudaMemcpy(out, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+        return fail(ctx, SNK_ERR_CUDA, "read_accumulator: upload");
+    }
+    if (num_frames) *num_frames = ctx->accum_frames;
+    return SNK_OK;
+}
+
+}  // extern "C"

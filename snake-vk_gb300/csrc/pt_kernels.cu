@@ -1,0 +1,229 @@
+// pt_kernels.cu -- wavefront path tracing: ray generation, shading with
+// next-event estimation, queue compaction and the per-pixel resolve.
+// Compiled with --fmad=false (exact binary32 operation order, see snk_device.cuh).
+//
+// The reference's pass 2 shades every pixel in one ray-generation thread and
+// adds a biased diffuse bounce (BounceDiffuse, Core/res/shaders/RayGen.rgen:139-213:
+// cos(dot(...)) weight, x0.25 inner bounces).  This path tracer replaces it with an
+// unbiased estimator for the reference's own BRDF (LightBuffers.glsl:104-144):
+//   - emission counted on camera hits only; every vertex does NEE toward the
+//     directional light (as RayClosestHit.rchit:136) and one power-sampled local
+//     light (sphere light or emissive triangle);
+//   - continuation is cosine-weighted; its weight f cos / pdf is
+//     albedo * (kd + pi * specular) for the reference's CookTorranceBRDF with
+//     albedo applied to both terms (RayGen.rgen:273);
+//   - russian roulette from segment rr_depth with survival min(max(beta), 0.95).
+// Random numbers: PCG32 streams keyed by (pixel, sample, segment, seed); each
+// vertex draws 6 numbers, the camera segment 2 more for the pixel jitter.
+#include "snk_frame.h"
+
+namespace snk {
+namespace {
+
+constexpr int BLK = 256;
+
+__device__ __forceinline__ void decode_path(const FrameParams& F, uint32_t p, uint32_t* gpix, uint32_t* s,
+                                            uint32_t* vi, uint32_t* x, uint32_t* y) {
+    *gpix = p / F.spp;
+    *s = p - *gpix * F.spp;
+    *vi = find_view(F.views, F.nviews, *gpix);
+    const ViewDev& V = F.views[*vi];
+    uint32_t local = *gpix - V.pixel_offset;
+    *x = local % V.v.width;
+    *y = local / V.v.width;
+}
+
+__global__ void __launch_bounds__(BLK) k_generate(FrameParams F) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) F.counters[CNT_QUEUE + 0] = F.n_paths;
+    for (uint32_t p = blockIdx.x * BLK + threadIdx.x; p < F.n_paths; p += gridDim.x * BLK) {
+        uint32_t gpix, s, vi, x, y;
+        decode_path(F, p, &gpix, &s, &vi, &x, &y);
+        const ViewDev& V = F.views[vi];
+        Pcg rng = pcg_stream(gpix, s, 0u, F.seed);
+        float j1 = pcg_float(rng), j2 = pcg_float(rng);
+        float jx = s == 0 ? 0.5f : j1, jy = s == 0 ? 0.5f : j2;
+        V3 d = camera_dir(V.v, x, y, jx, jy);
+        F.rays[0][2ull * p] = make_float4(V.v.pos[0], V.v.pos[1], V.v.pos[2], 0.0f);
+        F.rays[0][2ull * p + 1] = make_float4(d.x, d.y, d.z, T_FAR);
+        F.path_ids[0][p] = p;
+        F.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        F.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+__device__ __forceinline__ void write_gbuffer_hit(const ViewDev& V, uint32_t o, const Surface& s, float t, float2 mo) {
+    if (V.albedo) V.albedo[o] = make_float4(s.albedo.x, s.albedo.y, s.albedo.z, 1.0f);
+    if (V.normal) V.normal[o] = make_float4(s.n.x, s.n.y, s.n.z, 0.0f);
+    if (V.position) V.position[o] = make_float4(s.pos.x, s.pos.y, s.pos.z, 1.0f);
+    if (V.rma) V.rma[o] = make_float4(s.roughness, s.metallic, s.ao, 1.0f);
+    if (V.motion) V.motion[o] = mo;
+    if (V.depth) V.depth[o] = t;
+    if (V.mat_flags) V.mat_flags[o] = s.flags;
+    if (V.inst_id) V.inst_id[o] = s.inst;
+    if (V.prim_id) V.prim_id[o] = s.prim;
+}
+
+__device__ __forceinline__ void write_gbuffer_miss(const ViewDev& V, uint32_t o) {
+    float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (V.albedo) V.albedo[o] = z;
+    if (V.normal) V.normal[o] = z;
+    if (V.position) V.position[o] = z;
+    if (V.rma) V.rma[o] = z;
+    if (V.motion) V.motion[o] = make_float2(0.0f, 0.0f);
+    if (V.depth) V.depth[o] = -1.0f;
+    if (V.mat_flags) V.mat_flags[o] = 0u;
+    if (V.inst_id) V.inst_id[o] = INVALID;
+    if (V.prim_id) V.prim_id[o] = INVALID;
+}
+
+__global__ void __launch_bounds__(BLK) k_shade(FrameParams F, uint32_t d) {
+    const uint32_t cur = d & 1u, nxt = cur ^ 1u;
+    const uint32_t n = F.counters[CNT_QUEUE + d];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp_global = (blockIdx.x * BLK + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * BLK) >> 5;
+    const SceneDev& S = F.S;
+    for (uint32_t base = warp_global * 32u; base < n; base += nwarps * 32u) {
+        const uint32_t i = base + lane;
+        bool cont = false, sv0 = false, sv1 = false;
+        uint32_t p = 0;
+        float4 nr0 = make_float4(0, 0, 0, 0), nr1 = make_float4(0, 0, 0, 0);
+        if (i < n) {
+            p = F.path_ids[cur][i];
+            uint32_t gpix, s, vi, x, y;
+            decode_path(F, p, &gpix, &s, &vi, &x, &y);
+            const ViewDev& V = F.views[vi];
+            const uint32_t o = y * V.v.width + x;
+            float4 rd4 = F.rays[cur][2ull * i + 1];
+            V3 rd = v3(rd4.x, rd4.y, rd4.z);
+            HitDev h = F.hits[i];
+            float4* sr = F.shadow_rays + 4ull * i;
+            sr[1].w = -1.0f;
+            sr[3].w = -1.0f;
+            Pcg rng = pcg_stream(gpix, s, d, F.seed);
+            if (d == 0) { pcg_next(rng); pcg_next(rng); }
+            if (!h.flags) {
+                if (d == 0 && s == 0) write_gbuffer_miss(V, o);
+            } else {
+                Surface sf = surface_at(S, h.inst, h.prim, h.u, h.v, rd);
+                if (d == 0 && s == 0) write_gbuffer_hit(V, o, sf, h.t, motion_of(S, V.v, sf, x, y));
+                float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
+                float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
+                float4 b4 = F.beta[p];
+                V3 beta = v3(b4.x, b4.y, b4.z);
+                if (sf.flags & MAT_EMISSIVE) {
+                    if (d == 0) {
+                        float4 l4 = F.L[p];
+                        V3 Lp = add(v3(l4.x, l4.y, l4.z), cmul(beta, sf.albedo));
+                        F.L[p] = make_float4(Lp.x, Lp.y, Lp.z, 0.0f);
+                    }
+                } else {
+                    V3 v = neg(rd);
+                    V3 f0 = f0_of(sf.albedo, sf.metallic);
+                    V3 xb = add(sf.pos, mul(sf.n, SURFACE_BIAS));
+                    if (S.dir_light.enabled) {
+                        V3 c = calc_directional(load3(S.dir_light.dir), load3(S.dir_light.colour), v, f0, sf.n,
+                                                sf.roughness, sf.metallic, sf.albedo);
+                        if (maxc(c) > 0.0f) {
+                            V3 cb = cmul(beta, c);
+                            sr[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
+                            sr[1] = make_float4(S.dir_light.dir[0], S.dir_light.dir[1], S.dir_light.dir[2], T_FAR);
+                            F.shadow_contrib[2ull * i] = make_float4(cb.x, cb.y, cb.z, 0.0f);
+                            sv0 = true;
+                        }
+                    }
+                    V3 c, ldir;
+                    float ltmax;
+                    if (sample_local(S, sf, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
+                        V3 cb = cmul(beta, c);
+                        sr[2] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
+                        sr[3] = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
+                        F.shadow_contrib[2ull * i + 1] = make_float4(cb.x, cb.y, cb.z, 0.0f);
+                        sv1 = true;
+                    }
+                    bool alive = d + 1 < F.max_depth;
+                    if (alive && d + 1 >= F.rr_depth) {
+                        float ps = fmin_(maxc(beta), 0.95f);
+                        if (u_rr < ps) beta = v3(beta.x / ps, beta.y / ps, beta.z / ps);
+                        else alive = false;
+                    }
+                    if (alive) {
+                        float r = sqrtf(u_d1);
+                        float sp, cp;
+                        sincos2pi(u_d2, &sp, &cp);
+                        float lx = r * cp, ly = r * sp, lz = sqrtf(fmax_(0.0f, 1.0f - u_d1));
+                        V3 b1, b2;
+                        onb(sf.n, &b1, &b2);
+                        V3 wi = v3((b1.x * lx + b2.x * ly) + sf.n.x * lz, (b1.y * lx + b2.y * ly) + sf.n.y * lz,
+                                   (b1.z * lx + b2.z * ly) + sf.n.z * lz);
+                        if (dot(wi, sf.ng) > 0.0f) {
+                            Terms tm = brdf_terms(wi, v, f0, sf.n, sf.roughness, sf.metallic);
+                            V3 w = v3(sf.albedo.x * (tm.kd.x + tm.spec.x * PI), sf.albedo.y * (tm.kd.y + tm.spec.y * PI),
+                                      sf.albedo.z * (tm.kd.z + tm.spec.z * PI));
+                            beta = cmul(beta, w);
+                            F.beta[p] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+                            nr0 = make_float4(xb.x, xb.y, xb.z, EXT_TMIN);
+                            nr1 = make_float4(wi.x, wi.y, wi.z, T_FAR);
+                            cont = true;
+                        }
+                    }
+                }
+            }
+        }
+        // warp-ballot compaction of the continuing paths into the next queue
+        const unsigned full = 0xFFFFFFFFu;
+        unsigned m = __ballot_sync(full, cont);
+        unsigned sm = __popc(__ballot_sync(full, sv0)) + __popc(__ballot_sync(full, sv1));
+        uint32_t slot_base = 0;
+        if (lane == 0) {
+            if (m) slot_base = atomicAdd(&F.counters[CNT_QUEUE + d + 1], (uint32_t)__popc(m));
+            if (sm) atomicAdd(&F.counters[CNT_SHADOW_RAYS], sm);
+        }
+        slot_base = __shfl_sync(full, slot_base, 0);
+        if (cont) {
+            uint32_t j = slot_base + __popc(m & ((1u << lane) - 1u));
+            F.rays[nxt][2ull * j] = nr0;
+            F.rays[nxt][2ull * j + 1] = nr1;
+            F.path_ids[nxt][j] = p;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BLK) k_resolve(FrameParams F) {
+    const float inv = 1.0f / (float)F.spp;
+    for (uint32_t g = blockIdx.x * BLK + threadIdx.x; g < F.n_pixels; g += gridDim.x * BLK) {
+        uint32_t vi = find_view(F.views, F.nviews, g);
+        const ViewDev& V = F.views[vi];
+        uint32_t o = g - V.pixel_offset;
+        V3 sum = v3(0.0f, 0.0f, 0.0f);
+        for (uint32_t s = 0; s < F.spp; s++) {
+            float4 l = F.L[(size_t)g * F.spp + s];
+            sum = add(sum, v3(l.x, l.y, l.z));
+        }
+        float4 r = make_float4(sum.x * inv, sum.y * inv, sum.z * inv, 1.0f);
+        if (V.radiance) V.radiance[o] = r;
+        if (F.accumulate && vi == 0) {
+            double2 a0 = F.accum[2ull * o], a1 = F.accum[2ull * o + 1];
+            a0.x += (double)r.x; a0.y += (double)r.y; a1.x += (double)r.z; a1.y += 1.0;
+            F.accum[2ull * o] = a0;
+            F.accum[2ull * o + 1] = a1;
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_generate(const FrameParams& F, int grid, cudaStream_t s) {
+    k_generate<<<grid, BLK, 0, s>>>(F);
+    return cudaGetLastError();
+}
+cudaError_t launch_shade(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s) {
+    k_shade<<<grid, BLK, 0, s>>>(F, depth);
+    return cudaGetLastError();
+}
+cudaError_t launch_resolve(const FrameParams& F, int grid, cudaStream_t s) {
+    k_resolve<<<grid, BLK, 0, s>>>(F);
+    return cudaGetLastError();
+}
+
+}  // namespace snk

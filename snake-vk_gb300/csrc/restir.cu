@@ -1,0 +1,436 @@
+// restir.cu -- the reference's two-pass ReSTIR DI on CUDA.
+// Compiled with --fmad=false (exact binary32 operation order, see snk_device.cuh).
+//
+// Reference: Core/res/shaders/RayGen.rgen
+//   PixelReservoir ..................... :64-76 (48 bytes, FP32)
+//   Update*Reservoir ................... :215-239
+//   TriangleShadowTest / ComputeTriangleRadiance :241-282
+//   DoInitialWRS ....................... :296-357 (LIGHT_RIS_ITERS candidates per light kind)
+//   CombinePixelReservoir .............. :361-386
+//   WriteInitialReservoirs (temporal) .. :411-468 (M cap, normal test 0.95)
+//   ComputeAndWriteSpatialReservoirReuse :470-506
+//   CalculateRadianceFromReservoirs .... :508-528, main :530-570
+// dispatched by RT::RecordRenderCmdBuf (Core/src/rendering/Raytracing.cpp:250-263)
+// as two full-screen launches with a barrier between them; here: a primary-ray
+// G-buffer kernel, the initial+temporal kernel and the spatial+shading kernel.
+//
+// Deviations (the CPU oracle makes the same ones):
+//   - gold_noise / random() are replaced by PCG32 streams keyed by
+//     (pixel, frame, pass, seed); one number per decision, drawn in program order;
+//   - the point-light visibility direction of DoInitialWRS (:346) is
+//     (pos - biased_pos) / dist (the shader divides only biased_pos);
+//   - when temporal reuse is not applied the initial reservoir is written (the
+//     shader writes an empty one, :417-467), so the first frame is lit;
+//   - neighbour and history normals are fetched at the nearest texel; spatial
+//     reuse compares against this frame's normals (the shader samples the
+//     previous frame's normal image at :490);
+//   - FindNeighbourPixelCoord's unbounded retry loop (:400) is bounded to 8 tries.
+#include "snk_frame.h"
+#include "snk_trace.cuh"
+
+namespace snk {
+namespace {
+
+constexpr int RBLK = 128;
+
+struct Reservoir {
+    float w_sum_pl, w_pl;
+    uint32_t pl_idx, pl_m;
+    uint32_t em_inst, em_tri;
+    float em_u, em_v;
+    float w_sum_em, w_em;
+    uint32_t m_em, pad;
+};
+static_assert(sizeof(Reservoir) == 48, "reservoir layout");
+
+__device__ __forceinline__ Reservoir res_init() {
+    Reservoir r;
+    r.w_sum_pl = 0.0f; r.w_pl = 0.0f; r.pl_idx = INVALID; r.pl_m = 0;
+    r.em_inst = INVALID; r.em_tri = INVALID; r.em_u = 0.0f; r.em_v = 0.0f;
+    r.w_sum_em = 0.0f; r.w_em = 0.0f; r.m_em = 0; r.pad = 0;
+    return r;
+}
+__device__ __forceinline__ Reservoir res_load(const void* base, uint32_t i) {
+    const float4* p = reinterpret_cast<const float4*>(base) + 3ull * i;
+    Reservoir r;
+    float4* q = reinterpret_cast<float4*>(&r);
+    q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+    return r;
+}
+__device__ __forceinline__ void res_store(void* base, uint32_t i, const Reservoir& r) {
+    float4* p = reinterpret_cast<float4*>(base) + 3ull * i;
+    const float4* q = reinterpret_cast<const float4*>(&r);
+    p[0] = q[0]; p[1] = q[1]; p[2] = q[2];
+}
+
+struct Ctx {   // per-thread traversal context
+    const SceneDev* S;
+    uint2* sh;
+    uint32_t shadow_rays;
+};
+
+__device__ __noinline__ float shadow_test(Ctx& c, V3 o, V3 d, float tmax) {
+    TraceResult r;
+    c.shadow_rays++;
+    bool hit = trace_scene<true, false>(*c.S, o, d, SHADOW_TMIN, tmax, r, c.sh, threadIdx.x, RBLK, nullptr);
+    return hit ? 0.0f : 1.0f;
+}
+
+__device__ __noinline__ bool trace_primary(const SceneDev& S, V3 o, V3 d, TraceResult& r, uint2* sh) {
+    return trace_scene<false, false>(S, o, d, 0.0f, T_FAR, r, sh, threadIdx.x, RBLK, nullptr);
+}
+
+struct Shade { V3 ro, n, albedo, v, f0, biased; float rough, metal; };
+
+__device__ __forceinline__ bool update_pl(Reservoir& r, uint32_t idx, float w, Pcg& rng) {
+    r.pl_m++;
+    float u = pcg_float(rng);
+    r.w_sum_pl = r.w_sum_pl + w;
+    if (r.w_sum_pl > 0.0f && u < w / r.w_sum_pl) { r.pl_idx = idx; return true; }
+    return false;
+}
+__device__ __forceinline__ bool update_em(Reservoir& r, uint32_t inst, uint32_t tri, float bu, float bv, float w,
+                                          Pcg& rng) {
+    r.m_em++;
+    float u = pcg_float(rng);
+    r.w_sum_em = r.w_sum_em + w;
+    if (r.w_sum_em > 0.0f && u < w / r.w_sum_em) {
+        r.em_inst = inst; r.em_tri = tri; r.em_u = bu; r.em_v = bv;
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tri_point(const SceneDev& S, uint32_t inst, uint32_t tri, float bu, float bv, V3* p,
+                                          V3* pn) {
+    const InstShade& I = S.inst_shade[inst];
+    const MeshInfo& M = S.meshes[I.mesh_id];
+    const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
+    uint32_t i0 = M.vertex_offset + ix[0], i1 = M.vertex_offset + ix[1], i2 = M.vertex_offset + ix[2];
+    float bz = (1.0f - bu) - bv;
+    V3 q0 = load3(S.positions + 3ull * i0), q1 = load3(S.positions + 3ull * i1), q2 = load3(S.positions + 3ull * i2);
+    V3 q = add(add(mul(q0, bu), mul(q1, bv)), mul(q2, bz));
+    V3 nn;
+    if (M.has_normals)
+        nn = add(add(mul(load3(S.normals + 3ull * i0), bu), mul(load3(S.normals + 3ull * i1), bv)),
+                 mul(load3(S.normals + 3ull * i2), bz));
+    else
+        nn = cross(sub(q1, q0), sub(q2, q0));
+    *p = xform_point(I.m, q);
+    *pn = normalize(mat3_mul(I.nmat, nn));
+}
+
+__device__ __forceinline__ float tri_shadow(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, V3 surface_pos) {
+    V3 p, pn;
+    tri_point(*c.S, inst, tri, bu, bv, &p, &pn);
+    V3 target = add(p, mul(pn, 0.01f));
+    float dist = length(sub(surface_pos, target));
+    V3 dir = divs(sub(target, surface_pos), dist);
+    return shadow_test(c, surface_pos, dir, dist);
+}
+
+__device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, const Shade& sh,
+                                        bool shadow) {
+    const SceneDev& S = *c.S;
+    V3 p, pn;
+    tri_point(S, inst, tri, bu, bv, &p, &pn);
+    V3 em = load3(S.materials[S.inst_shade[inst].material_id].albedo);
+    V3 brdf = cook_torrance(brdf_terms(normalize(sub(p, sh.ro)), sh.v, sh.f0, sh.n, sh.rough, sh.metal));
+    V3 dd = sub(sh.ro, p);
+    float d2 = fabsf(dot(dd, dd));
+    V3 rad = v3(((em.x * sh.albedo.x) * brdf.x) / d2, ((em.y * sh.albedo.y) * brdf.y) / d2,
+                ((em.z * sh.albedo.z) * brdf.z) / d2);
+    if (shadow) {
+        V3 target = add(p, mul(pn, 0.01f));
+        float dist = length(sub(sh.biased, target));
+        V3 dir = divs(sub(target, sh.biased), dist);
+        rad = mul(rad, shadow_test(c, sh.biased, dir, dist));
+    }
+    return rad;
+}
+
+__device__ __noinline__ void combine(Ctx& c, Reservoir& cur, const Reservoir& nb, float& phat_pl, float& phat_em,
+                                     const Shade& sh, Pcg& rng) {
+    const SceneDev& S = *c.S;
+    if (nb.pl_idx != INVALID) {
+        const PointLightDev& L = S.point_lights[nb.pl_idx];
+        V3 lp = load3(L.pos);
+        float ld = length(sub(lp, sh.biased));
+        float vis = shadow_test(c, sh.biased, divs(sub(lp, sh.biased), ld), ld - 0.001f);
+        float p_hat = length(calc_pointlight(L, sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal, sh.albedo)) * vis;
+        float w = (p_hat * (float)nb.pl_m) * nb.w_pl;
+        if (update_pl(cur, nb.pl_idx, w, rng)) phat_pl = p_hat;
+    }
+    if (nb.em_inst != INVALID) {
+        V3 rad = tri_radiance(c, nb.em_inst, nb.em_tri, nb.em_u, nb.em_v, sh, true);
+        float p_hat = length(rad);
+        float w = (p_hat * nb.w_em) * (float)nb.m_em;
+        if (update_em(cur, nb.em_inst, nb.em_tri, nb.em_u, nb.em_v, w, rng)) phat_em = p_hat;
+    }
+}
+
+__device__ __forceinline__ Shade shade_of(const ViewParams& vw, V3 pos, V3 n, V3 albedo, float rough, float metal) {
+    Shade sh;
+    sh.ro = pos; sh.n = n; sh.albedo = albedo; sh.rough = rough; sh.metal = metal;
+    V3 cam = load3(vw.pos);
+    sh.v = normalize(sub(cam, pos));
+    sh.f0 = f0_of(albedo, metal);
+    float bias = 0.01f + fmax_(length(sub(cam, pos)) * 0.001f, 0.01f);
+    sh.biased = add(pos, mul(n, bias));
+    return sh;
+}
+
+__device__ __forceinline__ void flush_rays(uint32_t n, uint32_t* ctr) {
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xFFFFFFFFu, n, o);
+    if ((threadIdx.x & 31u) == 0 && n) atomicAdd(ctr, n);
+}
+
+// primary rays through pixel centres -> G-buffer outputs + ReSTIR surface data
+__global__ void __launch_bounds__(RBLK) k_restir_gbuffer(FrameParams F, uint32_t vi, RestirView R) {
+    __shared__ uint2 sh[STACK_SH * RBLK];
+    const ViewDev& V = F.views[vi];
+    const uint32_t W = V.v.width, H = V.v.height, n = W * H;
+    for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
+        uint32_t o = base + threadIdx.x;
+        if (o >= n) continue;
+        uint32_t x = o % W, y = o / W;
+        V3 rd = camera_dir(V.v, x, y, 0.5f, 0.5f);
+        TraceResult r;
+        if (trace_primary(F.S, load3(V.v.pos), rd, r, sh)) {
+            Surface s = surface_at(F.S, r.inst, r.prim, r.u, r.v, rd);
+            float2 mo = motion_of(F.S, V.v, s, x, y);
+            if (V.albedo) V.albedo[o] = make_float4(s.albedo.x, s.albedo.y, s.albedo.z, 1.0f);
+            if (V.normal) V.normal[o] = make_float4(s.n.x, s.n.y, s.n.z, 0.0f);
+            if (V.position) V.position[o] = make_float4(s.pos.x, s.pos.y, s.pos.z, 1.0f);
+            if (V.rma) V.rma[o] = make_float4(s.roughness, s.metallic, s.ao, 1.0f);
+            if (V.motion) V.motion[o] = mo;
+            if (V.depth) V.depth[o] = r.t;
+            if (V.mat_flags) V.mat_flags[o] = s.flags;
+            if (V.inst_id) V.inst_id[o] = s.inst;
+            if (V.prim_id) V.prim_id[o] = s.prim;
+            float kind = (s.flags & MAT_EMISSIVE) ? 2.0f : 1.0f;
+            R.g_pos[o] = make_float4(s.pos.x, s.pos.y, s.pos.z, kind);
+            R.g_normal[o] = make_float4(s.n.x, s.n.y, s.n.z, 0.0f);
+            R.g_albedo[o] = make_float4(s.albedo.x, s.albedo.y, s.albedo.z, s.roughness);
+            R.g_misc[o] = make_float4(s.metallic, mo.x, mo.y, 0.0f);
+        } else {
+            float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (V.albedo) V.albedo[o] = z;
+            if (V.normal) V.normal[o] = z;
+            if (V.position) V.position[o] = z;
+            if (V.rma) V.rma[o] = z;
+            if (V.motion) V.motion[o] = make_float2(0.0f, 0.0f);
+            if (V.depth) V.depth[o] = -1.0f;
+            if (V.mat_flags) V.mat_flags[o] = 0u;
+            if (V.inst_id) V.inst_id[o] = INVALID;
+            if (V.prim_id) V.prim_id[o] = INVALID;
+            R.g_pos[o] = z; R.g_normal[o] = z; R.g_albedo[o] = z; R.g_misc[o] = z;
+        }
+    }
+}
+
+// WriteInitialReservoirs: initial RIS + temporal reuse
+__global__ void __launch_bounds__(RBLK) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs) {
+    __shared__ uint2 sh[STACK_SH * RBLK];
+    const ViewDev& V = F.views[vi];
+    const SceneDev& S = F.S;
+    const uint32_t W = V.v.width, H = V.v.height, n = W * H;
+    Ctx c;
+    c.S = &F.S; c.sh = sh; c.shadow_rays = 0;
+    for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
+        uint32_t o = base + threadIdx.x;
+        if (o >= n) continue;
+        uint32_t x = o % W, y = o / W;
+        float4 gp = R.g_pos[o];
+        if (gp.w != 1.0f) { res_store(R.temporal, o, res_init()); continue; }
+        float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
+        V3 nrm = v3(gn.x, gn.y, gn.z);
+        Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
+        Pcg rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000001u, rs.seed);
+        Reservoir Rr = res_init();
+        float phat_pl = 0.0f, phat_em = 0.0f;
+        const uint32_t npl = S.num_point_lights;
+        if (npl > 0) {
+            for (uint32_t i = 0; i < rs.candidates; i++) {
+                uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
+                if (idx > npl - 1) idx = npl - 1;
+                float p_hat = length(calc_pointlight(S.point_lights[idx], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
+                                                     sh.albedo));
+                float w = p_hat / (1.0f / (float)npl);
+                if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
+            }
+        }
+        const uint32_t nem = S.num_emissive_instances;
+        if (nem > 0) {
+            for (uint32_t i = 0; i < rs.candidates; i++) {
+                uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
+                if (k > nem - 1) k = nem - 1;
+                uint32_t inst = S.emissive_instances[k];
+                const InstShade& I = S.inst_shade[inst];
+                const MeshInfo& M = S.meshes[I.mesh_id];
+                uint32_t ntri = M.num_triangles;
+                uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
+                if (tri > ntri - 1) tri = ntri - 1;
+                float bu = pcg_float(rng), bv = pcg_float(rng);
+                if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
+                const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
+                V3 p0 = load3(S.positions + 3ull * (M.vertex_offset + ix[0]));
+                V3 p1 = load3(S.positions + 3ull * (M.vertex_offset + ix[1]));
+                V3 p2 = load3(S.positions + 3ull * (M.vertex_offset + ix[2]));
+                float area = (I.det3 * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
+                V3 rad = tri_radiance(c, inst, tri, bu, bv, sh, false);
+                float p_hat = length(rad);
+                float pdf = 1.0f / ((float)(nem * ntri) * area);
+                float w = p_hat / pdf;
+                if (update_em(Rr, inst, tri, bu, bv, w, rng)) phat_em = p_hat;
+            }
+        }
+        if (Rr.pl_idx != INVALID) {
+            V3 lp = load3(S.point_lights[Rr.pl_idx].pos);
+            float dist = length(sub(lp, sh.biased));
+            float vis = shadow_test(c, sh.biased, divs(sub(lp, sh.biased), dist), dist);
+            Rr.w_pl = vis * ((Rr.w_sum_pl / (float)Rr.pl_m) / phat_pl);
+        } else {
+            Rr.w_pl = 0.0f;
+        }
+        if (Rr.em_inst != INVALID) {
+            float vis = tri_shadow(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh.biased);
+            Rr.w_em = vis * ((Rr.w_sum_em / (float)Rr.m_em) / phat_em);
+        } else {
+            Rr.w_em = 0.0f;
+        }
+        Reservoir out = Rr;
+        if (R.history_valid && rs.temporal != 0 && V.v.prev_valid) {
+            float hu = ((float)x + 0.5f) / (float)W + gm.y;
+            float hv = ((float)y + 0.5f) / (float)H + gm.z;
+            if (hu > 0.0f && hv > 0.0f && hu < 1.0f && hv < 1.0f) {
+                uint32_t hx = (uint32_t)(hu * (float)W), hy = (uint32_t)(hv * (float)H);
+                if (hx > W - 1) hx = W - 1;
+                if (hy > H - 1) hy = H - 1;
+                float4 pn = R.prev_normal[hy * W + hx];
+                if (dot(v3(pn.x, pn.y, pn.z), nrm) > 0.95f) {
+                    Reservoir Hh = res_load(R.history, hy * W + hx);
+                    float mcap = (float)rs.mcap;
+                    if ((float)Hh.pl_m > mcap * (float)Rr.pl_m) {
+                        Hh.w_sum_pl = Hh.w_sum_pl * ((mcap * (float)Rr.pl_m) / (float)Hh.pl_m);
+                        Hh.pl_m = rs.mcap * Rr.pl_m;
+                    }
+                    if ((float)Hh.m_em > mcap * (float)Rr.m_em) {
+                        Hh.w_sum_em = Hh.w_sum_em * ((mcap * (float)Rr.m_em) / (float)Hh.m_em);
+                        Hh.m_em = rs.mcap * Rr.m_em;
+                    }
+                    Reservoir T = res_init();
+                    float tp_pl = 0.0f, tp_em = 0.0f;
+                    combine(c, T, Rr, tp_pl, tp_em, sh, rng);
+                    combine(c, T, Hh, tp_pl, tp_em, sh, rng);
+                    T.m_em = Hh.m_em + Rr.m_em;
+                    T.pl_m = Hh.pl_m + Rr.pl_m;
+                    T.w_em = tp_em > 0.0f ? (T.w_sum_em / (float)T.m_em) / tp_em : 0.0f;
+                    T.w_pl = tp_pl > 0.0f ? (T.w_sum_pl / (float)T.pl_m) / tp_pl : 0.0f;
+                    out = T;
+                }
+            }
+        }
+        res_store(R.temporal, o, out);
+    }
+    flush_rays(c.shadow_rays, &F.counters[CNT_SHADOW_RAYS]);
+}
+
+// ComputeAndWriteSpatialReservoirReuse + CalculateRadianceFromReservoirs + main
+__global__ void __launch_bounds__(RBLK) k_restir_spatial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs) {
+    __shared__ uint2 sh[STACK_SH * RBLK];
+    const ViewDev& V = F.views[vi];
+    const SceneDev& S = F.S;
+    const uint32_t W = V.v.width, H = V.v.height, n = W * H;
+    Ctx c;
+    c.S = &F.S; c.sh = sh; c.shadow_rays = 0;
+    for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
+        uint32_t o = base + threadIdx.x;
+        if (o >= n) continue;
+        uint32_t x = o % W, y = o / W;
+        float4 gp = R.g_pos[o];
+        float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
+        V3 colour;
+        if (gp.w != 1.0f) {
+            res_store(R.spatial, o, res_init());
+            colour = gp.w == 2.0f ? v3(ga.x, ga.y, ga.z) : v3(0.0f, 0.0f, 0.0f);
+        } else {
+            V3 nrm = v3(gn.x, gn.y, gn.z);
+            Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
+            V3 light = v3(0.0f, 0.0f, 0.0f);
+            if (S.dir_light.enabled) {
+                V3 cdl = calc_directional(load3(S.dir_light.dir), load3(S.dir_light.colour), sh.v, sh.f0, sh.n, sh.rough,
+                                          sh.metal, sh.albedo);
+                light = mul(cdl, shadow_test(c, sh.biased, load3(S.dir_light.dir), 1000.0f));
+            }
+            Pcg rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000002u, rs.seed);
+            Reservoir Rr = res_init();
+            float phat_pl = 0.0f, phat_em = 0.0f;
+            Reservoir self = res_load(R.temporal, o);
+            combine(c, Rr, self, phat_pl, phat_em, sh, rng);
+            Rr.m_em += self.m_em;
+            Rr.pl_m += self.pl_m;
+            for (int i = 0; i < rs.spatial; i++) {
+                int nx = -1, ny = -1;
+                for (int tries = 0; tries < 8; tries++) {
+                    float ox = ((pcg_float(rng) - 0.5f) * 2.0f) * rs.radius;
+                    float oy = ((pcg_float(rng) - 0.5f) * 2.0f) * rs.radius;
+                    float fx = (float)x + ox, fy = (float)y + oy;
+                    if (fx >= 0.0f && fy >= 0.0f && fx < (float)W && fy < (float)H) { nx = (int)fx; ny = (int)fy; break; }
+                }
+                if (nx < 0) continue;
+                uint32_t q = (uint32_t)ny * W + (uint32_t)nx;
+                float4 qp = R.g_pos[q];
+                float4 qn4 = R.g_normal[q];
+                V3 qn = qp.w == 1.0f ? v3(qn4.x, qn4.y, qn4.z) : v3(0.0f, 0.0f, 0.0f);
+                if (dot(qn, nrm) < 0.95f) continue;
+                Reservoir Q = res_load(R.temporal, q);
+                combine(c, Rr, Q, phat_pl, phat_em, sh, rng);
+                Rr.m_em += Q.m_em;
+                Rr.pl_m += Q.pl_m;
+            }
+            Rr.w_em = phat_em > 0.0f ? (Rr.w_sum_em / phat_em) / (float)Rr.m_em : 0.0f;
+            Rr.w_pl = phat_pl > 0.0f ? (Rr.w_sum_pl / phat_pl) / (float)Rr.pl_m : 0.0f;
+            res_store(R.spatial, o, Rr);
+            V3 rad = v3(0.0f, 0.0f, 0.0f);
+            if (S.num_point_lights > 0 && Rr.pl_idx != INVALID) {
+                const PointLightDev& L = S.point_lights[Rr.pl_idx];
+                V3 lp = load3(L.pos);
+                float ld = length(sub(lp, sh.biased));
+                V3 cpl = calc_pointlight(L, sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal, sh.albedo);
+                cpl = mul(cpl, shadow_test(c, sh.biased, divs(sub(lp, sh.biased), ld), ld));
+                cpl = mul(cpl, Rr.w_pl);
+                rad = add(rad, cpl);
+            }
+            if (S.num_emissive_instances > 0 && Rr.em_inst != INVALID) {
+                V3 e = tri_radiance(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, true);
+                rad = add(rad, mul(e, Rr.w_em));
+            }
+            colour = add(light, rad);
+        }
+        float4 r4 = make_float4(colour.x, colour.y, colour.z, 1.0f);
+        if (V.radiance) V.radiance[o] = r4;
+        if (F.accumulate && vi == 0) {
+            double2 a0 = F.accum[2ull * o], a1 = F.accum[2ull * o + 1];
+            a0.x += (double)r4.x; a0.y += (double)r4.y; a1.x += (double)r4.z; a1.y += 1.0;
+            F.accum[2ull * o] = a0;
+            F.accum[2ull * o + 1] = a1;
+        }
+        // this frame's normals become the next frame's history normals (the
+        // initial pass of this frame has already consumed the previous ones)
+        R.prev_normal[o] = gp.w == 1.0f ? make_float4(gn.x, gn.y, gn.z, 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    flush_rays(c.shadow_rays, &F.counters[CNT_SHADOW_RAYS]);
+}
+
+}  // namespace
+
+cudaError_t launch_restir_stage(int stage, const FrameParams& F, uint32_t vi, const RestirView& R,
+                                const RestirSettings& rs, int grid, cudaStream_t s) {
+    if (stage == 0) k_restir_gbuffer<<<grid, RBLK, 0, s>>>(F, vi, R);
+    else if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs);
+    else k_restir_spatial<<<grid, RBLK, 0, s>>>(F, vi, R, rs);
+    return cudaGetLastError();
+}
+
+}  // namespace snk

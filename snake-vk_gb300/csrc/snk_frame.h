@@ -1,0 +1,75 @@
+// snk_frame.h -- wavefront frame state shared by the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "snk_shade.cuh"
+
+namespace snk {
+
+constexpr uint32_t MAX_DEPTH = 16;
+constexpr uint32_t MAX_VIEWS = 64;
+
+// counters (uint32) of one frame, zeroed at frame start
+constexpr uint32_t CNT_QUEUE = 0;         // [d]: rays queued for segment d
+constexpr uint32_t CNT_WORK_TRACE = 16;   // [d]: work fetch of the closest-hit pass of segment d
+constexpr uint32_t CNT_WORK_SHADOW = 32;  // [d]: work fetch of the shadow pass of segment d
+constexpr uint32_t CNT_SHADOW_RAYS = 48;  // valid shadow rays
+constexpr uint32_t CNT_TOTAL = 64;
+
+struct HitDev { float t; uint32_t inst, prim; float u, v; uint32_t flags; };
+static_assert(sizeof(HitDev) == 24, "hit layout");
+
+struct FrameParams {
+    SceneDev S;
+    const ViewDev* views;
+    uint32_t nviews;
+    uint32_t spp, max_depth, rr_depth, seed;
+    uint32_t n_paths;        // sum over views of width * height * spp
+    uint32_t n_pixels;       // sum over views of width * height
+    uint32_t accumulate;     // add view 0's radiance into accum
+    float4* rays[2];         // 2 float4 per ray: (origin, tmin), (direction, tmax)
+    uint32_t* path_ids[2];
+    HitDev* hits;
+    float4* beta;            // per path
+    float4* L;               // per path radiance
+    float4* shadow_rays;     // 2 rays per queue slot (4 float4), tmax < 0 = none
+    float4* shadow_contrib;  // 2 per queue slot
+    uint32_t* counters;
+    unsigned long long* trav_counters;   // closest: [0] nodes [1] triangles; shadow: [2] [3]
+    double2* accum;          // FP64 accumulator of view 0 (2 double2 per pixel)
+};
+
+// launch helpers (defined in pt_kernels.cu / trace_kernels.cu / restir.cu)
+cudaError_t launch_generate(const FrameParams& F, int grid, cudaStream_t s);
+cudaError_t launch_shade(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s);
+cudaError_t launch_resolve(const FrameParams& F, int grid, cudaStream_t s);
+cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
+cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
+cudaError_t launch_trace_rays(const SceneDev& S, const float4* rays, uint32_t n, HitDev* hits, bool any,
+                              uint32_t* work_counter, int grid, cudaStream_t s);
+
+// ReSTIR DI state of one view
+struct RestirView {
+    float4* g_pos;      // world position, w: 1 = valid non-emissive hit, 2 = emissive hit, 0 = miss
+    float4* g_normal;   // shading normal
+    float4* g_albedo;   // albedo, w = roughness
+    float4* g_misc;     // metallic, motion.x, motion.y
+    float4* prev_normal;
+    void* temporal;     // reservoirs (48 bytes per pixel)
+    void* history;      // final reservoirs of the previous frame
+    void* spatial;      // final reservoirs of this frame
+    uint32_t history_valid;
+};
+
+struct RestirSettings {
+    uint32_t frame_index, seed, candidates, mcap;
+    int32_t temporal, spatial;
+    float radius;
+    uint32_t pad;
+};
+
+// stage 0: primary G-buffer, 1: initial + temporal reuse, 2: spatial reuse + shading
+cudaError_t launch_restir_stage(int stage, const FrameParams& F, uint32_t view_index, const RestirView& R,
+                                const RestirSettings& rs, int grid, cudaStream_t s);
+
+}  // namespace snk

@@ -1,0 +1,108 @@
+// snk_host.h -- host-side helpers shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <utility>
+
+#include "snk_device.cuh"
+
+namespace snk {
+
+// Owning device allocation (cudaMalloc/cudaFree); grows, never shrinks.
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept { std::swap(p, o.p); std::swap(n, o.n); return *this; }
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t reserve(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) { p = nullptr; return e; }
+        n = count;
+        return cudaSuccess;
+    }
+    T* get() const { return p; }
+};
+
+// Error carrying a status code of snk_pt.h and a message.
+struct Status {
+    int code = 0;
+    std::string msg;
+    bool ok() const { return code == 0; }
+    static Status Ok() { return Status(); }
+    static Status Err(int c, std::string m) { Status s; s.code = c; s.msg = std::move(m); return s; }
+};
+
+#define SNK_TRY_CUDA(call)                                                                            \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return ::snk::Status::Err(e_ == cudaErrorMemoryAllocation ? 3 : 2,                        \
+                                      std::string(#call) + ": " + cudaGetErrorString(e_));           \
+    } while (0)
+
+#define SNK_TRY(expr)              \
+    do {                           \
+        ::snk::Status s_ = (expr); \
+        if (!s_.ok()) return s_;   \
+    } while (0)
+
+// ---- BVH builder ---------------------------------------------------------------
+struct BuildScratch {
+    DBuf<unsigned long long> keys, keys_alt;
+    DBuf<uint32_t> vals, vals_alt;
+    DBuf<int2> children;
+    DBuf<int> parent, flags;
+    DBuf<float4> node_lo, node_hi;
+    DBuf<uint32_t> leaf_count;
+    DBuf<uint2> tasks_a, tasks_b;
+    DBuf<uint32_t> counters;      // [0] tasks in, [1] tasks out, [2] wide nodes, [3] prims
+    DBuf<unsigned> cbounds;       // centroid bounds, order-preserving encoded
+    DBuf<unsigned char> cub_tmp;
+    DBuf<double> sah;             // SAH accumulator
+    size_t cap = 0;
+};
+
+struct BuildResult {
+    uint32_t num_nodes = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    double sah = 0.0;   // SAH cost of the wide BVH (internal 1, primitive 1, area relative to the root)
+};
+
+// Builds an 8-wide compressed BVH over n primitive boxes (prim_lo/prim_hi, xyz used).
+// Nodes are written at nodes[node_base + k] (root at node_base) with absolute child
+// indices; primitive slots are [prim_base, prim_base + n) and prim_order[k] receives
+// the primitive id stored in slot prim_base + k.
+Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
+                      uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t stream,
+                      BuildResult* out);
+
+// Per-triangle padded boxes of one mesh (object space).
+Status launch_triangle_boxes(const float* positions, const uint32_t* indices, uint32_t vertex_offset,
+                             uint32_t index_offset, uint32_t num_tris, float4* lo, float4* hi, cudaStream_t s);
+// Triangle records of one mesh from the build's primitive order.
+Status launch_fill_triangles(const uint32_t* prim_order, uint32_t n, const float* positions, const uint32_t* indices,
+                             uint32_t vertex_offset, uint32_t index_offset, TriRecord* out, cudaStream_t s);
+// World boxes of the listed instances (transform of the mesh bounds) for the instance BVH.
+Status launch_instance_boxes(const uint32_t* inst_list, uint32_t n, const InstShade* inst, const MeshInfo* meshes,
+                             float4* lo, float4* hi, cudaStream_t s);
+// tlas_prims[k] = inst_list[prim_order[k]]
+Status launch_map_prims(const uint32_t* prim_order, const uint32_t* inst_list, uint32_t n, uint32_t* out,
+                        cudaStream_t s);
+
+}  // namespace snk

@@ -1,0 +1,270 @@
+"""snkpt -- Python host side of the GB300 path-tracing core.
+
+Thin ctypes binding of ``libsnkpt.so`` (the C ABI of ``include/snk_pt.h``)
+plus :class:`RT`, which mirrors the reference's render-pass class
+(``Core/headers/rendering/Raytracing.h:11-31``: ``RT::Init``,
+``RT::RecordRenderCmdBuf``, ``RT::RtSettings``).
+
+There is no fallback: if the CUDA library is missing or no GPU is present the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsnkpt.so")
+
+EXPORTS = [
+    "snk_pt_abi_version", "snk_pt_create", "snk_pt_destroy", "snk_pt_set_stream", "snk_pt_get_last_error",
+    "snk_pt_get_stats", "snk_pt_upload_meshes", "snk_pt_set_instances", "snk_pt_set_materials",
+    "snk_pt_set_lights", "snk_pt_build", "snk_pt_render", "snk_pt_synchronize", "snk_pt_trace_rays",
+    "snk_pt_read_accumulator",
+]
+
+
+class SnkError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"snk_pt error {code}: {msg}")
+        self.code = code
+
+
+class Mesh(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("indices", C.c_void_p),
+                ("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32)]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_uint32), ("stream", C.c_void_p), ("reserved", C.c_uint64 * 4)]
+
+
+class ViewOutputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("radiance", "albedo", "normal", "position", "rma", "motion", "depth",
+                                          "mat_flags", "inst_id", "prim_id")] + \
+               [("memory", C.c_uint32), ("pad", C.c_uint32)]
+
+
+OUTPUT_NAMES = ("radiance", "albedo", "normal", "position", "rma", "motion", "depth", "mat_flags", "inst_id", "prim_id")
+OUTPUT_SHAPES = {"radiance": 4, "albedo": 4, "normal": 4, "position": 4, "rma": 4, "motion": 2, "depth": 1,
+                 "mat_flags": 1, "inst_id": 1, "prim_id": 1}
+OUTPUT_DTYPES = {"radiance": np.float32, "albedo": np.float32, "normal": np.float32, "position": np.float32,
+                 "rma": np.float32, "motion": np.float32, "depth": np.float32, "mat_flags": np.uint32,
+                 "inst_id": np.uint32, "prim_id": np.uint32}
+
+_lib = None
+
+
+def lib():
+    """Load libsnkpt.so (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, u32 = C.c_void_p, C.c_uint32
+        for name in EXPORTS:
+            getattr(L, name).restype = C.c_int
+        L.snk_pt_abi_version.argtypes = [C.POINTER(C.c_uint32)]
+        L.snk_pt_create.argtypes = [C.POINTER(Config), C.POINTER(vp)]
+        L.snk_pt_destroy.argtypes = [vp]
+        L.snk_pt_set_stream.argtypes = [vp, vp]
+        L.snk_pt_get_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.snk_pt_get_stats.argtypes = [vp, vp]
+        L.snk_pt_upload_meshes.argtypes = [vp, vp, u32]
+        L.snk_pt_set_instances.argtypes = [vp, vp, u32]
+        L.snk_pt_set_materials.argtypes = [vp, vp, u32]
+        L.snk_pt_set_lights.argtypes = [vp, vp, vp, u32]
+        L.snk_pt_build.argtypes = [vp]
+        L.snk_pt_render.argtypes = [vp, vp, u32, vp, vp]
+        L.snk_pt_synchronize.argtypes = [vp]
+        L.snk_pt_trace_rays.argtypes = [vp, vp, u32, vp, u32, u32]
+        L.snk_pt_read_accumulator.argtypes = [vp, vp, u32, C.POINTER(C.c_uint64)]
+        _lib = L
+    return _lib
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def _is_device(a) -> bool:
+    return hasattr(a, "is_cuda") and a.is_cuda
+
+
+class PathTracer:
+    """One library context (``snk_pt_ctx``): scene, acceleration structures, frame state."""
+
+    def __init__(self, device: int = 0, stream=None):
+        L = lib()
+        cfg = Config()
+        cfg.device = device
+        cfg.stream = None if stream is None else int(getattr(stream, "cuda_stream", stream))
+        h = C.c_void_p()
+        rc = L.snk_pt_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise SnkError(rc, "snk_pt_create failed (no usable CUDA device?)")
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().snk_pt_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            buf = C.create_string_buffer(1024)
+            lib().snk_pt_get_last_error(self._h, buf, 1024)
+            raise SnkError(rc, buf.value.decode(errors="replace"))
+
+    # ---- scene ---------------------------------------------------------------
+    def set_stream(self, stream):
+        self._check(lib().snk_pt_set_stream(self._h, None if stream is None else int(getattr(stream, "cuda_stream", stream))))
+
+    def upload_meshes(self, meshes):
+        arr = (Mesh * max(1, len(meshes)))()
+        keep = []
+        for i, m in enumerate(meshes):
+            p = np.ascontiguousarray(m.positions, np.float32)
+            n = None if m.normals is None else np.ascontiguousarray(m.normals, np.float32)
+            ix = np.ascontiguousarray(m.indices, np.uint32)
+            keep += [p, n, ix]
+            arr[i] = Mesh(p.ctypes.data, None if n is None else n.ctypes.data, ix.ctypes.data, p.shape[0], ix.shape[0])
+        self._check(lib().snk_pt_upload_meshes(self._h, arr, len(meshes)))
+
+    def set_instances(self, instances: np.ndarray):
+        a = np.ascontiguousarray(instances, abi.INSTANCE_DTYPE)
+        self._check(lib().snk_pt_set_instances(self._h, a.ctypes.data, len(a)))
+
+    def set_materials(self, materials: np.ndarray):
+        a = np.ascontiguousarray(materials, abi.MATERIAL_DTYPE)
+        self._check(lib().snk_pt_set_materials(self._h, a.ctypes.data, len(a)))
+
+    def set_lights(self, dir_light, point_lights):
+        dl = np.ascontiguousarray(np.asarray(dir_light, abi.DIR_LIGHT_DTYPE).reshape(1))
+        pl = np.ascontiguousarray(point_lights, abi.POINT_LIGHT_DTYPE)
+        self._check(lib().snk_pt_set_lights(self._h, dl.ctypes.data, pl.ctypes.data if len(pl) else None, len(pl)))
+
+    def build(self):
+        self._check(lib().snk_pt_build(self._h))
+
+    def load_scene(self, scene):
+        self.upload_meshes(scene.meshes)
+        self.set_materials(scene.materials)
+        self.set_lights(scene.dir_light, scene.point_lights)
+        self.set_instances(scene.instances)
+        self.build()
+
+    # ---- frames ----------------------------------------------------------------
+    def render(self, views, settings, outputs):
+        """views: list of abi.VIEW_DTYPE; outputs: list (one per view) of dicts name -> buffer.
+        Buffers are either all torch CUDA tensors (device outputs) or all numpy arrays (host)."""
+        v = np.ascontiguousarray(np.array([np.asarray(x, abi.VIEW_DTYPE) for x in views], abi.VIEW_DTYPE))
+        st = np.ascontiguousarray(np.asarray(settings, abi.SETTINGS_DTYPE).reshape(1))
+        outs = (ViewOutputs * len(views))()
+        if any(_is_device(b) for o in outputs for b in o.values() if b is not None):
+            import torch
+            torch.cuda.current_stream().synchronize()   # buffers were filled on torch's stream
+        for i, o in enumerate(outputs):
+            dev = any(_is_device(b) for b in o.values() if b is not None)
+            for k in OUTPUT_NAMES:
+                b = o.get(k)
+                setattr(outs[i], k, None if b is None else _ptr(b))
+            outs[i].memory = abi.MEM_DEVICE if dev else abi.MEM_HOST
+        self._check(lib().snk_pt_render(self._h, v.ctypes.data, len(views), st.ctypes.data, outs))
+
+    def synchronize(self):
+        self._check(lib().snk_pt_synchronize(self._h))
+
+    def trace_rays(self, rays, any_hit: bool = False):
+        """rays: numpy abi.RAY_DTYPE array (host) or a torch CUDA tensor of shape (n, 8) float32."""
+        flags = abi.TRACE_ANY_HIT if any_hit else 0
+        if _is_device(rays):
+            import torch
+            n = rays.shape[0]
+            hits = torch.empty((n, 6), dtype=torch.int32, device=rays.device)
+            torch.cuda.synchronize(rays.device)
+            self._check(lib().snk_pt_trace_rays(self._h, rays.data_ptr(), n, hits.data_ptr(), flags, abi.MEM_DEVICE))
+            return hits
+        r = np.ascontiguousarray(rays, abi.RAY_DTYPE)
+        hits = np.zeros(len(r), abi.HIT_DTYPE)
+        self._check(lib().snk_pt_trace_rays(self._h, r.ctypes.data, len(r), hits.ctypes.data, flags, abi.MEM_HOST))
+        return hits
+
+    def stats(self) -> dict:
+        s = np.zeros(1, abi.STATS_DTYPE)
+        self._check(lib().snk_pt_get_stats(self._h, s.ctypes.data))
+        d = {k: s[k][0].item() for k in abi.STATS_DTYPE.names if k not in ("pad", "stage_ms", "stage_launches")}
+        d["stage_ms"] = dict(zip(abi.STAGES, s["stage_ms"][0].tolist()))
+        d["stage_launches"] = dict(zip(abi.STAGES, s["stage_launches"][0].tolist()))
+        return d
+
+    def read_accumulator(self, width: int, height: int):
+        out = np.zeros((height * width, 4), np.float32)
+        nf = C.c_uint64()
+        self._check(lib().snk_pt_read_accumulator(self._h, out.ctypes.data, abi.MEM_HOST, C.byref(nf)))
+        return out, nf.value
+
+
+def alloc_outputs(width: int, height: int, device=None, names=OUTPUT_NAMES) -> dict:
+    """Output buffers of one view: torch CUDA tensors when ``device`` is given, else numpy."""
+    n = width * height
+    out = {}
+    for k in names:
+        c = OUTPUT_SHAPES[k]
+        shape = (n, c) if c > 1 else (n,)
+        if device is not None:
+            import torch
+            dt = torch.float32 if OUTPUT_DTYPES[k] == np.float32 else torch.int32
+            out[k] = torch.zeros(shape, dtype=dt, device=device)
+        else:
+            out[k] = np.zeros(shape, OUTPUT_DTYPES[k])
+    return out
+
+
+class RT:
+    """Mirror of the reference's ``SNAKE::RT`` (Core/headers/rendering/Raytracing.h:11-31).
+
+    ``init(scene)`` corresponds to ``RT::Init`` (descriptor table + pipeline;
+    here: upload + BVH builds), ``record_render(views, outputs, settings)`` to
+    ``RT::RecordRenderCmdBuf`` (the two-pass ReSTIR dispatch, or the wavefront
+    path tracer), and :class:`RT.RtSettings` to ``RT::RtSettings`` (defaults
+    temporal 1, spatial 3, ``Raytracing.h:13-16``).
+    """
+
+    class RtSettings:
+        def __init__(self, num_temporal_resamples: int = 1, num_spatial_resamples: int = 3):
+            self.num_temporal_resamples = num_temporal_resamples
+            self.num_spatial_resamples = num_spatial_resamples
+
+    def __init__(self, device: int = 0, stream=None):
+        self.tracer = PathTracer(device, stream)
+        self.frame_index = 0
+
+    def init(self, scene):
+        if scene is None or not len(scene.meshes):
+            raise SnkError(abi.MODE_PATH + 4, "RT::Init: scene has no meshes")
+        self.tracer.load_scene(scene)
+
+    def record_render(self, views, outputs, settings: "RT.RtSettings | None" = None, mode=abi.MODE_RESTIR_DI,
+                      **overrides):
+        s = settings or RT.RtSettings()
+        st = abi.settings(mode=mode, frame_index=self.frame_index, restir_temporal=s.num_temporal_resamples,
+                          restir_spatial=s.num_spatial_resamples, **overrides)
+        self.tracer.render(views, st, outputs)
+        self.frame_index += 1

@@ -1,0 +1,143 @@
+"""GPU frame parity: the wavefront path tracer and ReSTIR DI against the CPU
+oracle.  Tolerance: per-pixel radiance within 1e-4 relative (the arithmetic is
+specified to the operation, so in practice the values are identical); hit ids,
+hit distances and the G-buffer must be identical."""
+import numpy as np
+import pytest
+
+import oracle as O
+import snkpt
+from helpers import max_rel
+from snkpt import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4
+GBUF = ("albedo", "normal", "position", "rma", "motion", "depth", "mat_flags", "inst_id", "prim_id")
+
+
+def _gpu_frame(pt, views, st, device):
+    outs = [snkpt.alloc_outputs(int(v["width"]), int(v["height"]), device=device) for v in views]
+    pt.render(views, st, outs)
+    pt.synchronize()
+    res = []
+    for o in outs:
+        d = {}
+        for k, t in o.items():
+            a = t.cpu().numpy()
+            d[k] = a.view(np.uint32) if k in ("mat_flags", "inst_id", "prim_id") else a
+        res.append(d)
+    return res
+
+
+def _compare(g, r, what):
+    for k in GBUF:
+        assert np.array_equal(g[k], r[k]), f"{what}: G-buffer '{k}' differs at {int((g[k] != r[k]).sum())} entries"
+    m = max_rel(g["radiance"][:, :3], r["radiance"][:, :3])
+    assert m <= RTOL, f"{what}: radiance max relative error {m}"
+
+
+def test_path_config0_full(cuda, built_lib):
+    sc = scenes.config0()
+    st = abi.settings(spp=4, max_depth=4, rr_depth=3, seed=1)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    ctr = np.zeros(5, np.uint64)
+    r = O.OracleScene(sc).render_path(sc.views[0], st, counters=ctr)
+    _compare(g, r, "config 0")
+    s = pt.stats()
+    assert (s["rays_camera"], s["rays_extension"], s["rays_shadow"]) == tuple(int(x) for x in ctr[:3])
+    assert g["radiance"][:, :3].mean() > 0.0
+
+
+def test_path_config1_reduced_full_frame(cuda, built_lib):
+    sc = scenes.config1(width=480, height=270)
+    st = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=1)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    ctr = np.zeros(5, np.uint64)
+    r = O.OracleScene(sc).render_path(sc.views[0], st, counters=ctr)
+    _compare(g, r, "config 1 (480x270)")
+    s = pt.stats()
+    assert (s["rays_camera"], s["rays_extension"], s["rays_shadow"]) == tuple(int(x) for x in ctr[:3])
+
+
+def test_path_config1_1080p_sampled_pixels_and_determinism(cuda, built_lib):
+    sc = scenes.config1()
+    st = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=1)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    a = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    b = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    for k in a:
+        assert np.array_equal(a[k], b[k]), f"run-to-run difference in {k}"
+    rng = np.random.default_rng(42)
+    px = np.sort(rng.choice(1920 * 1080, 20000, replace=False)).astype(np.uint32)
+    r = O.OracleScene(sc).render_path(sc.views[0], st, pixels=px)
+    sub = {k: v[px] for k, v in a.items()}
+    _compare(sub, r, "config 1 1080p (20k sampled pixels)")
+
+
+def test_path_multi_view_batch(cuda, built_lib):
+    res = [(160, 90), (96, 54), (200, 120)]
+    sc = scenes.config3(resolutions=res)
+    st = abi.settings(spp=1, max_depth=6, rr_depth=3, seed=3)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    gs = _gpu_frame(pt, sc.views, st, cuda)
+    osc = O.OracleScene(sc)
+    base = 0
+    for v, g in zip(sc.views, gs):
+        r = osc.render_path(v, st, pixel_base=base)
+        _compare(g, r, f"multi-view {int(v['width'])}x{int(v['height'])}")
+        base += int(v["width"]) * int(v["height"])
+
+
+def test_host_outputs_match_device_outputs(cuda, built_lib):
+    sc = scenes.config0(width=128, height=128)
+    st = abi.settings(spp=2, max_depth=4)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    host = snkpt.alloc_outputs(128, 128)
+    pt.render([sc.views[0]], st, [host])
+    for k in g:
+        h = host[k].view(np.uint32) if k in ("mat_flags", "inst_id", "prim_id") else host[k]
+        assert np.array_equal(g[k], h), k
+
+
+def test_fp64_accumulator(cuda, built_lib):
+    sc = scenes.config0(width=64, height=64)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    frames = []
+    for f in range(4):
+        flags = abi.RENDER_ACCUMULATE_F64 | (abi.RENDER_RESET_ACCUM if f == 0 else 0)
+        st = abi.settings(spp=1, max_depth=4, seed=10 + f, flags=flags)
+        host = snkpt.alloc_outputs(64, 64, names=("radiance",))
+        pt.render([sc.views[0]], st, [host])
+        frames.append(host["radiance"].astype(np.float64))
+    acc, n = pt.read_accumulator(64, 64)
+    assert n == 4
+    mean = np.mean(frames, 0)
+    assert np.allclose(acc[:, :3], mean[:, :3], rtol=1e-6, atol=1e-7)
+
+
+def test_restir_config2_frames(cuda, built_lib):
+    W, H, F = 192, 108, 4
+    sc = scenes.config2(width=W, height=H, frames=F)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    osc = O.OracleScene(sc)
+    ors = O.OracleRestir(osc, W, H)
+    for f in range(F):
+        st = abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=f, seed=1)
+        g = _gpu_frame(pt, [sc.views[f]], st, cuda)[0]
+        ctr = np.zeros(5, np.uint64)
+        r, _ = ors.frame(sc.views[f], st, counters=ctr)
+        _compare(g, r, f"ReSTIR frame {f}")
+        s = pt.stats()
+        assert s["rays_shadow"] == int(ctr[2]), f"frame {f}: shadow ray count {s['rays_shadow']} vs {int(ctr[2])}"
+        assert g["radiance"][:, :3].mean() > 0.0

@@ -1,0 +1,117 @@
+"""GPU per-ray parity: closest hit (t, instance, triangle, barycentrics) and any
+hit of the CUDA traversal must equal the CPU oracle bit for bit."""
+import numpy as np
+import pytest
+
+import oracle as O
+import snkpt
+from helpers import assert_hits_equal, camera_rays, random_rays, shadow_rays
+from snkpt import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scenes_loaded(cuda, built_lib):
+    out = {}
+    for cfg, kw in [(0, {}), (1, {"width": 1920, "height": 1080}), (2, {"width": 640, "height": 360, "frames": 1}),
+                    (3, {"resolutions": [(1280, 720)]})]:
+        sc = scenes.make(cfg, **kw)
+        pt = snkpt.PathTracer(0)
+        pt.load_scene(sc)
+        out[cfg] = (sc, pt, O.OracleScene(sc))
+    return out
+
+
+@pytest.mark.parametrize("cfg,n_rand", [(0, 600_000), (1, 600_000), (2, 200_000), (3, 200_000)])
+def test_closest_hit_bit_exact(scenes_loaded, cfg, n_rand):
+    sc, pt, osc = scenes_loaded[cfg]
+    rng = np.random.default_rng(100 + cfg)
+    v = sc.views[0]
+    npix = int(v["width"]) * int(v["height"])
+    cam = camera_rays(v) if npix <= 1 << 20 else camera_rays(v, 400_000, rng)
+    rays = np.concatenate([cam, random_rays(sc, n_rand, rng)])
+    gpu = pt.trace_rays(rays)
+    ref = osc.trace(rays)
+    assert_hits_equal(gpu, ref, f"config {cfg} closest")
+    assert (ref["flags"] == 1).mean() > 0.3   # the ray sets actually hit geometry
+
+
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3])
+def test_any_hit_bit_exact(scenes_loaded, cfg):
+    sc, pt, osc = scenes_loaded[cfg]
+    rng = np.random.default_rng(200 + cfg)
+    rays = shadow_rays(sc, 300_000, rng)
+    gpu = pt.trace_rays(rays, any_hit=True)
+    ref = osc.trace(rays, any_hit=True)
+    assert np.array_equal(gpu["flags"], ref["flags"]), f"{int((gpu['flags'] != ref['flags']).sum())} differ"
+    occluded = ref["flags"].mean()
+    assert 0.02 < occluded < 0.98
+
+
+def test_device_buffers_match_host_buffers(scenes_loaded, cuda):
+    import torch
+    sc, pt, _ = scenes_loaded[1]
+    rng = np.random.default_rng(7)
+    rays = random_rays(sc, 100_000, rng)
+    host = pt.trace_rays(rays)
+    t = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(cuda)
+    dev = pt.trace_rays(t).cpu().numpy().view(abi.HIT_DTYPE).reshape(-1)
+    assert_hits_equal(dev, host, "device vs host buffers")
+
+
+def test_watertight_floor_grid(scenes_loaded):
+    sc, pt, _ = scenes_loaded[0]
+    xs = np.arange(0, 33) * (10.0 / 32) - 5.0
+    hx = (xs[:-1] + xs[1:]) / 2
+    pts = [(x, z) for x in xs[1:-1] for z in xs[1:-1]] + [(x, z) for x in hx for z in xs[1:-1]] + \
+          [(x, z) for x in xs[1:-1] for z in hx]
+    rays = np.zeros(len(pts), abi.RAY_DTYPE)
+    rays["o"] = [(x, 0.5, z) for x, z in pts]
+    rays["d"] = (0, -1, 0)
+    rays["tmax"] = 1e4
+    h = pt.trace_rays(rays)
+    assert (h["inst"] == 0).all() and (h["t"] == 0.5).all()
+
+
+def test_degenerate_rays(scenes_loaded):
+    sc, pt, osc = scenes_loaded[1]
+    rng = np.random.default_rng(9)
+    r = random_rays(sc, 4096, rng)
+    # axis-aligned directions (zero components), empty intervals, tiny tmax
+    r["d"][:1024] = np.eye(3)[rng.integers(0, 3, 1024)] * rng.choice([-1.0, 1.0], (1024, 1))
+    r["tmin"][1024:2048] = 5.0
+    r["tmax"][1024:2048] = 5.0
+    r["tmax"][2048:3072] = 1e-6
+    assert_hits_equal(pt.trace_rays(r), osc.trace(r), "degenerate rays")
+    assert (pt.trace_rays(r)["flags"][1024:2048] == 0).all()
+
+
+def test_empty_scene(cuda, built_lib):
+    pt = snkpt.PathTracer(0)
+    pt.upload_meshes([scenes.Mesh(np.zeros((0, 3), np.float32), None, np.zeros((0, 3), np.uint32))])
+    pt.set_materials(scenes.make_materials([((0.5, 0.5, 0.5), 0.5, 0.0, 0)]))
+    pt.set_lights(scenes.no_dir_light(), scenes.point_lights([]))
+    pt.set_instances(scenes.make_instances([(scenes.affine(), 0, 0)]))
+    pt.build()
+    rays = random_rays(scenes.config0(width=8, height=8), 1000, np.random.default_rng(1))
+    h = pt.trace_rays(rays)
+    assert (h["flags"] == 0).all() and (h["inst"] == abi.INVALID_INDEX).all()
+
+
+def test_invalid_scene_is_rejected(cuda, built_lib):
+    sc = scenes.config0(width=8, height=8)
+    pt = snkpt.PathTracer(0)
+    pt.upload_meshes(sc.meshes)
+    pt.set_materials(sc.materials)
+    pt.set_lights(sc.dir_light, sc.point_lights)
+    bad = sc.instances.copy()
+    bad[0]["mesh_id"] = 99
+    pt.set_instances(bad)
+    with pytest.raises(snkpt.SnkError) as e:
+        pt.build()
+    assert e.value.code == 1
+    bad = sc.instances.copy()
+    bad[0]["transform"][0] = np.nan
+    with pytest.raises(snkpt.SnkError):
+        pt.set_instances(bad)

@@ -1,0 +1,218 @@
+"""CPU tests of the oracle: pinned against published vectors, the golden float64
+transcription of the reference GLSL, closed-form intersection answers and a
+brute-force closest-hit search."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import assert_hits_equal, camera_rays, random_rays, shadow_rays
+from snkpt import abi, scenes
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_pcg32_published_vector():
+    # pcg32-demo (pcg-c-basic): pcg32_srandom_r(&rng, 42u, 54u), first six outputs
+    expect = [0xA15C02B7, 0x7B47F409, 0xBA1D3330, 0x83D2F293, 0xBFA4784B, 0xCBED606E]
+    assert O.pcg32(42, 54, 6).tolist() == expect
+
+
+def test_pcg_stream_properties():
+    a = O.pcg_stream(7, 0, 0, 1, 4096)
+    b = O.pcg_stream(7, 0, 0, 1, 4096)
+    c = O.pcg_stream(8, 0, 0, 1, 4096)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+    assert a.min() >= 0.0 and a.max() < 1.0
+    assert abs(a.mean() - 0.5) < 0.02
+
+
+def test_sincos2pi_accuracy():
+    u = np.concatenate([np.linspace(0, 1, 100001, endpoint=False), np.float32([0.25, 0.5, 0.75, 0.9999999])])
+    u = u.astype(np.float32)
+    s, c = O.sincos2pi(u)
+    ref = 2 * np.pi * u.astype(np.float64)
+    assert np.abs(s - np.sin(ref)).max() < 4e-7
+    assert np.abs(c - np.cos(ref)).max() < 4e-7
+    assert s[0] == 0.0 and c[0] == 1.0
+
+
+def _rel(a, b, floor):
+    return np.abs(np.asarray(a, np.float64) - b) / np.maximum(np.abs(b), floor)
+
+
+# binary32 vs the float64 transcription: near the GGX peak at low roughness the
+# NDF denominator n.h^2 (a^2 - 1) + 1 cancels, which costs ~1e-4 relative.
+BRDF_RTOL = 3e-4
+
+
+def test_brdf_matches_golden_glsl_transcription():
+    g = np.load(os.path.join(GOLDEN, "brdf.npz"))
+    out = O.brdf(g["brdf_in"])
+    ref = g["brdf_out"]
+    assert _rel(out, ref, 1e-3).max() < BRDF_RTOL
+    assert np.median(_rel(out, ref, 1e-3)) < 1e-6
+
+
+def test_directional_light_matches_golden():
+    g = np.load(os.path.join(GOLDEN, "brdf.npz"))
+    out = O.directional(g["dir_in"])
+    assert _rel(out, g["dir_out"], 1e-3).max() < BRDF_RTOL
+
+
+def test_pointlight_matches_golden():
+    g = np.load(os.path.join(GOLDEN, "brdf.npz"))
+    out = O.pointlight(g["pl_in"])
+    assert _rel(out, g["pl_out"], 1e-4).max() < BRDF_RTOL
+
+
+def _tri_rows(o, d, v0, v1, v2, tmin=0.0, tmax=1e4):
+    return np.array([list(o) + list(d) + list(v0) + list(v1) + list(v2) + [tmin, tmax]], np.float32)
+
+
+def test_watertight_known_answers():
+    v0, v1, v2 = (0, 0, 0), (1, 0, 0), (0, 0, 1)
+    r = O.tri(_tri_rows((0.25, 1, 0.25), (0, -1, 0), v0, v1, v2))[0]
+    assert r.tolist() == [1.0, 1.0, 0.25, 0.25]
+    # behind the origin, outside, parallel, beyond tmax, before tmin
+    assert O.tri(_tri_rows((0.25, -1, 0.25), (0, -1, 0), v0, v1, v2))[0][0] == 0.0
+    assert O.tri(_tri_rows((0.75, 1, 0.75), (0, -1, 0), v0, v1, v2))[0][0] == 0.0
+    assert O.tri(_tri_rows((0.25, 0, 0.25), (1, 0, 0), v0, v1, v2))[0][0] == 0.0
+    assert O.tri(_tri_rows((0.25, 1, 0.25), (0, -1, 0), v0, v1, v2, 0.0, 0.5))[0][0] == 0.0
+    assert O.tri(_tri_rows((0.25, 1, 0.25), (0, -1, 0), v0, v1, v2, 1.5, 2.0))[0][0] == 0.0
+    # exactly on the shared edge of two triangles of a quad: at least one reports the hit
+    q = [(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)]
+    for p in [(0.5, 1, 0.5), (0.25, 1, 0.25), (1, 1, 1), (0, 1, 0)]:
+        a = O.tri(_tri_rows(p, (0, -1, 0), q[0], q[2], q[1]))[0][0]
+        b = O.tri(_tri_rows(p, (0, -1, 0), q[0], q[3], q[2]))[0][0]
+        assert a + b >= 1.0, p
+
+
+def test_invert_affine():
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        M = scenes.affine(scenes.random_rotation(rng), rng.uniform(0.5, 4, 3), rng.uniform(-50, 50, 3))
+        inv, nm, det = O.invert_affine(M)
+        A = np.vstack([M.astype(np.float64), [0, 0, 0, 1]])
+        B = np.vstack([inv.reshape(3, 4).astype(np.float64), [0, 0, 0, 1]])
+        assert np.abs(A @ B - np.eye(4)).max() < 1e-5
+        assert np.allclose(nm.reshape(3, 3), np.linalg.inv(A[:3, :3]).T, atol=1e-6)
+        assert abs(det - np.linalg.det(A[:3, :3])) < 1e-3 * abs(det)
+
+
+def _brute_closest(scene, rays):
+    """Closest hit by testing every triangle of every instance (oracle's own
+    intersection routine on the object-space ray, no BVH)."""
+    hits = np.zeros(len(rays), abi.HIT_DTYPE)
+    hits["t"] = -1.0
+    hits["inst"] = abi.INVALID_INDEX
+    hits["prim"] = abi.INVALID_INDEX
+    best_t = np.full(len(rays), np.inf)
+    for ii, inst in enumerate(scene.instances):
+        m = scene.meshes[int(inst["mesh_id"])]
+        inv, _, _ = O.invert_affine(inst["transform"])
+        inv = inv.reshape(3, 4)
+        # object-space rays in float32, same order as the oracle
+        o = rays["o"].astype(np.float32)
+        d = rays["d"].astype(np.float32)
+        oo = ((inv[:, 0] * o[:, :1] + inv[:, 1] * o[:, 1:2]) + inv[:, 2] * o[:, 2:3]) + inv[:, 3]
+        od = (inv[:, 0] * d[:, :1] + inv[:, 1] * d[:, 1:2]) + inv[:, 2] * d[:, 2:3]
+        tri = m.positions[m.indices]  # (T,3,3)
+        for r in range(len(rays)):
+            rows = np.concatenate([np.tile(np.concatenate([oo[r], od[r]]), (len(tri), 1)), tri.reshape(-1, 9),
+                                   np.tile([rays["tmin"][r], rays["tmax"][r]], (len(tri), 1))], 1).astype(np.float32)
+            res = O.tri(rows)
+            for p in np.flatnonzero(res[:, 0] > 0):
+                t = res[p, 1]
+                key = (t, ii, p)
+                if t < best_t[r] or (t == best_t[r] and (ii, p) < (int(hits["inst"][r]), int(hits["prim"][r]))):
+                    best_t[r] = t
+                    hits[r] = (t, ii, p, res[p, 2], res[p, 3], 1)
+                del key
+    return hits
+
+
+def test_oracle_bvh_matches_brute_force():
+    sc = scenes.config0(width=32, height=32)
+    osc = O.OracleScene(sc)
+    rng = np.random.default_rng(11)
+    rays = np.concatenate([camera_rays(sc.views[0], 40, rng), random_rays(sc, 40, rng)])
+    assert_hits_equal(osc.trace(rays), _brute_closest(sc, rays), "oracle BVH vs brute force")
+
+
+def test_oracle_any_hit_consistent_with_closest():
+    sc = scenes.config1(width=64, height=36)
+    osc = O.OracleScene(sc)
+    rng = np.random.default_rng(5)
+    rays = shadow_rays(sc, 20000, rng)
+    closest = osc.trace(rays)
+    anyh = osc.trace(rays, any_hit=True)
+    assert np.array_equal(closest["flags"], anyh["flags"])
+
+
+def test_oracle_watertight_floor_grid():
+    sc = scenes.config0(width=16, height=16)
+    osc = O.OracleScene(sc)
+    xs = np.arange(0, 33) * (10.0 / 32) - 5.0
+    hx = (xs[:-1] + xs[1:]) / 2
+    pts = [(x, z) for x in xs[1:-1] for z in xs[1:-1]] + [(x, z) for x in hx for z in xs[1:-1]] + \
+          [(x, z) for x in xs[1:-1] for z in hx]
+    rays = np.zeros(len(pts), abi.RAY_DTYPE)
+    rays["o"] = [(x, 0.5, z) for x, z in pts]
+    rays["d"] = (0, -1, 0)
+    rays["tmax"] = 1e4
+    h = osc.trace(rays)
+    assert (h["inst"] == 0).all() and (h["t"] == 0.5).all()
+
+
+def test_oracle_render_thread_independent():
+    sc = scenes.config0(width=48, height=48)
+    osc = O.OracleScene(sc)
+    st = abi.settings(spp=2, max_depth=4, rr_depth=3)
+    a = osc.render_path(sc.views[0], st, nthreads=1)
+    b = osc.render_path(sc.views[0], st, nthreads=8)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert np.isfinite(a["radiance"]).all() and (a["radiance"][:, :3] >= 0).all()
+    # pixel subsets render the same values as the full frame
+    px = np.array([0, 17, 48 * 20 + 7, 48 * 48 - 1], np.uint32)
+    c = osc.render_path(sc.views[0], st, pixels=px)
+    assert np.array_equal(c["radiance"], a["radiance"][px])
+
+
+def test_oracle_restir_frames():
+    sc = scenes.config2(width=48, height=27, frames=3)
+    osc = O.OracleScene(sc)
+    rs = O.OracleRestir(osc, 48, 27)
+    ms = []
+    for f in range(3):
+        out, res = rs.frame(sc.views[f], abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=f))
+        assert np.isfinite(out["radiance"]).all()
+        assert (out["radiance"][:, :3] >= 0).all()
+        ms.append(int(res["m_em"].max()))
+    # temporal reuse accumulates history (M grows past one frame's candidates)
+    assert ms[0] >= 32 and ms[2] > ms[0]
+
+
+def test_scene_configs():
+    c0 = scenes.config0()
+    assert c0.num_instanced_triangles == 2048 + 10 + 60 + 2
+    c1 = scenes.config1(width=64, height=36)
+    assert c1.meshes[0].num_triangles == 1280 and c1.meshes[1].num_triangles == 131072
+    assert len(c1.instances) == 201 and len(c1.point_lights) == 16
+    c2 = scenes.config2(width=64, height=36, frames=2)
+    assert int((c2.materials["flags"] & abi.MAT_EMISSIVE).sum()) == 4096
+    c3 = scenes.config3(resolutions=[(64, 36)])
+    assert c3.meshes[1].num_triangles == 131072 and len(c3.instances) == 264
+    assert sum(w * h for w, h in scenes.CONFIG3_RESOLUTIONS) == 19_238_400
+
+
+@pytest.mark.parametrize("cfg", [0, 1])
+def test_oracle_deterministic_hits(cfg):
+    sc = scenes.make(cfg, width=32, height=18)
+    osc = O.OracleScene(sc)
+    rng = np.random.default_rng(cfg)
+    rays = random_rays(sc, 5000, rng)
+    assert_hits_equal(osc.trace(rays, nthreads=1), osc.trace(rays, nthreads=8), "thread count")
