@@ -291,6 +291,22 @@ int snk_pt_synchronize(snk_pt_ctx* ctx);
 int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit* hits,
                       uint32_t flags, uint32_t memory);
 
+/* No counterpart in the reference.  Plain path tracing (SNK_MODE_PATH) of one
+ * view with no device allocation, for callers that must not allocate while they
+ * render: an engine whose frame loop owns every device byte through its own
+ * allocator, or code where the device-wide synchronisation that cudaMalloc and
+ * cudaFree can cause would stall other work.  The scene must already be built
+ * (building allocates).  All wavefront scratch lives in one fixed array of
+ * 14,684,160 bytes that every GPU loading the library keeps until exit, so
+ * width * height * spp may not exceed SNK_NOALLOC_MAX_PATHS (larger views are
+ * rejected with SNK_ERR_INVALID_ARG).  Outputs must be device memory; the
+ * accumulate, profile and graph flags are rejected.  The first call on a device
+ * looks up the array's device address, so make it before any stream capture.
+ * Calls share the array: calls whose GPU work overlaps race. */
+#define SNK_NOALLOC_MAX_PATHS 65536u
+int snk_pt_render_noalloc(snk_pt_ctx* ctx, const snk_view* view, const snk_render_settings* settings,
+                          const snk_view_outputs* outputs);
+
 /* FP64 converged-image accumulator of view 0: copies the running mean (samples
  * accumulated so far) as float4 into out (memory space as given). */
 int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames);

@@ -902,3 +902,39 @@ int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64
 }
 
 }  // extern "C"
+
+// ---- read-only access to a context for entry points in other translation units
+namespace snk {
+
+bool ctx_view(snk_pt_ctx* ctx, CtxView* out) {
+    if (!ctx || !out) return false;
+    out->device = ctx->device;
+    out->stream = ctx->stream;
+    out->num_sms = ctx->num_sms;
+    out->built = ctx->built && !ctx->meshes_dirty && !ctx->inst_dirty && !ctx->mats_dirty && !ctx->lights_dirty;
+    out->scene = scene_dev(ctx);
+    out->h_counters = ctx->h_counters;
+    out->h_trav = ctx->h_trav;
+    return true;
+}
+
+int ctx_fail(snk_pt_ctx* ctx, int code, const char* msg) { return fail(ctx, code, msg); }
+
+void ctx_note_render(snk_pt_ctx* ctx, uint32_t mode, uint32_t depth, uint64_t paths, uint64_t pixels, bool counted) {
+    ctx->counters_pending = true;
+    ctx->timing_pending = false;
+    ctx->prof_pending = false;
+    ctx->last_mode = mode;
+    ctx->last_depth = depth;
+    ctx->last_paths = paths;
+    ctx->last_pixels = pixels;
+    ctx->last_count_nodes = counted ? 1u : 0u;
+    for (int k = 0; k < SNK_NUM_STAGES; k++) { ctx->stage_launches[k] = 0; ctx->stage_ms[k] = 0.0; }
+    ctx->stage_launches[SNK_STAGE_GENERATE] = 1;
+    ctx->stage_launches[SNK_STAGE_TRACE_CLOSEST] = depth;
+    ctx->stage_launches[SNK_STAGE_SHADE] = depth;
+    ctx->stage_launches[SNK_STAGE_TRACE_SHADOW] = depth;
+    ctx->stage_launches[SNK_STAGE_RESOLVE] = 1;
+}
+
+}  // namespace snk

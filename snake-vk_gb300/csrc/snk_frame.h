@@ -72,4 +72,23 @@ struct RestirSettings {
 cudaError_t launch_restir_stage(int stage, const FrameParams& F, uint32_t view_index, const RestirView& R,
                                 const RestirSettings& rs, int grid, cudaStream_t s);
 
+// Read-only view of a context (defined in api.cu) for entry points that live in
+// other translation units.
+struct CtxView {
+    int device;
+    cudaStream_t stream;
+    int num_sms;
+    bool built;                 // scene uploaded and built, nothing pending
+    SceneDev scene;
+    uint32_t* h_counters;       // pinned host copy of the frame counters (CNT_TOTAL)
+    unsigned long long* h_trav; // pinned host copy of the traversal counters (4)
+};
+
+}  // namespace snk
+
+struct snk_pt_ctx;
+namespace snk {
+bool ctx_view(snk_pt_ctx* ctx, CtxView* out);
+int ctx_fail(snk_pt_ctx* ctx, int code, const char* msg);
+void ctx_note_render(snk_pt_ctx* ctx, uint32_t mode, uint32_t depth, uint64_t paths, uint64_t pixels, bool counted);
 }  // namespace snk

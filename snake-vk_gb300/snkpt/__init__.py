@@ -24,7 +24,7 @@ EXPORTS = [
     "snk_pt_abi_version", "snk_pt_create", "snk_pt_destroy", "snk_pt_set_stream", "snk_pt_get_last_error",
     "snk_pt_get_stats", "snk_pt_upload_meshes", "snk_pt_set_instances", "snk_pt_set_materials",
     "snk_pt_set_lights", "snk_pt_build", "snk_pt_render", "snk_pt_synchronize", "snk_pt_trace_rays",
-    "snk_pt_read_accumulator",
+    "snk_pt_read_accumulator", "snk_pt_render_noalloc",
 ]
 
 
@@ -56,6 +56,8 @@ OUTPUT_DTYPES = {"radiance": np.float32, "albedo": np.float32, "normal": np.floa
                  "rma": np.float32, "motion": np.float32, "depth": np.float32, "mat_flags": np.uint32,
                  "inst_id": np.uint32, "prim_id": np.uint32}
 
+NOALLOC_MAX_PATHS = 65536   # SNK_NOALLOC_MAX_PATHS
+
 _lib = None
 
 
@@ -84,6 +86,7 @@ def lib():
         L.snk_pt_synchronize.argtypes = [vp]
         L.snk_pt_trace_rays.argtypes = [vp, vp, u32, vp, u32, u32]
         L.snk_pt_read_accumulator.argtypes = [vp, vp, u32, C.POINTER(C.c_uint64)]
+        L.snk_pt_render_noalloc.argtypes = [vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -187,6 +190,21 @@ class PathTracer:
                 setattr(outs[i], k, None if b is None else _ptr(b))
             outs[i].memory = abi.MEM_DEVICE if dev else abi.MEM_HOST
         self._check(lib().snk_pt_render(self._h, v.ctypes.data, len(views), st.ctypes.data, outs))
+
+    def render_noalloc(self, view, settings, outputs: dict):
+        """Path-traced render of one small view through snk_pt_render_noalloc: no
+        device allocation; outputs must be torch CUDA tensors; at most
+        NOALLOC_MAX_PATHS = width * height * spp paths."""
+        v = np.ascontiguousarray(np.asarray(view, abi.VIEW_DTYPE).reshape(1))
+        st = np.ascontiguousarray(np.asarray(settings, abi.SETTINGS_DTYPE).reshape(1))
+        o = ViewOutputs()
+        for k in OUTPUT_NAMES:
+            b = outputs.get(k)
+            setattr(o, k, None if b is None else _ptr(b))
+        o.memory = abi.MEM_DEVICE
+        import torch
+        torch.cuda.current_stream().synchronize()
+        self._check(lib().snk_pt_render_noalloc(self._h, v.ctypes.data, st.ctypes.data, C.byref(o)))
 
     def synchronize(self):
         self._check(lib().snk_pt_synchronize(self._h))

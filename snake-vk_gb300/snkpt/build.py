@@ -30,6 +30,7 @@ UNITS = {
     "trace_kernels.cu": False,
     "pt_kernels.cu": True,
     "restir.cu": True,
+    "noalloc.cu": False,
 }
 
 
