@@ -203,6 +203,10 @@ def run_ours(args):
     pt.load_scene(sc)
     outs = snkpt.alloc_outputs(W, H, device=dev)
     torch.cuda.synchronize()
+    tuning = pt.get_tuning()
+    if not args.no_autotune:
+        # untimed: the project's autotuner picks the launch knobs for this workload
+        tuning = pt.autotune([view], abi.settings(spp=1, max_depth=4, rr_depth=3, seed=7), frames_per_trial=3)
 
     def settings(seed, flags=abi.RENDER_PROFILE):
         return abi.settings(spp=1, max_depth=4, rr_depth=3, seed=seed, flags=flags)
@@ -305,7 +309,8 @@ def run_ours(args):
             "dtype": "f32", "data": "synthetic (seeded scene generator)",
             "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": 1, "max_depth": 4,
                        "rays_per_frame": rays / args.steps, "parallelism": f"replicas x{ws}",
-                       "l2": "flushed between steps (256 MiB memset on the same stream, untimed)"},
+                       "l2": "flushed between steps (256 MiB memset on the same stream, untimed)",
+                       "tuning": tuning},
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": e2e_s / args.steps * 1e3},
@@ -329,6 +334,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -248,6 +248,18 @@ typedef struct snk_pt_stats {
     uint64_t stage_launches[8];  /* kernel launches per stage of the last render */
 } snk_pt_stats;
 
+/* Launch knobs of the wavefront (0 = default).  The reference has no equivalent:
+ * its dispatch shape is fixed by traceRaysKHR(W, H, 1) (Raytracing.cpp:253,260). */
+typedef struct snk_tuning {
+    uint32_t trace_blocks_per_sm;   /* persistent traversal grid = SMs x this (16) */
+    uint32_t shade_blocks_per_sm;   /* generate / shade / resolve grid = SMs x this (8) */
+    uint32_t ray_chunk;             /* rays a warp takes per global work fetch (64) */
+    uint32_t refill_idle;           /* hand new rays to a warp when this many lanes idle (4) */
+    uint32_t prim_bias;             /* warp runs a primitive step if 4*n_prim >= bias*n_node (4) */
+    uint32_t trace_variant;         /* registers: 0 <= 85 (6 blocks/SM), 1 <= 64, 2 unconstrained */
+    uint32_t reserved[2];
+} snk_tuning;
+
 /* ---- lifetime ---------------------------------------------------------------- */
 int snk_pt_abi_version(uint32_t* version);
 /* RT::Init (Raytracing.cpp:269-278) */
@@ -280,6 +292,15 @@ int snk_pt_build(snk_pt_ctx* ctx);
  * work is enqueued (device outputs) or after host outputs are written. */
 int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views,
                   const snk_render_settings* settings, const snk_view_outputs* outputs);
+
+/* Launch knobs of this context (snk_tuning; zero fields mean the defaults). */
+int snk_pt_set_tuning(snk_pt_ctx* ctx, const snk_tuning* tuning);
+int snk_pt_get_tuning(const snk_pt_ctx* ctx, snk_tuning* tuning);
+/* Autotuner: times frames_per_trial renders of the given views/settings for each
+ * candidate knob value (coordinate descent, two passes), keeps the fastest
+ * setting in the context and returns it.  Outputs are not written. */
+int snk_pt_autotune(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, const snk_render_settings* settings,
+                    uint32_t frames_per_trial, snk_tuning* best);
 
 /* Waits for the context's stream and reports device-side errors (a traversal
  * bound that was hit) of the work issued so far.  The reference has no

@@ -107,6 +107,8 @@ struct snk_pt_ctx {
     bool prof_pending = false;
     double stage_ms[SNK_NUM_STAGES] = {0};
     uint64_t stage_launches[SNK_NUM_STAGES] = {0};
+
+    snk_tuning tune{};   // launch knobs (zero = defaults)
 };
 
 namespace {
@@ -441,6 +443,16 @@ void** out_slots(snk_view_outputs& o) { return reinterpret_cast<void**>(&o); }
 void** dev_slots(ViewDev& v) { return reinterpret_cast<void**>(&v.radiance); }
 
 int grid_of(snk_pt_ctx* ctx, int per_sm) { return ctx->num_sms * per_sm; }
+int trace_grid(snk_pt_ctx* ctx) { return grid_of(ctx, ctx->tune.trace_blocks_per_sm ? (int)ctx->tune.trace_blocks_per_sm : 16); }
+int shade_grid(snk_pt_ctx* ctx) { return grid_of(ctx, ctx->tune.shade_blocks_per_sm ? (int)ctx->tune.shade_blocks_per_sm : 8); }
+TraceTuning trace_tuning(snk_pt_ctx* ctx) {
+    TraceTuning t;
+    t.chunk = ctx->tune.ray_chunk;
+    t.refill_idle = ctx->tune.refill_idle;
+    t.prim_bias = ctx->tune.prim_bias;
+    t.variant = ctx->tune.trace_variant;
+    return t;
+}
 
 // Runs one kernel launch; with profiling on, brackets it with an event pair.
 template <class Fn>
@@ -664,6 +676,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     F.seed = rs.seed;
     F.n_paths = n_paths;
     F.n_pixels = (uint32_t)n_pixels;
+    F.tune = trace_tuning(ctx);
     const bool count_nodes = (rs.flags & SNK_RENDER_COUNT_NODES) != 0;
     const bool profile = (rs.flags & SNK_RENDER_PROFILE) != 0;
     if (ctx->prof_pending) cudaStreamSynchronize(st);   // events of the previous frame are reused
@@ -705,7 +718,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         F.hits = ctx->hits.p; F.beta = ctx->beta.p; F.L = ctx->L.p;
         F.shadow_rays = ctx->srays.p; F.shadow_contrib = ctx->scontrib.p;
         cudaEventRecord(ctx->ev0, st);
-        const int g8 = grid_of(ctx, 8), g16 = grid_of(ctx, 16);
+        const int g8 = shade_grid(ctx), g16 = trace_grid(ctx);
         cudaError_t e = staged(ctx, profile, SNK_STAGE_GENERATE, [&] { return launch_generate(F, g8, st); });
         for (uint32_t d = 0; d < rs.max_depth && e == cudaSuccess; d++) {
             e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
@@ -746,7 +759,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             cudaError_t e = cudaSuccess;
             for (int k = 0; k < 3 && e == cudaSuccess; k++)
                 e = staged(ctx, profile, SNK_STAGE_RESTIR_GBUFFER + k,
-                           [&] { return launch_restir_stage(k, F, v, RV, s, grid_of(ctx, 16), st); });
+                           [&] { return launch_restir_stage(k, F, v, RV, s, trace_grid(ctx), st); });
             if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("restir launch: ") + cudaGetErrorString(e));
             std::swap(R.hist, R.spat);
             R.history_valid = 1;
@@ -782,6 +795,91 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     return SNK_OK;
 }
 
+int snk_pt_set_tuning(snk_pt_ctx* ctx, const snk_tuning* t) {
+    if (!ctx || !t) return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: null argument");
+    if (t->trace_blocks_per_sm > 64 || t->shade_blocks_per_sm > 64 || t->ray_chunk > 4096 || t->refill_idle > 32 ||
+        t->prim_bias > 64 || t->trace_variant > 2)
+        return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: knob out of range");
+    ctx->tune = *t;
+    return SNK_OK;
+}
+
+int snk_pt_get_tuning(const snk_pt_ctx* ctx, snk_tuning* t) {
+    if (!ctx || !t) return SNK_ERR_INVALID_ARG;
+    *t = ctx->tune;
+    return SNK_OK;
+}
+
+int snk_pt_autotune(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, const snk_render_settings* settings,
+                    uint32_t frames, snk_tuning* best) {
+    if (!ctx || !views || !settings || num_views == 0) return fail(ctx, SNK_ERR_INVALID_ARG, "autotune: bad arguments");
+    if (settings->mode != SNK_MODE_PATH) return fail(ctx, SNK_ERR_UNSUPPORTED, "autotune: path mode only");
+    if (frames == 0) frames = 3;
+    std::vector<snk_view_outputs> outs(num_views);
+    std::memset(outs.data(), 0, outs.size() * sizeof(snk_view_outputs));
+    snk_render_settings rs = *settings;
+    rs.flags &= ~(SNK_RENDER_ACCUMULATE_F64 | SNK_RENDER_RESET_ACCUM | SNK_RENDER_COUNT_NODES | SNK_RENDER_PROFILE);
+    auto trial = [&](const snk_tuning& t, double* ms) -> int {
+        ctx->tune = t;
+        int rc = snk_pt_render(ctx, views, num_views, &rs, outs.data());   // warm-up
+        if (rc) return rc;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, ctx->stream);
+        for (uint32_t f = 0; f < frames && rc == 0; f++) {
+            rs.seed = settings->seed + 1 + f;
+            rc = snk_pt_render(ctx, views, num_views, &rs, outs.data());
+        }
+        cudaEventRecord(b, ctx->stream);
+        cudaEventSynchronize(b);
+        float m = 0.0f;
+        cudaEventElapsedTime(&m, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        *ms = m;
+        return rc;
+    };
+    snk_tuning cur = ctx->tune;
+    if (!cur.trace_blocks_per_sm) cur.trace_blocks_per_sm = 16;
+    if (!cur.shade_blocks_per_sm) cur.shade_blocks_per_sm = 8;
+    if (!cur.ray_chunk) cur.ray_chunk = 64;
+    if (!cur.refill_idle) cur.refill_idle = 4;
+    if (!cur.prim_bias) cur.prim_bias = 4;
+    double best_ms = 0.0;
+    int rc = trial(cur, &best_ms);
+    if (rc) return rc;
+    struct Knob { uint32_t* field; std::vector<uint32_t> values; };
+    for (int pass = 0; pass < 2; pass++) {
+        snk_tuning cand = cur;
+        Knob knobs[] = {
+            {&cand.trace_blocks_per_sm, {4, 8, 12, 16, 24, 32}},
+            {&cand.trace_variant, {0, 1, 2}},
+            {&cand.refill_idle, {1, 2, 4, 8, 16}},
+            {&cand.ray_chunk, {32, 64, 128, 256}},
+            {&cand.prim_bias, {2, 4, 8}},
+            {&cand.shade_blocks_per_sm, {4, 8, 16}},
+        };
+        for (Knob& k : knobs) {
+            uint32_t keep = *k.field;
+            for (uint32_t v : k.values) {
+                if (v == keep) continue;
+                cand = cur;
+                // the Knob pointers refer to `cand`; rewrite the field through the same offset
+                *k.field = v;
+                double ms = 0.0;
+                rc = trial(cand, &ms);
+                if (rc) return rc;
+                if (ms < best_ms) { best_ms = ms; cur = cand; }
+            }
+            cand = cur;
+        }
+    }
+    ctx->tune = cur;
+    if (best) *best = cur;
+    return SNK_OK;
+}
+
 int snk_pt_synchronize(snk_pt_ctx* ctx) {
     if (!ctx) return SNK_ERR_INVALID_ARG;
     API_TRY(set_device(ctx));
@@ -813,7 +911,7 @@ int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit*
     if (ctx->tr_work.reserve(1) || cudaMemsetAsync(ctx->tr_work.p, 0, sizeof(uint32_t), st))
         return fail(ctx, SNK_ERR_CUDA, "trace_rays: work counter");
     cudaError_t e = launch_trace_rays(scene_dev(ctx), d_rays, n, d_hits, (flags & SNK_TRACE_ANY_HIT) != 0,
-                                      ctx->tr_work.p, grid_of(ctx, 16), st);
+                                      ctx->tr_work.p, trace_grid(ctx), trace_tuning(ctx), st);
     if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("trace_rays: ") + cudaGetErrorString(e));
     if (memory == SNK_MEM_HOST &&
         cudaMemcpyAsync(hits, d_hits, sizeof(snk_hit) * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess)

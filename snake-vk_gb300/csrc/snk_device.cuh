@@ -302,24 +302,27 @@ struct SceneDev {
 // watertight ray/triangle test
 // --------------------------------------------------------------------------
 struct WRay {
-    float o[3], d[3];
+    float o[3];
     int kx, ky, kz;
     float Sx, Sy, Sz;
 };
-SNK_HD WRay wray_setup(V3 o, V3 d) {
+SNK_HD WRay wray_setup(V3 o, V3 dv) {
     WRay r;
     r.o[0] = o.x; r.o[1] = o.y; r.o[2] = o.z;
-    r.d[0] = d.x; r.d[1] = d.y; r.d[2] = d.z;
+    float d[3] = {dv.x, dv.y, dv.z};
     int kz = 0;
-    if (fabsf(r.d[1]) > fabsf(r.d[kz])) kz = 1;
-    if (fabsf(r.d[2]) > fabsf(r.d[kz])) kz = 2;
+    if (fabsf(d[1]) > fabsf(d[0])) kz = 1;
+    if (fabsf(d[2]) > fabsf(kz == 1 ? d[1] : d[0])) kz = 2;
     int kx = kz + 1; if (kx == 3) kx = 0;
     int ky = kx + 1; if (ky == 3) ky = 0;
-    if (r.d[kz] < 0.0f) { int t = kx; kx = ky; ky = t; }
+    if (d[kz] < 0.0f) { int t = kx; kx = ky; ky = t; }
     r.kx = kx; r.ky = ky; r.kz = kz;
-    r.Sx = r.d[kx] / r.d[kz];
-    r.Sy = r.d[ky] / r.d[kz];
-    r.Sz = 1.0f / r.d[kz];
+    float dx = kx == 0 ? d[0] : (kx == 1 ? d[1] : d[2]);
+    float dy = ky == 0 ? d[0] : (ky == 1 ? d[1] : d[2]);
+    float dz = kz == 0 ? d[0] : (kz == 1 ? d[1] : d[2]);
+    r.Sx = dx / dz;
+    r.Sy = dy / dz;
+    r.Sz = 1.0f / dz;
     return r;
 }
 SNK_HD float sel3(const float* a, int k) { return k == 0 ? a[0] : (k == 1 ? a[1] : a[2]); }

@@ -19,6 +19,14 @@ constexpr uint32_t CNT_TOTAL = 64;
 struct HitDev { float t; uint32_t inst, prim; float u, v; uint32_t flags; };
 static_assert(sizeof(HitDev) == 24, "hit layout");
 
+// traversal knobs (zero = default), chosen by snk_pt_set_tuning / the autotuner
+struct TraceTuning {
+    uint32_t chunk;        // rays a warp takes per global fetch (default 64)
+    uint32_t refill_idle;  // refill a warp when at least this many lanes are idle (default 4)
+    uint32_t prim_bias;    // primitive step when 4 * n_prim >= prim_bias * n_node (default 4)
+    uint32_t variant;      // registers: 0 <= 85 (6 blocks / SM), 1 <= 64 (8 blocks), 2 unconstrained
+};
+
 struct FrameParams {
     SceneDev S;
     const ViewDev* views;
@@ -37,6 +45,7 @@ struct FrameParams {
     uint32_t* counters;
     unsigned long long* trav_counters;   // closest: [0] nodes [1] triangles; shadow: [2] [3]
     double2* accum;          // FP64 accumulator of view 0 (2 double2 per pixel)
+    TraceTuning tune;
 };
 
 // launch helpers (defined in pt_kernels.cu / trace_kernels.cu / restir.cu)
@@ -46,7 +55,7 @@ cudaError_t launch_resolve(const FrameParams& F, int grid, cudaStream_t s);
 cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
 cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
 cudaError_t launch_trace_rays(const SceneDev& S, const float4* rays, uint32_t n, HitDev* hits, bool any,
-                              uint32_t* work_counter, int grid, cudaStream_t s);
+                              uint32_t* work_counter, int grid, const TraceTuning& tune, cudaStream_t s);
 
 // ReSTIR DI state of one view
 struct RestirView {

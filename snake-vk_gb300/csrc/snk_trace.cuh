@@ -39,60 +39,65 @@ struct NodeRay {
     uint32_t oct;   // bit i set when direction component i is negative
 };
 
+// Reciprocal for box tests only (they need to be conservative, not exact): the
+// fast approximate division is within 2 ulp, far inside the 1e-5 slack.
 __device__ __forceinline__ float safe_rcp(float d) {
-    return 1.0f / (fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d));
+    return __fdividef(1.0f, fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d));
 }
 
 __device__ __forceinline__ NodeRay make_node_ray(V3 o, V3 d) {
     NodeRay r;
     r.ox = o.x; r.oy = o.y; r.oz = o.z;
     r.idx = safe_rcp(d.x); r.idy = safe_rcp(d.y); r.idz = safe_rcp(d.z);
-    r.oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    // sign bits (not d < 0): -0.0 has a negative reciprocal and must enter through the high plane
+    r.oct = (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) | ((__float_as_uint(d.z) >> 31) << 2);
     return r;
 }
 
-__device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) { return (float)((w >> (8u * k)) & 0xFFu); }
+// Exact byte -> float: the byte is placed in the mantissa of 2^23 (one byte
+// permute) and 2^23 is subtracted (exact), keeping the conversion off the XU pipe.
+__device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k)) - 8388608.0f;
+}
 
 // Tests the 8 children of node idx.  ngroup <- (child_base, internal hits << 24 | imask)
 // with internal hit bits at position (slot ^ oct); tgroup <- (prim_base, primitive hits).
+// Near/far planes are swapped once per node by the ray octant, the hit masks are
+// built without branches, and a slack of 1e-5 of the entry/exit distances keeps
+// the test conservative.
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ nodes, uint32_t idx, const NodeRay& r,
                                                float tmin, float tmax, uint2& ngroup, uint2& tgroup) {
     const float4* np = reinterpret_cast<const float4*>(nodes + idx);
     float4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
     uint32_t e = __float_as_uint(w0.w);
-    float sx = __uint_as_float((e & 0xFFu) << 23);
-    float sy = __uint_as_float(((e >> 8) & 0xFFu) << 23);
-    float sz = __uint_as_float(((e >> 16) & 0xFFu) << 23);
+    float ax = __uint_as_float((e & 0xFFu) << 23) * r.idx;
+    float ay = __uint_as_float(((e >> 8) & 0xFFu) << 23) * r.idy;
+    float az = __uint_as_float(((e >> 16) & 0xFFu) << 23) * r.idz;
     uint32_t imask = e >> 24;
-    float ax = sx * r.idx, ay = sy * r.idy, az = sz * r.idz;
     float bx = (w0.x - r.ox) * r.idx, by = (w0.y - r.oy) * r.idy, bz = (w0.z - r.oz) * r.idz;
-    uint32_t meta_lo = __float_as_uint(w1.z), meta_hi = __float_as_uint(w1.w);
-    uint32_t qlx[2] = {__float_as_uint(w2.x), __float_as_uint(w2.y)};
-    uint32_t qly[2] = {__float_as_uint(w2.z), __float_as_uint(w2.w)};
-    uint32_t qlz[2] = {__float_as_uint(w3.x), __float_as_uint(w3.y)};
-    uint32_t qhx[2] = {__float_as_uint(w3.z), __float_as_uint(w3.w)};
-    uint32_t qhy[2] = {__float_as_uint(w4.x), __float_as_uint(w4.y)};
-    uint32_t qhz[2] = {__float_as_uint(w4.z), __float_as_uint(w4.w)};
+    const bool sx = r.oct & 1u, sy = r.oct & 2u, sz = r.oct & 4u;
+    uint32_t lx0 = __float_as_uint(w2.x), lx1 = __float_as_uint(w2.y), ly0 = __float_as_uint(w2.z),
+             ly1 = __float_as_uint(w2.w), lz0 = __float_as_uint(w3.x), lz1 = __float_as_uint(w3.y),
+             hx0 = __float_as_uint(w3.z), hx1 = __float_as_uint(w3.w), hy0 = __float_as_uint(w4.x),
+             hy1 = __float_as_uint(w4.y), hz0 = __float_as_uint(w4.z), hz1 = __float_as_uint(w4.w);
+    // near / far plane words per axis (a negative direction enters through the high plane)
+    uint32_t nx[2] = {sx ? hx0 : lx0, sx ? hx1 : lx1}, fx[2] = {sx ? lx0 : hx0, sx ? lx1 : hx1};
+    uint32_t ny[2] = {sy ? hy0 : ly0, sy ? hy1 : ly1}, fy[2] = {sy ? ly0 : hy0, sy ? ly1 : hy1};
+    uint32_t nz[2] = {sz ? hz0 : lz0, sz ? hz1 : lz1}, fz[2] = {sz ? lz0 : hz0, sz ? lz1 : hz1};
+    uint32_t meta[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
     uint32_t hit_int = 0, hit_prim = 0;
 #pragma unroll
     for (int s = 0; s < 8; s++) {
-        uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
-        if (meta == 0) continue;
         const int h = s >> 2, k = s & 3;
-        float tx0 = __fmaf_rn(byte_f(qlx[h], k), ax, bx), tx1 = __fmaf_rn(byte_f(qhx[h], k), ax, bx);
-        float ty0 = __fmaf_rn(byte_f(qly[h], k), ay, by), ty1 = __fmaf_rn(byte_f(qhy[h], k), ay, by);
-        float tz0 = __fmaf_rn(byte_f(qlz[h], k), az, bz), tz1 = __fmaf_rn(byte_f(qhz[h], k), az, bz);
-        float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-        float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
-        float slack = (fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f;
-        if (tn <= tf + slack) {
-            if (meta & 0x80u) {
-                hit_int |= 1u << ((uint32_t)s ^ r.oct);
-            } else {
-                uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
-                hit_prim |= ((1u << cnt) - 1u) << off;
-            }
-        }
+        float tn = fmaxf(fmaxf(__fmaf_rn(byte_f(nx[h], k), ax, bx), __fmaf_rn(byte_f(ny[h], k), ay, by)),
+                         fmaxf(__fmaf_rn(byte_f(nz[h], k), az, bz), tmin));
+        float tf = fminf(fminf(__fmaf_rn(byte_f(fx[h], k), ax, bx), __fmaf_rn(byte_f(fy[h], k), ay, by)),
+                         fminf(__fmaf_rn(byte_f(fz[h], k), az, bz), tmax));
+        uint32_t m = (meta[h] >> (8 * k)) & 0xFFu;
+        bool hit = (tn <= tf + ((fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f)) && m != 0u;
+        // internal children: meta 0x80 (count bits 0); leaves: (count << 5) | offset
+        hit_int |= (hit && (m & 0x80u)) ? (1u << ((uint32_t)s ^ r.oct)) : 0u;
+        hit_prim |= hit ? (((1u << ((m >> 5) & 3u)) - 1u) << (m & 31u)) : 0u;
     }
     ngroup = make_uint2(__float_as_uint(w1.x), (hit_int << 24) | imask);
     tgroup = make_uint2(__float_as_uint(w1.y), hit_prim);
@@ -106,9 +111,9 @@ struct TraceCounters { unsigned long long nodes, tris; };
 // deeper entries in a local array.
 struct ShortStack {
     uint2* sh;
+    uint2* spill;   // STACK_MAX - STACK_SH entries (a local array of the caller)
     uint32_t tid, nthreads;
     int sp;
-    uint2 spill[STACK_MAX - STACK_SH];
     __device__ __forceinline__ bool push(uint2 v) {
         if (sp < STACK_SH) sh[sp * nthreads + tid] = v;
         else if (sp < STACK_MAX) spill[sp - STACK_SH] = v;
@@ -122,103 +127,152 @@ struct ShortStack {
     }
 };
 
+// Resumable traversal state of one ray.  The work is split into single units so
+// a warp can vote each iteration which kind of unit its lanes execute together:
+//   node_step()  intersect one internal child of the current node group
+//   prim_step()  test one primitive of the current primitive group (a triangle,
+//                or at the instance level: enter that instance's BLAS)
+//   settle()     pop the stack until there is work again, leaving the BLAS
+//                when its part of the stack is used up; true when finished
+template <bool ANY, bool COUNT>
+struct Traverser {
+    V3 o, d;             // world-space ray
+    float tmin, tmax;
+    NodeRay cr;          // ray of the current level (world or object space)
+    WRay tr;             // object-space watertight set-up (valid in a BLAS)
+    float best_t, best_u, best_v;
+    uint32_t best_inst, best_prim;
+    uint2 ngroup, tgroup;
+    int level, blas_sp;
+    uint32_t cur_inst, steps;
+    unsigned err;
+    bool done;
+    ShortStack st;
+
+    __device__ __forceinline__ void init(const SceneDev& S, V3 o_, V3 d_, float tmin_, float tmax_, uint2* sh,
+                                         uint2* spill, uint32_t tid, uint32_t nthreads) {
+        o = o_; d = d_; tmin = tmin_; tmax = tmax_;
+        cr = make_node_ray(o, d);
+        best_t = tmax; best_u = 0.0f; best_v = 0.0f; best_inst = INVALID; best_prim = INVALID;
+        level = 0; blas_sp = 0; cur_inst = 0; steps = 0; err = 0; done = false;
+        st.sh = sh; st.spill = spill; st.tid = tid; st.nthreads = nthreads; st.sp = 0;
+        ngroup = S.tlas_root == INVALID ? make_uint2(0u, 0u) : make_uint2(S.tlas_root, (1u << (24 + cr.oct)) | 1u);
+        tgroup = make_uint2(0u, 0u);
+    }
+
+    __device__ __forceinline__ bool has_node() const { return ngroup.y > 0x00FFFFFFu; }
+    __device__ __forceinline__ bool has_prim() const { return tgroup.y != 0u; }
+
+    __device__ __forceinline__ void fail(unsigned e) { err |= e; done = true; }
+
+    // Pops until a node or primitive group is pending; sets done when the ray is finished.
+    __device__ __forceinline__ void settle() {
+        while (!done && !has_node() && !has_prim()) {
+            if (level == 1 && st.sp == blas_sp) { level = 0; cr = make_node_ray(o, d); }
+            if (st.sp == 0) { done = true; return; }
+            uint2 g = st.pop();
+            if (g.y > 0x00FFFFFFu) ngroup = g;
+            else tgroup = g;
+        }
+    }
+
+    __device__ __forceinline__ void node_step(const SceneDev& S, TraceCounters* ctr) {
+        if (++steps > MAX_TRAVERSAL_STEPS) { fail(ERR_STEP_LIMIT); return; }
+        // a pending primitive group is postponed onto the stack
+        if (has_prim()) {
+            if (!st.push(tgroup)) { fail(ERR_STACK_OVERFLOW); return; }
+            tgroup = make_uint2(0u, 0u);
+        }
+        uint32_t k = __ffs(ngroup.y >> 24) - 1;
+        ngroup.y &= ~(1u << (24 + k));
+        uint32_t slot = k ^ cr.oct;
+        uint32_t child = ngroup.x + __popc(ngroup.y & ((1u << slot) - 1u) & 0xFFu);
+        if (has_node()) {
+            if (!st.push(ngroup)) { fail(ERR_STACK_OVERFLOW); return; }
+        }
+        if (COUNT) ctr->nodes++;
+        if (child >= (level ? S.num_blas_nodes : S.num_tlas_nodes)) { fail(ERR_BAD_INDEX); return; }
+        intersect_node(level ? S.blas_nodes : S.tlas_nodes, child, cr, tmin, best_t, ngroup, tgroup);
+    }
+
+    __device__ __forceinline__ void prim_step(const SceneDev& S, TraceCounters* ctr) {
+        if (++steps > MAX_TRAVERSAL_STEPS) { fail(ERR_STEP_LIMIT); return; }
+        uint32_t k = __ffs(tgroup.y) - 1;
+        tgroup.y &= tgroup.y - 1u;
+        uint32_t pidx = tgroup.x + k;
+        if (level == 0) {
+            if (pidx >= S.num_tlas_prims) { fail(ERR_BAD_INDEX); return; }
+            uint32_t inst = __ldg(&S.tlas_prims[pidx]);
+            if (inst >= S.num_instances) { fail(ERR_BAD_INDEX); return; }
+            if (has_prim()) {
+                if (!st.push(tgroup)) { fail(ERR_STACK_OVERFLOW); return; }
+            }
+            if (has_node()) {
+                if (!st.push(ngroup)) { fail(ERR_STACK_OVERFLOW); return; }
+            }
+            const float4* ip = reinterpret_cast<const float4*>(S.inst_trace + inst);
+            float4 r0 = __ldg(ip), r1 = __ldg(ip + 1), r2 = __ldg(ip + 2);
+            uint32_t root = __ldg(reinterpret_cast<const uint32_t*>(ip + 3));
+            float inv[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+            V3 oo = xform_point_rn(inv, o);
+            V3 od = xform_dir_rn(inv, d);
+            cr = make_node_ray(oo, od);
+            tr = wray_setup(oo, od);
+            blas_sp = st.sp;
+            level = 1;
+            cur_inst = inst;
+            ngroup = make_uint2(root, (1u << (24 + cr.oct)) | 1u);
+            tgroup = make_uint2(0u, 0u);
+        } else {
+            if (pidx >= S.num_tris) { fail(ERR_BAD_INDEX); return; }
+            if (COUNT) ctr->tris++;
+            const float4* tp = reinterpret_cast<const float4*>(S.tris + pidx);
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            float va[3] = {a.x, a.y, a.z}, vb[3] = {b.x, b.y, b.z}, vc[3] = {c.x, c.y, c.z};
+            float t, b1, b2;
+            if (intersect_tri(tr, va, vb, vc, tmin, tmax, &t, &b1, &b2)) {
+                uint32_t prim = __float_as_uint(a.w);
+                bool better = best_inst == INVALID || t < best_t ||
+                              (t == best_t && (cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)));
+                if (ANY || better) {
+                    best_t = t; best_inst = cur_inst; best_prim = prim; best_u = b1; best_v = b2;
+                }
+                if (ANY) done = true;
+            }
+        }
+    }
+
+    // Result once done; traversal errors are reported through the scene's
+    // error word and read as a miss.
+    __device__ __forceinline__ bool finish(const SceneDev& S, TraceResult& res) {
+        res.hit = false;
+        res.t = -1.0f; res.u = 0.0f; res.v = 0.0f; res.inst = INVALID; res.prim = INVALID;
+        if (err) {
+            if (S.error_word) atomicOr(S.error_word, err);
+            return false;
+        }
+        if (best_inst != INVALID) {
+            res.hit = true; res.t = best_t; res.inst = best_inst; res.prim = best_prim; res.u = best_u; res.v = best_v;
+        }
+        return res.hit;
+    }
+};
+
+// Traces one ray to completion by itself (for kernels that trace inline, e.g.
+// the ReSTIR passes): primitives first, then nodes.
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ bool trace_scene(const SceneDev& S, V3 o, V3 d, float tmin, float tmax, TraceResult& res,
-                                         uint2* sh_stack, uint32_t tid, uint32_t nthreads, TraceCounters* ctr) {
-    res.hit = false;
-    res.t = -1.0f; res.u = 0.0f; res.v = 0.0f; res.inst = INVALID; res.prim = INVALID;
-    if (S.tlas_root == INVALID) return false;
-    const NodeRay wr = make_node_ray(o, d);
-    NodeRay cr = wr;
-    WRay tri_ray;
-    float best_t = tmax;
-    bool found = false;
-    uint32_t best_inst = INVALID, best_prim = INVALID;
-    float best_u = 0.0f, best_v = 0.0f;
-    int level = 0, blas_sp = 0;
-    uint32_t cur_inst = 0;
-    ShortStack st;
-    st.sh = sh_stack; st.tid = tid; st.nthreads = nthreads; st.sp = 0;
-    uint2 ngroup = make_uint2(S.tlas_root, (1u << (24 + cr.oct)) | 1u);
-    uint32_t steps = 0;
-    unsigned err = 0;
-    while (true) {
-        if (++steps > MAX_TRAVERSAL_STEPS) { err |= ERR_STEP_LIMIT; break; }
-        uint2 tgroup = make_uint2(0u, 0u);
-        if (ngroup.y > 0x00FFFFFFu) {
-            uint32_t k = __ffs(ngroup.y >> 24) - 1;
-            ngroup.y &= ~(1u << (24 + k));
-            uint32_t slot = k ^ cr.oct;
-            uint32_t child = ngroup.x + __popc(ngroup.y & ((1u << slot) - 1u) & 0xFFu);
-            if (ngroup.y > 0x00FFFFFFu) {
-                if (!st.push(ngroup)) { err |= ERR_STACK_OVERFLOW; break; }
-            }
-            if (COUNT) ctr->nodes++;
-            if (child >= (level ? S.num_blas_nodes : S.num_tlas_nodes)) { err |= ERR_BAD_INDEX; break; }
-            intersect_node(level ? S.blas_nodes : S.tlas_nodes, child, cr, tmin, best_t, ngroup, tgroup);
-        } else {
-            tgroup = ngroup;
-            ngroup = make_uint2(0u, 0u);
-        }
-        while (tgroup.y != 0u) {
-            uint32_t k = __ffs(tgroup.y) - 1;
-            tgroup.y &= tgroup.y - 1u;
-            uint32_t pidx = tgroup.x + k;
-            if (level == 0) {
-                if (pidx >= S.num_tlas_prims) { err |= ERR_BAD_INDEX; break; }
-                uint32_t inst = __ldg(&S.tlas_prims[pidx]);
-                if (inst >= S.num_instances) { err |= ERR_BAD_INDEX; break; }
-                if (tgroup.y != 0u && !st.push(tgroup)) { err |= ERR_STACK_OVERFLOW; break; }
-                if (ngroup.y > 0x00FFFFFFu && !st.push(ngroup)) { err |= ERR_STACK_OVERFLOW; break; }
-                const float4* ip = reinterpret_cast<const float4*>(S.inst_trace + inst);
-                float4 r0 = __ldg(ip), r1 = __ldg(ip + 1), r2 = __ldg(ip + 2), r3 = __ldg(ip + 3);
-                float inv[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
-                V3 oo = xform_point_rn(inv, o);
-                V3 od = xform_dir_rn(inv, d);
-                cr = make_node_ray(oo, od);
-                tri_ray = wray_setup(oo, od);
-                blas_sp = st.sp;
-                level = 1;
-                cur_inst = inst;
-                ngroup = make_uint2(__float_as_uint(r3.x), (1u << (24 + cr.oct)) | 1u);
-                tgroup.y = 0u;
-                break;
-            } else {
-                if (pidx >= S.num_tris) { err |= ERR_BAD_INDEX; break; }
-                if (COUNT) ctr->tris++;
-                const float4* tp = reinterpret_cast<const float4*>(S.tris + pidx);
-                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                float va[3] = {a.x, a.y, a.z}, vb[3] = {b.x, b.y, b.z}, vc[3] = {c.x, c.y, c.z};
-                float t, b1, b2;
-                if (intersect_tri(tri_ray, va, vb, vc, tmin, tmax, &t, &b1, &b2)) {
-                    uint32_t prim = __float_as_uint(a.w);
-                    if (ANY) {
-                        found = true; best_t = t; best_inst = cur_inst; best_prim = prim; best_u = b1; best_v = b2;
-                        goto done;
-                    }
-                    bool better = !found || t < best_t ||
-                                  (t == best_t && (cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)));
-                    if (better) {
-                        found = true; best_t = t; best_inst = cur_inst; best_prim = prim; best_u = b1; best_v = b2;
-                    }
-                }
-            }
-        }
-        if (err) break;
-        if (ngroup.y > 0x00FFFFFFu) continue;
-        if (level == 1 && st.sp == blas_sp) { level = 0; cr = wr; }
-        if (st.sp == 0) break;
-        ngroup = st.pop();
+                                            uint2* sh_stack, uint32_t tid, uint32_t nthreads, TraceCounters* ctr) {
+    Traverser<ANY, COUNT> tv;
+    uint2 spill[STACK_MAX - STACK_SH];
+    tv.init(S, o, d, tmin, tmax, sh_stack, spill, tid, nthreads);
+    for (;;) {
+        tv.settle();
+        if (tv.done) break;
+        if (tv.has_prim()) tv.prim_step(S, ctr);
+        else tv.node_step(S, ctr);
     }
-done:
-    if (err) {
-        if (S.error_word) atomicOr(S.error_word, err);
-        return false;
-    }
-    if (found) {
-        res.hit = true; res.t = best_t; res.inst = best_inst; res.prim = best_prim; res.u = best_u; res.v = best_v;
-    }
-    return found;
+    return tv.finish(S, res);
 }
 
 }  // namespace snk

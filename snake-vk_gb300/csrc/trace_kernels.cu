@@ -1,10 +1,13 @@
 // trace_kernels.cu -- persistent traversal kernels of the wavefront.
 //
-// One thread traces one ray; warps fetch 32 rays at a time from a global work
-// counter (persistent threads, Aila & Laine, HPG 2009), so the grid is a fixed
-// multiple of the SM count and the number of rays is read on the device (which
-// keeps the frame capturable in a CUDA graph).  The short traversal stack of
-// every thread lives in shared memory (STACK_SH entries) with a local spill.
+// One lane traces one ray.  Warps are persistent (the grid is a fixed multiple
+// of the SM count and the number of rays is read on the device, which keeps the
+// frame capturable in a CUDA graph).  Each warp takes chunks of CHUNK rays from
+// a global counter and, between traversal steps, hands a new ray to every lane
+// whose ray has finished, so lanes do not idle until the warp's longest ray ends
+// (Aila & Laine, HPG 2009, persistent threads with ray replacement).  The short
+// traversal stack of every lane lives in shared memory (STACK_SH entries) with a
+// local spill.
 #include "snk_frame.h"
 #include "snk_trace.cuh"
 
@@ -12,6 +15,36 @@ namespace snk {
 namespace {
 
 constexpr int TBLK = 128;
+
+struct Knobs {
+    uint32_t chunk;
+    int refill_idle;
+    uint32_t prim_bias;
+    __device__ __forceinline__ explicit Knobs(const TraceTuning& t)
+        : chunk(t.chunk ? t.chunk : 64u), refill_idle(t.refill_idle ? (int)t.refill_idle : 4),
+          prim_bias(t.prim_bias ? t.prim_bias : 4u) {}
+};
+
+// One warp-voted traversal step: every active lane first pops until it has work
+// (or finishes); then the warp runs either a node step in the lanes that have an
+// internal child pending or a primitive step in the lanes that have a primitive
+// pending, whichever more lanes want.  Returns true for a lane whose ray finished.
+template <class TV>
+__device__ __forceinline__ bool warp_step(TV& tv, bool active, const SceneDev& S, TraceCounters* ctr,
+                                          uint32_t prim_bias) {
+    if (active) tv.settle();
+    const bool live = active && !tv.done;
+    const unsigned want_prim = __ballot_sync(0xFFFFFFFFu, live && tv.has_prim());
+    const unsigned want_node = __ballot_sync(0xFFFFFFFFu, live && tv.has_node());
+    const bool prims = 4u * (uint32_t)__popc(want_prim) >= prim_bias * (uint32_t)__popc(want_node);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (prims) {
+        if ((want_prim >> lane) & 1u) tv.prim_step(S, ctr);
+    } else {
+        if ((want_node >> lane) & 1u) tv.node_step(S, ctr);
+    }
+    return active && tv.done;
+}
 
 template <bool COUNT>
 __device__ __forceinline__ void flush_counts(const TraceCounters& c, unsigned long long* out) {
@@ -24,91 +57,180 @@ __device__ __forceinline__ void flush_counts(const TraceCounters& c, unsigned lo
     if ((threadIdx.x & 31u) == 0) { atomicAdd(&out[0], a); atomicAdd(&out[1], b); }
 }
 
+// Warp-uniform source of ray indices: a local chunk refilled from `work`.
+struct RayFeed {
+    uint32_t next, end;
+    bool exhausted;
+    __device__ __forceinline__ void init() { next = 0; end = 0; exhausted = false; }
+    // Assigns new indices to the idle lanes (mask `idle`); returns this lane's index
+    // or INVALID.  Must be called by the whole warp.
+    __device__ __forceinline__ uint32_t refill(unsigned idle, uint32_t lane, uint32_t* work, uint32_t n,
+                                               uint32_t chunk) {
+        if (next >= end && !exhausted) {
+            uint32_t b = 0;
+            if (lane == 0) b = atomicAdd(work, chunk);
+            b = __shfl_sync(0xFFFFFFFFu, b, 0);
+            if (b >= n) {
+                exhausted = true;
+            } else {
+                next = b;
+                end = min(b + chunk, n);
+            }
+        }
+        uint32_t mine = INVALID;
+        if (next < end) {
+            uint32_t i = next + __popc(idle & ((1u << lane) - 1u));
+            if (((idle >> lane) & 1u) && i < end) mine = i;
+            next = min(next + (uint32_t)__popc(idle), end);
+        }
+        return mine;
+    }
+    __device__ __forceinline__ bool done() const { return exhausted && next >= end; }
+};
+
 // closest hit of the rays queued for segment d
-template <bool COUNT>
-__global__ void __launch_bounds__(TBLK) k_trace_closest(FrameParams F, uint32_t d) {
+template <bool COUNT, int MINB>
+__global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uint32_t d) {
+    const Knobs kn(F.tune);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
     const uint32_t n = F.counters[CNT_QUEUE + d];
     const float4* rays = F.rays[d & 1u];
     uint32_t* work = &F.counters[CNT_WORK_TRACE + d];
     const uint32_t lane = threadIdx.x & 31u;
     TraceCounters ctr{0ull, 0ull};
+    Traverser<false, COUNT> tv;
+    uint2 spill[STACK_MAX - STACK_SH];
+    RayFeed feed;
+    feed.init();
+    bool active = false;
+    uint32_t ri = 0;
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        uint32_t i = base + lane;
-        if (i < n) {
-            float4 a = __ldg(rays + 2ull * i), b = __ldg(rays + 2ull * i + 1);
+        unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+        if (__popc(~act) >= kn.refill_idle && !feed.done()) {
+            uint32_t i = feed.refill(~act, lane, work, n, kn.chunk);
+            if (i != INVALID) {
+                float4 a = __ldg(rays + 2ull * i), b = __ldg(rays + 2ull * i + 1);
+                tv.init(F.S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
+                ri = i;
+                active = true;
+            }
+            act = __ballot_sync(0xFFFFFFFFu, active);
+        }
+        if (act == 0) {
+            if (feed.done()) break;
+            continue;
+        }
+        if (warp_step(tv, active, F.S, &ctr, kn.prim_bias)) {
             TraceResult r;
-            trace_scene<false, COUNT>(F.S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, r, sh_stack, threadIdx.x,
-                                      TBLK, &ctr);
+            tv.finish(F.S, r);
             HitDev h;
             h.t = r.t; h.inst = r.inst; h.prim = r.prim; h.u = r.u; h.v = r.v; h.flags = r.hit ? 1u : 0u;
-            uint2* dst = reinterpret_cast<uint2*>(F.hits + i);
+            uint2* dst = reinterpret_cast<uint2*>(F.hits + ri);
             const uint2* src = reinterpret_cast<const uint2*>(&h);
             dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2];
+            active = false;
         }
     }
     flush_counts<COUNT>(ctr, F.trav_counters);
 }
 
-// shadow rays of segment d: up to two per queue slot (directional light, local
-// light), traced in that order; an unoccluded one adds its contribution to the
-// path radiance (the same order as the CPU oracle, so sums are bit-identical)
-template <bool COUNT>
-__global__ void __launch_bounds__(TBLK) k_trace_shadow(FrameParams F, uint32_t d) {
+// shadow rays of segment d: entry 2*slot + k (k = 0 directional light, 1 local
+// light); tmax < 0 marks an empty entry.  The visibility goes to the w component
+// of the entry's contribution; k_accum_shadow adds the visible contributions in
+// entry order (the same order as the CPU oracle, so sums are bit-identical).
+template <bool COUNT, int MINB>
+__global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint32_t d) {
+    const Knobs kn(F.tune);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
-    const uint32_t n = F.counters[CNT_QUEUE + d];
-    const uint32_t* pids = F.path_ids[d & 1u];
+    const uint32_t n = 2u * F.counters[CNT_QUEUE + d];
     uint32_t* work = &F.counters[CNT_WORK_SHADOW + d];
     const uint32_t lane = threadIdx.x & 31u;
     TraceCounters ctr{0ull, 0ull};
+    Traverser<true, COUNT> tv;
+    uint2 spill[STACK_MAX - STACK_SH];
+    RayFeed feed;
+    feed.init();
+    bool active = false;
+    uint32_t ri = 0;
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        uint32_t i = base + lane;
-        if (i < n) {
-            uint32_t p = pids[i];
-            for (int k = 0; k < 2; k++) {
-                const float4* sr = F.shadow_rays + 4ull * i + 2 * k;
+        unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+        if (__popc(~act) >= kn.refill_idle && !feed.done()) {
+            uint32_t i = feed.refill(~act, lane, work, n, kn.chunk);
+            if (i != INVALID) {
+                const float4* sr = F.shadow_rays + 2ull * i;
                 float4 b = sr[1];
-                if (b.w < 0.0f) continue;
-                float4 a = sr[0];
-                TraceResult r;
-                bool occ = trace_scene<true, COUNT>(F.S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, r, sh_stack,
-                                                    threadIdx.x, TBLK, &ctr);
-                if (!occ) {
-                    float4 c = F.shadow_contrib[2ull * i + k];
-                    float4 l = F.L[p];
-                    F.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.0f);
+                if (b.w < 0.0f) {
+                    F.shadow_contrib[i].w = 0.0f;
+                } else {
+                    float4 a = sr[0];
+                    tv.init(F.S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
+                    ri = i;
+                    active = true;
                 }
             }
+            act = __ballot_sync(0xFFFFFFFFu, active);
+        }
+        if (act == 0) {
+            if (feed.done()) break;
+            continue;
+        }
+        if (warp_step(tv, active, F.S, &ctr, kn.prim_bias)) {
+            TraceResult r;
+            bool occ = tv.finish(F.S, r);
+            F.shadow_contrib[ri].w = occ ? 0.0f : 1.0f;
+            active = false;
         }
     }
     flush_counts<COUNT>(ctr, F.trav_counters ? F.trav_counters + 2 : nullptr);
 }
 
+// adds the visible shadow-ray contributions of segment d to the path radiance
+__global__ void __launch_bounds__(256) k_accum_shadow(FrameParams F, uint32_t d) {
+    const uint32_t n = F.counters[CNT_QUEUE + d];
+    const uint32_t* pids = F.path_ids[d & 1u];
+    for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
+        float4 c0 = F.shadow_contrib[2ull * i], c1 = F.shadow_contrib[2ull * i + 1];
+        if (c0.w == 0.0f && c1.w == 0.0f) continue;
+        uint32_t p = pids[i];
+        float4 l = F.L[p];
+        if (c0.w != 0.0f) l = make_float4(l.x + c0.x, l.y + c0.y, l.z + c0.z, 0.0f);
+        if (c1.w != 0.0f) l = make_float4(l.x + c1.x, l.y + c1.y, l.z + c1.z, 0.0f);
+        F.L[p] = l;
+    }
+}
+
 // generic trace of an array of rays (the snk_pt_trace_rays test hook)
 template <bool ANY>
-__global__ void __launch_bounds__(TBLK) k_trace_rays(SceneDev S, const float4* __restrict__ rays, uint32_t n,
-                                                     HitDev* hits, uint32_t* work) {
+__global__ void __launch_bounds__(TBLK, 6) k_trace_rays(SceneDev S, const float4* __restrict__ rays, uint32_t n,
+                                                     HitDev* hits, uint32_t* work, TraceTuning tune) {
+    const Knobs kn(tune);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
     const uint32_t lane = threadIdx.x & 31u;
+    Traverser<ANY, false> tv;
+    uint2 spill[STACK_MAX - STACK_SH];
+    RayFeed feed;
+    feed.init();
+    bool active = false;
+    uint32_t ri = 0;
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        uint32_t i = base + lane;
-        if (i < n) {
-            float4 a = __ldg(rays + 2ull * i), b = __ldg(rays + 2ull * i + 1);
+        unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+        if (__popc(~act) >= kn.refill_idle && !feed.done()) {
+            uint32_t i = feed.refill(~act, lane, work, n, kn.chunk);
+            if (i != INVALID) {
+                float4 a = __ldg(rays + 2ull * i), b = __ldg(rays + 2ull * i + 1);
+                tv.init(S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
+                ri = i;
+                active = true;
+            }
+            act = __ballot_sync(0xFFFFFFFFu, active);
+        }
+        if (act == 0) {
+            if (feed.done()) break;
+            continue;
+        }
+        if (warp_step(tv, active, S, nullptr, kn.prim_bias)) {
             TraceResult r;
-            bool hit = trace_scene<ANY, false>(S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, r, sh_stack,
-                                               threadIdx.x, TBLK, nullptr);
+            bool hit = tv.finish(S, r);
             HitDev h;
             if (ANY) {
                 h.t = hit ? 1.0f : -1.0f; h.inst = INVALID; h.prim = INVALID; h.u = 0.0f; h.v = 0.0f;
@@ -116,29 +238,48 @@ __global__ void __launch_bounds__(TBLK) k_trace_rays(SceneDev S, const float4* _
             } else {
                 h.t = r.t; h.inst = r.inst; h.prim = r.prim; h.u = r.u; h.v = r.v; h.flags = hit ? 1u : 0u;
             }
-            hits[i] = h;
+            hits[ri] = h;
+            active = false;
         }
     }
 }
 
 }  // namespace
 
+// register budget variants: 0 -> at most 85 registers (6 blocks of 128 per SM),
+// 1 -> 64 registers (8 blocks), 2 -> unconstrained (4 blocks)
+template <bool COUNT>
+void launch_closest_variant(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s) {
+    if (F.tune.variant == 1) k_trace_closest<COUNT, 8><<<grid, TBLK, 0, s>>>(F, depth);
+    else if (F.tune.variant == 2) k_trace_closest<COUNT, 4><<<grid, TBLK, 0, s>>>(F, depth);
+    else k_trace_closest<COUNT, 6><<<grid, TBLK, 0, s>>>(F, depth);
+}
+template <bool COUNT>
+void launch_shadow_variant(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s) {
+    if (F.tune.variant == 1) k_trace_shadow<COUNT, 8><<<grid, TBLK, 0, s>>>(F, depth);
+    else if (F.tune.variant == 2) k_trace_shadow<COUNT, 4><<<grid, TBLK, 0, s>>>(F, depth);
+    else k_trace_shadow<COUNT, 6><<<grid, TBLK, 0, s>>>(F, depth);
+}
+
 cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s) {
-    if (count) k_trace_closest<true><<<grid, TBLK, 0, s>>>(F, depth);
-    else k_trace_closest<false><<<grid, TBLK, 0, s>>>(F, depth);
+    if (count) launch_closest_variant<true>(F, depth, grid, s);
+    else launch_closest_variant<false>(F, depth, grid, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s) {
-    if (count) k_trace_shadow<true><<<grid, TBLK, 0, s>>>(F, depth);
-    else k_trace_shadow<false><<<grid, TBLK, 0, s>>>(F, depth);
+    if (count) launch_shadow_variant<true>(F, depth, grid, s);
+    else launch_shadow_variant<false>(F, depth, grid, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_accum_shadow<<<grid / 2 > 0 ? grid / 2 : 1, 256, 0, s>>>(F, depth);
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_rays(const SceneDev& S, const float4* rays, uint32_t n, HitDev* hits, bool any,
-                              uint32_t* work, int grid, cudaStream_t s) {
-    if (any) k_trace_rays<true><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work);
-    else k_trace_rays<false><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work);
+                              uint32_t* work, int grid, const TraceTuning& tune, cudaStream_t s) {
+    if (any) k_trace_rays<true><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
+    else k_trace_rays<false><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
     return cudaGetLastError();
 }
 

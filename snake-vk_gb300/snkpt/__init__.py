@@ -24,7 +24,8 @@ EXPORTS = [
     "snk_pt_abi_version", "snk_pt_create", "snk_pt_destroy", "snk_pt_set_stream", "snk_pt_get_last_error",
     "snk_pt_get_stats", "snk_pt_upload_meshes", "snk_pt_set_instances", "snk_pt_set_materials",
     "snk_pt_set_lights", "snk_pt_build", "snk_pt_render", "snk_pt_synchronize", "snk_pt_trace_rays",
-    "snk_pt_read_accumulator", "snk_pt_render_noalloc",
+    "snk_pt_read_accumulator", "snk_pt_render_noalloc", "snk_pt_set_tuning", "snk_pt_get_tuning",
+    "snk_pt_autotune",
 ]
 
 
@@ -41,6 +42,24 @@ class Mesh(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_uint32), ("stream", C.c_void_p), ("reserved", C.c_uint64 * 4)]
+
+
+class Tuning(C.Structure):
+    """snk_tuning: launch knobs of the wavefront (0 = default)."""
+    _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("shade_blocks_per_sm", C.c_uint32),
+                ("ray_chunk", C.c_uint32), ("refill_idle", C.c_uint32), ("prim_bias", C.c_uint32),
+                ("trace_variant", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+    KNOBS = ("trace_blocks_per_sm", "shade_blocks_per_sm", "ray_chunk", "refill_idle", "prim_bias", "trace_variant")
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k in self.KNOBS}
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "Tuning":
+        t = cls()
+        for k in cls.KNOBS:
+            setattr(t, k, int(d.get(k, 0)))
+        return t
 
 
 class ViewOutputs(C.Structure):
@@ -87,6 +106,9 @@ def lib():
         L.snk_pt_trace_rays.argtypes = [vp, vp, u32, vp, u32, u32]
         L.snk_pt_read_accumulator.argtypes = [vp, vp, u32, C.POINTER(C.c_uint64)]
         L.snk_pt_render_noalloc.argtypes = [vp, vp, vp, vp]
+        L.snk_pt_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.snk_pt_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.snk_pt_autotune.argtypes = [vp, vp, u32, vp, u32, C.POINTER(Tuning)]
         _lib = L
     return _lib
 
@@ -208,6 +230,52 @@ class PathTracer:
 
     def synchronize(self):
         self._check(lib().snk_pt_synchronize(self._h))
+
+    # ---- launch knobs ------------------------------------------------------------
+    def set_tuning(self, tuning: "Tuning | dict"):
+        t = tuning if isinstance(tuning, Tuning) else Tuning.from_dict(tuning)
+        self._check(lib().snk_pt_set_tuning(self._h, C.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self._check(lib().snk_pt_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, views, settings, frames_per_trial: int = 3, cache: str | None = None, key: str = "") -> dict:
+        """Coordinate-descent search of the launch knobs on this workload (the
+        library's snk_pt_autotune).  With ``cache`` (a JSON file) a result stored
+        under (device name, key) is reused instead of searching again."""
+        import json
+        dev_key = None
+        if cache:
+            import torch
+            dev_key = f"{torch.cuda.get_device_name()}|{key}"
+            if os.path.exists(cache):
+                try:
+                    stored = json.load(open(cache)).get(dev_key)
+                except ValueError:
+                    stored = None
+                if stored:
+                    self.set_tuning(stored)
+                    return stored
+        v = np.ascontiguousarray(np.array([np.asarray(x, abi.VIEW_DTYPE) for x in views], abi.VIEW_DTYPE))
+        st = np.ascontiguousarray(np.asarray(settings, abi.SETTINGS_DTYPE).reshape(1))
+        best = Tuning()
+        self._check(lib().snk_pt_autotune(self._h, v.ctypes.data, len(views), st.ctypes.data, frames_per_trial,
+                                          C.byref(best)))
+        result = best.as_dict()
+        if cache:
+            data = {}
+            if os.path.exists(cache):
+                try:
+                    data = json.load(open(cache))
+                except ValueError:
+                    data = {}
+            data[dev_key] = result
+            os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
+            with open(cache, "w") as f:
+                json.dump(data, f, indent=1, sort_keys=True)
+        return result
 
     def trace_rays(self, rays, any_hit: bool = False):
         """rays: numpy abi.RAY_DTYPE array (host) or a torch CUDA tensor of shape (n, 8) float32."""

@@ -141,3 +141,23 @@ def test_restir_config2_frames(cuda, built_lib):
         s = pt.stats()
         assert s["rays_shadow"] == int(ctr[2]), f"frame {f}: shadow ray count {s['rays_shadow']} vs {int(ctr[2])}"
         assert g["radiance"][:, :3].mean() > 0.0
+
+
+def test_launch_knobs_do_not_change_results(cuda, built_lib):
+    """Every autotuner candidate must render the same bits (the knobs only move work)."""
+    sc = scenes.config1(width=320, height=180)
+    st = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=5)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    base = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    for knobs in [dict(trace_blocks_per_sm=4, ray_chunk=32, refill_idle=1, prim_bias=2, trace_variant=1),
+                  dict(trace_blocks_per_sm=32, ray_chunk=256, refill_idle=16, prim_bias=8, shade_blocks_per_sm=4)]:
+        pt.set_tuning(knobs)
+        g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+        for k in g:
+            assert np.array_equal(g[k], base[k]), (knobs, k)
+    best = pt.autotune([sc.views[0]], st, frames_per_trial=1)
+    assert best["trace_blocks_per_sm"] > 0 and best["ray_chunk"] > 0
+    g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    for k in g:
+        assert np.array_equal(g[k], base[k]), ("autotuned", k)
