@@ -328,6 +328,29 @@ int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit*
 int snk_pt_render_noalloc(snk_pt_ctx* ctx, const snk_view* view, const snk_render_settings* settings,
                           const snk_view_outputs* outputs);
 
+/* ---- MLP radiance cache (no counterpart in the reference) ------------------------
+ * 64 encoded inputs -> 4 x 64 ReLU -> RGB, no biases; SNK_CACHE_NUM_WEIGHTS FP32
+ * master weights, row-major W_l[in][out], layers concatenated (4 x 64x64, 64x3).
+ * A query/sample record is 16 floats: position xyz, roughness, outgoing direction
+ * xyz, metallic, shading normal xyz, 0, albedo xyz, 0.  A training sample appends
+ * 4 floats: target radiance rgb and a weight (0 or 1). */
+#define SNK_CACHE_NUM_WEIGHTS 16576u
+/* He-uniform initialisation from a PCG32 stream, Adam state cleared. */
+int snk_pt_cache_reset(snk_pt_ctx* ctx, uint32_t seed);
+int snk_pt_cache_set_weights(snk_pt_ctx* ctx, const float* weights, uint32_t n);
+int snk_pt_cache_get_weights(snk_pt_ctx* ctx, float* weights, uint32_t n);
+/* positions are normalised to this box (default: the built scene's bounds) */
+int snk_pt_cache_set_bounds(snk_pt_ctx* ctx, const float lo[3], const float hi[3]);
+/* the 64 input features of n records, as the network consumes them (BF16 values) */
+int snk_pt_cache_encode(snk_pt_ctx* ctx, const float* records, uint32_t n, float* features, uint32_t memory);
+/* network outputs (n x 3) for n records */
+int snk_pt_cache_infer(snk_pt_ctx* ctx, const float* records, uint32_t n, float* out, uint32_t memory);
+/* one training step on n samples (20 floats each): relative-L2 loss, gradient
+ * summed over the batch, Adam (lr; lr = 0 computes the gradient only).
+ * grad (SNK_CACHE_NUM_WEIGHTS floats, host) and loss may be NULL. */
+int snk_pt_cache_train(snk_pt_ctx* ctx, const float* samples, uint32_t n, float lr, float* grad, float* loss,
+                       uint32_t memory);
+
 /* FP64 converged-image accumulator of view 0: copies the running mean (samples
  * accumulated so far) as float4 into out (memory space as given). */
 int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames);

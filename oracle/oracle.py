@@ -70,6 +70,10 @@ def lib():
         L.snko_num_local_lights.argtypes = [vp]
         L.snko_num_local_lights.restype = u32
         L.snko_hardware_threads.restype = u32
+        L.snko_mlp_forward.argtypes = [vp, vp, u32, vp]
+        L.snko_mlp_grad.argtypes = [vp, vp, vp, vp, u32, vp, C.c_int]
+        L.snko_mlp_grad.restype = C.c_double
+        L.snko_mlp_adam.argtypes = [vp, vp, vp, vp, u32, C.c_double, C.c_double, C.c_double, C.c_double]
         _lib = L
     return _lib
 
@@ -249,3 +253,34 @@ def invert_affine(m: np.ndarray):
     det = np.zeros(1, np.float32)
     lib().snko_invert_affine(_p(m), _p(inv), _p(nm), _p(det))
     return inv, nm, float(det[0])
+
+
+# ---- MLP radiance cache reference (FP64) -------------------------------------------
+MLP_NW = 4 * 64 * 64 + 64 * 3
+
+
+def mlp_forward(W, x):
+    W = np.ascontiguousarray(W, np.float64)
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros((x.shape[0], 3))
+    lib().snko_mlp_forward(_p(W), _p(x), x.shape[0], _p(y))
+    return y
+
+
+def mlp_grad(W, x, t, w=None, relative=True):
+    """(loss, dL/dW) of the relative-L2 loss over the batch (FP64); relative=False: plain L2."""
+    W = np.ascontiguousarray(W, np.float64)
+    x = np.ascontiguousarray(x, np.float64)
+    t = np.ascontiguousarray(t, np.float64)
+    w = np.ones(x.shape[0]) if w is None else np.ascontiguousarray(w, np.float64)
+    dW = np.zeros(MLP_NW)
+    loss = lib().snko_mlp_grad(_p(W), _p(x), _p(t), _p(w), x.shape[0], _p(dW), 1 if relative else 0)
+    return loss, dW
+
+
+def mlp_adam(W, m, v, dW, step, lr=1e-2, b1=0.9, b2=0.99, eps=1e-8):
+    """One Adam step in place on float64 arrays."""
+    for a in (W, m, v):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    dW = np.ascontiguousarray(dW, np.float64)
+    lib().snko_mlp_adam(_p(W), _p(m), _p(v), _p(dW), step, lr, b1, b2, eps)

@@ -1508,3 +1508,94 @@ uint32_t snko_num_local_lights(void* sp) { return (uint32_t)((Scene*)sp)->lights
 uint32_t snko_hardware_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
 
 }  // extern "C"
+
+// ---- MLP radiance cache reference (FP64) ------------------------------------
+// Network: 64 inputs -> 4 x (64, ReLU) -> 3 linear outputs, no biases.  Weights
+// are row-major W_l[in][out] concatenated (4 x 64x64, then 64x3 = 16576 floats).
+// Loss: relative L2 of Mueller et al. 2021 (radiance caching), mean over the
+// batch and the 3 channels: (y - t)^2 / (sg(y)^2 + 0.01); sample weight w in {0,1}.
+static const int MLP_IN = 64, MLP_HID = 64, MLP_OUT = 3;
+static const size_t MLP_NW = 4 * 64 * 64 + 64 * 3;
+static inline size_t mlp_off(int l) { return (size_t)l * 64 * 64; }
+
+static void mlp_forward_one(const double* W, const double* x, double act[4][64], double* y) {
+    const double* in = x;
+    for (int l = 0; l < 4; l++) {
+        const double* Wl = W + mlp_off(l);
+        for (int o = 0; o < 64; o++) {
+            double s = 0.0;
+            for (int i = 0; i < 64; i++) s += in[i] * Wl[i * 64 + o];
+            act[l][o] = s > 0.0 ? s : 0.0;
+        }
+        in = act[l];
+    }
+    const double* W5 = W + mlp_off(4);
+    for (int o = 0; o < 3; o++) {
+        double s = 0.0;
+        for (int i = 0; i < 64; i++) s += in[i] * W5[i * 3 + o];
+        y[o] = s;
+    }
+}
+
+extern "C" void snko_mlp_forward(const double* W, const double* x, uint32_t n, double* y) {
+    double act[4][64];
+    for (uint32_t s = 0; s < n; s++) mlp_forward_one(W, x + 64 * (size_t)s, act, y + 3 * (size_t)s);
+}
+
+// loss and dL/dW over a batch (weights w per sample; normaliser = 3 * n).
+// relative = 0 uses a plain L2 (denominator 1), for finite-difference checks of
+// the back-propagation (the relative loss's stop-gradient makes its gradient
+// differ from the derivative of its value on purpose).
+extern "C" double snko_mlp_grad(const double* W, const double* x, const double* t, const double* wt, uint32_t n,
+                                double* dW, int relative) {
+    std::memset(dW, 0, MLP_NW * sizeof(double));
+    double loss = 0.0;
+    const double norm = 1.0 / (3.0 * (double)n);
+    double act[4][64], y[3], g[64], gn[64];
+    for (uint32_t s = 0; s < n; s++) {
+        const double* xs = x + 64 * (size_t)s;
+        mlp_forward_one(W, xs, act, y);
+        double gy[3];
+        for (int c = 0; c < 3; c++) {
+            double d = y[c] - t[3 * (size_t)s + c];
+            double den = relative ? y[c] * y[c] + 0.01 : 1.0;
+            loss += wt[s] * d * d / den * norm;
+            gy[c] = wt[s] * 2.0 * d / den * norm;
+        }
+        // output layer
+        double* dW5 = dW + mlp_off(4);
+        const double* W5 = W + mlp_off(4);
+        for (int i = 0; i < 64; i++) {
+            for (int c = 0; c < 3; c++) dW5[i * 3 + c] += act[3][i] * gy[c];
+            double s5 = 0.0;
+            for (int c = 0; c < 3; c++) s5 += W5[i * 3 + c] * gy[c];
+            g[i] = act[3][i] > 0.0 ? s5 : 0.0;
+        }
+        for (int l = 3; l >= 0; l--) {
+            const double* in = l == 0 ? xs : act[l - 1];
+            double* dWl = dW + mlp_off(l);
+            const double* Wl = W + mlp_off(l);
+            for (int i = 0; i < 64; i++)
+                for (int o = 0; o < 64; o++) dWl[i * 64 + o] += in[i] * g[o];
+            if (l == 0) break;
+            for (int i = 0; i < 64; i++) {
+                double sgi = 0.0;
+                for (int o = 0; o < 64; o++) sgi += Wl[i * 64 + o] * g[o];
+                gn[i] = act[l - 1][i] > 0.0 ? sgi : 0.0;
+            }
+            std::memcpy(g, gn, sizeof(g));
+        }
+    }
+    return loss;
+}
+
+// one Adam step (Kingma & Ba 2015) in place; step >= 1
+extern "C" void snko_mlp_adam(double* W, double* m, double* v, const double* dW, uint32_t step, double lr,
+                              double b1, double b2, double eps) {
+    double c1 = 1.0 - std::pow(b1, (double)step), c2 = 1.0 - std::pow(b2, (double)step);
+    for (size_t i = 0; i < MLP_NW; i++) {
+        m[i] = b1 * m[i] + (1.0 - b1) * dW[i];
+        v[i] = b2 * v[i] + (1.0 - b2) * dW[i] * dW[i];
+        W[i] -= lr * (m[i] / c1) / (std::sqrt(v[i] / c2) + eps);
+    }
+}

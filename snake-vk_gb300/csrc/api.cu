@@ -14,6 +14,7 @@
 #include "../../include/snk_pt.h"
 #include "snk_frame.h"
 #include "snk_host.h"
+#include "snk_mlp.h"
 
 using namespace snk;
 
@@ -109,6 +110,14 @@ struct snk_pt_ctx {
     uint64_t stage_launches[SNK_NUM_STAGES] = {0};
 
     snk_tuning tune{};   // launch knobs (zero = defaults)
+
+    // MLP radiance cache
+    MlpState mlp;
+    EncodeParams cache_ep{};
+    bool cache_bounds_set = false;
+    float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {1, 1, 1};
+    DBuf<float4> cache_in;
+    DBuf<float> cache_out, cache_grad;
 };
 
 namespace {
@@ -256,6 +265,26 @@ Status build_instances(snk_pt_ctx* ctx) {
         T.pad = 0;
         if (T.blas_root != INVALID) list.push_back((uint32_t)i);
         if (ctx->materials[in.material_id].flags & SNK_MAT_EMISSIVE) emissive.push_back((uint32_t)i);
+    }
+    {   // world bounds of the scene (positions of the radiance cache are normalised to them)
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (uint32_t i : list) {
+            const snk_instance& in = ctx->instances[i];
+            const MeshInfo& M = ctx->h_meshes[in.mesh_id];
+            for (int c = 0; c < 8; c++) {
+                double p[3] = {(c & 1) ? M.hi[0] : M.lo[0], (c & 2) ? M.hi[1] : M.lo[1], (c & 4) ? M.hi[2] : M.lo[2]};
+                for (int r = 0; r < 3; r++) {
+                    double v = in.transform[4 * r] * p[0] + in.transform[4 * r + 1] * p[1] + in.transform[4 * r + 2] * p[2] +
+                               in.transform[4 * r + 3];
+                    lo[r] = std::min(lo[r], v);
+                    hi[r] = std::max(hi[r], v);
+                }
+            }
+        }
+        for (int r = 0; r < 3; r++) {
+            ctx->scene_lo[r] = list.empty() ? 0.0f : (float)lo[r];
+            ctx->scene_hi[r] = list.empty() ? 1.0f : (float)hi[r];
+        }
     }
     SNK_TRY(upload(ctx->d_inst_trace, it.data(), it.size(), st));
     SNK_TRY(upload(ctx->d_inst_shade, is.data(), is.size(), st));
@@ -877,6 +906,150 @@ int snk_pt_autotune(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, 
     }
     ctx->tune = cur;
     if (best) *best = cur;
+    return SNK_OK;
+}
+
+namespace {
+
+EncodeParams cache_encode_params(snk_pt_ctx* ctx) {
+    EncodeParams ep;
+    const float* lo = ctx->cache_bounds_set ? ctx->cache_ep.lo : ctx->scene_lo;
+    for (int a = 0; a < 3; a++) {
+        ep.lo[a] = lo[a];
+        if (ctx->cache_bounds_set) {
+            ep.inv_ext[a] = ctx->cache_ep.inv_ext[a];
+        } else {
+            float ext = ctx->scene_hi[a] - ctx->scene_lo[a];
+            ep.inv_ext[a] = ext > 0.0f ? 1.0f / ext : 1.0f;
+        }
+    }
+    return ep;
+}
+
+Status cache_ensure(snk_pt_ctx* ctx) {
+    if (ctx->mlp.ready) return Status::Ok();
+    // He-uniform initialisation from a PCG32 stream (seed 1)
+    std::vector<float> w(MLP_NW);
+    Pcg rng = pcg_stream(0x4D4C5031u, 0u, 0u, 1u);
+    for (int i = 0; i < MLP_NW; i++) {
+        const float s = i < 4 * 4096 ? std::sqrt(6.0f / 64.0f) : std::sqrt(6.0f / 64.0f) * 0.1f;
+        w[i] = (pcg_float(rng) * 2.0f - 1.0f) * s;
+    }
+    SNK_TRY(mlp_init(ctx->mlp, w.data(), ctx->stream));
+    return Status::Ok();
+}
+
+// copies n*floats_per host records into the context's device staging buffer
+Status cache_stage(snk_pt_ctx* ctx, const float* src, uint32_t n, uint32_t floats_per, uint32_t memory,
+                   const float4** out) {
+    if (memory == SNK_MEM_DEVICE) { *out = reinterpret_cast<const float4*>(src); return Status::Ok(); }
+    SNK_TRY_CUDA(ctx->cache_in.reserve(((size_t)n * floats_per + 3) / 4));
+    SNK_TRY_CUDA(cudaMemcpyAsync(ctx->cache_in.p, src, (size_t)n * floats_per * sizeof(float), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    *out = ctx->cache_in.p;
+    return Status::Ok();
+}
+
+}  // namespace
+
+int snk_pt_cache_reset(snk_pt_ctx* ctx, uint32_t seed) {
+    if (!ctx) return SNK_ERR_INVALID_ARG;
+    API_TRY(set_device(ctx));
+    std::vector<float> w(MLP_NW);
+    Pcg rng = pcg_stream(0x4D4C5031u, 0u, 0u, seed);
+    for (int i = 0; i < MLP_NW; i++) {
+        const float s = i < 4 * 4096 ? std::sqrt(6.0f / 64.0f) : std::sqrt(6.0f / 64.0f) * 0.1f;
+        w[i] = (pcg_float(rng) * 2.0f - 1.0f) * s;
+    }
+    API_TRY(mlp_init(ctx->mlp, w.data(), ctx->stream));
+    return SNK_OK;
+}
+
+int snk_pt_cache_set_weights(snk_pt_ctx* ctx, const float* w, uint32_t n) {
+    if (!ctx || !w || n != (uint32_t)MLP_NW) return fail(ctx, SNK_ERR_INVALID_ARG, "cache_set_weights: need 16576 weights");
+    API_TRY(set_device(ctx));
+    API_TRY(mlp_init(ctx->mlp, w, ctx->stream));
+    return SNK_OK;
+}
+
+int snk_pt_cache_get_weights(snk_pt_ctx* ctx, float* w, uint32_t n) {
+    if (!ctx || !w || n != (uint32_t)MLP_NW) return fail(ctx, SNK_ERR_INVALID_ARG, "cache_get_weights: need 16576 weights");
+    API_TRY(set_device(ctx));
+    API_TRY(cache_ensure(ctx));
+    if (cudaMemcpyAsync(w, ctx->mlp.w.p, MLP_NW * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream) ||
+        cudaStreamSynchronize(ctx->stream))
+        return fail(ctx, SNK_ERR_CUDA, "cache_get_weights: copy");
+    return SNK_OK;
+}
+
+int snk_pt_cache_set_bounds(snk_pt_ctx* ctx, const float lo[3], const float hi[3]) {
+    if (!ctx || !lo || !hi) return fail(ctx, SNK_ERR_INVALID_ARG, "cache_set_bounds: null argument");
+    for (int a = 0; a < 3; a++) {
+        if (!(hi[a] > lo[a])) return fail(ctx, SNK_ERR_INVALID_ARG, "cache_set_bounds: empty box");
+        ctx->cache_ep.lo[a] = lo[a];
+        ctx->cache_ep.inv_ext[a] = 1.0f / (hi[a] - lo[a]);
+    }
+    ctx->cache_bounds_set = true;
+    return SNK_OK;
+}
+
+int snk_pt_cache_encode(snk_pt_ctx* ctx, const float* records, uint32_t n, float* features, uint32_t memory) {
+    if (!ctx || (n && (!records || !features)) || memory > SNK_MEM_HOST) return fail(ctx, SNK_ERR_INVALID_ARG, "cache_encode: bad arguments");
+    API_TRY(set_device(ctx));
+    if (n == 0) return SNK_OK;
+    const float4* rec;
+    API_TRY(cache_stage(ctx, records, n, 16, memory, &rec));
+    float* out = features;
+    if (memory == SNK_MEM_HOST) {
+        if (ctx->cache_out.reserve((size_t)n * 64)) return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "cache_encode: buffer");
+        out = ctx->cache_out.p;
+    }
+    API_TRY(mlp_encode(rec, n, cache_encode_params(ctx), out, ctx->stream));
+    if (memory == SNK_MEM_HOST &&
+        cudaMemcpyAsync(features, out, (size_t)n * 64 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream))
+        return fail(ctx, SNK_ERR_CUDA, "cache_encode: copy");
+    if (cudaStreamSynchronize(ctx->stream)) return fail(ctx, SNK_ERR_CUDA, "cache_encode: sync");
+    return SNK_OK;
+}
+
+int snk_pt_cache_infer(snk_pt_ctx* ctx, const float* records, uint32_t n, float* outp, uint32_t memory) {
+    if (!ctx || (n && (!records || !outp)) || memory > SNK_MEM_HOST) return fail(ctx, SNK_ERR_INVALID_ARG, "cache_infer: bad arguments");
+    API_TRY(set_device(ctx));
+    API_TRY(cache_ensure(ctx));
+    if (n == 0) return SNK_OK;
+    const float4* rec;
+    API_TRY(cache_stage(ctx, records, n, 16, memory, &rec));
+    float* out = outp;
+    if (memory == SNK_MEM_HOST) {
+        if (ctx->cache_out.reserve((size_t)n * 3)) return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "cache_infer: buffer");
+        out = ctx->cache_out.p;
+    }
+    API_TRY(mlp_infer(ctx->mlp, rec, nullptr, n, cache_encode_params(ctx), out, nullptr, nullptr, grid_of(ctx, 4),
+                      ctx->stream));
+    if (memory == SNK_MEM_HOST &&
+        cudaMemcpyAsync(outp, out, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream))
+        return fail(ctx, SNK_ERR_CUDA, "cache_infer: copy");
+    if (cudaStreamSynchronize(ctx->stream)) return fail(ctx, SNK_ERR_CUDA, "cache_infer: sync");
+    return SNK_OK;
+}
+
+int snk_pt_cache_train(snk_pt_ctx* ctx, const float* samples, uint32_t n, float lr, float* grad, float* loss,
+                       uint32_t memory) {
+    if (!ctx || (n && !samples) || memory > SNK_MEM_HOST || !(lr >= 0.0f))
+        return fail(ctx, SNK_ERR_INVALID_ARG, "cache_train: bad arguments");
+    API_TRY(set_device(ctx));
+    API_TRY(cache_ensure(ctx));
+    if (n == 0) return SNK_OK;
+    const float4* s;
+    API_TRY(cache_stage(ctx, samples, n, 20, memory, &s));
+    if (grad && ctx->cache_grad.reserve(MLP_NW)) return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "cache_train: buffer");
+    float l = 0.0f;
+    API_TRY(mlp_train_step(ctx->mlp, s, n, cache_encode_params(ctx), lr, grad ? ctx->cache_grad.p : nullptr, &l,
+                           ctx->stream));
+    if (grad && (cudaMemcpyAsync(grad, ctx->cache_grad.p, MLP_NW * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream) ||
+                 cudaStreamSynchronize(ctx->stream)))
+        return fail(ctx, SNK_ERR_CUDA, "cache_train: copy");
+    if (loss) *loss = l;
     return SNK_OK;
 }
 

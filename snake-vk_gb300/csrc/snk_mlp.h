@@ -1,0 +1,45 @@
+// snk_mlp.h -- MLP radiance cache: sizes, weight layouts and host entry points.
+#pragma once
+#include <cmath>
+#include <vector>
+
+#include "snk_host.h"
+
+namespace snk {
+
+constexpr int MLP_NW = 4 * 64 * 64 + 64 * 3;   // master weights (FP32)
+// master weight offset of layer l (W_l[in][out], row major)
+#define MLP_OFF(l) ((l) * 4096)
+// fragment-ordered BF16 copies, in uint2 words (one B fragment per lane per tile)
+#define MLP_FWD_OFF(l) ((l) < 4 ? (l) * 1024 : 4096)      // 4 x (4 k-tiles x 8 n-tiles x 32), then 4 x 1 x 32
+constexpr int MLP_FWD_WORDS = 4096 + 128;
+#define MLP_BWD_OFF(l) ((l) < 4 ? ((l) - 1) * 1024 : 3072) // transposed layers 1..3, then layer 4 (1 x 8 x 32)
+constexpr int MLP_BWD_WORDS = 3072 + 256;
+
+struct EncodeParams {
+    float lo[3];        // scene box the positions are normalised to
+    float inv_ext[3];
+};
+
+struct AdamParams {
+    float lr, b1, b2, eps, c1, c2;   // c1, c2: bias corrections 1 - b^step
+};
+
+struct MlpState {
+    DBuf<float> w, m, v;             // FP32 master weights and Adam moments
+    DBuf<uint2> wf, wb;              // BF16 forward / transposed copies (fragment order)
+    DBuf<float> part, loss;          // per-CTA gradient partials and losses
+    uint32_t step = 0;
+    bool ready = false;
+};
+
+Status mlp_init(MlpState& M, const float* w_host, cudaStream_t st);
+// records: 4 float4 per query (position+roughness, direction+metallic, normal, albedo+path id)
+Status mlp_infer(const MlpState& M, const float4* rec, const uint32_t* n_dev, uint32_t n, const EncodeParams& ep,
+                 float* out, const float4* beta, float4* L, int grid, cudaStream_t st);
+Status mlp_encode(const float4* rec, uint32_t n, const EncodeParams& ep, float* out, cudaStream_t st);
+// samples: 5 float4 each (the 4 record words, then target rgb + weight)
+Status mlp_train_step(MlpState& M, const float4* samples, uint32_t n, const EncodeParams& ep, float lr,
+                      float* grad_out, float* loss_host, cudaStream_t st);
+
+}  // namespace snk

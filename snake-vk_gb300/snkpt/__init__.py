@@ -25,7 +25,8 @@ EXPORTS = [
     "snk_pt_get_stats", "snk_pt_upload_meshes", "snk_pt_set_instances", "snk_pt_set_materials",
     "snk_pt_set_lights", "snk_pt_build", "snk_pt_render", "snk_pt_synchronize", "snk_pt_trace_rays",
     "snk_pt_read_accumulator", "snk_pt_render_noalloc", "snk_pt_set_tuning", "snk_pt_get_tuning",
-    "snk_pt_autotune",
+    "snk_pt_autotune", "snk_pt_cache_reset", "snk_pt_cache_set_weights", "snk_pt_cache_get_weights",
+    "snk_pt_cache_set_bounds", "snk_pt_cache_encode", "snk_pt_cache_infer", "snk_pt_cache_train",
 ]
 
 
@@ -76,6 +77,7 @@ OUTPUT_DTYPES = {"radiance": np.float32, "albedo": np.float32, "normal": np.floa
                  "inst_id": np.uint32, "prim_id": np.uint32}
 
 NOALLOC_MAX_PATHS = 65536   # SNK_NOALLOC_MAX_PATHS
+CACHE_NUM_WEIGHTS = 16576   # SNK_CACHE_NUM_WEIGHTS
 
 _lib = None
 
@@ -109,6 +111,13 @@ def lib():
         L.snk_pt_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.snk_pt_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.snk_pt_autotune.argtypes = [vp, vp, u32, vp, u32, C.POINTER(Tuning)]
+        L.snk_pt_cache_reset.argtypes = [vp, u32]
+        L.snk_pt_cache_set_weights.argtypes = [vp, vp, u32]
+        L.snk_pt_cache_get_weights.argtypes = [vp, vp, u32]
+        L.snk_pt_cache_set_bounds.argtypes = [vp, vp, vp]
+        L.snk_pt_cache_encode.argtypes = [vp, vp, u32, vp, u32]
+        L.snk_pt_cache_infer.argtypes = [vp, vp, u32, vp, u32]
+        L.snk_pt_cache_train.argtypes = [vp, vp, u32, C.c_float, vp, C.POINTER(C.c_float), u32]
         _lib = L
     return _lib
 
@@ -230,6 +239,45 @@ class PathTracer:
 
     def synchronize(self):
         self._check(lib().snk_pt_synchronize(self._h))
+
+    # ---- MLP radiance cache --------------------------------------------------------
+    def cache_reset(self, seed: int = 1):
+        self._check(lib().snk_pt_cache_reset(self._h, seed))
+
+    def cache_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        self._check(lib().snk_pt_cache_set_weights(self._h, w.ctypes.data, w.size))
+
+    def cache_get_weights(self):
+        w = np.zeros(CACHE_NUM_WEIGHTS, np.float32)
+        self._check(lib().snk_pt_cache_get_weights(self._h, w.ctypes.data, w.size))
+        return w
+
+    def cache_set_bounds(self, lo, hi):
+        lo = np.ascontiguousarray(lo, np.float32)
+        hi = np.ascontiguousarray(hi, np.float32)
+        self._check(lib().snk_pt_cache_set_bounds(self._h, lo.ctypes.data, hi.ctypes.data))
+
+    def cache_encode(self, records):
+        r = np.ascontiguousarray(records, np.float32).reshape(-1, 16)
+        out = np.zeros((r.shape[0], 64), np.float32)
+        self._check(lib().snk_pt_cache_encode(self._h, r.ctypes.data, r.shape[0], out.ctypes.data, abi.MEM_HOST))
+        return out
+
+    def cache_infer(self, records):
+        r = np.ascontiguousarray(records, np.float32).reshape(-1, 16)
+        out = np.zeros((r.shape[0], 3), np.float32)
+        self._check(lib().snk_pt_cache_infer(self._h, r.ctypes.data, r.shape[0], out.ctypes.data, abi.MEM_HOST))
+        return out
+
+    def cache_train(self, samples, lr: float = 1e-2, want_grad: bool = False):
+        """One training step on host samples (n x 20 floats); returns (loss, grad or None)."""
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 20)
+        grad = np.zeros(CACHE_NUM_WEIGHTS, np.float32) if want_grad else None
+        loss = C.c_float()
+        self._check(lib().snk_pt_cache_train(self._h, s.ctypes.data, s.shape[0], lr,
+                                             None if grad is None else grad.ctypes.data, C.byref(loss), abi.MEM_HOST))
+        return loss.value, grad
 
     # ---- launch knobs ------------------------------------------------------------
     def set_tuning(self, tuning: "Tuning | dict"):

@@ -31,6 +31,7 @@ UNITS = {
     "pt_kernels.cu": True,
     "restir.cu": True,
     "noalloc.cu": False,
+    "mlp_cache.cu": False,
 }
 
 
