@@ -141,6 +141,84 @@ def cpu_baseline(scene, view, settings):
             "sample": f"one full 1920x1080 frame of the same workload ({rays} rays, {dt:.2f} s wall)"}
 
 
+def cache_vs_plain(pt_mod, abi, scenes, device, frames=120, check=(60,), ref_spp=4096, plain_max_spp=64):
+    """Second half of the metric: ms/frame to equal relMSE vs an FP64-accumulated
+    converged render, MLP cache vs plain, on the config-4 scene at 1080p.
+
+    The cache trains online along the 120-frame seeded spline (one cache frame per
+    spline frame).  At each checked frame: reference = FP64 mean of ref_spp plain
+    1-spp frames (depth 8); relMSE(x) = mean (x - ref)^2 / (ref^2 + 0.01); the
+    plain tracer's relMSE is measured for the mean of k 1-spp frames, k = 1..64,
+    and the k matching the cache's 1-spp relMSE is interpolated in log-log.
+    Frame times: CUDA events around each render call on the library's stream."""
+    import torch
+    W, H = 1920, 1080
+    sc = scenes.config4(width=W, height=H, frames=frames)
+    stream = torch.cuda.Stream(device=device)
+    pt = pt_mod.PathTracer(device.index or 0, stream=stream)
+    pt.load_scene(sc)
+    out = pt_mod.alloc_outputs(W, H, device=device, names=("radiance",))
+
+    def timed(view, st):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        pt.render([view], st, [out])
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def relmse(x, ref):
+        return float(np.mean((x[:, :3] - ref[:, :3]) ** 2 / (ref[:, :3] ** 2 + 1e-2)))
+
+    pt.cache_reset(1)
+    results = []
+    cache_ms = []
+    for f in range(frames):
+        v = sc.views[f]
+        st = abi.settings(mode=abi.MODE_PATH_CACHE, spp=1, max_depth=6, seed=10_000 + f, frame_index=f)
+        ms = timed(v, st)
+        if f >= 10:
+            cache_ms.append(ms)
+        if f not in check:
+            continue
+        x_cache = out["radiance"].cpu().numpy().astype(np.float64)
+        for k in range(ref_spp):   # converged reference of this frame
+            flags = abi.RENDER_ACCUMULATE_F64 | (abi.RENDER_RESET_ACCUM if k == 0 else 0)
+            pt.render([v], abi.settings(spp=1, max_depth=8, seed=500_000 + k, flags=flags), [{}])
+        ref, _ = pt.read_accumulator(W, H)
+        ref = ref.astype(np.float64)
+        acc = np.zeros((W * H, 4))
+        curve, plain_ms = {}, []
+        for k in range(1, plain_max_spp + 1):
+            plain_ms.append(timed(v, abi.settings(spp=1, max_depth=6, seed=900_000 + k)))
+            acc += out["radiance"].cpu().numpy()
+            if k & (k - 1) == 0:
+                curve[k] = relmse(acc / k, ref)
+        e_cache = relmse(x_cache, ref)
+        ks = sorted(curve)
+        k_eq = float(ks[-1])
+        for k0, k1 in zip(ks, ks[1:]):
+            if curve[k0] >= e_cache >= curve[k1]:
+                t = (np.log(curve[k0]) - np.log(e_cache)) / (np.log(curve[k0]) - np.log(curve[k1]))
+                k_eq = float(np.exp(np.log(k0) + t * (np.log(k1) - np.log(k0))))
+                break
+        if e_cache > curve[1]:
+            k_eq = curve[1] / e_cache
+        t_plain = float(np.median(plain_ms))
+        results.append({"frame": f, "cache_relmse_1spp": e_cache, "plain_relmse_vs_spp": curve,
+                        "plain_spp_for_equal_relmse": k_eq, "plain_ms_per_spp": t_plain,
+                        "plain_ms_for_equal_relmse": k_eq * t_plain,
+                        "mean_radiance": {"reference": float(ref[:, :3].mean()), "cache": float(x_cache[:, :3].mean())}})
+    t_cache = float(np.median(cache_ms))
+    ratio = float(np.mean([t_cache / r["plain_ms_for_equal_relmse"] for r in results]))
+    return {"metric": "ms/frame to equal relMSE vs converged: MLP-cache vs plain", "unit": "ratio",
+            "value": ratio, "higher_is_better": False, "cache_ms_per_frame": t_cache,
+            "workload": "config 4: 64 value-noise terrain tiles + 200 icospheres, 1920x1080, 1 spp, depth 6, "
+                        "cache MLP 64-4x64-3 BF16, 65536 samples/frame, Adam 1e-2, spread threshold 0.01",
+            "reference": f"FP64 mean of {ref_spp} plain 1-spp frames (depth 8)", "checked_frames": list(check),
+            "frames": frames, "checks": results}
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -320,6 +398,9 @@ def run_ours(args):
     if rank == 0:
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(sc, view, settings(1, 0))
+        if args.cache_eval != "off":
+            checks = (60,) if args.cache_eval == "quick" else tuple(range(9, 120, 10))
+            line["cache_vs_plain"] = cache_vs_plain(snkpt, abi, scenes, dev, check=checks)
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
@@ -335,6 +416,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--cache-eval", default="quick", choices=["off", "quick", "full"],
+                    help="MLP cache vs plain at equal relMSE: quick = one checked frame, full = every 10th frame")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -77,7 +77,10 @@ extern "C" {
 #define SNK_STAGE_RESTIR_GBUFFER  5
 #define SNK_STAGE_RESTIR_INITIAL  6
 #define SNK_STAGE_RESTIR_SPATIAL  7
-#define SNK_NUM_STAGES            8
+#define SNK_STAGE_CACHE_INFER     8
+#define SNK_STAGE_CACHE_SAMPLES   9
+#define SNK_STAGE_CACHE_TRAIN    10
+#define SNK_NUM_STAGES           12
 
 /* trace flags */
 #define SNK_TRACE_ANY_HIT 1u
@@ -185,7 +188,10 @@ typedef struct snk_render_settings {
     int32_t  restir_temporal;    /* num_temporal_resamples (0 disables temporal reuse) */
     int32_t  restir_spatial;     /* num_spatial_resamples */
     float    restir_radius;      /* spatial radius in pixels (30) */
-    uint32_t reserved[4];
+    uint32_t cache_train_paths;  /* SNK_MODE_PATH_CACHE: training paths per frame (0: 16384) */
+    uint32_t cache_train_steps;  /* Adam steps per frame over the 4 x paths samples (0: 4) */
+    float    cache_spread;       /* path-spread threshold c for cache termination (0: 0.01) */
+    float    cache_lr;           /* Adam learning rate (0: 1e-2; < 0: no update) */
 } snk_render_settings;
 
 /* Outputs of one view (RaytracingResources, RenderCommon.h:6-35, plus img_output).
@@ -244,8 +250,10 @@ typedef struct snk_pt_stats {
     double   last_render_ms;     /* device time of the last render (CUDA events) */
     uint32_t device_error;       /* last device error word (0 = none) */
     uint32_t pad;
-    double   stage_ms[8];        /* device time per stage of the last render (SNK_RENDER_PROFILE) */
-    uint64_t stage_launches[8];  /* kernel launches per stage of the last render */
+    double   stage_ms[12];       /* device time per stage of the last render (SNK_RENDER_PROFILE) */
+    uint64_t stage_launches[12]; /* kernel launches per stage of the last render */
+    uint64_t cache_queries;      /* paths terminated into the radiance cache */
+    uint64_t cache_samples;      /* training samples of the last frame */
 } snk_pt_stats;
 
 /* Launch knobs of the wavefront (0 = default).  The reference has no equivalent:

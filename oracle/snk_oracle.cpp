@@ -21,7 +21,8 @@
 // Not in the reference (specified by the project):
 //   watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2(1) 2013)
 //   PCG32 (O'Neill 2014, pcg32_random_r / pcg32_srandom_r), splitmix64 keying
-//   unbiased path tracer with NEE replacing the biased BounceDiffuse (RayGen.rgen:139-213)
+//   unbiased path tracer with NEE replacing the biased BounceDiffuse (RayGen.rgen:139-213),
+//   continuation sampled from a GGX-NDF / cosine mixture
 //   binned-SAH BVH (its shape does not affect results: closest hit is the
 //   minimum of (t, instance, triangle) over all valid triangle hits)
 //
@@ -59,7 +60,8 @@ struct View {
 };
 struct Settings {
     uint32_t mode, spp, max_depth, rr_depth, seed, frame_index, flags, restir_candidates, restir_mcap;
-    int32_t restir_temporal, restir_spatial; float restir_radius; uint32_t reserved[4];
+    int32_t restir_temporal, restir_spatial; float restir_radius;
+    uint32_t cache_train_paths, cache_train_steps; float cache_spread, cache_lr;
 };
 struct Ray { float ox, oy, oz, tmin, dx, dy, dz, tmax; };
 struct Hit { float t; uint32_t inst, prim; float u, v; uint32_t flags; };
@@ -838,6 +840,52 @@ static bool sample_local(const Scene& S, const Surface& s, V3 v, V3 f0, V3 xb, f
     return true;
 }
 
+// Continuation direction: with probability p_spec a GGX half-vector sample of
+// the reference's DistributionGGX (LightBuffers.glsl:69-80, roughness^2 = alpha),
+// otherwise cosine-weighted; weight = albedo * CookTorrance(l) / mixture pdf
+// (the reference's BRDF with albedo on both terms, RayGen.rgen:273).
+static inline bool sample_continuation(const Surface& s, V3 v, V3 f0, float u_lobe, float u1, float u2, V3* wi,
+                                       V3* weight, float* pdf_out) {
+    const float p_spec = s.metallic > 0.5f ? 0.75f : 0.25f;
+    V3 b1, b2;
+    onb(s.n, &b1, &b2);
+    float sp, cp;
+    sincos2pi(u2, &sp, &cp);
+    V3 l;
+    if (u_lobe < p_spec) {
+        float a = s.roughness * s.roughness;
+        float a2 = a * a;
+        float cos2 = (1.0f - u1) / (1.0f + (a2 - 1.0f) * u1);
+        float ch = std::sqrt(cos2);
+        float sh = std::sqrt(fmaxf_(0.0f, 1.0f - cos2));
+        float hx = sh * cp, hy = sh * sp;
+        V3 h = v3((b1.x * hx + b2.x * hy) + s.n.x * ch, (b1.y * hx + b2.y * hy) + s.n.y * ch,
+                  (b1.z * hx + b2.z * hy) + s.n.z * ch);
+        float vh2 = 2.0f * dot(v, h);
+        l = sub(mul(h, vh2), v);
+    } else {
+        float r = std::sqrt(u1);
+        float lx = r * cp, ly = r * sp, lz = std::sqrt(fmaxf_(0.0f, 1.0f - u1));
+        l = v3((b1.x * lx + b2.x * ly) + s.n.x * lz, (b1.y * lx + b2.y * ly) + s.n.y * lz,
+               (b1.z * lx + b2.z * ly) + s.n.z * lz);
+    }
+    if (!(dot(l, s.ng) > 0.0f)) return false;
+    float ndl = dot(s.n, l);
+    if (!(ndl > 0.0f)) return false;
+    V3 vl = add(v, l);
+    float vl2 = dot(vl, vl);
+    V3 hh = vl2 > 0.0f ? divs(vl, std::sqrt(vl2)) : s.n;
+    float D = distribution_ggx(hh, s.n, s.roughness);
+    float pdf_spec = (D * fmaxf_(dot(s.n, hh), 0.0f)) / (4.0f * fmaxf_(dot(v, hh), 1e-6f));
+    float pdf = p_spec * pdf_spec + (1.0f - p_spec) * (ndl / PI);
+    if (!(pdf > 0.0f)) return false;
+    V3 ct = cook_torrance(brdf_terms(l, v, f0, s.n, s.roughness, s.metallic));
+    *weight = v3((s.albedo.x * ct.x) / pdf, (s.albedo.y * ct.y) / pdf, (s.albedo.z * ct.z) / pdf);
+    *wi = l;
+    *pdf_out = pdf;
+    return true;
+}
+
 static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uint32_t pixel_key, uint32_t sample,
                      const Settings& st, GSample* g, Counters* ctr) {
     Pcg rng = pcg_stream(pixel_key, sample, 0, st.seed);
@@ -860,6 +908,7 @@ static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uin
         }
         float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
         float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
+        float u_lobe = pcg_float(rng);
         if (s.flags & MAT_EMISSIVE) {
             if (d == 0) L = add(L, cmul(beta, s.albedo));
             break;
@@ -886,18 +935,9 @@ static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uin
             if (!(u_rr < p)) break;
             beta = v3(beta.x / p, beta.y / p, beta.z / p);
         }
-        float r = std::sqrt(u_d1);
-        float sp, cp;
-        sincos2pi(u_d2, &sp, &cp);
-        float lx = r * cp, ly = r * sp, lz = std::sqrt(fmaxf_(0.0f, 1.0f - u_d1));
-        V3 b1, b2;
-        onb(s.n, &b1, &b2);
-        V3 wi = v3((b1.x * lx + b2.x * ly) + s.n.x * lz, (b1.y * lx + b2.y * ly) + s.n.y * lz,
-                   (b1.z * lx + b2.z * ly) + s.n.z * lz);
-        if (!(dot(wi, s.ng) > 0.0f)) break;
-        Terms tm = brdf_terms(wi, v, f0, s.n, s.roughness, s.metallic);
-        V3 w = v3(s.albedo.x * (tm.kd.x + tm.spec.x * PI), s.albedo.y * (tm.kd.y + tm.spec.y * PI),
-                  s.albedo.z * (tm.kd.z + tm.spec.z * PI));
+        V3 wi, w;
+        float pdf;
+        if (!sample_continuation(s, v, f0, u_lobe, u_d1, u_d2, &wi, &w, &pdf)) break;
         beta = cmul(beta, w);
         ro = xb;
         rd = wi;

@@ -118,9 +118,15 @@ struct snk_pt_ctx {
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {1, 1, 1};
     DBuf<float4> cache_in;
     DBuf<float> cache_out, cache_grad;
+    DBuf<float2> c_spread;
+    DBuf<float4> c_qrec, c_qbeta, c_trec, c_tbeta, c_tL, c_samples;
+    uint64_t last_cache_samples = 0;
 };
 
 namespace {
+
+EncodeParams cache_encode_params(snk_pt_ctx* ctx);
+Status cache_ensure(snk_pt_ctx* ctx);
 
 int fail(snk_pt_ctx* c, int code, const std::string& msg) {
     if (c) c->err = msg;
@@ -651,9 +657,10 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     if (!views || !settings || !outputs || num_views == 0 || num_views > MAX_VIEWS)
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad views/settings/outputs");
     const snk_render_settings& rs = *settings;
-    if (rs.mode != SNK_MODE_PATH && rs.mode != SNK_MODE_RESTIR_DI)
+    if (rs.mode != SNK_MODE_PATH && rs.mode != SNK_MODE_RESTIR_DI && rs.mode != SNK_MODE_PATH_CACHE)
         return fail(ctx, SNK_ERR_UNSUPPORTED, "render: mode not supported by this entry point");
-    if (rs.mode == SNK_MODE_PATH && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
+    const bool path_like = rs.mode == SNK_MODE_PATH || rs.mode == SNK_MODE_PATH_CACHE;
+    if (path_like && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: spp must be >= 1 and 1 <= max_depth <= 16");
     uint64_t n_pixels = 0;
     for (uint32_t v = 0; v < num_views; v++) {
@@ -661,12 +668,16 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         if (outputs[v].memory > SNK_MEM_HOST) return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad memory space");
         n_pixels += (uint64_t)views[v].width * views[v].height;
     }
-    const uint32_t spp = rs.mode == SNK_MODE_PATH ? rs.spp : 1u;
+    const uint32_t spp = path_like ? rs.spp : 1u;
     if (n_pixels * spp >= (1ull << 31)) return fail(ctx, SNK_ERR_INVALID_ARG, "render: too many paths");
     API_TRY(set_device(ctx));
     API_TRY(ensure_built(ctx));
     cudaStream_t st = ctx->stream;
-    const uint32_t n_paths = (uint32_t)(n_pixels * spp);
+    const bool cache = rs.mode == SNK_MODE_PATH_CACHE;
+    const uint32_t n_train = cache ? (rs.cache_train_paths ? rs.cache_train_paths : 16384u) : 0u;
+    if (n_train > (1u << 22)) return fail(ctx, SNK_ERR_INVALID_ARG, "render: too many cache training paths");
+    const uint32_t n_render = (uint32_t)(n_pixels * spp);
+    const uint32_t n_paths = n_render + n_train;
 
     // per-view device descriptors (host outputs go through staging buffers)
     std::vector<ViewDev> vd(num_views);
@@ -737,7 +748,30 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         cudaMemsetAsync(ctx->trav.p, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess)
         return fail(ctx, SNK_ERR_CUDA, "counter reset");
 
-    if (rs.mode == SNK_MODE_PATH) {
+    if (path_like) {
+        if (cache) {
+            API_TRY(cache_ensure(ctx));
+            const size_t nv = (size_t)n_train * TRAIN_V;
+            if (ctx->c_spread.reserve(n_paths) || ctx->c_qrec.reserve(4ull * n_render) || ctx->c_qbeta.reserve(n_render) ||
+                ctx->c_trec.reserve(4 * nv) || ctx->c_tbeta.reserve(nv) || ctx->c_tL.reserve(nv) ||
+                ctx->c_samples.reserve(5 * nv))
+                return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "render: cache buffers");
+            F.cache = 1;
+            F.n_render = n_render;
+            F.n_train = n_train;
+            F.frame = rs.frame_index;
+            F.spread_c = rs.cache_spread > 0.0f ? rs.cache_spread : 0.01f;
+            F.spread = ctx->c_spread.p;
+            F.qrec = ctx->c_qrec.p;
+            F.qbeta = ctx->c_qbeta.p;
+            F.train_rec = ctx->c_trec.p;
+            F.train_beta = ctx->c_tbeta.p;
+            F.train_L = ctx->c_tL.p;
+            F.samples = ctx->c_samples.p;
+            if (cudaMemsetAsync(F.train_beta, 0, nv * sizeof(float4), st) ||
+                cudaMemsetAsync(F.train_L, 0, nv * sizeof(float4), st))
+                return fail(ctx, SNK_ERR_CUDA, "render: cache buffer reset");
+        }
         if (ctx->rays0.reserve(2ull * n_paths) || ctx->rays1.reserve(2ull * n_paths) || ctx->pid0.reserve(n_paths) ||
             ctx->pid1.reserve(n_paths) || ctx->hits.reserve(n_paths) || ctx->beta.reserve(n_paths) ||
             ctx->L.reserve(n_paths) || ctx->srays.reserve(4ull * n_paths) || ctx->scontrib.reserve(2ull * n_paths))
@@ -757,7 +791,32 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
                            [&] { return launch_trace_shadow(F, d, g16, count_nodes, st); });
         }
+        if (cache && e == cudaSuccess) {
+            const EncodeParams ep = cache_encode_params(ctx);
+            e = staged(ctx, profile, SNK_STAGE_CACHE_INFER, [&] {
+                Status s = mlp_infer(ctx->mlp, F.qrec, F.counters + CNT_CACHE_QUERIES, 0u, ep, nullptr, F.qbeta, F.L,
+                                     grid_of(ctx, 4), st);
+                return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
+            });
+        }
         if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_RESOLVE, [&] { return launch_resolve(F, g8, st); });
+        if (cache && e == cudaSuccess) {
+            e = staged(ctx, profile, SNK_STAGE_CACHE_SAMPLES, [&] { return launch_make_samples(F, g8, st); });
+            const EncodeParams ep = cache_encode_params(ctx);
+            const uint32_t steps = rs.cache_train_steps ? rs.cache_train_steps : 4u;
+            const uint32_t total = n_train * TRAIN_V, chunk = (total + steps - 1) / steps;
+            // cache_lr: 0 -> 1e-2; negative -> the network is not updated (gradients only)
+            const float lr = rs.cache_lr > 0.0f ? rs.cache_lr : (rs.cache_lr < 0.0f ? 0.0f : 1e-2f);
+            for (uint32_t k = 0; k < steps && e == cudaSuccess; k++) {
+                const uint32_t b = k * chunk, cnt = b < total ? std::min(chunk, total - b) : 0u;
+                if (cnt == 0) break;
+                e = staged(ctx, profile, SNK_STAGE_CACHE_TRAIN, [&] {
+                    Status s = mlp_train_step(ctx->mlp, F.samples + 5ull * b, cnt, ep, lr, nullptr, nullptr, st);
+                    return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
+                });
+            }
+            ctx->last_cache_samples = total;
+        }
         cudaEventRecord(ctx->ev1, st);
         if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
     } else {
@@ -909,6 +968,7 @@ int snk_pt_autotune(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, 
     return SNK_OK;
 }
 
+extern "C++" {
 namespace {
 
 EncodeParams cache_encode_params(snk_pt_ctx* ctx) {
@@ -951,6 +1011,7 @@ Status cache_stage(snk_pt_ctx* ctx, const float* src, uint32_t n, uint32_t float
 }
 
 }  // namespace
+}  // extern "C++"
 
 int snk_pt_cache_reset(snk_pt_ctx* ctx, uint32_t seed) {
     if (!ctx) return SNK_ERR_INVALID_ARG;
@@ -1109,7 +1170,9 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
         ctx->counters_pending = false;
     }
     const uint32_t* c = ctx->h_counters;
-    if (ctx->last_mode == SNK_MODE_PATH) {
+    out->cache_queries = ctx->last_mode == SNK_MODE_PATH_CACHE ? c[CNT_CACHE_QUERIES] : 0;
+    out->cache_samples = ctx->last_mode == SNK_MODE_PATH_CACHE ? ctx->last_cache_samples : 0;
+    if (ctx->last_mode == SNK_MODE_PATH || ctx->last_mode == SNK_MODE_PATH_CACHE) {
         out->rays_camera = ctx->last_paths;
         uint64_t ext = 0;
         for (uint32_t d = 1; d < ctx->last_depth; d++) ext += c[CNT_QUEUE + d];

@@ -9,12 +9,12 @@
 //   - emission counted on camera hits only; every vertex does NEE toward the
 //     directional light (as RayClosestHit.rchit:136) and one power-sampled local
 //     light (sphere light or emissive triangle);
-//   - continuation is cosine-weighted; its weight f cos / pdf is
-//     albedo * (kd + pi * specular) for the reference's CookTorranceBRDF with
-//     albedo applied to both terms (RayGen.rgen:273);
+//   - continuation samples a GGX-NDF / cosine mixture; its weight is
+//     albedo * CookTorranceBRDF(l) / pdf for the reference's BRDF with albedo
+//     applied to both terms (RayGen.rgen:273);
 //   - russian roulette from segment rr_depth with survival min(max(beta), 0.95).
 // Random numbers: PCG32 streams keyed by (pixel, sample, segment, seed); each
-// vertex draws 6 numbers, the camera segment 2 more for the pixel jitter.
+// vertex draws 7 numbers, the camera segment 2 more for the pixel jitter.
 #include "snk_frame.h"
 
 namespace snk {
@@ -22,15 +22,27 @@ namespace {
 
 constexpr int BLK = 256;
 
-__device__ __forceinline__ void decode_path(const FrameParams& F, uint32_t p, uint32_t* gpix, uint32_t* s,
+// Path p -> (global pixel, sample key, view, x, y).  In radiance-cache mode the
+// paths from n_render on are training paths: pixel chosen by a hash of (path,
+// frame), sample key 0x40000000 | index (its own random streams, jittered ray,
+// no G-buffer writes).
+__device__ __forceinline__ bool decode_path(const FrameParams& F, uint32_t p, uint32_t* gpix, uint32_t* s,
                                             uint32_t* vi, uint32_t* x, uint32_t* y) {
-    *gpix = p / F.spp;
-    *s = p - *gpix * F.spp;
+    bool train = F.cache && p >= F.n_render;
+    if (!train) {
+        *gpix = p / F.spp;
+        *s = p - *gpix * F.spp;
+    } else {
+        const uint32_t tid = p - F.n_render;
+        *gpix = (uint32_t)(splitmix64(((uint64_t)F.frame << 32) | tid) % (uint64_t)F.n_pixels);
+        *s = 0x40000000u | tid;
+    }
     *vi = find_view(F.views, F.nviews, *gpix);
     const ViewDev& V = F.views[*vi];
     uint32_t local = *gpix - V.pixel_offset;
     *x = local % V.v.width;
     *y = local / V.v.width;
+    return train;
 }
 
 __global__ void __launch_bounds__(BLK) k_generate(FrameParams F) {
@@ -48,6 +60,7 @@ __global__ void __launch_bounds__(BLK) k_generate(FrameParams F) {
         F.path_ids[0][p] = p;
         F.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         F.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (F.cache) F.spread[p] = make_float2(0.0f, 0.0f);
     }
 }
 
@@ -85,13 +98,14 @@ __global__ void __launch_bounds__(BLK) k_shade(FrameParams F, uint32_t d) {
     const SceneDev& S = F.S;
     for (uint32_t base = warp_global * 32u; base < n; base += nwarps * 32u) {
         const uint32_t i = base + lane;
-        bool cont = false, sv0 = false, sv1 = false;
+        bool cont = false, sv0 = false, sv1 = false, query = false;
         uint32_t p = 0;
         float4 nr0 = make_float4(0, 0, 0, 0), nr1 = make_float4(0, 0, 0, 0);
+        float4 q0, q1, q2, q3, qb;
         if (i < n) {
             p = F.path_ids[cur][i];
             uint32_t gpix, s, vi, x, y;
-            decode_path(F, p, &gpix, &s, &vi, &x, &y);
+            const bool train = decode_path(F, p, &gpix, &s, &vi, &x, &y);
             const ViewDev& V = F.views[vi];
             const uint32_t o = y * V.v.width + x;
             float4 rd4 = F.rays[cur][2ull * i + 1];
@@ -102,16 +116,46 @@ __global__ void __launch_bounds__(BLK) k_shade(FrameParams F, uint32_t d) {
             sr[3].w = -1.0f;
             Pcg rng = pcg_stream(gpix, s, d, F.seed);
             if (d == 0) { pcg_next(rng); pcg_next(rng); }
+            const bool gbuf = d == 0 && s == 0 && !train;
             if (!h.flags) {
-                if (d == 0 && s == 0) write_gbuffer_miss(V, o);
+                if (gbuf) write_gbuffer_miss(V, o);
             } else {
                 Surface sf = surface_at(S, h.inst, h.prim, h.u, h.v, rd);
-                if (d == 0 && s == 0) write_gbuffer_hit(V, o, sf, h.t, motion_of(S, V.v, sf, x, y));
+                if (gbuf) write_gbuffer_hit(V, o, sf, h.t, motion_of(S, V.v, sf, x, y));
                 float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
                 float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
+                float u_lobe = pcg_float(rng);
                 float4 b4 = F.beta[p];
                 V3 beta = v3(b4.x, b4.y, b4.z);
-                if (sf.flags & MAT_EMISSIVE) {
+                bool to_cache = false;
+                if (F.cache) {
+                    // path spread (Mueller et al. 2021): a0 = t^2 / (4 pi cos) at the primary
+                    // vertex; later vertices add sqrt(t^2 / (pdf cos)); the path is handed
+                    // to the cache once spread^2 > c a0
+                    float2 sp = F.spread[p];
+                    const float cosv = fmax_(fabsf(dot(sf.n, rd)), 1e-6f);
+                    if (d == 0) sp = make_float2((h.t * h.t) / ((4.0f * PI) * cosv), 0.0f);
+                    else sp.y = sp.y + sqrtf((h.t * h.t) / (fmax_(b4.w, 1e-6f) * cosv));
+                    F.spread[p] = sp;
+                    to_cache = !train && d >= 1 && !(sf.flags & MAT_EMISSIVE) && (sp.y * sp.y > F.spread_c * sp.x);
+                    if (train && d < TRAIN_V && !(sf.flags & MAT_EMISSIVE)) {
+                        const uint32_t slot = (p - F.n_render) * TRAIN_V + d;
+                        float4* r = F.train_rec + 4ull * slot;
+                        r[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, sf.roughness);
+                        r[1] = make_float4(-rd.x, -rd.y, -rd.z, sf.metallic);
+                        r[2] = make_float4(sf.n.x, sf.n.y, sf.n.z, 0.0f);
+                        r[3] = make_float4(sf.albedo.x, sf.albedo.y, sf.albedo.z, 0.0f);
+                        F.train_beta[slot] = make_float4(beta.x, beta.y, beta.z, 1.0f);
+                    }
+                }
+                if (to_cache) {
+                    q0 = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, sf.roughness);
+                    q1 = make_float4(-rd.x, -rd.y, -rd.z, sf.metallic);
+                    q2 = make_float4(sf.n.x, sf.n.y, sf.n.z, 0.0f);
+                    q3 = make_float4(sf.albedo.x, sf.albedo.y, sf.albedo.z, __uint_as_float(p));
+                    qb = make_float4(beta.x, beta.y, beta.z, 0.0f);
+                    query = true;
+                } else if (sf.flags & MAT_EMISSIVE) {
                     if (d == 0) {
                         float4 l4 = F.L[p];
                         V3 Lp = add(v3(l4.x, l4.y, l4.z), cmul(beta, sf.albedo));
@@ -148,20 +192,12 @@ __global__ void __launch_bounds__(BLK) k_shade(FrameParams F, uint32_t d) {
                         else alive = false;
                     }
                     if (alive) {
-                        float r = sqrtf(u_d1);
-                        float sp, cp;
-                        sincos2pi(u_d2, &sp, &cp);
-                        float lx = r * cp, ly = r * sp, lz = sqrtf(fmax_(0.0f, 1.0f - u_d1));
-                        V3 b1, b2;
-                        onb(sf.n, &b1, &b2);
-                        V3 wi = v3((b1.x * lx + b2.x * ly) + sf.n.x * lz, (b1.y * lx + b2.y * ly) + sf.n.y * lz,
-                                   (b1.z * lx + b2.z * ly) + sf.n.z * lz);
-                        if (dot(wi, sf.ng) > 0.0f) {
-                            Terms tm = brdf_terms(wi, v, f0, sf.n, sf.roughness, sf.metallic);
-                            V3 w = v3(sf.albedo.x * (tm.kd.x + tm.spec.x * PI), sf.albedo.y * (tm.kd.y + tm.spec.y * PI),
-                                      sf.albedo.z * (tm.kd.z + tm.spec.z * PI));
+                        V3 wi, w;
+                        float pdf;
+                        if (sample_continuation(sf, v, f0, u_lobe, u_d1, u_d2, &wi, &w, &pdf)) {
                             beta = cmul(beta, w);
-                            F.beta[p] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+                            // w: pdf of the sampled direction, used by the spread heuristic
+                            F.beta[p] = make_float4(beta.x, beta.y, beta.z, pdf);
                             nr0 = make_float4(xb.x, xb.y, xb.z, EXT_TMIN);
                             nr1 = make_float4(wi.x, wi.y, wi.z, T_FAR);
                             cont = true;
@@ -186,6 +222,45 @@ __global__ void __launch_bounds__(BLK) k_shade(FrameParams F, uint32_t d) {
             F.rays[nxt][2ull * j + 1] = nr1;
             F.path_ids[nxt][j] = p;
         }
+        if (F.cache) {
+            const unsigned qm = __ballot_sync(full, query);
+            uint32_t qbase = 0;
+            if (lane == 0 && qm) qbase = atomicAdd(&F.counters[CNT_CACHE_QUERIES], (uint32_t)__popc(qm));
+            qbase = __shfl_sync(full, qbase, 0);
+            if (query) {
+                const uint32_t j = qbase + __popc(qm & ((1u << lane) - 1u));
+                F.qrec[4ull * j] = q0;
+                F.qrec[4ull * j + 1] = q1;
+                F.qrec[4ull * j + 2] = q2;
+                F.qrec[4ull * j + 3] = q3;
+                F.qbeta[j] = qb;
+            }
+        }
+    }
+}
+
+// training samples of the cache: target at recorded vertex i of a training path =
+// (radiance gathered at vertices i, i+1, ...) / throughput at i; weight 0 when the
+// vertex was not reached or its throughput has a zero channel
+__global__ void __launch_bounds__(BLK) k_make_samples(FrameParams F) {
+    const uint32_t n = F.n_train * TRAIN_V;
+    for (uint32_t idx = blockIdx.x * BLK + threadIdx.x; idx < n; idx += gridDim.x * BLK) {
+        const uint32_t tid = idx / TRAIN_V, i = idx - tid * TRAIN_V;
+        const float4 b = F.train_beta[idx];
+        const bool valid = b.w != 0.0f && b.x > 0.0f && b.y > 0.0f && b.z > 0.0f;
+        float4 sum = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (uint32_t k = i; k < TRAIN_V; k++) {
+            const float4 l = F.train_L[tid * TRAIN_V + k];
+            sum = make_float4(sum.x + l.x, sum.y + l.y, sum.z + l.z, 0.0f);
+        }
+        float4* s = F.samples + 5ull * idx;
+        const float4* r = F.train_rec + 4ull * idx;
+        const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        s[0] = valid ? r[0] : z;
+        s[1] = valid ? r[1] : z;
+        s[2] = valid ? r[2] : z;
+        s[3] = valid ? r[3] : z;
+        s[4] = valid ? make_float4(sum.x / b.x, sum.y / b.y, sum.z / b.z, 1.0f) : z;
     }
 }
 
@@ -223,6 +298,10 @@ cudaError_t launch_shade(const FrameParams& F, uint32_t depth, int grid, cudaStr
 }
 cudaError_t launch_resolve(const FrameParams& F, int grid, cudaStream_t s) {
     k_resolve<<<grid, BLK, 0, s>>>(F);
+    return cudaGetLastError();
+}
+cudaError_t launch_make_samples(const FrameParams& F, int grid, cudaStream_t s) {
+    k_make_samples<<<grid, BLK, 0, s>>>(F);
     return cudaGetLastError();
 }
 

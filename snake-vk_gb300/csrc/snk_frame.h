@@ -14,7 +14,9 @@ constexpr uint32_t CNT_QUEUE = 0;         // [d]: rays queued for segment d
 constexpr uint32_t CNT_WORK_TRACE = 16;   // [d]: work fetch of the closest-hit pass of segment d
 constexpr uint32_t CNT_WORK_SHADOW = 32;  // [d]: work fetch of the shadow pass of segment d
 constexpr uint32_t CNT_SHADOW_RAYS = 48;  // valid shadow rays
+constexpr uint32_t CNT_CACHE_QUERIES = 49; // paths terminated into the radiance cache
 constexpr uint32_t CNT_TOTAL = 64;
+constexpr uint32_t TRAIN_V = 4;           // recorded vertices per cache training path
 
 struct HitDev { float t; uint32_t inst, prim; float u, v; uint32_t flags; };
 static_assert(sizeof(HitDev) == 24, "hit layout");
@@ -46,12 +48,23 @@ struct FrameParams {
     unsigned long long* trav_counters;   // closest: [0] nodes [1] triangles; shadow: [2] [3]
     double2* accum;          // FP64 accumulator of view 0 (2 double2 per pixel)
     TraceTuning tune;
+    // radiance cache mode: paths [0, n_render) render pixels, [n_render, n_paths) train
+    uint32_t cache, n_render, n_train, frame;
+    float spread_c;
+    float2* spread;          // per path: (a0, accumulated spread)
+    float4* qrec;            // 4 float4 per cache query (record), path id in qrec[3].w
+    float4* qbeta;           // throughput of each query
+    float4* train_rec;       // n_train * TRAIN_V records (4 float4)
+    float4* train_beta;      // n_train * TRAIN_V (throughput, valid)
+    float4* train_L;         // n_train * TRAIN_V radiance gathered at each vertex
+    float4* samples;         // n_train * TRAIN_V training samples (5 float4)
 };
 
 // launch helpers (defined in pt_kernels.cu / trace_kernels.cu / restir.cu)
 cudaError_t launch_generate(const FrameParams& F, int grid, cudaStream_t s);
 cudaError_t launch_shade(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s);
 cudaError_t launch_resolve(const FrameParams& F, int grid, cudaStream_t s);
+cudaError_t launch_make_samples(const FrameParams& F, int grid, cudaStream_t s);
 cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
 cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
 cudaError_t launch_trace_rays(const SceneDev& S, const float4* rays, uint32_t n, HitDev* hits, bool any,

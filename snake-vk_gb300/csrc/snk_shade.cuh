@@ -179,6 +179,52 @@ __device__ __forceinline__ bool sample_local(const SceneDev& S, const Surface& s
     return true;
 }
 
+// Continuation direction: with probability p_spec a GGX half-vector sample of
+// the reference's DistributionGGX (LightBuffers.glsl:69-80, roughness^2 = alpha),
+// otherwise cosine-weighted; weight = albedo * CookTorrance(l) / mixture pdf
+// (the reference's BRDF with albedo on both terms, RayGen.rgen:273).
+__device__ __forceinline__ bool sample_continuation(const Surface& s, V3 v, V3 f0, float u_lobe, float u1, float u2,
+                                                    V3* wi, V3* weight, float* pdf_out) {
+    const float p_spec = s.metallic > 0.5f ? 0.75f : 0.25f;
+    V3 b1, b2;
+    onb(s.n, &b1, &b2);
+    float sp, cp;
+    sincos2pi(u2, &sp, &cp);
+    V3 l;
+    if (u_lobe < p_spec) {
+        float a = s.roughness * s.roughness;
+        float a2 = a * a;
+        float cos2 = (1.0f - u1) / (1.0f + (a2 - 1.0f) * u1);
+        float ch = sqrtf(cos2);
+        float sh = sqrtf(fmax_(0.0f, 1.0f - cos2));
+        float hx = sh * cp, hy = sh * sp;
+        V3 h = v3((b1.x * hx + b2.x * hy) + s.n.x * ch, (b1.y * hx + b2.y * hy) + s.n.y * ch,
+                  (b1.z * hx + b2.z * hy) + s.n.z * ch);
+        float vh2 = 2.0f * dot(v, h);
+        l = sub(mul(h, vh2), v);
+    } else {
+        float r = sqrtf(u1);
+        float lx = r * cp, ly = r * sp, lz = sqrtf(fmax_(0.0f, 1.0f - u1));
+        l = v3((b1.x * lx + b2.x * ly) + s.n.x * lz, (b1.y * lx + b2.y * ly) + s.n.y * lz,
+               (b1.z * lx + b2.z * ly) + s.n.z * lz);
+    }
+    if (!(dot(l, s.ng) > 0.0f)) return false;
+    float ndl = dot(s.n, l);
+    if (!(ndl > 0.0f)) return false;
+    V3 vl = add(v, l);
+    float vl2 = dot(vl, vl);
+    V3 hh = vl2 > 0.0f ? divs(vl, sqrtf(vl2)) : s.n;
+    float D = distribution_ggx(hh, s.n, s.roughness);
+    float pdf_spec = (D * fmax_(dot(s.n, hh), 0.0f)) / (4.0f * fmax_(dot(v, hh), 1e-6f));
+    float pdf = p_spec * pdf_spec + (1.0f - p_spec) * (ndl / PI);
+    if (!(pdf > 0.0f)) return false;
+    V3 ct = cook_torrance(brdf_terms(l, v, f0, s.n, s.roughness, s.metallic));
+    *weight = v3((s.albedo.x * ct.x) / pdf, (s.albedo.y * ct.y) / pdf, (s.albedo.z * ct.z) / pdf);
+    *wi = l;
+    *pdf_out = pdf;
+    return true;
+}
+
 // CalcPointlight (LightBuffers.glsl:147-157)
 __device__ __forceinline__ V3 calc_pointlight(const PointLightDev& L, V3 v, V3 f0, V3 world_pos, V3 n, float roughness,
                                               float metallic, V3 albedo) {

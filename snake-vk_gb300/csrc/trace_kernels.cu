@@ -196,6 +196,13 @@ __global__ void __launch_bounds__(256) k_accum_shadow(FrameParams F, uint32_t d)
         if (c0.w != 0.0f) l = make_float4(l.x + c0.x, l.y + c0.y, l.z + c0.z, 0.0f);
         if (c1.w != 0.0f) l = make_float4(l.x + c1.x, l.y + c1.y, l.z + c1.z, 0.0f);
         F.L[p] = l;
+        if (F.cache && p >= F.n_render) {   // radiance gathered at this vertex of a training path
+            const uint32_t slot = (p - F.n_render) * TRAIN_V + (d < TRAIN_V - 1 ? d : TRAIN_V - 1);
+            float4 v = F.train_L[slot];
+            if (c0.w != 0.0f) v = make_float4(v.x + c0.x, v.y + c0.y, v.z + c0.z, 0.0f);
+            if (c1.w != 0.0f) v = make_float4(v.x + c1.x, v.y + c1.y, v.z + c1.z, 0.0f);
+            F.train_L[slot] = v;
+        }
     }
 }
 

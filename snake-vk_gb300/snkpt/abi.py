@@ -60,7 +60,8 @@ SETTINGS_DTYPE = np.dtype([
     ("mode", "<u4"), ("spp", "<u4"), ("max_depth", "<u4"), ("rr_depth", "<u4"),
     ("seed", "<u4"), ("frame_index", "<u4"), ("flags", "<u4"), ("restir_candidates", "<u4"),
     ("restir_mcap", "<u4"), ("restir_temporal", "<i4"), ("restir_spatial", "<i4"),
-    ("restir_radius", "<f4"), ("reserved", "<u4", (4,)),
+    ("restir_radius", "<f4"), ("cache_train_paths", "<u4"), ("cache_train_steps", "<u4"),
+    ("cache_spread", "<f4"), ("cache_lr", "<f4"),
 ])
 assert SETTINGS_DTYPE.itemsize == 64
 
@@ -77,11 +78,12 @@ STATS_DTYPE = np.dtype([
     ("shadow_triangle_tests", "<u8"), ("wide_nodes", "<u8"),
     ("triangles", "<u8"), ("instances", "<u8"), ("blas_sah_cost", "<f8"),
     ("last_render_ms", "<f8"), ("device_error", "<u4"), ("pad", "<u4"),
-    ("stage_ms", "<f8", (8,)), ("stage_launches", "<u8", (8,)),
+    ("stage_ms", "<f8", (12,)), ("stage_launches", "<u8", (12,)), ("cache_queries", "<u8"),
+    ("cache_samples", "<u8"),
 ])
-assert STATS_DTYPE.itemsize == 232
+assert STATS_DTYPE.itemsize == 312
 STAGES = ("generate", "trace_closest", "shade", "trace_shadow", "resolve", "restir_gbuffer", "restir_initial",
-          "restir_spatial")
+          "restir_spatial", "cache_infer", "cache_samples", "cache_train", "unused")
 
 MODE_PATH, MODE_RESTIR_DI, MODE_PATH_CACHE = 0, 1, 2
 RENDER_ACCUMULATE_F64, RENDER_RESET_ACCUM, RENDER_COUNT_NODES, RENDER_USE_GRAPH, RENDER_PROFILE = 1, 2, 4, 8, 16
@@ -93,10 +95,13 @@ INVALID_INDEX = 0xFFFFFFFF
 
 def settings(mode=MODE_PATH, spp=1, max_depth=4, rr_depth=3, seed=1, frame_index=0, flags=0,
              restir_candidates=32, restir_mcap=20, restir_temporal=1, restir_spatial=5,
-             restir_radius=30.0) -> np.ndarray:
+             restir_radius=30.0, cache_train_paths=0, cache_train_steps=0, cache_spread=0.0,
+             cache_lr=0.0) -> np.ndarray:
     s = np.zeros((), SETTINGS_DTYPE)
     s["mode"], s["spp"], s["max_depth"], s["rr_depth"] = mode, spp, max_depth, rr_depth
     s["seed"], s["frame_index"], s["flags"] = seed, frame_index, flags
     s["restir_candidates"], s["restir_mcap"] = restir_candidates, restir_mcap
     s["restir_temporal"], s["restir_spatial"], s["restir_radius"] = restir_temporal, restir_spatial, restir_radius
+    s["cache_train_paths"], s["cache_train_steps"] = cache_train_paths, cache_train_steps
+    s["cache_spread"], s["cache_lr"] = cache_spread, cache_lr
     return s

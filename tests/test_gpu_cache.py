@@ -1,0 +1,75 @@
+"""GPU tests of path tracing with the online-trained MLP radiance cache."""
+import numpy as np
+import pytest
+
+import snkpt
+from snkpt import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def frame(pt, view, st, cuda, names=("radiance",)):
+    w, h = int(view["width"]), int(view["height"])
+    out = snkpt.alloc_outputs(w, h, device=cuda, names=names)
+    pt.render([view], st, [out])
+    pt.synchronize()
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def rel_mse(x, ref, eps=1e-2):
+    x = np.asarray(x, np.float64)[:, :3]
+    ref = np.asarray(ref, np.float64)[:, :3]
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + eps)))
+
+
+def test_cache_mode_without_termination_matches_plain(cuda, built_lib):
+    sc = scenes.config1(width=320, height=180)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    names = ("radiance", "albedo", "normal", "depth", "inst_id", "prim_id", "motion")
+    plain = frame(pt, sc.views[0], abi.settings(spp=1, max_depth=6, seed=9), cuda, names)
+    cached = frame(pt, sc.views[0], abi.settings(mode=abi.MODE_PATH_CACHE, spp=1, max_depth=6, seed=9,
+                                                 cache_spread=1e30), cuda, names)
+    for k in names:
+        assert np.array_equal(plain[k], cached[k]), k
+    s = pt.stats()
+    assert s["cache_queries"] == 0 and s["cache_samples"] == 16384 * 4
+
+
+def test_cache_learns_what_truncation_loses(cuda, built_lib):
+    """Against an FP64-accumulated converged image: the trained cache must recover
+    most of the energy that the same cache-truncated paths lose without it."""
+    W, H = 160, 90
+    sc = scenes.config3(resolutions=[(W, H)])
+    view = sc.views[0]
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    for f in range(256):   # converged reference: 256 spp, depth 8, FP64 accumulation
+        flags = abi.RENDER_ACCUMULATE_F64 | (abi.RENDER_RESET_ACCUM if f == 0 else 0)
+        pt.render([view], abi.settings(spp=1, max_depth=8, seed=100 + f, flags=flags), [{}])
+    ref, nf = pt.read_accumulator(W, H)
+    assert nf == 256
+
+    def mean_frames(mode_kw, seeds):
+        acc = np.zeros((W * H, 4))
+        for s in seeds:
+            acc += frame(pt, view, abi.settings(spp=1, max_depth=6, seed=s, **mode_kw), cuda)["radiance"]
+        return acc / len(seeds)
+
+    # truncation without the cache: zero network, no training
+    pt.cache_set_weights(np.zeros(snkpt.CACHE_NUM_WEIGHTS, np.float32))
+    trunc = mean_frames(dict(mode=abi.MODE_PATH_CACHE, cache_lr=-1.0, frame_index=0), range(1000, 1032))
+    assert pt.stats()["cache_queries"] > 0
+    # trained cache
+    pt.cache_reset(1)
+    for f in range(60):
+        frame(pt, view, abi.settings(mode=abi.MODE_PATH_CACHE, spp=1, max_depth=6, seed=2000 + f, frame_index=f), cuda)
+    cached = mean_frames(dict(mode=abi.MODE_PATH_CACHE, cache_lr=-1.0, frame_index=99), range(3000, 3032))
+    plain = mean_frames(dict(mode=abi.MODE_PATH), range(4000, 4032))
+    e_trunc, e_cache, e_plain = rel_mse(trunc, ref), rel_mse(cached, ref), rel_mse(plain, ref)
+    assert np.isfinite(cached).all()
+    # energy: truncation is dark, the cache restores the missing radiance
+    lum = lambda x: float(np.mean(x[:, :3]))
+    assert lum(trunc) < lum(ref)
+    assert abs(lum(cached) - lum(ref)) < 0.5 * abs(lum(trunc) - lum(ref))
+    assert e_cache < e_trunc, (e_cache, e_trunc, e_plain)
