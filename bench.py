@@ -219,6 +219,48 @@ def cache_vs_plain(pt_mod, abi, scenes, device, frames=120, check=(60,), ref_spp
             "frames": frames, "checks": results}
 
 
+def batched_views(snkpt, abi, scenes, device, stream, tuning, frames=5, warmup=3, scale=1):
+    """Eight uneven views (640x360 .. 3840x2160, 19.2 Mpixels; each side divided
+    by `scale`) of the terrain scene in one render call, 1 spp, depth 6: direct
+    stream launches against CUDA-graph replay of the same frame.  Device-resident
+    outputs; events on the library's stream around each frame, which include the
+    host's launch (or capture + graph update) work."""
+    import torch
+    res_list = [(w // scale, h // scale) for w, h in scenes.CONFIG3_RESOLUTIONS]
+    sc = scenes.config3(resolutions=res_list)
+    pt = snkpt.PathTracer(device.index or 0, stream=stream)
+    pt.load_scene(sc)
+    if tuning:
+        pt.set_tuning(tuning)
+    outs = [snkpt.alloc_outputs(int(v["width"]), int(v["height"]), device=device, names=("radiance",))
+            for v in sc.views]
+    npx = sum(w * h for w, h in res_list)
+    res = {"workload": f"config 3: 64 terrain tiles (256x256 grid) + 200 icospheres, 8 views "
+                       f"{res_list[0][0]}x{res_list[0][1]}..{res_list[-1][0]}x{res_list[-1][1]} ({npx:,} px) in one "
+                       f"call, 1 spp, depth 6",
+           "blas_triangles": int(pt.stats()["triangles"]), "views": len(sc.views)}
+    for name, flags in (("stream", 0), ("graph", abi.RENDER_USE_GRAPH)):
+        for k in range(warmup):
+            pt.render(sc.views, abi.settings(spp=1, max_depth=6, rr_depth=3, seed=500 + k, flags=flags), outs)
+            pt.stats()
+        torch.cuda.synchronize()
+        ms, rays = 0.0, 0
+        for k in range(frames):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            pt.render(sc.views, abi.settings(spp=1, max_depth=6, rr_depth=3, seed=600 + k, flags=flags), outs)
+            b.record(stream)
+            s = pt.stats()
+            rays += s["rays_camera"] + s["rays_extension"] + s["rays_shadow"]
+            b.synchronize()
+            ms += a.elapsed_time(b)
+        res[name] = {"Mrays_per_s": rays / (ms / 1e3) / 1e6, "ms_per_frame": ms / frames,
+                     "rays_per_frame": rays / frames}
+    del outs, pt
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -398,6 +440,9 @@ def run_ours(args):
     if rank == 0:
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(sc, view, settings(1, 0))
+        if not args.no_batched:
+            line["batched_views"] = batched_views(snkpt, abi, scenes, dev, stream, tuning)
+            line["batched_views_small"] = batched_views(snkpt, abi, scenes, dev, stream, tuning, frames=20, scale=8)
         if args.cache_eval != "off":
             checks = (60,) if args.cache_eval == "quick" else tuple(range(9, 120, 10))
             line["cache_vs_plain"] = cache_vs_plain(snkpt, abi, scenes, dev, check=checks)
@@ -416,6 +461,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 8-view batched (config 3) measurement")
     ap.add_argument("--cache-eval", default="quick", choices=["off", "quick", "full"],
                     help="MLP cache vs plain at equal relMSE: quick = one checked frame, full = every 10th frame")
     args = ap.parse_args()

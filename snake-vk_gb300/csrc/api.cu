@@ -110,6 +110,8 @@ struct snk_pt_ctx {
     uint64_t stage_launches[SNK_NUM_STAGES] = {0};
 
     snk_tuning tune{};   // launch knobs (zero = defaults)
+    cudaGraphExec_t graph_exec = nullptr;   // replayed frame (SNK_RENDER_USE_GRAPH)
+    uint64_t graph_launches = 0;
 
     // MLP radiance cache
     MlpState mlp;
@@ -562,6 +564,7 @@ int snk_pt_destroy(snk_pt_ctx* ctx) {
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     cudaStream_t s = ctx->own_stream ? ctx->stream : nullptr;
     delete ctx;
     if (s) cudaStreamDestroy(s);
@@ -744,9 +747,16 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "counters");
     F.counters = ctx->counters.p;
     F.trav_counters = count_nodes ? ctx->trav.p : nullptr;
-    if (cudaMemsetAsync(ctx->counters.p, 0, CNT_TOTAL * sizeof(uint32_t), st) != cudaSuccess ||
-        cudaMemsetAsync(ctx->trav.p, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess)
-        return fail(ctx, SNK_ERR_CUDA, "counter reset");
+    auto reset_counters = [&]() -> cudaError_t {
+        cudaError_t r = cudaMemsetAsync(ctx->counters.p, 0, CNT_TOTAL * sizeof(uint32_t), st);
+        if (r == cudaSuccess) r = cudaMemsetAsync(ctx->trav.p, 0, 4 * sizeof(unsigned long long), st);
+        return r;
+    };
+    // CUDA-graph replay (path modes): the frame's memsets and kernels are captured
+    // once and replayed; a new capture with different parameters updates the
+    // instantiated graph in place (cudaGraphExecUpdate) when the topology matches
+    const bool use_graph = (rs.flags & SNK_RENDER_USE_GRAPH) && path_like && !profile;
+    if (!use_graph && reset_counters() != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, "counter reset");
 
     if (path_like) {
         if (cache) {
@@ -771,6 +781,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (cudaMemsetAsync(F.train_beta, 0, nv * sizeof(float4), st) ||
                 cudaMemsetAsync(F.train_L, 0, nv * sizeof(float4), st))
                 return fail(ctx, SNK_ERR_CUDA, "render: cache buffer reset");
+            const uint32_t steps = rs.cache_train_steps ? rs.cache_train_steps : 4u;
+            API_TRY(mlp_train_reserve(ctx->mlp, (uint32_t)((nv + steps - 1) / steps)));
         }
         if (ctx->rays0.reserve(2ull * n_paths) || ctx->rays1.reserve(2ull * n_paths) || ctx->pid0.reserve(n_paths) ||
             ctx->pid1.reserve(n_paths) || ctx->hits.reserve(n_paths) || ctx->beta.reserve(n_paths) ||
@@ -780,9 +792,14 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         F.path_ids[0] = ctx->pid0.p; F.path_ids[1] = ctx->pid1.p;
         F.hits = ctx->hits.p; F.beta = ctx->beta.p; F.L = ctx->L.p;
         F.shadow_rays = ctx->srays.p; F.shadow_contrib = ctx->scontrib.p;
-        cudaEventRecord(ctx->ev0, st);
+        if (!use_graph) cudaEventRecord(ctx->ev0, st);
         const int g8 = shade_grid(ctx), g16 = trace_grid(ctx);
-        cudaError_t e = staged(ctx, profile, SNK_STAGE_GENERATE, [&] { return launch_generate(F, g8, st); });
+        cudaError_t e = cudaSuccess;
+        if (use_graph) {
+            e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) e = reset_counters();
+        }
+        if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_GENERATE, [&] { return launch_generate(F, g8, st); });
         for (uint32_t d = 0; d < rs.max_depth && e == cudaSuccess; d++) {
             e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
                        [&] { return launch_trace_closest(F, d, g16, count_nodes, st); });
@@ -816,6 +833,26 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 });
             }
             ctx->last_cache_samples = total;
+        }
+        if (use_graph) {
+            cudaGraph_t graph = nullptr;
+            cudaError_t ec = cudaStreamEndCapture(st, &graph);
+            if (e == cudaSuccess) e = ec;
+            if (e == cudaSuccess && ctx->graph_exec) {
+                cudaGraphExecUpdateResultInfo info;
+                if (cudaGraphExecUpdate(ctx->graph_exec, graph, &info) != cudaSuccess) {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(ctx->graph_exec);
+                    ctx->graph_exec = nullptr;
+                }
+            }
+            if (e == cudaSuccess && !ctx->graph_exec) e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e == cudaSuccess) {
+                cudaEventRecord(ctx->ev0, st);
+                e = cudaGraphLaunch(ctx->graph_exec, st);
+                ctx->graph_launches++;
+            }
         }
         cudaEventRecord(ctx->ev1, st);
         if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));

@@ -492,6 +492,10 @@ Status mlp_init(MlpState& M, const float* w_host, cudaStream_t st) {
     SNK_TRY_CUDA(cudaMemsetAsync(M.v.p, 0, MLP_NW * sizeof(float), st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.wf.p, 0, MLP_FWD_WORDS * sizeof(uint2), st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.wb.p, 0, MLP_BWD_WORDS * sizeof(uint2), st));
+    // the training kernel's shared memory exceeds the default limit (set here, not
+    // per launch, so frames can be captured into CUDA graphs)
+    SNK_TRY_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(TrainSmem)));
     AdamParams ap{};   // lr 0: only refresh the BF16 copies
     k_mlp_adam<<<(MLP_NW + 255) / 256, 256, 0, st>>>(M.w.p, 0, M.w.p, M.m.p, M.v.p, ap,
                                                      reinterpret_cast<unsigned short*>(M.wf.p),
@@ -515,14 +519,19 @@ Status mlp_encode(const float4* rec, uint32_t n, const EncodeParams& ep, float* 
     return Status::Ok();
 }
 
+Status mlp_train_reserve(MlpState& M, uint32_t n) {
+    const uint32_t ctas = (n + TRAIN_ROWS - 1) / TRAIN_ROWS;
+    SNK_TRY_CUDA(M.part.reserve((size_t)ctas * MLP_NW));
+    SNK_TRY_CUDA(M.loss.reserve(ctas));
+    return Status::Ok();
+}
+
 Status mlp_train_step(MlpState& M, const float4* samples, uint32_t n, const EncodeParams& ep, float lr,
                       float* grad_out, float* loss_host, cudaStream_t st) {
     if (n == 0) return Status::Ok();
     const uint32_t ctas = (n + TRAIN_ROWS - 1) / TRAIN_ROWS;
-    SNK_TRY_CUDA(M.part.reserve((size_t)ctas * MLP_NW));
-    SNK_TRY_CUDA(M.loss.reserve(ctas));
-    SNK_TRY_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(TrainSmem)));
+    Status rs = mlp_train_reserve(M, n);
+    if (!rs.ok()) return rs;
     k_mlp_train<<<ctas, 256, sizeof(TrainSmem), st>>>(M.wf.p, M.wb.p, samples, n, ep, 1.0f / (3.0f * (float)n),
                                                       M.part.p, M.loss.p);
     SNK_TRY_CUDA(cudaGetLastError());

@@ -39,6 +39,9 @@ Status mlp_infer(const MlpState& M, const float4* rec, const uint32_t* n_dev, ui
                  float* out, const float4* beta, float4* L, int grid, cudaStream_t st);
 Status mlp_encode(const float4* rec, uint32_t n, const EncodeParams& ep, float* out, cudaStream_t st);
 // samples: 5 float4 each (the 4 record words, then target rgb + weight)
+// grows the per-CTA gradient/loss buffers for batches of up to n samples (call
+// before a stream capture: the training step itself then allocates nothing)
+Status mlp_train_reserve(MlpState& M, uint32_t n);
 Status mlp_train_step(MlpState& M, const float4* samples, uint32_t n, const EncodeParams& ep, float lr,
                       float* grad_out, float* loss_host, cudaStream_t st);
 

@@ -161,3 +161,33 @@ def test_launch_knobs_do_not_change_results(cuda, built_lib):
     g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
     for k in g:
         assert np.array_equal(g[k], base[k]), ("autotuned", k)
+
+
+def test_graph_replay_matches_stream_launches(cuda, built_lib):
+    """SNK_RENDER_USE_GRAPH captures the frame into a CUDA graph and replays it,
+    updating the instantiated graph as frame parameters change; the images (and
+    the online-trained cache weights) must equal those of direct launches."""
+    res = [(160, 90), (96, 54), (200, 120)]
+    sc = scenes.config3(resolutions=res)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    for f in range(3):
+        st = abi.settings(spp=1, max_depth=6, rr_depth=3, seed=20 + f, frame_index=f)
+        base = _gpu_frame(pt, sc.views, st, cuda)
+        st["flags"] = abi.RENDER_USE_GRAPH
+        got = _gpu_frame(pt, sc.views, st, cuda)
+        for g, b in zip(got, base):
+            for k in b:
+                assert np.array_equal(g[k], b[k]), (f, k)
+    # cache mode: training kernels (Adam step counters) are captured each frame
+    weights = []
+    for flags in (0, abi.RENDER_USE_GRAPH):
+        pt.cache_reset(2)
+        imgs = []
+        for f in range(4):
+            st = abi.settings(mode=abi.MODE_PATH_CACHE, spp=1, max_depth=6, seed=50 + f, frame_index=f, flags=flags)
+            imgs.append(_gpu_frame(pt, sc.views[:1], st, cuda)[0]["radiance"])
+        weights.append((pt.cache_get_weights(), imgs))
+    assert np.array_equal(weights[0][0], weights[1][0])
+    for a, b in zip(weights[0][1], weights[1][1]):
+        assert np.array_equal(a, b)
