@@ -265,8 +265,14 @@ typedef struct snk_tuning {
     uint32_t refill_idle;           /* hand new rays to a warp when this many lanes idle (4) */
     uint32_t prim_bias;             /* warp runs a primitive step if 4*n_prim >= bias*n_node (4) */
     uint32_t trace_variant;         /* registers: 0 <= 85 (6 blocks/SM), 1 <= 64, 2 unconstrained */
-    uint32_t reserved[2];
+    uint32_t bvh_treelet_passes;    /* treelet restructuring passes of later mesh BVH builds (3);
+                                       SNK_TREELET_PASSES_NONE builds the plain LBVH */
+    uint32_t tlas_treelet_passes;   /* the same for the per-frame instance BVH (1); up to 1024
+                                       instances it is built in one launch by locally-ordered
+                                       clustering, and the passes refine that tree */
 } snk_tuning;
+
+#define SNK_TREELET_PASSES_NONE 0xFFFFFFFFu
 
 /* ---- lifetime ---------------------------------------------------------------- */
 int snk_pt_abi_version(uint32_t* version);

@@ -70,6 +70,8 @@ struct snk_pt_ctx {
     DBuf<float> d_cdf, d_pmf;
     uint32_t n_emissive = 0, n_local = 0;
     DBuf<unsigned> d_err;
+    DBuf<SmallBuildOut> d_small_out;   // result record of the single-launch instance BVH build
+    bool tlas_small = false;
 
     BuildScratch scratch;
     DBuf<float4> d_box_lo, d_box_hi;
@@ -184,6 +186,10 @@ void invert_affine(const float* mf, float* inv_out, float* nmat_out, float* det_
     *det_out = (float)det;
 }
 
+int treelet_passes(uint32_t knob, int dflt) {
+    return knob == SNK_TREELET_PASSES_NONE ? 0 : (knob ? (int)knob : dflt);
+}
+
 Status build_meshes(snk_pt_ctx* ctx) {
     cudaStream_t st = ctx->stream;
     size_t nv = 0, ni = 0, nt = 0;
@@ -228,7 +234,8 @@ Status build_meshes(snk_pt_ctx* ctx) {
                                       ctx->d_box_lo.p, ctx->d_box_hi.p, st));
         BuildResult br;
         SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, mi.num_triangles, ctx->d_blas.p,
-                               node_base, prim_base, ctx->d_prim_order.p, st, &br));
+                               node_base, prim_base, ctx->d_prim_order.p, st, &br,
+                               treelet_passes(ctx->tune.bvh_treelet_passes, 3)));
         SNK_TRY(launch_fill_triangles(ctx->d_prim_order.p, mi.num_triangles, ctx->d_pos.p, ctx->d_idx.p,
                                       mi.vertex_offset, mi.index_offset, ctx->d_tris.p + prim_base, st));
         mi.blas_root = node_base;
@@ -371,15 +378,26 @@ Status build_instances(snk_pt_ctx* ctx) {
         SNK_TRY_CUDA(ctx->d_tlas_prims.reserve(n));
         SNK_TRY(launch_instance_boxes(ctx->d_inst_list.p, n, ctx->d_inst_shade.p, ctx->d_meshes.p, ctx->d_box_lo.p,
                                       ctx->d_box_hi.p, st));
-        BuildResult br;
-        SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
-                               ctx->d_prim_order.p, st, &br));
+        const int passes = treelet_passes(ctx->tune.tlas_treelet_passes, 1);
+        if (n <= (uint32_t)SMALL_BUILD_MAX) {
+            // one launch, no host round trip; the node count stays on the device
+            // (traversal bounds its node indices by the capacity, n + 1)
+            SNK_TRY_CUDA(ctx->d_small_out.reserve(1));
+            SNK_TRY(build_wide_bvh_small(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
+                                         ctx->d_prim_order.p, passes, ctx->d_small_out.p, ctx->d_err.p, st));
+            ctx->tlas_nodes = n + 1;
+            ctx->tlas_small = true;
+        } else {
+            BuildResult br;
+            SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
+                                   ctx->d_prim_order.p, st, &br, passes));
+            ctx->tlas_nodes = br.num_nodes;
+            ctx->tlas_small = false;
+        }
         SNK_TRY(launch_map_prims(ctx->d_prim_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
         ctx->tlas_root = 0;
-        ctx->tlas_nodes = br.num_nodes;
         ctx->tlas_prim_count = n;
     }
-    SNK_TRY_CUDA(cudaStreamSynchronize(st));
     return Status::Ok();
 }
 
@@ -460,7 +478,7 @@ Status check_device_error(snk_pt_ctx* ctx) {
     if (e) {
         SNK_TRY_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
         return Status::Err(SNK_ERR_LIMIT, std::string("device traversal bound hit (error word ") + std::to_string(e) +
-                                              "): bit 1 stack depth, bit 2 step limit, bit 4 bad index");
+                                              "): bit 1 stack depth, bit 2 step limit, bit 4 bad index, bit 8 instance BVH build");
     }
     return Status::Ok();
 }
@@ -923,7 +941,9 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
 int snk_pt_set_tuning(snk_pt_ctx* ctx, const snk_tuning* t) {
     if (!ctx || !t) return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: null argument");
     if (t->trace_blocks_per_sm > 64 || t->shade_blocks_per_sm > 64 || t->ray_chunk > 4096 || t->refill_idle > 32 ||
-        t->prim_bias > 64 || t->trace_variant > 2)
+        t->prim_bias > 64 || t->trace_variant > 2 || 
+        (t->bvh_treelet_passes > 16 && t->bvh_treelet_passes != SNK_TREELET_PASSES_NONE) ||
+        (t->tlas_treelet_passes > 16 && t->tlas_treelet_passes != SNK_TREELET_PASSES_NONE))
         return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: knob out of range");
     ctx->tune = *t;
     return SNK_OK;
@@ -1235,7 +1255,14 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
         out->stage_ms[k] = ctx->stage_ms[k];
         out->stage_launches[k] = ctx->stage_launches[k];
     }
-    out->wide_nodes = ctx->blas_nodes + ctx->tlas_nodes;
+    uint64_t tlas_nodes = ctx->tlas_nodes;
+    if (ctx->tlas_small && ctx->tlas_root != INVALID && ctx->d_small_out.p) {
+        SmallBuildOut r{};
+        if (cudaMemcpyAsync(&r, ctx->d_small_out.p, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
+            cudaStreamSynchronize(ctx->stream) == cudaSuccess)
+            tlas_nodes = r.num_nodes;
+    }
+    out->wide_nodes = ctx->blas_nodes + tlas_nodes;
     out->triangles = ctx->total_tris;
     out->instances = ctx->instances.size();
     out->blas_sah_cost = ctx->blas_sah;

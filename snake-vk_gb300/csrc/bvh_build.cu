@@ -11,6 +11,15 @@
 //   3. radix sort of (code, primitive) pairs (CUB DeviceRadixSort)
 //   4. binary radix tree (Karras, HPG 2012): one thread per internal node
 //   5. bottom-up boxes and leaf counts (atomic arrival flags)
+//   5b. treelet restructuring (Karras & Aila, HPG 2013): bottom-up over the binary
+//      tree, every node whose subtree holds >= 7 primitives roots a treelet of 7
+//      leaves (grown by opening the largest-area treelet leaf); one warp finds the
+//      SAH-optimal binary topology of those 7 leaves by dynamic programming over
+//      all 127 leaf subsets and every 2-partition of each, and rewrites the
+//      treelet's 6 internal nodes in place.  Subtrees of <= 3 primitives are
+//      costed as the leaves the collapse will make of them.  Repeated for a few
+//      passes; the result is deterministic (each treelet depends only on its
+//      finished subtrees, ties break on the lowest subset index).
 //   6. top-down collapse to 8-wide nodes, one thread per output node, level by
 //      level: a node's children start as its binary children; the internal child
 //      with the largest surface area and more than 3 leaves is replaced by its two
@@ -20,6 +29,11 @@
 //      slot ^ ray_octant in increasing order is roughly front to back.  Child boxes
 //      are quantised outwards to 8 bits per plane.
 //   7. SAH cost of the result (for quality reporting).
+//
+// Mesh BVHs (built once, at load) take the multi-launch pipeline above.  The
+// per-frame instance BVH of up to 1024 instances is built by one single-CTA
+// launch instead (k_build_small: clustering in shared memory, then treelet passes
+// and the same collapse), so that a frame's rebuild costs no host round trip.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "snk_host.h"
@@ -35,6 +49,14 @@ __device__ __forceinline__ unsigned enc_f(float f) {
 }
 __device__ __forceinline__ float dec_f(unsigned u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// loads of tree data written by other threads during the build: through L2 for
+// global memory (G), plain for shared memory (the single-CTA builder)
+template <bool G, class T>
+__device__ __forceinline__ T ldx(const T* p) {
+    if constexpr (G) return __ldcg(p);
+    else return *p;
 }
 
 __global__ void k_init_bounds(unsigned* cb) {
@@ -74,11 +96,8 @@ __device__ __forceinline__ unsigned long long spread21(unsigned long long x) {
     return x;
 }
 
-__global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict__ hi, uint32_t n,
-                         const unsigned* cb, unsigned long long* keys, uint32_t* vals) {
-    uint32_t i = blockIdx.x * BLK + threadIdx.x;
-    if (i >= n) return;
-    float4 a = lo[i], b = hi[i];
+// cb: encoded centroid bounds (min xyz, max xyz)
+__device__ __forceinline__ unsigned long long morton_of(float4 a, float4 b, const unsigned* cb) {
     float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
     unsigned long long q[3];
     for (int k = 0; k < 3; k++) {
@@ -88,7 +107,14 @@ __global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict
         f = fminf(fmaxf(f, 0.0f), 1.0f);
         q[k] = (unsigned long long)fminf(f * 2097152.0f, 2097151.0f);
     }
-    keys[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    return (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+}
+
+__global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict__ hi, uint32_t n,
+                         const unsigned* cb, unsigned long long* keys, uint32_t* vals) {
+    uint32_t i = blockIdx.x * BLK + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = morton_of(lo[i], hi[i], cb);
     vals[i] = i;
 }
 
@@ -99,9 +125,7 @@ __device__ __forceinline__ int delta(const unsigned long long* __restrict__ k, i
     return __clzll(a ^ b);
 }
 
-__global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int2* children, int* parent) {
-    int i = blockIdx.x * BLK + threadIdx.x;
-    if (i >= n - 1) return;
+__device__ void karras_node(int i, const unsigned long long* __restrict__ keys, int n, int2* children, int* parent) {
     int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
     int dmin = delta(keys, n, i, i - d);
     int lmax = 2;
@@ -124,28 +148,38 @@ __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int
     parent[right] = i;
 }
 
-__global__ void k_bottom_up(const uint32_t* __restrict__ sorted, const float4* __restrict__ plo,
-                            const float4* __restrict__ phi, int n, const int2* __restrict__ children,
-                            const int* __restrict__ parent, int* flags, float4* node_lo, float4* node_hi,
-                            uint32_t* leaf_count) {
-    int j = blockIdx.x * BLK + threadIdx.x;
-    if (j >= n) return;
+__global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int2* children, int* parent) {
+    int i = blockIdx.x * BLK + threadIdx.x;
+    if (i < n - 1) karras_node(i, keys, n, children, parent);
+}
+
+template <bool G>
+__device__ __forceinline__ void mem_fence() {
+    if constexpr (G) __threadfence();
+    else __threadfence_block();
+}
+
+// boxes and primitive counts from leaf j to the root (the second thread to
+// arrive at a node completes it)
+template <bool G>
+__device__ void bottom_up_leaf(int j, const uint32_t* __restrict__ sorted, const float4* __restrict__ plo,
+                               const float4* __restrict__ phi, int n, const int2* children, const int* parent,
+                               int* flags, float4* node_lo, float4* node_hi, uint32_t* leaf_count) {
     int node = n - 1 + j;
     uint32_t prim = sorted[j];
-    float4 lo = plo[prim], hi = phi[prim];
-    node_lo[node] = lo;
-    node_hi[node] = hi;
+    node_lo[node] = plo[prim];
+    node_hi[node] = phi[prim];
     leaf_count[node] = 1;
     if (n == 1) return;
     int p = parent[node];
     while (p >= 0) {
-        __threadfence();
+        mem_fence<G>();
         if (atomicAdd(&flags[p], 1) == 0) return;
-        __threadfence();
+        mem_fence<G>();
         int2 ch = children[p];
-        float4 al = __ldcg(&node_lo[ch.x]), ah = __ldcg(&node_hi[ch.x]);
-        float4 bl = __ldcg(&node_lo[ch.y]), bh = __ldcg(&node_hi[ch.y]);
-        uint32_t ca = __ldcg(&leaf_count[ch.x]), cb = __ldcg(&leaf_count[ch.y]);
+        float4 al = ldx<G>(&node_lo[ch.x]), ah = ldx<G>(&node_hi[ch.x]);
+        float4 bl = ldx<G>(&node_lo[ch.y]), bh = ldx<G>(&node_hi[ch.y]);
+        uint32_t ca = ldx<G>(&leaf_count[ch.x]), cb = ldx<G>(&leaf_count[ch.y]);
         node_lo[p] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.0f);
         node_hi[p] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f);
         leaf_count[p] = ca + cb;
@@ -153,9 +187,229 @@ __global__ void k_bottom_up(const uint32_t* __restrict__ sorted, const float4* _
     }
 }
 
+__global__ void k_bottom_up(const uint32_t* __restrict__ sorted, const float4* __restrict__ plo,
+                            const float4* __restrict__ phi, int n, const int2* __restrict__ children,
+                            const int* __restrict__ parent, int* flags, float4* node_lo, float4* node_hi,
+                            uint32_t* leaf_count) {
+    int j = blockIdx.x * BLK + threadIdx.x;
+    if (j < n) bottom_up_leaf<true>(j, sorted, plo, phi, n, children, parent, flags, node_lo, node_hi, leaf_count);
+}
+
 __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
     float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
     return dx * dy + dy * dz + dz * dx;
+}
+
+// ---- treelet restructuring -----------------------------------------------------
+constexpr int TL_LEAVES = 7;
+constexpr int TL_SUBSETS = 1 << TL_LEAVES;
+constexpr int TL_WARPS = BLK / 32;
+constexpr float SAH_CI = 1.2f;   // binary internal node
+constexpr float SAH_CT = 1.0f;   // primitive
+constexpr uint32_t LEAF_MAX = 3; // subtrees the collapse turns into leaves
+
+struct TreeletSmem {
+    float area[TL_SUBSETS];
+    float cost[TL_SUBSETS];
+    uint32_t count[TL_SUBSETS];
+    uint8_t part[TL_SUBSETS];
+    float4 lo[TL_LEAVES], hi[TL_LEAVES];
+    float leaf_cost[TL_LEAVES];
+    uint32_t leaf_cnt[TL_LEAVES];
+    int leaf[TL_LEAVES];
+    int inner[TL_LEAVES - 1];
+};
+
+__device__ __forceinline__ float node_cost(float area, uint32_t cnt, float split_cost) {
+    return cnt <= LEAF_MAX ? SAH_CT * area * (float)cnt : SAH_CI * area + split_cost;
+}
+
+// Optimises the treelet rooted at `root` (all 32 lanes of the warp call this).
+template <bool G>
+__device__ void treelet_optimise(int root, int nl, int2* children, int* parent, float4* node_lo, float4* node_hi,
+                                 uint32_t* leaf_count, float* cost, TreeletSmem& T) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t total = ldx<G>(&leaf_count[root]);
+    if (total < (uint32_t)TL_LEAVES) {
+        // small subtree: only its cost (boxes and counts are already final)
+        if (lane == 0) {
+            int2 ch = ldx<G>(&children[root]);
+            float c = ldx<G>(&cost[ch.x]) + ldx<G>(&cost[ch.y]);
+            cost[root] = node_cost(half_area(ldx<G>(&node_lo[root]), ldx<G>(&node_hi[root])), total, c);
+        }
+        __syncwarp();
+        return;
+    }
+    if (lane == 0) {
+        int2 ch = ldx<G>(&children[root]);
+        int L[TL_LEAVES];
+        float A[TL_LEAVES];
+        L[0] = ch.x; L[1] = ch.y;
+        A[0] = half_area(ldx<G>(&node_lo[ch.x]), ldx<G>(&node_hi[ch.x]));
+        A[1] = half_area(ldx<G>(&node_lo[ch.y]), ldx<G>(&node_hi[ch.y]));
+        T.inner[0] = root;
+        int nleaf = 2, ninner = 1;
+        while (nleaf < TL_LEAVES) {
+            int best = -1;
+            float ba = -1.0f;
+            for (int k = 0; k < nleaf; k++)
+                if (L[k] < nl && A[k] > ba) { ba = A[k]; best = k; }
+            // (a subtree of >= 7 primitives always has an internal node to open)
+            int2 c2 = ldx<G>(&children[L[best]]);
+            T.inner[ninner++] = L[best];
+            L[best] = c2.x;
+            A[best] = half_area(ldx<G>(&node_lo[c2.x]), ldx<G>(&node_hi[c2.x]));
+            L[nleaf] = c2.y;
+            A[nleaf] = half_area(ldx<G>(&node_lo[c2.y]), ldx<G>(&node_hi[c2.y]));
+            nleaf++;
+        }
+        for (int k = 0; k < TL_LEAVES; k++) {
+            T.leaf[k] = L[k];
+            T.lo[k] = ldx<G>(&node_lo[L[k]]);
+            T.hi[k] = ldx<G>(&node_hi[L[k]]);
+            T.leaf_cost[k] = ldx<G>(&cost[L[k]]);
+            T.leaf_cnt[k] = ldx<G>(&leaf_count[L[k]]);
+        }
+    }
+    __syncwarp();
+    // subset areas and primitive counts
+    for (int sub = lane + 1; sub < TL_SUBSETS; sub += 32) {
+        float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+        uint32_t cnt = 0;
+        for (int k = 0; k < TL_LEAVES; k++) {
+            if (!(sub & (1 << k))) continue;
+            float4 a = T.lo[k], b = T.hi[k];
+            lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
+            hi.x = fmaxf(hi.x, b.x); hi.y = fmaxf(hi.y, b.y); hi.z = fmaxf(hi.z, b.z);
+            cnt += T.leaf_cnt[k];
+        }
+        T.area[sub] = half_area(lo, hi);
+        T.count[sub] = cnt;
+        if (__popc(sub) == 1) { T.cost[sub] = T.leaf_cost[__ffs(sub) - 1]; T.part[sub] = 0; }
+    }
+    __syncwarp();
+    // subsets of 2..6 leaves, by size; every unordered 2-partition (the part that
+    // holds the lowest leaf is enumerated)
+    for (int size = 2; size < TL_LEAVES; size++) {
+        for (int sub = lane + 1; sub < TL_SUBSETS; sub += 32) {
+            if (__popc(sub) != size) continue;
+            const int low = sub & -sub, rest = sub ^ low;
+            float best = 3.4e38f;
+            int bp = 0;
+            // P = low | q over the proper subsets q of rest (q = rest would be all of sub)
+            for (int q = (rest - 1) & rest;; q = (q - 1) & rest) {
+                const int P = low | q;
+                float c = T.cost[P] + T.cost[sub ^ P];
+                if (c < best || (c == best && P < bp)) { best = c; bp = P; }
+                if (q == 0) break;
+            }
+            T.cost[sub] = node_cost(T.area[sub], T.count[sub], best);
+            T.part[sub] = (uint8_t)bp;
+        }
+        __syncwarp();
+    }
+    // the full set: 63 partitions across the warp
+    {
+        const int full = TL_SUBSETS - 1;
+        float best = 3.4e38f;
+        int bp = 0;
+        for (int q = lane; q < (TL_SUBSETS >> 1) - 1; q += 32) {
+            int P = 1 | (q << 1);
+            float c = T.cost[P] + T.cost[full ^ P];
+            if (c < best || (c == best && P < bp)) { best = c; bp = P; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            float ob = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+            int op = __shfl_xor_sync(0xFFFFFFFFu, bp, o);
+            if (ob < best || (ob == best && op < bp)) { best = ob; bp = op; }
+        }
+        if (lane == 0) {
+            T.cost[full] = node_cost(T.area[full], T.count[full], best);
+            T.part[full] = (uint8_t)bp;
+        }
+    }
+    __syncwarp();
+    // rewrite the treelet's internal nodes (lane 0; 6 nodes)
+    if (lane == 0) {
+        int stk_sub[TL_LEAVES], stk_node[TL_LEAVES];
+        int sp = 0, next = 1;
+        stk_sub[sp] = TL_SUBSETS - 1; stk_node[sp] = T.inner[0]; sp++;
+        while (sp > 0) {
+            --sp;
+            const int sub = stk_sub[sp], node = stk_node[sp];
+            const int P = T.part[sub], Q = sub ^ P;
+            int cidx[2];
+            const int halves[2] = {P, Q};
+            for (int h = 0; h < 2; h++) {
+                const int hs = halves[h];
+                if (__popc(hs) == 1) {
+                    cidx[h] = T.leaf[__ffs(hs) - 1];
+                } else {
+                    cidx[h] = T.inner[next++];
+                    stk_sub[sp] = hs; stk_node[sp] = cidx[h]; sp++;
+                }
+                parent[cidx[h]] = node;
+            }
+            children[node] = make_int2(cidx[0], cidx[1]);
+            float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+            for (int k = 0; k < TL_LEAVES; k++) {
+                if (!(sub & (1 << k))) continue;
+                float4 a = T.lo[k], b = T.hi[k];
+                lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
+                hi.x = fmaxf(hi.x, b.x); hi.y = fmaxf(hi.y, b.y); hi.z = fmaxf(hi.z, b.z);
+            }
+            node_lo[node] = lo;
+            node_hi[node] = hi;
+            leaf_count[node] = T.count[sub];
+            cost[node] = T.cost[sub];
+        }
+    }
+    __syncwarp();
+}
+
+// One restructuring pass, leaf j of this thread (every lane of the warp calls
+// it): each thread climbs towards the root; the second thread to reach a node
+// hands that node's treelet to its whole warp.
+template <bool G>
+__device__ void treelet_climb(int j, int n, int2* children, int* parent, int* flags, float4* node_lo,
+                              float4* node_hi, uint32_t* leaf_count, float* cost, TreeletSmem& T) {
+    const int nl = n - 1;
+    bool active = j < n;
+    int cur = nl + j;
+    if (active) cost[cur] = SAH_CT * half_area(node_lo[cur], node_hi[cur]);
+    while (true) {
+        int p = -1;
+        bool ready = false;
+        if (active) {
+            p = ldx<G>(&parent[cur]);
+            if (p < 0) {
+                active = false;
+            } else {
+                mem_fence<G>();
+                if (atomicAdd(&flags[p], 1) == 0) active = false;
+                else ready = true;
+                mem_fence<G>();
+            }
+        }
+        unsigned m = __ballot_sync(0xFFFFFFFFu, ready);
+        while (m) {
+            const int l = __ffs(m) - 1;
+            m &= m - 1;
+            const int root = __shfl_sync(0xFFFFFFFFu, p, l);
+            treelet_optimise<G>(root, nl, children, parent, node_lo, node_hi, leaf_count, cost, T);
+        }
+        mem_fence<G>();
+        if (ready) cur = p;
+        if (!__any_sync(0xFFFFFFFFu, active)) break;
+    }
+}
+
+__global__ void __launch_bounds__(BLK) k_treelet_pass(int n, int2* children, int* parent, int* flags,
+                                                      float4* node_lo, float4* node_hi, uint32_t* leaf_count,
+                                                      float* cost) {
+    __shared__ TreeletSmem smem[TL_WARPS];
+    treelet_climb<true>(blockIdx.x * BLK + threadIdx.x, n, children, parent, flags, node_lo, node_hi, leaf_count,
+                        cost, smem[threadIdx.x >> 5]);
 }
 
 // smallest power-of-two exponent (biased) with 2^(e-127) >= x; at least 1
@@ -167,14 +421,13 @@ __device__ __forceinline__ uint32_t ceil_exp_biased(float x) {
     return e > 254u ? 254u : e;
 }
 
-__global__ void k_collapse(const uint2* __restrict__ tasks_in, uint32_t* counters, uint2* tasks_out, int n,
-                           const int2* __restrict__ children, const float4* __restrict__ node_lo,
-                           const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
-                           const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
-                           uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area) {
-    uint32_t ti = blockIdx.x * BLK + threadIdx.x;
-    if (ti >= counters[0]) return;
-    uint2 task = tasks_in[ti];
+// One output node: task = (binary node, wide node slot).  counters: [1] tasks
+// out, [2] wide nodes, [3] primitive slots, [4] capacity error bits.
+__device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, int n,
+                              const int2* __restrict__ children, const float4* __restrict__ node_lo,
+                              const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
+                              const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
+                              uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area) {
     int b = (int)task.x;
     uint32_t w = task.y;
     const int nl = n - 1;  // first leaf id
@@ -315,6 +568,251 @@ __global__ void k_collapse(const uint2* __restrict__ tasks_in, uint32_t* counter
     for (int k = 0; k < 5; k++) dst[k] = src[k];
 }
 
+__global__ void k_collapse(const uint2* __restrict__ tasks_in, uint32_t* counters, uint2* tasks_out, int n,
+                           const int2* __restrict__ children, const float4* __restrict__ node_lo,
+                           const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
+                           const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
+                           uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area) {
+    uint32_t ti = blockIdx.x * BLK + threadIdx.x;
+    if (ti >= counters[0]) return;
+    collapse_task(tasks_in[ti], counters, tasks_out, n, children, node_lo, node_hi, leaf_count, sorted, nodes,
+                  node_base, prim_base, prim_order, sah, root_half_area);
+}
+
+// ---- single-CTA agglomerative builder for small primitive sets -----------------
+// The per-frame instance BVH (<= 1024 instances): one block of 1024 threads, every
+// array in shared memory, one launch, no host synchronisation.  Locally-ordered
+// clustering (PLOC, Meister & Bittner, TVCG 2018): clusters start as the
+// primitives in Morton order; every round, each cluster finds the neighbour
+// within PLOC_RADIUS positions whose merged box has the least surface area (ties:
+// the lower position), mutual nearest neighbours merge into a new binary node, and
+// the cluster list is compacted in order.  The globally closest pair is always
+// mutual, so every round merges at least once.  Large boxes (a ground plane that
+// spans the scene) are nobody's nearest neighbour and end up near the root.
+// Internal node ids count down from n-2 as merges happen (the last merge is the
+// root, node 0); leaves are n-1 + their Morton position, so the 8-wide collapse
+// above applies unchanged.
+constexpr int SMALL_THREADS = 1024;
+constexpr int PLOC_RADIUS = 16;
+static_assert(SMALL_BUILD_MAX == SMALL_THREADS, "one cluster per thread");
+
+struct SmallSmem {
+    unsigned long long keys[SMALL_BUILD_MAX];
+    uint32_t vals[SMALL_BUILD_MAX];            // primitive at Morton position k
+    int clusters[2][SMALL_BUILD_MAX];          // node ids of the live clusters, in order
+    int2 children[SMALL_BUILD_MAX];
+    float4 node_lo[2 * SMALL_BUILD_MAX], node_hi[2 * SMALL_BUILD_MAX];
+    uint32_t leaf_count[2 * SMALL_BUILD_MAX];
+    uint2 tasks[2][SMALL_BUILD_MAX];
+    int parent[2 * SMALL_BUILD_MAX];           // treelet passes
+    int flags[SMALL_BUILD_MAX];
+    float cost[2 * SMALL_BUILD_MAX];
+    uint32_t warp_sums[32];
+    uint32_t counters[8];
+    unsigned cb[6];
+    double sah;
+    TreeletSmem tl[SMALL_THREADS / 32];
+};
+static_assert(sizeof(SmallSmem) <= 227 * 1024, "single-CTA builder exceeds shared memory");
+
+__device__ __forceinline__ float4 f4min(float4 a, float4 b) {
+    return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
+}
+__device__ __forceinline__ float4 f4max(float4 a, float4 b) {
+    return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.0f);
+}
+
+// inclusive block-wide sum of v (all SMALL_THREADS threads); *total = block sum
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) warp_sums[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += t;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t r = v + (warp ? warp_sums[warp - 1] : 0u);
+    *total = warp_sums[31];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(SMALL_THREADS, 1)
+k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, int n, int passes, WideNode* nodes,
+              uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, SmallBuildOut* out, unsigned* err_word) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SmallSmem& S = *reinterpret_cast<SmallSmem*>(smem_raw);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    // 1. centroid bounds
+    if (tid < 6) S.cb[tid] = tid < 3 ? 0xFFFFFFFFu : 0u;
+    __syncthreads();
+    {
+        unsigned mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
+        if (tid < n) {
+            const float4 a = plo[tid], b = phi[tid];
+            const float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+            for (int k = 0; k < 3; k++) { mn[k] = enc_f(c[k]); mx[k] = mn[k]; }
+        }
+        for (int k = 0; k < 3; k++) {
+            const unsigned a = __reduce_min_sync(0xFFFFFFFFu, mn[k]), b = __reduce_max_sync(0xFFFFFFFFu, mx[k]);
+            if ((tid & 31) == 0) { atomicMin(&S.cb[k], a); atomicMax(&S.cb[3 + k], b); }
+        }
+    }
+    __syncthreads();
+    // 2. Morton codes, padded to a power of two with keys that sort last
+    int n2 = 1;
+    while (n2 < n) n2 <<= 1;
+    for (int i = tid; i < n2; i += nt) {
+        S.keys[i] = i < n ? morton_of(plo[i], phi[i], S.cb) : ~0ull;
+        S.vals[i] = (uint32_t)i;
+    }
+    __syncthreads();
+    // 3. bitonic sort by (code, index): the order of a stable radix sort
+    for (int k = 2; k <= n2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < n2; i += nt) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long ka = S.keys[i], kb = S.keys[ixj];
+                    const uint32_t va = S.vals[i], vb = S.vals[ixj];
+                    const bool gt = ka > kb || (ka == kb && va > vb);
+                    if (gt == ((i & k) == 0)) {
+                        S.keys[i] = kb; S.keys[ixj] = ka;
+                        S.vals[i] = vb; S.vals[ixj] = va;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // 4. leaves and the initial cluster list
+    const int nl = n - 1;
+    if (tid < n) {
+        const uint32_t p = S.vals[tid];
+        S.node_lo[nl + tid] = plo[p];
+        S.node_hi[nl + tid] = phi[p];
+        S.leaf_count[nl + tid] = 1;
+        S.clusters[0][tid] = nl + tid;
+    }
+    if (tid == 0) { S.counters[5] = (uint32_t)n; S.counters[6] = 0u; }
+    __syncthreads();
+    // 5. clustering rounds (thread i owns cluster position i)
+    int cur = 0, rounds = 0;
+    uint32_t m = (uint32_t)n;
+    uint32_t next_id = n > 1 ? (uint32_t)(n - 2) : 0u;
+    while (m > 1 && rounds < SMALL_BUILD_MAX) {
+        const int i = tid;
+        int nn = -1;
+        float4 mylo = make_float4(0.f, 0.f, 0.f, 0.f), myhi = mylo;
+        if (i < (int)m) {
+            const int ci = S.clusters[cur][i];
+            mylo = S.node_lo[ci];
+            myhi = S.node_hi[ci];
+            float best = 3.4e38f;
+            const int j0 = max(0, i - PLOC_RADIUS), j1 = min((int)m - 1, i + PLOC_RADIUS);
+            for (int j = j0; j <= j1; j++) {
+                if (j == i) continue;
+                const int cj = S.clusters[cur][j];
+                const float a = half_area(f4min(mylo, S.node_lo[cj]), f4max(myhi, S.node_hi[cj]));
+                if (a < best) { best = a; nn = j; }   // increasing j: ties keep the lower position
+            }
+        }
+        S.tasks[0][tid].x = (uint32_t)nn;   // scratch: nearest neighbour per position
+        __syncthreads();
+        bool merge = false, keep = false;
+        if (i < (int)m) {
+            const bool mutual = nn >= 0 && (int)S.tasks[0][nn].x == i;
+            merge = mutual && i < nn;
+            keep = !mutual || i < nn;
+        }
+        uint32_t total_keep, total_merge;
+        const uint32_t kpos = block_scan(keep ? 1u : 0u, S.warp_sums, &total_keep) - (keep ? 1u : 0u);
+        const uint32_t mrank = block_scan(merge ? 1u : 0u, S.warp_sums, &total_merge) - (merge ? 1u : 0u);
+        if (keep) {
+            int id = S.clusters[cur][i];
+            if (merge) {
+                const int cj = S.clusters[cur][nn];
+                id = (int)(next_id - mrank);
+                S.children[id] = make_int2(S.clusters[cur][i], cj);
+                S.node_lo[id] = f4min(mylo, S.node_lo[cj]);
+                S.node_hi[id] = f4max(myhi, S.node_hi[cj]);
+                S.leaf_count[id] = S.leaf_count[S.clusters[cur][i]] + S.leaf_count[cj];
+            }
+            S.clusters[cur ^ 1][kpos] = id;
+        }
+        if (total_merge == 0 && tid == 0) S.counters[6] |= 16u;   // no progress (cannot happen)
+        next_id -= total_merge;
+        m = total_keep;
+        cur ^= 1;
+        rounds++;
+        __syncthreads();
+        if (total_merge == 0) break;
+    }
+    if (tid == 0 && n > 1 && (next_id != 0xFFFFFFFFu || S.clusters[cur][0] != 0)) S.counters[6] |= 16u;
+    __syncthreads();
+    // 5b. optional treelet restructuring of the clustered tree (leaves dealt
+    // round-robin over the 32 warps so that treelets that become ready together
+    // run in different warps)
+    if (passes > 0 && n >= TL_LEAVES + 1 && S.counters[6] == 0u) {
+        if (tid == 0) S.parent[0] = -1;
+        if (tid < n - 1) {
+            const int2 ch = S.children[tid];
+            S.parent[ch.x] = tid;
+            S.parent[ch.y] = tid;
+        }
+        for (int pass = 0; pass < passes; pass++) {
+            if (tid < n) S.flags[tid] = 0;
+            __syncthreads();
+            treelet_climb<false>((tid & 31) * 32 + (tid >> 5), n, S.children, S.parent, S.flags, S.node_lo,
+                                 S.node_hi, S.leaf_count, S.cost, S.tl[tid >> 5]);
+            __syncthreads();
+        }
+    }
+    // 6. collapse, level by level
+    const float4 rlo = S.node_lo[0], rhi = S.node_hi[0];
+    float rha = half_area(rlo, rhi);
+    if (!(rha > 0.0f)) rha = 1.0f;
+    if (tid == 0) {
+        S.tasks[0][0] = make_uint2(0u, node_base);
+        S.counters[0] = 1u; S.counters[1] = 0u; S.counters[2] = 1u; S.counters[3] = 0u; S.counters[4] = 0u;
+        S.sah = 0.0;
+    }
+    __syncthreads();
+    int cc = 0, level = 0;
+    for (; level < 4096; level++) {
+        const uint32_t nin = S.counters[0];
+        if (nin == 0) break;
+        for (uint32_t t = tid; t < nin; t += nt)
+            collapse_task(S.tasks[cc][t], S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
+                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, &S.sah, rha);
+        __syncthreads();
+        if (tid == 0) { S.counters[0] = S.counters[1]; S.counters[1] = 0u; }
+        cc ^= 1;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        uint32_t e = S.counters[4] | S.counters[6];
+        if (S.counters[3] != (uint32_t)n) e |= 4u;
+        if (level >= 4096) e |= 8u;
+        out->num_nodes = S.counters[2];
+        out->prims = S.counters[3];
+        out->error = e;
+        out->sah = 1.0 + S.sah;
+        out->lo[0] = rlo.x; out->lo[1] = rlo.y; out->lo[2] = rlo.z; out->lo[3] = 0.0f;
+        out->hi[0] = rhi.x; out->hi[1] = rhi.y; out->hi[2] = rhi.z; out->hi[3] = 0.0f;
+        if (e && err_word) atomicOr(err_word, 8u);
+    }
+}
+
 __global__ void k_triangle_boxes(const float* __restrict__ pos, const uint32_t* __restrict__ idx, uint32_t vo,
                                  uint32_t io, uint32_t nt, float4* lo, float4* hi) {
     uint32_t t = blockIdx.x * BLK + threadIdx.x;
@@ -384,7 +882,7 @@ inline unsigned grid_for(uint32_t n) { return (n + BLK - 1) / BLK; }
 
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t st,
-                      BuildResult* out) {
+                      BuildResult* out, int treelet_passes) {
     if (n == 0) return Status::Err(1, "build_wide_bvh: no primitives");
     if (n > (1u << 30)) return Status::Err(1, "build_wide_bvh: too many primitives");
     SNK_TRY_CUDA(sc.keys.reserve(n));
@@ -397,6 +895,7 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
     SNK_TRY_CUDA(sc.node_lo.reserve(2 * (size_t)n));
     SNK_TRY_CUDA(sc.node_hi.reserve(2 * (size_t)n));
     SNK_TRY_CUDA(sc.leaf_count.reserve(2 * (size_t)n));
+    SNK_TRY_CUDA(sc.cost.reserve(2 * (size_t)n));
     SNK_TRY_CUDA(sc.tasks_a.reserve(n));
     SNK_TRY_CUDA(sc.tasks_b.reserve(n));
     SNK_TRY_CUDA(sc.counters.reserve(5));
@@ -425,6 +924,14 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
     k_bottom_up<<<g, BLK, 0, st>>>(sorted, prim_lo, prim_hi, (int)n, sc.children.p, sc.parent.p, sc.flags.p,
                                    sc.node_lo.p, sc.node_hi.p, sc.leaf_count.p);
     SNK_TRY_CUDA(cudaGetLastError());
+    if (n >= (uint32_t)TL_LEAVES + 1) {
+        for (int pass = 0; pass < treelet_passes; pass++) {
+            SNK_TRY_CUDA(cudaMemsetAsync(sc.flags.p, 0, sizeof(int) * n, st));
+            k_treelet_pass<<<g, BLK, 0, st>>>((int)n, sc.children.p, sc.parent.p, sc.flags.p, sc.node_lo.p,
+                                              sc.node_hi.p, sc.leaf_count.p, sc.cost.p);
+            SNK_TRY_CUDA(cudaGetLastError());
+        }
+    }
 
     float4 rlo, rhi;
     SNK_TRY_CUDA(cudaMemcpyAsync(&rlo, sc.node_lo.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
@@ -466,6 +973,18 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
     out->sah = 1.0 + sah;
     out->lo[0] = rlo.x; out->lo[1] = rlo.y; out->lo[2] = rlo.z;
     out->hi[0] = rhi.x; out->hi[1] = rhi.y; out->hi[2] = rhi.z;
+    return Status::Ok();
+}
+
+Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
+                            uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
+                            SmallBuildOut* out, unsigned* err_word, cudaStream_t st) {
+    if (n == 0 || n > (uint32_t)SMALL_BUILD_MAX) return Status::Err(1, "build_wide_bvh_small: bad primitive count");
+    SNK_TRY_CUDA(cudaFuncSetAttribute(k_build_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(SmallSmem)));
+    k_build_small<<<1, SMALL_THREADS, sizeof(SmallSmem), st>>>(prim_lo, prim_hi, (int)n, treelet_passes, nodes,
+                                                                node_base, prim_base, prim_order, out, err_word);
+    SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }
 

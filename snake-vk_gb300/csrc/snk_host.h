@@ -70,6 +70,7 @@ struct BuildScratch {
     DBuf<int> parent, flags;
     DBuf<float4> node_lo, node_hi;
     DBuf<uint32_t> leaf_count;
+    DBuf<float> cost;             // binary-tree SAH cost per node (treelet restructuring)
     DBuf<uint2> tasks_a, tasks_b;
     DBuf<uint32_t> counters;      // [0] tasks in, [1] tasks out, [2] wide nodes, [3] prims
     DBuf<unsigned> cbounds;       // centroid bounds, order-preserving encoded
@@ -90,7 +91,21 @@ struct BuildResult {
 // the primitive id stored in slot prim_base + k.
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t stream,
-                      BuildResult* out);
+                      BuildResult* out, int treelet_passes);
+
+// Single-launch build for n <= SMALL_BUILD_MAX primitives (one CTA, shared
+// memory, no host synchronisation); same algorithm and output layout as
+// build_wide_bvh.  The result record stays on the device.  A build error (never
+// seen for a correct tree) sets out->error and bit 8 of *err_word.
+constexpr int SMALL_BUILD_MAX = 1024;
+struct SmallBuildOut {
+    uint32_t num_nodes, prims, error, pad;
+    double sah;
+    float lo[4], hi[4];
+};
+Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
+                            uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
+                            SmallBuildOut* out, unsigned* err_word, cudaStream_t stream);
 
 // Per-triangle padded boxes of one mesh (object space).
 Status launch_triangle_boxes(const float* positions, const uint32_t* indices, uint32_t vertex_offset,

@@ -49,8 +49,9 @@ class Tuning(C.Structure):
     """snk_tuning: launch knobs of the wavefront (0 = default)."""
     _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("shade_blocks_per_sm", C.c_uint32),
                 ("ray_chunk", C.c_uint32), ("refill_idle", C.c_uint32), ("prim_bias", C.c_uint32),
-                ("trace_variant", C.c_uint32), ("reserved", C.c_uint32 * 2)]
-    KNOBS = ("trace_blocks_per_sm", "shade_blocks_per_sm", "ray_chunk", "refill_idle", "prim_bias", "trace_variant")
+                ("trace_variant", C.c_uint32), ("bvh_treelet_passes", C.c_uint32), ("tlas_treelet_passes", C.c_uint32)]
+    KNOBS = ("trace_blocks_per_sm", "shade_blocks_per_sm", "ray_chunk", "refill_idle", "prim_bias", "trace_variant",
+             "bvh_treelet_passes", "tlas_treelet_passes")
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k in self.KNOBS}
@@ -76,6 +77,7 @@ OUTPUT_DTYPES = {"radiance": np.float32, "albedo": np.float32, "normal": np.floa
                  "rma": np.float32, "motion": np.float32, "depth": np.float32, "mat_flags": np.uint32,
                  "inst_id": np.uint32, "prim_id": np.uint32}
 
+TREELET_PASSES_NONE = 0xFFFFFFFF
 NOALLOC_MAX_PATHS = 65536   # SNK_NOALLOC_MAX_PATHS
 CACHE_NUM_WEIGHTS = 16576   # SNK_CACHE_NUM_WEIGHTS
 

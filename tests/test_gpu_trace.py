@@ -115,3 +115,27 @@ def test_invalid_scene_is_rejected(cuda, built_lib):
     bad[0]["transform"][0] = np.nan
     with pytest.raises(snkpt.SnkError):
         pt.set_instances(bad)
+
+
+def test_treelet_restructuring_lowers_sah_and_keeps_hits(cuda, built_lib):
+    """The restructured BVH must have a lower SAH cost and fewer node visits than
+    the plain LBVH while every hit stays identical (hits do not depend on the tree)."""
+    sc = scenes.config3(resolutions=[(320, 180)])
+    rng = np.random.default_rng(11)
+    rays = np.concatenate([camera_rays(sc.views[0]), random_rays(sc, 100_000, rng)])
+    st = abi.settings(spp=1, max_depth=4, seed=3, flags=abi.RENDER_COUNT_NODES)
+    res = {}
+    for passes in (snkpt.TREELET_PASSES_NONE, 1, 0):   # none, one pass, default (3)
+        pt = snkpt.PathTracer(0)
+        pt.set_tuning({"bvh_treelet_passes": passes})
+        pt.load_scene(sc)
+        hits = pt.trace_rays(rays)
+        pt.render([sc.views[0]], st, [{}])
+        s = pt.stats()
+        res[passes] = (s["blas_sah_cost"], hits, s["node_visits"] / (s["rays_camera"] + s["rays_extension"]))
+    plain, one, full = res[snkpt.TREELET_PASSES_NONE], res[1], res[0]
+    assert_hits_equal(one[1], plain[1], "one treelet pass vs plain LBVH")
+    assert_hits_equal(full[1], plain[1], "three treelet passes vs plain LBVH")
+    assert full[0] < one[0] < plain[0], (plain[0], one[0], full[0])
+    assert full[2] < plain[2], (plain[2], full[2])
+    assert_hits_equal(full[1], O.OracleScene(sc).trace(rays), "restructured BVH vs oracle")
