@@ -705,11 +705,13 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
     }
     if (tid == 0) { S.counters[5] = (uint32_t)n; S.counters[6] = 0u; }
     __syncthreads();
-    // 5. clustering rounds (thread i owns cluster position i)
+    // 5. clustering rounds (thread i owns cluster position i) while more than 32
+    // clusters remain; the last 32 finish inside warp 0 (every cluster sees every
+    // other one, rounds synchronise through shuffles instead of block barriers)
     int cur = 0, rounds = 0;
     uint32_t m = (uint32_t)n;
     uint32_t next_id = n > 1 ? (uint32_t)(n - 2) : 0u;
-    while (m > 1 && rounds < SMALL_BUILD_MAX) {
+    while (m > 32 && rounds < SMALL_BUILD_MAX) {
         const int i = tid;
         int nn = -1;
         float4 mylo = make_float4(0.f, 0.f, 0.f, 0.f), myhi = mylo;
@@ -734,9 +736,12 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
             merge = mutual && i < nn;
             keep = !mutual || i < nn;
         }
-        uint32_t total_keep, total_merge;
-        const uint32_t kpos = block_scan(keep ? 1u : 0u, S.warp_sums, &total_keep) - (keep ? 1u : 0u);
-        const uint32_t mrank = block_scan(merge ? 1u : 0u, S.warp_sums, &total_merge) - (merge ? 1u : 0u);
+        // one scan of both counts: kept clusters in the low half, merges in the high half
+        uint32_t totals;
+        const uint32_t v = (keep ? 1u : 0u) | (merge ? 0x10000u : 0u);
+        const uint32_t incl = block_scan(v, S.warp_sums, &totals);
+        const uint32_t kpos = (incl & 0xFFFFu) - (keep ? 1u : 0u), mrank = (incl >> 16) - (merge ? 1u : 0u);
+        const uint32_t total_keep = totals & 0xFFFFu, total_merge = totals >> 16;
         if (keep) {
             int id = S.clusters[cur][i];
             if (merge) {
@@ -757,6 +762,69 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
         __syncthreads();
         if (total_merge == 0) break;
     }
+    if (tid < 32 && m > 1 && m <= 32) {
+        const int lane = tid;
+        const bool live0 = lane < (int)m;
+        int id = live0 ? S.clusters[cur][lane] : -1;
+        float4 lo = live0 ? S.node_lo[id] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 hi = live0 ? S.node_hi[id] : lo;
+        uint32_t cnt = live0 ? S.leaf_count[id] : 0u;
+        for (int r = 0; m > 1 && r < 64; r++) {
+            const bool live = lane < (int)m;
+            float best = 3.4e38f;
+            int nn = -1;
+            for (int j = 0; j < (int)m; j++) {
+                const float4 ol = make_float4(__shfl_sync(0xFFFFFFFFu, lo.x, j), __shfl_sync(0xFFFFFFFFu, lo.y, j),
+                                              __shfl_sync(0xFFFFFFFFu, lo.z, j), 0.0f);
+                const float4 oh = make_float4(__shfl_sync(0xFFFFFFFFu, hi.x, j), __shfl_sync(0xFFFFFFFFu, hi.y, j),
+                                              __shfl_sync(0xFFFFFFFFu, hi.z, j), 0.0f);
+                if (j == lane || !live) continue;
+                const float a = half_area(f4min(lo, ol), f4max(hi, oh));
+                if (a < best) { best = a; nn = j; }
+            }
+            const int nn_of_nn = __shfl_sync(0xFFFFFFFFu, nn, nn < 0 ? lane : nn);
+            const bool mutual = live && nn >= 0 && nn_of_nn == lane;
+            const bool merge = mutual && lane < nn;
+            const bool keep = live && (!mutual || lane < nn);
+            const unsigned mm = __ballot_sync(0xFFFFFFFFu, merge), km = __ballot_sync(0xFFFFFFFFu, keep);
+            const unsigned below = (1u << lane) - 1u;
+            // partner data (for the merging lane)
+            const int pid = __shfl_sync(0xFFFFFFFFu, id, nn < 0 ? lane : nn);
+            const float4 pl = make_float4(__shfl_sync(0xFFFFFFFFu, lo.x, nn < 0 ? lane : nn),
+                                          __shfl_sync(0xFFFFFFFFu, lo.y, nn < 0 ? lane : nn),
+                                          __shfl_sync(0xFFFFFFFFu, lo.z, nn < 0 ? lane : nn), 0.0f);
+            const float4 ph = make_float4(__shfl_sync(0xFFFFFFFFu, hi.x, nn < 0 ? lane : nn),
+                                          __shfl_sync(0xFFFFFFFFu, hi.y, nn < 0 ? lane : nn),
+                                          __shfl_sync(0xFFFFFFFFu, hi.z, nn < 0 ? lane : nn), 0.0f);
+            const uint32_t pc = __shfl_sync(0xFFFFFFFFu, cnt, nn < 0 ? lane : nn);
+            if (merge) {
+                const int nid = (int)(next_id - (uint32_t)__popc(mm & below));
+                S.children[nid] = make_int2(id, pid);
+                lo = f4min(lo, pl);
+                hi = f4max(hi, ph);
+                cnt += pc;
+                S.node_lo[nid] = lo;
+                S.node_hi[nid] = hi;
+                S.leaf_count[nid] = cnt;
+                id = nid;
+            }
+            if (mm == 0u) { if (lane == 0) S.counters[6] |= 16u; break; }
+            next_id -= (uint32_t)__popc(mm);
+            // compact: lane k takes the k-th kept cluster
+            const int k = lane < __popc(km) ? (int)__fns(km, 0, lane + 1) : lane;
+            id = __shfl_sync(0xFFFFFFFFu, id, k);
+            lo = make_float4(__shfl_sync(0xFFFFFFFFu, lo.x, k), __shfl_sync(0xFFFFFFFFu, lo.y, k),
+                             __shfl_sync(0xFFFFFFFFu, lo.z, k), 0.0f);
+            hi = make_float4(__shfl_sync(0xFFFFFFFFu, hi.x, k), __shfl_sync(0xFFFFFFFFu, hi.y, k),
+                             __shfl_sync(0xFFFFFFFFu, hi.z, k), 0.0f);
+            cnt = __shfl_sync(0xFFFFFFFFu, cnt, k);
+            m = (uint32_t)__popc(km);
+        }
+        if (lane == 0) S.clusters[cur][0] = id;
+        if (lane == 0 && m != 1u) S.counters[6] |= 16u;
+        __syncwarp();
+    }
+    __syncthreads();
     if (tid == 0 && n > 1 && (next_id != 0xFFFFFFFFu || S.clusters[cur][0] != 0)) S.counters[6] |= 16u;
     __syncthreads();
     // 5b. optional treelet restructuring of the clustered tree (leaves dealt
