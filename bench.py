@@ -120,7 +120,7 @@ def profile_traffic():
     if not os.path.exists(PROFILE_SUMMARY):
         return None
     for line in open(PROFILE_SUMMARY):
-        if line.startswith("dram_bytes_per_launch_full_frame:"):
+        if line.startswith("dram_bytes_per_launch:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -259,6 +259,40 @@ def batched_views(snkpt, abi, scenes, device, stream, tuning, frames=5, warmup=3
     del outs, pt
     torch.cuda.empty_cache()
     return res
+
+
+def taa_bench(snkpt, device, stream, frames=20, warmup=3):
+    """TAA resolve of a 1920x1080 RGBA32F frame with RG32F motion (device buffers,
+    CUDA events on the resolver's stream, L2 flushed between frames).  Algorithmic
+    bytes: 88 per pixel (16 radiance + 8 motion + 16 history + 8 previous motion
+    read; 16 out + 16 next history + 8 next previous motion written)."""
+    import torch
+    W, H = 1920, 1080
+    g = torch.Generator(device=device)
+    g.manual_seed(7)
+    rad = torch.rand((W * H, 4), device=device, generator=g)
+    mot = (torch.rand((W * H, 2), device=device, generator=g) - 0.5) * 0.01
+    out = torch.empty_like(rad)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    t = snkpt.TaaResolve(W, H, device=device.index or 0, stream=stream)
+    for _ in range(warmup):
+        t.resolve(rad, mot, out)
+    ms = 0.0
+    for _ in range(frames):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        t.resolve(rad, mot, out)
+        b.record(stream)
+        b.synchronize()
+        ms += a.elapsed_time(b)
+    ms /= frames
+    gbs = 88.0 * W * H / (ms / 1e3) / 1e9
+    peak, kind = measured_peaks()
+    return {"workload": "TAA resolve, 1920x1080 RGBA32F + RG32F motion", "kernel": "k_taa_resolve",
+            "ms_per_frame": ms, "Mpixels_per_s": W * H / (ms / 1e3) / 1e6, "achieved_GBs": gbs,
+            "peak_GBs": peak, "frac": gbs / peak, "bytes_per_pixel": 88}
 
 
 def run_reference(args):
@@ -440,6 +474,7 @@ def run_ours(args):
     if rank == 0:
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(sc, view, settings(1, 0))
+        line["taa"] = taa_bench(snkpt, dev, stream)
         if not args.no_batched:
             line["batched_views"] = batched_views(snkpt, abi, scenes, dev, stream, tuning)
             line["batched_views_small"] = batched_views(snkpt, abi, scenes, dev, stream, tuning, frames=20, scale=8)

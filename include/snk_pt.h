@@ -369,6 +369,25 @@ int snk_pt_cache_train(snk_pt_ctx* ctx, const float* samples, uint32_t n, float 
  * accumulated so far) as float4 into out (memory space as given). */
 int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames);
 
+/* ---- TAA resolve ---------------------------------------------------------------
+ * TAA_ResolvePass (Core/src/renderpasses/TAA_ResolvePass.cpp:6-56) running
+ * TAA_Resolve.comp (Core/res/shaders/TAA_Resolve.comp:12-86): 3x3 neighbourhood
+ * mean/variance box (gamma 0.55), history fetched bilinearly at the motion-
+ * reprojected coordinate (repeat addressing, as the pass's sampler) and clipped
+ * to the box, 0.9 history blend, velocity-based disocclusion towards the mean.
+ * The object owns the history and previous-motion images (the pass's
+ * m_history_image / m_prev_frame_velocity_image) and updates them after each
+ * resolve, as the pass's two blits do.  radiance: RGBA32F, motion: RG32F (the
+ * render pass's outputs), out: RGBA32F, width x height, row-major; out may equal
+ * radiance (resolved in place, as the pass does).  The first resolve after create
+ * or reset takes the current frame as its history. */
+typedef struct snk_taa snk_taa;
+int snk_taa_create(int32_t device, void* stream, uint32_t width, uint32_t height, snk_taa** out);
+int snk_taa_destroy(snk_taa* taa);
+int snk_taa_reset(snk_taa* taa);
+int snk_taa_resolve(snk_taa* taa, const float* radiance, const float* motion, float* out, uint32_t memory);
+int snk_taa_get_last_error(const snk_taa* taa, char* buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

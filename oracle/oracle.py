@@ -73,6 +73,7 @@ def lib():
         L.snko_mlp_forward.argtypes = [vp, vp, u32, vp]
         L.snko_mlp_grad.argtypes = [vp, vp, vp, vp, u32, vp, C.c_int]
         L.snko_mlp_grad.restype = C.c_double
+        L.snko_taa_resolve.argtypes = [u32, u32, vp, vp, vp, vp, vp]
         L.snko_mlp_adam.argtypes = [vp, vp, vp, vp, u32, C.c_double, C.c_double, C.c_double, C.c_double]
         _lib = L
     return _lib
@@ -284,3 +285,27 @@ def mlp_adam(W, m, v, dW, step, lr=1e-2, b1=0.9, b2=0.99, eps=1e-8):
         assert a.dtype == np.float64 and a.flags.c_contiguous
     dW = np.ascontiguousarray(dW, np.float64)
     lib().snko_mlp_adam(_p(W), _p(m), _p(v), _p(dW), step, lr, b1, b2, eps)
+
+
+class OracleTaa:
+    """TAA_ResolvePass on the CPU: history and previous motion images, the first
+    resolve takes the current frame as its history (as snk_taa_resolve)."""
+
+    def __init__(self, width: int, height: int):
+        self.w, self.h = int(width), int(height)
+        self.hist = None
+        self.pmot = None
+
+    def reset(self):
+        self.hist = None
+        self.pmot = None
+
+    def resolve(self, radiance, motion):
+        cur = np.ascontiguousarray(radiance, np.float32).reshape(self.h * self.w, 4)
+        mot = np.ascontiguousarray(motion, np.float32).reshape(self.h * self.w, 2)
+        if self.hist is None:
+            self.hist, self.pmot = cur.copy(), mot.copy()
+        out = np.empty_like(cur)
+        lib().snko_taa_resolve(self.w, self.h, _p(cur), _p(mot), _p(self.hist), _p(self.pmot), _p(out))
+        self.hist, self.pmot = out.copy(), mot.copy()
+        return out

@@ -1639,3 +1639,100 @@ extern "C" void snko_mlp_adam(double* W, double* m, double* v, const double* dW,
         W[i] -= lr * (m[i] / c1) / (std::sqrt(v[i] / c2) + eps);
     }
 }
+
+// ---- TAA resolve ----------------------------------------------------------------
+// TAA_Resolve.comp (Core/res/shaders/TAA_Resolve.comp:12-86) per pixel, reading the
+// unresolved frame for every neighbourhood; history and previous velocity fetched
+// as texture() with a linear filter and repeat addressing (the pass's sampler,
+// Core/src/resources/Images.cpp:16-36), in FP32 with exact weights.  Binary32
+// basic operations in the shader's order (compiled with -ffp-contract=off).
+namespace {
+inline int taa_wrap(int i, int n) {
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+void taa_bilinear(const float* img, int C, int w, int h, float cu, float cv, float* o) {
+    const float u = cu * (float)w - 0.5f, v = cv * (float)h - 0.5f;
+    const float fu = std::floor(u), fv = std::floor(v);
+    const float a = u - fu, b = v - fv;
+    const int i0 = taa_wrap((int)fu, w), i1 = taa_wrap((int)fu + 1, w);
+    const int j0 = taa_wrap((int)fv, h), j1 = taa_wrap((int)fv + 1, h);
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    const float* t00 = img + ((size_t)j0 * w + i0) * C;
+    const float* t10 = img + ((size_t)j0 * w + i1) * C;
+    const float* t01 = img + ((size_t)j1 * w + i0) * C;
+    const float* t11 = img + ((size_t)j1 * w + i1) * C;
+    for (int c = 0; c < C; c++) o[c] = ((w00 * t00[c] + w10 * t10[c]) + w01 * t01[c]) + w11 * t11[c];
+}
+}  // namespace
+
+// cur: w*h RGBA, motion: w*h RG, hist: w*h RGBA, pmot: w*h RG -> out: w*h RGBA
+extern "C" void snko_taa_resolve(uint32_t w, uint32_t h, const float* cur, const float* motion, const float* hist,
+                                 const float* pmot, float* out) {
+    const int W = (int)w, H = (int)h;
+    for (int y = 0; y < H; y++) {
+        for (int x = 0; x < W; x++) {
+            const size_t pix = (size_t)y * W + x;
+            const float velx = motion[2 * pix], vely = motion[2 * pix + 1];
+            float hx = ((float)x + 0.5f) / (float)W + velx;
+            float hy = ((float)y + 0.5f) / (float)H + vely;
+            hx = std::fmin(std::fmax(hx, 0.0f), 1.0f);
+            hy = std::fmin(std::fmax(hy, 0.0f), 1.0f);
+            const float* c0 = cur + 4 * pix;
+            float mn[3] = {9999.0f, 9999.0f, 9999.0f}, mx[3] = {-9999.0f, -9999.0f, -9999.0f};
+            float m[3] = {0.0f, 0.0f, 0.0f}, m2[3] = {0.0f, 0.0f, 0.0f};
+            for (int ox = -1; ox <= 1; ox++) {
+                for (int oy = -1; oy <= 1; oy++) {
+                    const int qx = std::min(std::max(x + ox, 0), W - 1), qy = std::min(std::max(y + oy, 0), H - 1);
+                    const float* q = cur + 4 * ((size_t)qy * W + qx);
+                    for (int c = 0; c < 3; c++) {
+                        const float col = std::fmax(q[c], 0.0f);
+                        mn[c] = std::fmin(mn[c], col);
+                        mx[c] = std::fmax(mx[c], col);
+                        m[c] = m[c] + col;
+                        m2[c] = m2[c] + col * col;
+                    }
+                }
+            }
+            const float inv9 = 1.0f / 9.0f, gamma = 0.55f, eps = 0.00000001f;
+            float mu[3], minc[3], maxc[3], p[3];
+            for (int c = 0; c < 3; c++) {
+                mu[c] = m[c] * inv9;
+                const float sigma = std::sqrt(std::fabs(m2[c] * inv9 - mu[c] * mu[c]));
+                minc[c] = mu[c] - gamma * sigma;
+                maxc[c] = mu[c] + gamma * sigma;
+                p[c] = std::fmin(std::fmax(mu[c], mn[c]), mx[c]);
+            }
+            float hc4[4];
+            taa_bilinear(hist, 4, W, H, hx, hy, hc4);
+            float r[3];
+            for (int c = 0; c < 3; c++) r[c] = std::fmax(hc4[c], 0.0f) - p[c];
+            for (int c = 0; c < 3; c++) {
+                const float rmax = maxc[c] - p[c];
+                if (r[c] > rmax + eps) {
+                    const float s = rmax / r[c];
+                    for (int k = 0; k < 3; k++) r[k] = r[k] * s;
+                }
+            }
+            for (int c = 0; c < 3; c++) {
+                const float rmin = minc[c] - p[c];
+                if (r[c] < rmin - eps) {
+                    const float s = rmin / r[c];
+                    for (int k = 0; k < 3; k++) r[k] = r[k] * s;
+                }
+            }
+            float pv[2];
+            taa_bilinear(pmot, 2, W, H, hx, hy, pv);
+            const float vx = pv[0] + velx, vy = pv[1] + vely;
+            const float vlen = std::sqrt(vx * vx + vy * vy);
+            const float dis = std::fmin(std::fmax((vlen - 0.001f) * 10.0f, 0.0f), 1.0f);
+            float* o = out + 4 * pix;
+            for (int c = 0; c < 3; c++) {
+                const float hcol = p[c] + r[c];
+                const float f = c0[c] * (1.0f - 0.9f) + hcol * 0.9f;
+                o[c] = f * (1.0f - dis) + mu[c] * dis;
+            }
+            o[3] = 1.0f;
+        }
+    }
+}

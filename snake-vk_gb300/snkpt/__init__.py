@@ -27,6 +27,7 @@ EXPORTS = [
     "snk_pt_read_accumulator", "snk_pt_render_noalloc", "snk_pt_set_tuning", "snk_pt_get_tuning",
     "snk_pt_autotune", "snk_pt_cache_reset", "snk_pt_cache_set_weights", "snk_pt_cache_get_weights",
     "snk_pt_cache_set_bounds", "snk_pt_cache_encode", "snk_pt_cache_infer", "snk_pt_cache_train",
+    "snk_taa_create", "snk_taa_destroy", "snk_taa_reset", "snk_taa_resolve", "snk_taa_get_last_error",
 ]
 
 
@@ -120,6 +121,11 @@ def lib():
         L.snk_pt_cache_encode.argtypes = [vp, vp, u32, vp, u32]
         L.snk_pt_cache_infer.argtypes = [vp, vp, u32, vp, u32]
         L.snk_pt_cache_train.argtypes = [vp, vp, u32, C.c_float, vp, C.POINTER(C.c_float), u32]
+        L.snk_taa_create.argtypes = [C.c_int32, vp, u32, u32, C.POINTER(vp)]
+        L.snk_taa_destroy.argtypes = [vp]
+        L.snk_taa_reset.argtypes = [vp]
+        L.snk_taa_resolve.argtypes = [vp, vp, vp, vp, u32]
+        L.snk_taa_get_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
         _lib = L
     return _lib
 
@@ -371,6 +377,58 @@ def alloc_outputs(width: int, height: int, device=None, names=OUTPUT_NAMES) -> d
         else:
             out[k] = np.zeros(shape, OUTPUT_DTYPES[k])
     return out
+
+
+class TaaResolve:
+    """TAA_ResolvePass mirror (snk_taa_*): owns the history and previous-motion
+    images of one view and resolves a frame's radiance with its motion vectors.
+    Buffers: radiance (W*H, 4) float32, motion (W*H, 2) float32, either numpy
+    arrays (host) or torch CUDA tensors (device, on the resolver's stream)."""
+
+    def __init__(self, width: int, height: int, device: int = 0, stream=None):
+        self.width, self.height = int(width), int(height)
+        h = C.c_void_p()
+        s = None if stream is None else int(getattr(stream, "cuda_stream", stream))
+        rc = lib().snk_taa_create(device, s, self.width, self.height, C.byref(h))
+        if rc != 0:
+            raise SnkError(rc, "snk_taa_create failed")
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().snk_taa_destroy(h)
+            self._h = None
+
+    def _check(self, rc: int):
+        if rc != 0:
+            buf = C.create_string_buffer(512)
+            lib().snk_taa_get_last_error(self._h, buf, 512)
+            raise SnkError(rc, buf.value.decode(errors="replace"))
+
+    def reset(self):
+        self._check(lib().snk_taa_reset(self._h))
+
+    def resolve(self, radiance, motion, out=None):
+        """Resolves into `out` (default: a new array/tensor; may be `radiance`
+        itself for the in-place form of the reference pass)."""
+        dev = _is_device(radiance)
+        if dev != _is_device(motion):
+            raise ValueError("radiance and motion must both be host arrays or both device tensors")
+        if dev:
+            import torch
+            if out is None:
+                out = torch.empty_like(radiance)
+            torch.cuda.current_stream().synchronize()
+            self._check(lib().snk_taa_resolve(self._h, _ptr(radiance), _ptr(motion), _ptr(out), abi.MEM_DEVICE))
+        else:
+            radiance = np.ascontiguousarray(radiance, np.float32)
+            motion = np.ascontiguousarray(motion, np.float32)
+            if out is None:
+                out = np.empty_like(radiance)
+            self._check(lib().snk_taa_resolve(self._h, radiance.ctypes.data, motion.ctypes.data, out.ctypes.data,
+                                              abi.MEM_HOST))
+        return out
 
 
 class RT:

@@ -32,6 +32,7 @@ UNITS = {
     "restir.cu": True,
     "noalloc.cu": False,
     "mlp_cache.cu": False,
+    "taa.cu": True,
 }
 
 

@@ -216,3 +216,14 @@ def test_oracle_deterministic_hits(cfg):
     rng = np.random.default_rng(cfg)
     rays = random_rays(sc, 5000, rng)
     assert_hits_equal(osc.trace(rays, nthreads=1), osc.trace(rays, nthreads=8), "thread count")
+
+
+def test_taa_oracle_matches_golden_restatement():
+    """The oracle's TAA resolve equals the independent numpy binary32 restatement
+    (tests/golden/make_taa_golden.py) bit for bit over a 3-frame sequence."""
+    d = np.load(os.path.join(GOLDEN, "taa.npz"))
+    w, h = int(d["width"]), int(d["height"])
+    t = O.OracleTaa(w, h)
+    for f in range(d["radiance"].shape[0]):
+        o = t.resolve(d["radiance"][f], d["motion"][f])
+        assert np.array_equal(o.view(np.uint32), d["resolved"][f].view(np.uint32)), f
