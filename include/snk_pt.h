@@ -249,7 +249,7 @@ typedef struct snk_pt_stats {
     double   blas_sah_cost;      /* SAH cost of the BLASes (surface-area weighted) */
     double   last_render_ms;     /* device time of the last render (CUDA events) */
     uint32_t device_error;       /* last device error word (0 = none) */
-    uint32_t pad;
+    uint32_t instance_bvh_refits; /* instance BVH updates done by refit since create */
     double   stage_ms[12];       /* device time per stage of the last render (SNK_RENDER_PROFILE) */
     uint64_t stage_launches[12]; /* kernel launches per stage of the last render */
     uint64_t cache_queries;      /* paths terminated into the radiance cache */
@@ -270,6 +270,12 @@ typedef struct snk_tuning {
     uint32_t tlas_treelet_passes;   /* the same for the per-frame instance BVH (1); up to 1024
                                        instances it is built in one launch by locally-ordered
                                        clustering, and the passes refine that tree */
+    uint32_t tlas_refit_interval;   /* 0: rebuild the instance BVH on every instance update (as
+                                       TlasSystem::BuildTlas, TlasSystem.cpp:16-20); k >= 1:
+                                       refit it (same topology, new boxes) when only transforms
+                                       or materials changed, with a full rebuild every k-th
+                                       update (instance BVHs of up to 1024 instances) */
+    uint32_t reserved[3];
 } snk_tuning;
 
 #define SNK_TREELET_PASSES_NONE 0xFFFFFFFFu

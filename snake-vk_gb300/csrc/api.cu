@@ -72,6 +72,13 @@ struct snk_pt_ctx {
     DBuf<unsigned> d_err;
     DBuf<SmallBuildOut> d_small_out;   // result record of the single-launch instance BVH build
     bool tlas_small = false;
+    // instance BVH refit state: exact node boxes and depths, primitive order and
+    // the mesh of every listed instance at the last full build
+    DBuf<float4> d_tlas_box;
+    DBuf<uint32_t> d_tlas_depth, d_tlas_order;
+    std::vector<uint32_t> tlas_meshes;
+    uint32_t tlas_updates_since_build = 0;
+    uint64_t tlas_builds = 0, tlas_refits = 0;
 
     BuildScratch scratch;
     DBuf<float4> d_box_lo, d_box_hi;
@@ -364,7 +371,10 @@ Status build_instances(snk_pt_ctx* ctx) {
     SNK_TRY(upload(ctx->d_cdf, cdf.data(), cdf.size(), st));
     SNK_TRY(upload(ctx->d_pmf, pmf.data(), pmf.size(), st));
 
-    // instance BVH (rebuilt whenever instances change, as TlasSystem::BuildTlas)
+    // instance BVH (rebuilt whenever instances change, as TlasSystem::BuildTlas,
+    // or refitted when the tuning asks for it and the topology allows it)
+    const uint32_t prev_root = ctx->tlas_root;
+    const uint64_t prev_prims = ctx->tlas_prim_count;
     ctx->tlas_root = INVALID;
     ctx->tlas_nodes = 0;
     ctx->tlas_prim_count = 0;
@@ -379,20 +389,50 @@ Status build_instances(snk_pt_ctx* ctx) {
         SNK_TRY(launch_instance_boxes(ctx->d_inst_list.p, n, ctx->d_inst_shade.p, ctx->d_meshes.p, ctx->d_box_lo.p,
                                       ctx->d_box_hi.p, st));
         const int passes = treelet_passes(ctx->tune.tlas_treelet_passes, 1);
+        std::vector<uint32_t> meshes_now(n);
+        for (uint32_t k = 0; k < n; k++) meshes_now[k] = ctx->instances[list[k]].mesh_id;
+        const uint32_t interval = ctx->tune.tlas_refit_interval;
+        const bool refit = interval > 0 && ctx->tlas_small && prev_root != INVALID &&
+                           n <= (uint32_t)SMALL_BUILD_MAX && prev_prims == n && meshes_now == ctx->tlas_meshes &&
+                           ctx->tlas_updates_since_build + 1 < interval;
+        if (refit) {
+            // same instances on the same meshes: new boxes into the existing tree
+            SNK_TRY(refit_wide_bvh_small(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
+                                         ctx->d_tlas_order.p, ctx->d_small_out.p, ctx->d_tlas_box.p,
+                                         ctx->d_tlas_depth.p, ctx->d_err.p, st));
+            ctx->tlas_updates_since_build++;
+            ctx->tlas_refits++;
+            ctx->tlas_root = prev_root;   // the primitive map and counts are unchanged
+            ctx->tlas_nodes = n + 1;
+            ctx->tlas_prim_count = n;
+            return Status::Ok();
+        }
         if (n <= (uint32_t)SMALL_BUILD_MAX) {
             // one launch, no host round trip; the node count stays on the device
             // (traversal bounds its node indices by the capacity, n + 1)
             SNK_TRY_CUDA(ctx->d_small_out.reserve(1));
+            SNK_TRY_CUDA(ctx->d_tlas_box.reserve(2ull * (n + 1)));
+            SNK_TRY_CUDA(ctx->d_tlas_depth.reserve(n + 1));
+            SNK_TRY_CUDA(ctx->d_tlas_order.reserve(n));
             SNK_TRY(build_wide_bvh_small(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
-                                         ctx->d_prim_order.p, passes, ctx->d_small_out.p, ctx->d_err.p, st));
+                                         ctx->d_tlas_order.p, passes, ctx->d_small_out.p, ctx->d_err.p,
+                                         ctx->d_tlas_box.p, ctx->d_tlas_depth.p, st));
+            SNK_TRY(launch_map_prims(ctx->d_tlas_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
             ctx->tlas_nodes = n + 1;
             ctx->tlas_small = true;
+            ctx->tlas_meshes = meshes_now;
+            ctx->tlas_updates_since_build = 0;
+            ctx->tlas_builds++;
+            ctx->tlas_root = 0;
+            ctx->tlas_prim_count = n;
+            return Status::Ok();
         } else {
             BuildResult br;
             SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
                                    ctx->d_prim_order.p, st, &br, passes));
             ctx->tlas_nodes = br.num_nodes;
             ctx->tlas_small = false;
+            ctx->tlas_builds++;
         }
         SNK_TRY(launch_map_prims(ctx->d_prim_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
         ctx->tlas_root = 0;
@@ -1270,6 +1310,7 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     unsigned e = 0;
     if (ctx->d_err.p) cudaMemcpy(&e, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost);
     out->device_error = e;
+    out->instance_bvh_refits = (uint32_t)ctx->tlas_refits;
     return SNK_OK;
 }
 

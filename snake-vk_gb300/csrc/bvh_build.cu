@@ -421,6 +421,33 @@ __device__ __forceinline__ uint32_t ceil_exp_biased(float x) {
     return e > 254u ? 254u : e;
 }
 
+// 8-bit child-box quantisation of a wide node: a power-of-two scale per axis
+// (the smallest with 255 steps covering the parent box, rounded up) and child
+// planes rounded outwards, so the decoded boxes always contain the exact ones.
+struct QuantFrame {
+    float p[3], inv_scale[3];
+    uint32_t eb[3];
+};
+__device__ __forceinline__ QuantFrame quant_frame(float4 plo, float4 phi) {
+    QuantFrame F;
+    const float ex_[3] = {__fsub_ru(phi.x, plo.x), __fsub_ru(phi.y, plo.y), __fsub_ru(phi.z, plo.z)};
+    F.p[0] = plo.x; F.p[1] = plo.y; F.p[2] = plo.z;
+    for (int a = 0; a < 3; a++) {
+        F.eb[a] = ceil_exp_biased(__fdiv_ru(ex_[a], 255.0f));
+        F.inv_scale[a] = __uint_as_float((254u - F.eb[a]) << 23);   // 2^(127 - (eb - 127))
+    }
+    return F;
+}
+__device__ __forceinline__ void quant_child(const QuantFrame& F, float4 a4, float4 z4, WideNode& node, int s) {
+    const float clo[3] = {a4.x, a4.y, a4.z}, chi[3] = {z4.x, z4.y, z4.z};
+    for (int a = 0; a < 3; a++) {
+        const float ql = floorf(__fmul_rd(__fsub_rd(clo[a], F.p[a]), F.inv_scale[a]));
+        const float qh = ceilf(__fmul_ru(__fsub_ru(chi[a], F.p[a]), F.inv_scale[a]));
+        node.qlo[a][s] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
+        node.qhi[a][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
+    }
+}
+
 // One output node: task = (binary node, wide node slot).  counters: [1] tasks
 // out, [2] wide nodes, [3] primitive slots, [4] capacity error bits.
 __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, int n,
@@ -498,22 +525,14 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
         atomicOr(&counters[4], 1u);
         return;
     }
-    // quantisation frame
-    float ex_[3] = {__fsub_ru(phi.x, plo.x), __fsub_ru(phi.y, plo.y), __fsub_ru(phi.z, plo.z)};
-    uint32_t eb[3];
-    float inv_scale[3];
-    for (int a = 0; a < 3; a++) {
-        eb[a] = ceil_exp_biased(__fdiv_ru(ex_[a], 255.0f));
-        inv_scale[a] = __uint_as_float((254u - eb[a]) << 23);   // 2^(127 - (eb - 127))
-    }
+    const QuantFrame F = quant_frame(plo, phi);
     WideNode node;
     node.px = plo.x; node.py = plo.y; node.pz = plo.z;
-    node.ex = (uint8_t)eb[0]; node.ey = (uint8_t)eb[1]; node.ez = (uint8_t)eb[2];
+    node.ex = (uint8_t)F.eb[0]; node.ey = (uint8_t)F.eb[1]; node.ez = (uint8_t)F.eb[2];
     node.imask = 0;
     node.child_base = node_base + child_local;
     node.prim_base = prim_base + prim_local;
     uint32_t rank = 0, off = 0;
-    float p3[3] = {plo.x, plo.y, plo.z};
     double local_sah = 0.0;
     for (int s = 0; s < 8; s++) {
         int c = slot_child[s];
@@ -523,13 +542,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
             continue;
         }
         float4 a4 = node_lo[c], z4 = node_hi[c];
-        float clo[3] = {a4.x, a4.y, a4.z}, chi[3] = {z4.x, z4.y, z4.z};
-        for (int a = 0; a < 3; a++) {
-            float ql = floorf(__fmul_rd(__fsub_rd(clo[a], p3[a]), inv_scale[a]));
-            float qh = ceilf(__fmul_ru(__fsub_ru(chi[a], p3[a]), inv_scale[a]));
-            node.qlo[a][s] = (uint8_t)fminf(fmaxf(ql, 0.0f), 255.0f);
-            node.qhi[a][s] = (uint8_t)fminf(fmaxf(qh, 0.0f), 255.0f);
-        }
+        quant_child(F, a4, z4, node, s);
         float ha = half_area(a4, z4) / root_half_area;
         if (c < nl && leaf_count[c] > 3u) {
             node.meta[s] = 0x80u;
@@ -648,7 +661,8 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warp_sums, 
 
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
 k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, int n, int passes, WideNode* nodes,
-              uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, SmallBuildOut* out, unsigned* err_word) {
+              uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, SmallBuildOut* out, unsigned* err_word,
+              float4* wide_box, uint32_t* wide_depth) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmallSmem& S = *reinterpret_cast<SmallSmem*>(smem_raw);
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -859,9 +873,18 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
     for (; level < 4096; level++) {
         const uint32_t nin = S.counters[0];
         if (nin == 0) break;
-        for (uint32_t t = tid; t < nin; t += nt)
-            collapse_task(S.tasks[cc][t], S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
+        for (uint32_t t = tid; t < nin; t += nt) {
+            const uint2 task = S.tasks[cc][t];
+            // refit data: exact box and depth of every wide node
+            const uint32_t local = task.y - node_base;
+            if (local <= (uint32_t)n) {
+                wide_box[2 * local] = S.node_lo[task.x];
+                wide_box[2 * local + 1] = S.node_hi[task.x];
+                wide_depth[local] = (uint32_t)level;
+            }
+            collapse_task(task, S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
                           S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, &S.sah, rha);
+        }
         __syncthreads();
         if (tid == 0) { S.counters[0] = S.counters[1]; S.counters[1] = 0u; }
         cc ^= 1;
@@ -874,10 +897,72 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
         out->num_nodes = S.counters[2];
         out->prims = S.counters[3];
         out->error = e;
+        out->max_depth = level > 0 ? (uint32_t)(level - 1) : 0u;
         out->sah = 1.0 + S.sah;
         out->lo[0] = rlo.x; out->lo[1] = rlo.y; out->lo[2] = rlo.z; out->lo[3] = 0.0f;
         out->hi[0] = rhi.x; out->hi[1] = rhi.y; out->hi[2] = rhi.z; out->hi[3] = 0.0f;
         if (e && err_word) atomicOr(err_word, 8u);
+    }
+}
+
+// Refit of a wide BVH made by k_build_small, for moved primitives: the topology
+// (child and primitive slots) stays, every node's exact box and quantised child
+// planes are recomputed, deepest level first (one block, a barrier per level).
+__global__ void __launch_bounds__(SMALL_THREADS, 1)
+k_refit_small(WideNode* nodes, uint32_t node_base, uint32_t prim_base, const SmallBuildOut* info,
+              float4* wide_box, const uint32_t* wide_depth, const uint32_t* prim_order,
+              const float4* __restrict__ plo, const float4* __restrict__ phi, int n, unsigned* err_word) {
+    const uint32_t nn = info->num_nodes;
+    if (info->error || nn == 0 || nn > (uint32_t)n + 1u) return;
+    const int max_depth = (int)min(info->max_depth, 4095u);
+    for (int level = max_depth; level >= 0; level--) {
+        for (uint32_t k = threadIdx.x; k < nn; k += blockDim.x) {
+            if (wide_depth[k] != (uint32_t)level) continue;
+            WideNode node;
+            const uint4* src = reinterpret_cast<const uint4*>(nodes + node_base + k);
+            uint4* dst4 = reinterpret_cast<uint4*>(&node);
+            for (int q = 0; q < 5; q++) dst4[q] = src[q];
+            float4 clo[8], chi[8];
+            float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+            bool bad = false;
+            for (int s = 0; s < 8; s++) {
+                const uint32_t meta = node.meta[s];
+                clo[s] = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f);
+                chi[s] = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+                if (meta == 0u) continue;
+                if (meta == 0x80u) {
+                    const uint32_t child = node.child_base + (uint32_t)__popc(node.imask & ((1u << s) - 1u)) - node_base;
+                    if (child >= nn) { bad = true; continue; }
+                    clo[s] = wide_box[2 * child];
+                    chi[s] = wide_box[2 * child + 1];
+                } else {
+                    const uint32_t cnt = meta >> 5, off = meta & 31u;
+                    for (uint32_t j = 0; j < cnt; j++) {
+                        const uint32_t slot = node.prim_base + off + j - prim_base;
+                        if (slot >= (uint32_t)n) { bad = true; continue; }
+                        const uint32_t li = prim_order[slot];
+                        if (li >= (uint32_t)n) { bad = true; continue; }
+                        clo[s] = f4min(clo[s], plo[li]);
+                        chi[s] = f4max(chi[s], phi[li]);
+                    }
+                }
+                lo = f4min(lo, clo[s]);
+                hi = f4max(hi, chi[s]);
+            }
+            if (bad) { atomicOr(err_word, 8u); continue; }
+            const QuantFrame F = quant_frame(lo, hi);
+            node.px = lo.x; node.py = lo.y; node.pz = lo.z;
+            node.ex = (uint8_t)F.eb[0]; node.ey = (uint8_t)F.eb[1]; node.ez = (uint8_t)F.eb[2];
+            for (int s = 0; s < 8; s++) {
+                if (node.meta[s] == 0u) continue;
+                quant_child(F, clo[s], chi[s], node, s);
+            }
+            uint4* out4 = reinterpret_cast<uint4*>(nodes + node_base + k);
+            for (int q = 0; q < 5; q++) out4[q] = dst4[q];
+            wide_box[2 * k] = lo;
+            wide_box[2 * k + 1] = hi;
+        }
+        __syncthreads();
     }
 }
 
@@ -1046,12 +1131,25 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
 
 Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                             uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
-                            SmallBuildOut* out, unsigned* err_word, cudaStream_t st) {
+                            SmallBuildOut* out, unsigned* err_word, float4* wide_box, uint32_t* wide_depth,
+                            cudaStream_t st) {
     if (n == 0 || n > (uint32_t)SMALL_BUILD_MAX) return Status::Err(1, "build_wide_bvh_small: bad primitive count");
     SNK_TRY_CUDA(cudaFuncSetAttribute(k_build_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(SmallSmem)));
     k_build_small<<<1, SMALL_THREADS, sizeof(SmallSmem), st>>>(prim_lo, prim_hi, (int)n, treelet_passes, nodes,
-                                                                node_base, prim_base, prim_order, out, err_word);
+                                                                node_base, prim_base, prim_order, out, err_word,
+                                                                wide_box, wide_depth);
+    SNK_TRY_CUDA(cudaGetLastError());
+    return Status::Ok();
+}
+
+Status refit_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
+                            uint32_t node_base, uint32_t prim_base, const uint32_t* prim_order,
+                            const SmallBuildOut* info, float4* wide_box, const uint32_t* wide_depth, unsigned* err_word,
+                            cudaStream_t st) {
+    if (n == 0 || n > (uint32_t)SMALL_BUILD_MAX) return Status::Err(1, "refit_wide_bvh_small: bad primitive count");
+    k_refit_small<<<1, SMALL_THREADS, 0, st>>>(nodes, node_base, prim_base, info, wide_box, wide_depth, prim_order,
+                                               prim_lo, prim_hi, (int)n, err_word);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }

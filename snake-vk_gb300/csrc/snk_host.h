@@ -99,13 +99,22 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
 // seen for a correct tree) sets out->error and bit 8 of *err_word.
 constexpr int SMALL_BUILD_MAX = 1024;
 struct SmallBuildOut {
-    uint32_t num_nodes, prims, error, pad;
+    uint32_t num_nodes, prims, error, max_depth;
     double sah;
     float lo[4], hi[4];
 };
+// wide_box (2 x (n + 1) float4: exact lo, hi per wide node) and wide_depth
+// (n + 1) receive what a later refit needs.
 Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                             uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
-                            SmallBuildOut* out, unsigned* err_word, cudaStream_t stream);
+                            SmallBuildOut* out, unsigned* err_word, float4* wide_box, uint32_t* wide_depth,
+                            cudaStream_t stream);
+// Refit of a tree made by build_wide_bvh_small for the same n primitives in new
+// boxes (prim_order as that build wrote it; everything stays on the device).
+Status refit_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
+                            uint32_t node_base, uint32_t prim_base, const uint32_t* prim_order,
+                            const SmallBuildOut* info, float4* wide_box, const uint32_t* wide_depth,
+                            unsigned* err_word, cudaStream_t stream);
 
 // Per-triangle padded boxes of one mesh (object space).
 Status launch_triangle_boxes(const float* positions, const uint32_t* indices, uint32_t vertex_offset,

@@ -50,9 +50,10 @@ class Tuning(C.Structure):
     """snk_tuning: launch knobs of the wavefront (0 = default)."""
     _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("shade_blocks_per_sm", C.c_uint32),
                 ("ray_chunk", C.c_uint32), ("refill_idle", C.c_uint32), ("prim_bias", C.c_uint32),
-                ("trace_variant", C.c_uint32), ("bvh_treelet_passes", C.c_uint32), ("tlas_treelet_passes", C.c_uint32)]
+                ("trace_variant", C.c_uint32), ("bvh_treelet_passes", C.c_uint32), ("tlas_treelet_passes", C.c_uint32),
+                ("tlas_refit_interval", C.c_uint32), ("reserved", C.c_uint32 * 3)]
     KNOBS = ("trace_blocks_per_sm", "shade_blocks_per_sm", "ray_chunk", "refill_idle", "prim_bias", "trace_variant",
-             "bvh_treelet_passes", "tlas_treelet_passes")
+             "bvh_treelet_passes", "tlas_treelet_passes", "tlas_refit_interval")
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k in self.KNOBS}
@@ -351,7 +352,7 @@ class PathTracer:
     def stats(self) -> dict:
         s = np.zeros(1, abi.STATS_DTYPE)
         self._check(lib().snk_pt_get_stats(self._h, s.ctypes.data))
-        d = {k: s[k][0].item() for k in abi.STATS_DTYPE.names if k not in ("pad", "stage_ms", "stage_launches")}
+        d = {k: s[k][0].item() for k in abi.STATS_DTYPE.names if k not in ("stage_ms", "stage_launches")}
         d["stage_ms"] = dict(zip(abi.STAGES, s["stage_ms"][0].tolist()))
         d["stage_launches"] = dict(zip(abi.STAGES, s["stage_launches"][0].tolist()))
         return d

@@ -77,7 +77,7 @@ STATS_DTYPE = np.dtype([
     ("node_visits", "<u8"), ("triangle_tests", "<u8"), ("shadow_node_visits", "<u8"),
     ("shadow_triangle_tests", "<u8"), ("wide_nodes", "<u8"),
     ("triangles", "<u8"), ("instances", "<u8"), ("blas_sah_cost", "<f8"),
-    ("last_render_ms", "<f8"), ("device_error", "<u4"), ("pad", "<u4"),
+    ("last_render_ms", "<f8"), ("device_error", "<u4"), ("instance_bvh_refits", "<u4"),
     ("stage_ms", "<f8", (12,)), ("stage_launches", "<u8", (12,)), ("cache_queries", "<u8"),
     ("cache_samples", "<u8"),
 ])

@@ -139,3 +139,40 @@ def test_treelet_restructuring_lowers_sah_and_keeps_hits(cuda, built_lib):
     assert full[0] < one[0] < plain[0], (plain[0], one[0], full[0])
     assert full[2] < plain[2], (plain[2], full[2])
     assert_hits_equal(full[1], O.OracleScene(sc).trace(rays), "restructured BVH vs oracle")
+
+
+def test_instance_bvh_refit_keeps_hits(cuda, built_lib):
+    """Refitting the instance BVH (tlas_refit_interval) while instances move must
+    give the same hits as rebuilding it every update, and as the oracle."""
+    sc = scenes.config1(width=320, height=180)
+    rng = np.random.default_rng(21)
+    rays = np.concatenate([camera_rays(sc.views[0]), random_rays(sc, 100_000, rng)])
+    refit = snkpt.PathTracer(0)
+    refit.set_tuning({"tlas_refit_interval": 1000})
+    refit.load_scene(sc)
+    build = snkpt.PathTracer(0)
+    build.load_scene(sc)
+    inst = np.array(sc.instances, copy=True)
+    for f in range(5):
+        prev = inst["transform"].copy()
+        move = rng.normal(0.0, 2.0 + 4.0 * f, (len(inst), 3)).astype(np.float32)
+        move[-1] = 0.0                                      # the ground stays
+        t = inst["transform"].reshape(-1, 3, 4)
+        t[:, :, 3] += move
+        inst["transform"] = t.reshape(inst["transform"].shape)
+        inst["prev_transform"] = prev
+        refit.set_instances(inst)
+        build.set_instances(inst)
+        a, b = refit.trace_rays(rays), build.trace_rays(rays)
+        assert_hits_equal(a, b, f"refit vs rebuild, update {f}")
+    assert refit.stats()["instance_bvh_refits"] == 5
+    assert build.stats()["instance_bvh_refits"] == 0
+    sc.instances = inst
+    assert_hits_equal(a, O.OracleScene(sc).trace(rays), "refit vs oracle")
+    st = abi.settings(spp=1, max_depth=3, seed=4)
+    outs = [snkpt.alloc_outputs(320, 180, device=cuda) for _ in range(2)]
+    refit.render([sc.views[0]], st, [outs[0]])
+    build.render([sc.views[0]], st, [outs[1]])
+    refit.synchronize(); build.synchronize()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k].cpu().numpy(), outs[1][k].cpu().numpy()), k
