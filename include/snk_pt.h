@@ -375,6 +375,46 @@ int snk_pt_cache_train(snk_pt_ctx* ctx, const float* samples, uint32_t n, float 
  * accumulated so far) as float4 into out (memory space as given). */
 int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames);
 
+/* ---- .meshdata assets ------------------------------------------------------------
+ * Reader of the reference's binary mesh asset: AssetLoader::DeserializeMeshData
+ * (Core/src/assets/AssetLoader.cpp:166-211) of files written by
+ * SerializeMeshDataBinary (:146-164) through ByteSerializer
+ * (Core/headers/util/ByteSerializer.h:18-112).  Layout, little-endian, 64-bit
+ * byte counts: u64 uuid; name (u64 count + bytes); submeshes (u64 count + 20-byte
+ * records below); u32 num_vertices; u32 num_indices; positions, normals, tangents
+ * (u64 count + 12-byte vec3 each); tex_coords (u64 count + 8-byte vec2 each);
+ * indices (u64 count + u32 each); material UUIDs and texture UUIDs (u64 count +
+ * u64 each).  Every count is checked against the remaining bytes, and the vertex
+ * arrays against num_vertices / num_indices (the reference asserts only the
+ * former): a malformed file is SNK_ERR_INVALID_ARG with a message, never a read
+ * out of bounds.  Trailing bytes are ignored, as in the reference. */
+typedef struct snk_meshdata snk_meshdata;
+typedef struct snk_submesh {          /* Submesh, Core/headers/assets/MeshData.h:11-17 */
+    uint32_t num_indices, num_vertices, base_vertex, base_index, material_index;
+} snk_submesh;
+typedef struct snk_meshdata_info {    /* views into the loaded asset (valid until free) */
+    uint64_t           uuid;
+    const char*        name;
+    uint64_t           name_len;
+    uint32_t           num_submeshes, num_vertices, num_indices, num_materials, num_textures, pad;
+    const snk_submesh* submeshes;
+    const float*       positions;     /* num_vertices x 3 */
+    const float*       normals;       /* num_vertices x 3 */
+    const float*       tangents;      /* num_vertices x 3 */
+    const float*       tex_coords;    /* num_vertices x 2 */
+    const uint32_t*    indices;       /* num_indices */
+    const uint64_t*    materials;     /* material asset UUIDs (submesh material_index selects one) */
+    const uint64_t*    textures;      /* texture asset UUIDs */
+} snk_meshdata_info;
+/* copies what it needs out of bytes; err (may be NULL) receives the reason of a failure */
+int snk_meshdata_load(const void* bytes, size_t size, snk_meshdata** out, char* err, size_t err_len);
+int snk_meshdata_get_info(const snk_meshdata* md, snk_meshdata_info* info);
+/* One submesh as an snk_mesh for snk_pt_upload_meshes (one BLAS per submesh, as
+ * BLAS::GenerateFromMeshData, Core/src/resources/TLAS.cpp:109-186): positions and
+ * normals from base_vertex, indices from base_index (local to the submesh). */
+int snk_meshdata_submesh(const snk_meshdata* md, uint32_t index, snk_mesh* out);
+int snk_meshdata_free(snk_meshdata* md);
+
 /* ---- TAA resolve ---------------------------------------------------------------
  * TAA_ResolvePass (Core/src/renderpasses/TAA_ResolvePass.cpp:6-56) running
  * TAA_Resolve.comp (Core/res/shaders/TAA_Resolve.comp:12-86): 3x3 neighbourhood

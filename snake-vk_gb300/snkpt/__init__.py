@@ -28,6 +28,7 @@ EXPORTS = [
     "snk_pt_autotune", "snk_pt_cache_reset", "snk_pt_cache_set_weights", "snk_pt_cache_get_weights",
     "snk_pt_cache_set_bounds", "snk_pt_cache_encode", "snk_pt_cache_infer", "snk_pt_cache_train",
     "snk_taa_create", "snk_taa_destroy", "snk_taa_reset", "snk_taa_resolve", "snk_taa_get_last_error",
+    "snk_meshdata_load", "snk_meshdata_get_info", "snk_meshdata_submesh", "snk_meshdata_free",
 ]
 
 
@@ -127,6 +128,10 @@ def lib():
         L.snk_taa_reset.argtypes = [vp]
         L.snk_taa_resolve.argtypes = [vp, vp, vp, vp, u32]
         L.snk_taa_get_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.snk_meshdata_load.argtypes = [vp, C.c_size_t, C.POINTER(vp), C.c_char_p, C.c_size_t]
+        L.snk_meshdata_get_info.argtypes = [vp, vp]
+        L.snk_meshdata_submesh.argtypes = [vp, u32, C.POINTER(Mesh)]
+        L.snk_meshdata_free.argtypes = [vp]
         _lib = L
     return _lib
 

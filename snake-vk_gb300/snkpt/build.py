@@ -33,6 +33,7 @@ UNITS = {
     "noalloc.cu": False,
     "mlp_cache.cu": False,
     "taa.cu": True,
+    "meshdata.cpp": False,
 }
 
 
