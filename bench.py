@@ -295,6 +295,42 @@ def taa_bench(snkpt, device, stream, frames=20, warmup=3):
             "peak_GBs": peak, "frac": gbs / peak, "bytes_per_pixel": 88}
 
 
+def particle_bench(pt, abi, scene, device, n=100_000, steps=20, warmup=3):
+    """Particle collision queries on the benchmark scene: per step, the scene probe
+    of 100k particles (3 collision rays for each awake particle + 1 gravity ray)
+    through snk_pt_particle_probe with device buffers; particles placed just
+    short of surfaces hit by random rays (traced by the library itself)."""
+    import torch
+    rng = np.random.default_rng(11)
+    lo = np.min([np.min(m.positions, 0) for m in scene.meshes], 0) - 60.0
+    hi = np.max([np.max(m.positions, 0) for m in scene.meshes], 0) + 60.0
+    rays = np.zeros(4 * n, abi.RAY_DTYPE)
+    rays["o"] = rng.uniform([0.0, 1.0, 0.0], [100.0, 60.0, 100.0], (4 * n, 3))
+    d = rng.normal(size=(4 * n, 3))
+    rays["d"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmax"] = 1e4
+    hits = pt.trace_rays(rays)
+    ok = np.nonzero(hits["flags"] == 1)[0][:n]
+    p = np.zeros(len(ok), abi.PARTICLE_DTYPE)
+    p["position_radius"][:, :3] = rays["o"][ok] + rays["d"][ok] * (hits["t"][ok, None] - 0.3)
+    p["position_radius"][:, 3] = 0.25
+    p["velocity"][:, :3] = rng.normal(0.0, 3.0, (len(ok), 3))
+    p["velocity"][:, 3] = 1.0
+    t = torch.from_numpy(p.view(np.float32).reshape(-1, 12).copy()).to(device)
+    for _ in range(warmup):
+        pt.particle_probe(t, 1.0 / 120.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pt.particle_probe(t, 1.0 / 120.0)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / steps * 1e3
+    del lo, hi
+    return {"workload": f"{len(ok)} particles, 4 rays each (3 collision + gravity), config 1 scene",
+            "ms_per_step": ms, "Mrays_per_s": 4 * len(ok) / (ms / 1e3) / 1e6,
+            "note": "wall clock around the C-ABI call (synchronising), device buffers"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -492,6 +528,7 @@ def run_ours(args):
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(sc, view, settings(1, 0))
         line["taa"] = taa_bench(snkpt, dev, stream)
+        line["particles"] = particle_bench(pt, abi, sc, dev)
         if not args.no_batched:
             line["batched_views"] = batched_views(snkpt, abi, scenes, dev, stream, tuning)
             line["batched_views_small"] = batched_views(snkpt, abi, scenes, dev, stream, tuning, frames=20, scale=8)

@@ -375,6 +375,42 @@ int snk_pt_cache_train(snk_pt_ctx* ctx, const float* samples, uint32_t n, float 
  * accumulated so far) as float4 into out (memory space as given). */
 int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames);
 
+/* ---- particle collision queries -----------------------------------------------------
+ * The scene queries of the particle update pass (ParticleUpdate.rgen, run by
+ * ParticleSystem, Core/src/scene/ParticleSystem.cpp:60-62): rays whose closest
+ * hit returns the contact of ParticleUpdate.rchit:41-67 -- interpolated vertex
+ * normal through the instance's normal matrix, contact point origin + t*dir, and
+ * contact velocity (contact point - previous-frame transform of the hit point) /
+ * timestep.  The shader's rays use TerminateOnFirstHit, whose chosen hit depends
+ * on the driver's traversal order; these queries return the closest hit. */
+typedef struct snk_particle {         /* Particle, Core/res/shaders/Particle.glsl:3-7 */
+    float position_radius[4];
+    float velocity[4];                /* w: 1 awake, 0 asleep */
+    float colour[4];
+} snk_particle;
+typedef struct snk_contact {          /* RayPayload, ParticleUpdate.rgen:5-10 */
+    float normal[3];
+    float distance;                   /* hit t; -1 when nothing was hit */
+    float position[3];
+    float pad0;
+    float velocity[3];
+    float pad1;
+} snk_contact;
+/* traceRayEXT + ParticleUpdate.rchit for each ray (closest hit in (tmin, tmax)) */
+int snk_pt_contact_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, float timestep, snk_contact* out,
+                        uint32_t memory);
+/* Per particle, the scene part of ParticleUpdate.rgen main (:151-166): for an awake
+ * particle with non-zero speed the three TraceCollisionRay probes (:101-124; velocity
+ * direction, then the unnormalised right and up vectors, from the particle's back,
+ * lengths speed*DT + 2r and 2r) keeping the hit with the largest relative speed,
+ * and CalculateGravity (:150-165, DT = 1/120): gravity_dv[i] = -9.8*DT when the
+ * downward ray of length r + 0.001 hits nothing, else 0. */
+int snk_pt_particle_probe(snk_pt_ctx* ctx, const snk_particle* particles, uint32_t n, float timestep,
+                          snk_contact* candidate, float* gravity_dv, uint32_t memory);
+/* ConstrainOffsetWithScene (:126-148) of offsets (n x 3 floats) -> out (n x 3). */
+int snk_pt_particle_constrain(snk_pt_ctx* ctx, const snk_particle* particles, const float* offsets, uint32_t n,
+                              float timestep, float* out, uint32_t memory);
+
 /* ---- .meshdata assets ------------------------------------------------------------
  * Reader of the reference's binary mesh asset: AssetLoader::DeserializeMeshData
  * (Core/src/assets/AssetLoader.cpp:166-211) of files written by

@@ -74,6 +74,9 @@ def lib():
         L.snko_mlp_grad.argtypes = [vp, vp, vp, vp, u32, vp, C.c_int]
         L.snko_mlp_grad.restype = C.c_double
         L.snko_taa_resolve.argtypes = [u32, u32, vp, vp, vp, vp, vp]
+        L.snko_contact_rays.argtypes = [vp, vp, u32, C.c_float, vp, u32]
+        L.snko_particle_probe.argtypes = [vp, vp, u32, C.c_float, vp, vp, u32]
+        L.snko_particle_constrain.argtypes = [vp, vp, vp, u32, C.c_float, vp, u32]
         L.snko_mlp_adam.argtypes = [vp, vp, vp, vp, u32, C.c_double, C.c_double, C.c_double, C.c_double]
         _lib = L
     return _lib
@@ -149,6 +152,29 @@ class OracleScene:
                               nthreads or threads(), ctr.ctypes.data_as(C.POINTER(C.c_uint64)))
         assert rc == 0, rc
         return hits
+
+    def contact_rays(self, rays, timestep: float, nthreads: int | None = None):
+        rays = np.ascontiguousarray(rays, abi.RAY_DTYPE)
+        out = np.zeros(len(rays), abi.CONTACT_DTYPE)
+        rc = lib().snko_contact_rays(self._h, _p(rays), len(rays), timestep, _p(out), nthreads or threads())
+        assert rc == 0, rc
+        return out
+
+    def particle_probe(self, particles, timestep: float, nthreads: int | None = None):
+        p = np.ascontiguousarray(particles, abi.PARTICLE_DTYPE)
+        cand = np.zeros(len(p), abi.CONTACT_DTYPE)
+        grav = np.zeros(len(p), np.float32)
+        rc = lib().snko_particle_probe(self._h, _p(p), len(p), timestep, _p(cand), _p(grav), nthreads or threads())
+        assert rc == 0, rc
+        return cand, grav
+
+    def particle_constrain(self, particles, offsets, timestep: float, nthreads: int | None = None):
+        p = np.ascontiguousarray(particles, abi.PARTICLE_DTYPE)
+        off = np.ascontiguousarray(offsets, np.float32).reshape(len(p), 3)
+        out = np.zeros_like(off)
+        rc = lib().snko_particle_constrain(self._h, _p(p), _p(off), len(p), timestep, _p(out), nthreads or threads())
+        assert rc == 0, rc
+        return out
 
     def render_path(self, view, settings, pixels=None, pixel_base: int = 0, nthreads: int | None = None,
                     counters=None) -> dict:

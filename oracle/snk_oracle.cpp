@@ -1736,3 +1736,126 @@ extern "C" void snko_taa_resolve(uint32_t w, uint32_t h, const float* cur, const
         }
     }
 }
+
+// ---- particle collision queries ---------------------------------------------------
+// ParticleUpdate.rchit:41-67 for the closest hit of a ray, and the scene part of
+// ParticleUpdate.rgen (TraceCollisionRay :101-124, ConstrainOffsetWithScene
+// :126-148, CalculateGravity :150-165, main :151-166).  The shader's rays stop at
+// the first hit the driver finds; these use the closest hit.
+namespace {
+struct ContactRec { float n[3]; float dist; float p[3]; float pad0; float v[3]; float pad1; };
+struct ParticleRec { float pr[4], vel[4], col[4]; };
+const float PARTICLE_DT = 1.0f / 120.0f;   // Particle.glsl:1
+
+struct Contact { V3 n; float dist; V3 p; V3 v; };
+
+Contact contact_ray(const Scene& S, V3 o, V3 d, float tmin, float tmax, float timestep) {
+    Contact c;
+    c.n = v3(0.0f, 0.0f, 0.0f); c.p = c.n; c.v = c.n;
+    c.dist = -1.0f;
+    HitRec h;
+    if (!trace(S, o, d, tmin, tmax, false, &h, nullptr)) return c;
+    const InstData& I = S.insts[h.inst];
+    const MeshData& M = S.meshes[I.in.mesh_id];
+    const uint32_t* ix = &M.idx[3 * h.prim];
+    const V3 p0 = load3(&M.pos[3 * ix[0]]), p1 = load3(&M.pos[3 * ix[1]]), p2 = load3(&M.pos[3 * ix[2]]);
+    const float b0 = (1.0f - h.u) - h.v;
+    const V3 p = add(add(mul(p0, b0), mul(p1, h.u)), mul(p2, h.v));
+    V3 nn;
+    if (M.has_normals) {
+        const V3 n0 = load3(&M.nrm[3 * ix[0]]), n1 = load3(&M.nrm[3 * ix[1]]), n2 = load3(&M.nrm[3 * ix[2]]);
+        nn = add(add(mul(n0, b0), mul(n1, h.u)), mul(n2, h.v));
+    } else {
+        nn = cross(sub(p1, p0), sub(p2, p0));
+    }
+    c.n = normalize(mat3_mul(I.nmat, nn));
+    c.p = add(o, mul(d, h.t));
+    const V3 prev = xform_point(I.in.prev_transform, p);
+    c.v = v3((c.p.x - prev.x) / timestep, (c.p.y - prev.y) / timestep, (c.p.z - prev.z) / timestep);
+    c.dist = h.t;
+    return c;
+}
+
+void store_contact(ContactRec* o, const Contact& c) {
+    o->n[0] = c.n.x; o->n[1] = c.n.y; o->n[2] = c.n.z; o->dist = c.dist;
+    o->p[0] = c.p.x; o->p[1] = c.p.y; o->p[2] = c.p.z; o->pad0 = 0.0f;
+    o->v[0] = c.v.x; o->v[1] = c.v.y; o->v[2] = c.v.z; o->pad1 = 0.0f;
+}
+}  // namespace
+
+extern "C" int snko_contact_rays(void* sp, const Ray* rays, uint32_t n, float timestep, ContactRec* out,
+                                 uint32_t nthreads) {
+    Scene& S = *(Scene*)sp;
+    if (!S.built) return 4;
+    parallel_for(n, nthreads, 1024, [&](uint32_t b, uint32_t e, uint32_t) {
+        for (uint32_t i = b; i < e; i++) {
+            const Ray& r = rays[i];
+            store_contact(out + i, contact_ray(S, v3(r.ox, r.oy, r.oz), v3(r.dx, r.dy, r.dz), r.tmin, r.tmax, timestep));
+        }
+    });
+    return 0;
+}
+
+extern "C" int snko_particle_probe(void* sp, const ParticleRec* P, uint32_t n, float timestep, ContactRec* cand_out,
+                                   float* gravity, uint32_t nthreads) {
+    Scene& S = *(Scene*)sp;
+    if (!S.built) return 4;
+    parallel_for(n, nthreads, 1024, [&](uint32_t b, uint32_t e, uint32_t) {
+        for (uint32_t i = b; i < e; i++) {
+            const ParticleRec& q = P[i];
+            const V3 pos = v3(q.pr[0], q.pr[1], q.pr[2]), vel = v3(q.vel[0], q.vel[1], q.vel[2]);
+            const float rad = q.pr[3];
+            const bool asleep = q.vel[3] < 0.5f;
+            Contact cand;
+            cand.n = v3(0.0f, 0.0f, 0.0f); cand.p = cand.n; cand.v = cand.n;
+            cand.dist = -1.0f;
+            float best = 0.0f;
+            const float speed = length(vel);
+            if (!asleep && speed > 0.0f && speed <= 3.0e38f) {
+                const V3 vdir = v3(vel.x / speed, vel.y / speed, vel.z / speed);
+                const V3 right = std::fabs(dot(vdir, v3(0.0f, 1.0f, 0.0f))) > 0.99f ? cross(vdir, v3(0.0f, 0.0f, 1.0f))
+                                                                                 : cross(vdir, v3(0.0f, 1.0f, 0.0f));
+                const V3 up = cross(right, vdir);
+                const V3 dirs[3] = {vdir, right, up};
+                for (int k = 0; k < 3; k++) {
+                    const float len = k == 0 ? speed * PARTICLE_DT + rad * 2.0f : rad * 2.0f;
+                    const V3 o = sub(pos, mul(dirs[k], rad));
+                    const Contact c = contact_ray(S, o, dirs[k], 0.0f, len, timestep);
+                    const float w = length(sub(c.v, vel));
+                    if (c.dist > 0.0f && w > best) { best = w; cand = c; }
+                }
+            }
+            store_contact(cand_out + i, cand);
+            const Contact g = contact_ray(S, pos, v3(0.0f, -1.0f, 0.0f), 0.0f, rad + 0.001f, timestep);
+            gravity[i] = g.dist < 0.0f ? -9.8f * PARTICLE_DT : 0.0f;
+        }
+    });
+    return 0;
+}
+
+extern "C" int snko_particle_constrain(void* sp, const ParticleRec* P, const float* off, uint32_t n, float timestep,
+                                       float* out, uint32_t nthreads) {
+    Scene& S = *(Scene*)sp;
+    if (!S.built) return 4;
+    parallel_for(n, nthreads, 1024, [&](uint32_t b, uint32_t e, uint32_t) {
+        for (uint32_t i = b; i < e; i++) {
+            const ParticleRec& q = P[i];
+            const V3 o = v3(off[3 * (size_t)i], off[3 * (size_t)i + 1], off[3 * (size_t)i + 2]);
+            const float len = length(o);
+            V3 res = v3(0.0f, 0.0f, 0.0f);
+            if (!(len < 0.00001f)) {
+                const V3 dir = v3(o.x / len, o.y / len, o.z / len);
+                const float rad = q.pr[3];
+                const Contact c = contact_ray(S, v3(q.pr[0], q.pr[1], q.pr[2]), dir, 0.0f, len + rad, timestep);
+                if (c.dist > 0.0f) {
+                    const float m = std::fmax(c.dist - rad * 0.9f, 0.0f), s = rad * 0.05f;
+                    res = add(mul(dir, m), mul(c.n, s));
+                } else {
+                    res = o;
+                }
+            }
+            out[3 * (size_t)i] = res.x; out[3 * (size_t)i + 1] = res.y; out[3 * (size_t)i + 2] = res.z;
+        }
+    });
+    return 0;
+}

@@ -15,6 +15,7 @@
 #include "snk_frame.h"
 #include "snk_host.h"
 #include "snk_mlp.h"
+#include "snk_particles.h"
 
 using namespace snk;
 
@@ -70,6 +71,7 @@ struct snk_pt_ctx {
     DBuf<float> d_cdf, d_pmf;
     uint32_t n_emissive = 0, n_local = 0;
     DBuf<unsigned> d_err;
+    DBuf<unsigned char> q_in, q_in2, q_out, q_out2;   // staging of the particle / contact queries
     DBuf<SmallBuildOut> d_small_out;   // result record of the single-launch instance BVH build
     bool tlas_small = false;
     // instance BVH refit state: exact node boxes and depths, primitive order and
@@ -1247,6 +1249,93 @@ int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit*
     if (memory == SNK_MEM_HOST &&
         cudaMemcpyAsync(hits, d_hits, sizeof(snk_hit) * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return fail(ctx, SNK_ERR_CUDA, "trace_rays: hit download");
+    API_TRY(check_device_error(ctx));
+    return SNK_OK;
+}
+
+extern "C++" {
+namespace {
+// device view of a caller buffer: the buffer itself, or a staging copy of it
+template <class T>
+T* stage_in(snk_pt_ctx* ctx, DBuf<unsigned char>& b, const void* src, size_t bytes, uint32_t memory, Status* st) {
+    if (memory == SNK_MEM_DEVICE) return reinterpret_cast<T*>(const_cast<void*>(src));
+    if (b.reserve(bytes ? bytes : 1)) { *st = Status::Err(SNK_ERR_OUT_OF_MEMORY, "query staging"); return nullptr; }
+    if (bytes && cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream)) {
+        *st = Status::Err(SNK_ERR_CUDA, "query upload");
+        return nullptr;
+    }
+    return reinterpret_cast<T*>(b.p);
+}
+template <class T>
+T* stage_out(DBuf<unsigned char>& b, void* dst, size_t bytes, uint32_t memory, Status* st) {
+    if (memory == SNK_MEM_DEVICE) return reinterpret_cast<T*>(dst);
+    if (b.reserve(bytes ? bytes : 1)) { *st = Status::Err(SNK_ERR_OUT_OF_MEMORY, "query staging"); return nullptr; }
+    return reinterpret_cast<T*>(b.p);
+}
+Status download(snk_pt_ctx* ctx, void* dst, const void* src, size_t bytes, uint32_t memory) {
+    if (memory == SNK_MEM_HOST && bytes)
+        SNK_TRY_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return Status::Ok();
+}
+}  // namespace
+}  // extern "C++"
+
+int snk_pt_contact_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, float timestep, snk_contact* out,
+                        uint32_t memory) {
+    if (!ctx || (n && (!rays || !out)) || memory > SNK_MEM_HOST || !(timestep > 0.0f))
+        return fail(ctx, SNK_ERR_INVALID_ARG, "contact_rays: bad arguments");
+    API_TRY(set_device(ctx));
+    API_TRY(ensure_built(ctx));
+    if (n == 0) return SNK_OK;
+    Status st;
+    const float4* d_rays = stage_in<const float4>(ctx, ctx->q_in, rays, sizeof(snk_ray) * (size_t)n, memory, &st);
+    ContactOut* d_out = stage_out<ContactOut>(ctx->q_out, out, sizeof(snk_contact) * (size_t)n, memory, &st);
+    if (!st.ok()) return fail(ctx, st);
+    cudaError_t e = launch_contact_rays(scene_dev(ctx), d_rays, n, timestep, d_out, grid_of(ctx, 16), ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("contact_rays: ") + cudaGetErrorString(e));
+    API_TRY(download(ctx, out, d_out, sizeof(snk_contact) * (size_t)n, memory));
+    API_TRY(check_device_error(ctx));
+    return SNK_OK;
+}
+
+int snk_pt_particle_probe(snk_pt_ctx* ctx, const snk_particle* particles, uint32_t n, float timestep,
+                          snk_contact* candidate, float* gravity_dv, uint32_t memory) {
+    if (!ctx || (n && (!particles || !candidate || !gravity_dv)) || memory > SNK_MEM_HOST || !(timestep > 0.0f))
+        return fail(ctx, SNK_ERR_INVALID_ARG, "particle_probe: bad arguments");
+    API_TRY(set_device(ctx));
+    API_TRY(ensure_built(ctx));
+    if (n == 0) return SNK_OK;
+    Status st;
+    const ParticleDev* d_p =
+        stage_in<const ParticleDev>(ctx, ctx->q_in, particles, sizeof(snk_particle) * (size_t)n, memory, &st);
+    ContactOut* d_c = stage_out<ContactOut>(ctx->q_out, candidate, sizeof(snk_contact) * (size_t)n, memory, &st);
+    float* d_g = stage_out<float>(ctx->q_out2, gravity_dv, sizeof(float) * (size_t)n, memory, &st);
+    if (!st.ok()) return fail(ctx, st);
+    cudaError_t e = launch_particle_probe(scene_dev(ctx), d_p, n, timestep, d_c, d_g, grid_of(ctx, 16), ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("particle_probe: ") + cudaGetErrorString(e));
+    API_TRY(download(ctx, candidate, d_c, sizeof(snk_contact) * (size_t)n, memory));
+    API_TRY(download(ctx, gravity_dv, d_g, sizeof(float) * (size_t)n, memory));
+    API_TRY(check_device_error(ctx));
+    return SNK_OK;
+}
+
+int snk_pt_particle_constrain(snk_pt_ctx* ctx, const snk_particle* particles, const float* offsets, uint32_t n,
+                              float timestep, float* out, uint32_t memory) {
+    if (!ctx || (n && (!particles || !offsets || !out)) || memory > SNK_MEM_HOST || !(timestep > 0.0f))
+        return fail(ctx, SNK_ERR_INVALID_ARG, "particle_constrain: bad arguments");
+    API_TRY(set_device(ctx));
+    API_TRY(ensure_built(ctx));
+    if (n == 0) return SNK_OK;
+    Status st;
+    const ParticleDev* d_p =
+        stage_in<const ParticleDev>(ctx, ctx->q_in, particles, sizeof(snk_particle) * (size_t)n, memory, &st);
+    const float* d_off = stage_in<const float>(ctx, ctx->q_in2, offsets, 3 * sizeof(float) * (size_t)n, memory, &st);
+    float* d_out = stage_out<float>(ctx->q_out, out, 3 * sizeof(float) * (size_t)n, memory, &st);
+    if (!st.ok()) return fail(ctx, st);
+    cudaError_t e =
+        launch_particle_constrain(scene_dev(ctx), d_p, d_off, n, timestep, d_out, grid_of(ctx, 16), ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("particle_constrain: ") + cudaGetErrorString(e));
+    API_TRY(download(ctx, out, d_out, 3 * sizeof(float) * (size_t)n, memory));
     API_TRY(check_device_error(ctx));
     return SNK_OK;
 }

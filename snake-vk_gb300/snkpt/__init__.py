@@ -29,6 +29,7 @@ EXPORTS = [
     "snk_pt_cache_set_bounds", "snk_pt_cache_encode", "snk_pt_cache_infer", "snk_pt_cache_train",
     "snk_taa_create", "snk_taa_destroy", "snk_taa_reset", "snk_taa_resolve", "snk_taa_get_last_error",
     "snk_meshdata_load", "snk_meshdata_get_info", "snk_meshdata_submesh", "snk_meshdata_free",
+    "snk_pt_contact_rays", "snk_pt_particle_probe", "snk_pt_particle_constrain",
 ]
 
 
@@ -132,6 +133,9 @@ def lib():
         L.snk_meshdata_get_info.argtypes = [vp, vp]
         L.snk_meshdata_submesh.argtypes = [vp, u32, C.POINTER(Mesh)]
         L.snk_meshdata_free.argtypes = [vp]
+        L.snk_pt_contact_rays.argtypes = [vp, vp, u32, C.c_float, vp, u32]
+        L.snk_pt_particle_probe.argtypes = [vp, vp, u32, C.c_float, vp, vp, u32]
+        L.snk_pt_particle_constrain.argtypes = [vp, vp, vp, u32, C.c_float, vp, u32]
         _lib = L
     return _lib
 
@@ -353,6 +357,41 @@ class PathTracer:
         hits = np.zeros(len(r), abi.HIT_DTYPE)
         self._check(lib().snk_pt_trace_rays(self._h, r.ctypes.data, len(r), hits.ctypes.data, flags, abi.MEM_HOST))
         return hits
+
+    # ---- particle collision queries (ParticleUpdate.rgen / .rchit) -------------------
+    def contact_rays(self, rays, timestep: float):
+        """Closest-hit contacts (abi.CONTACT_DTYPE) of host rays (abi.RAY_DTYPE)."""
+        r = np.ascontiguousarray(rays, abi.RAY_DTYPE)
+        out = np.zeros(len(r), abi.CONTACT_DTYPE)
+        self._check(lib().snk_pt_contact_rays(self._h, r.ctypes.data, len(r), timestep, out.ctypes.data,
+                                              abi.MEM_HOST))
+        return out
+
+    def particle_probe(self, particles, timestep: float):
+        """(candidate contact, gravity velocity change) per particle; host or CUDA buffers."""
+        if _is_device(particles):
+            import torch
+            n = particles.shape[0]
+            cand = torch.empty((n, 12), dtype=torch.float32, device=particles.device)
+            grav = torch.empty(n, dtype=torch.float32, device=particles.device)
+            torch.cuda.synchronize(particles.device)
+            self._check(lib().snk_pt_particle_probe(self._h, particles.data_ptr(), n, timestep, cand.data_ptr(),
+                                                    grav.data_ptr(), abi.MEM_DEVICE))
+            return cand, grav
+        p = np.ascontiguousarray(particles, abi.PARTICLE_DTYPE)
+        cand = np.zeros(len(p), abi.CONTACT_DTYPE)
+        grav = np.zeros(len(p), np.float32)
+        self._check(lib().snk_pt_particle_probe(self._h, p.ctypes.data, len(p), timestep, cand.ctypes.data,
+                                                grav.ctypes.data, abi.MEM_HOST))
+        return cand, grav
+
+    def particle_constrain(self, particles, offsets, timestep: float):
+        p = np.ascontiguousarray(particles, abi.PARTICLE_DTYPE)
+        off = np.ascontiguousarray(offsets, np.float32).reshape(len(p), 3)
+        out = np.zeros_like(off)
+        self._check(lib().snk_pt_particle_constrain(self._h, p.ctypes.data, off.ctypes.data, len(p), timestep,
+                                                    out.ctypes.data, abi.MEM_HOST))
+        return out
 
     def stats(self) -> dict:
         s = np.zeros(1, abi.STATS_DTYPE)

@@ -72,6 +72,13 @@ HIT_DTYPE = np.dtype([("t", "<f4"), ("inst", "<u4"), ("prim", "<u4"), ("u", "<f4
                       ("flags", "<u4")])
 assert HIT_DTYPE.itemsize == 24
 
+# snk_particle (Particle.glsl:3-7) and snk_contact (ParticleUpdate.rgen:5-10)
+PARTICLE_DTYPE = np.dtype([("position_radius", "<f4", (4,)), ("velocity", "<f4", (4,)), ("colour", "<f4", (4,))])
+assert PARTICLE_DTYPE.itemsize == 48
+CONTACT_DTYPE = np.dtype([("normal", "<f4", (3,)), ("distance", "<f4"), ("position", "<f4", (3,)), ("pad0", "<f4"),
+                          ("velocity", "<f4", (3,)), ("pad1", "<f4")])
+assert CONTACT_DTYPE.itemsize == 48
+
 STATS_DTYPE = np.dtype([
     ("rays_camera", "<u8"), ("rays_extension", "<u8"), ("rays_shadow", "<u8"),
     ("node_visits", "<u8"), ("triangle_tests", "<u8"), ("shadow_node_visits", "<u8"),

@@ -34,6 +34,7 @@ UNITS = {
     "mlp_cache.cu": False,
     "taa.cu": True,
     "meshdata.cpp": False,
+    "particles.cu": True,
 }
 
 
