@@ -72,10 +72,19 @@ class ClockSampler:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the sampler's first line comes after nvidia-smi has started: wait for it
+        # (up to 3 s) so that the timed region is covered from its start
+        t0 = time.time()
+        while time.time() - t0 < 3.0:
+            self.f.flush()
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self) -> dict | None:
         if self.proc is None:
@@ -442,7 +451,6 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier()
     total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    clk = clocks.stop()
     if ws > 1:
         import torch.distributed as dist
         t = torch.tensor([total_ms], device=dev)
@@ -505,6 +513,7 @@ def run_ours(args):
         refit_rays += s["rays_camera"] + s["rays_extension"] + s["rays_shadow"]
     refit_s = time.perf_counter() - t0
     pt.set_tuning(tuning)
+    clk = clocks.stop()   # sampled over the device-timed and the end-to-end frames
     h2d = inst.nbytes + abi.VIEW_DTYPE.itemsize + abi.SETTINGS_DTYPE.itemsize
     d2h = host_rad.nbytes
 
