@@ -275,7 +275,9 @@ typedef struct snk_tuning {
                                        refit it (same topology, new boxes) when only transforms
                                        or materials changed, with a full rebuild every k-th
                                        update (instance BVHs of up to 1024 instances) */
-    uint32_t reserved[3];
+    uint32_t bvh_leaf_max;          /* primitives per leaf of later mesh BVH builds, 1..4 (1) */
+    uint32_t tlas_leaf_max;         /* instances per leaf of the instance BVH, 1..4 (1) */
+    uint32_t reserved;
 } snk_tuning;
 
 #define SNK_TREELET_PASSES_NONE 0xFFFFFFFFu

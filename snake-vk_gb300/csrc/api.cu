@@ -195,6 +195,8 @@ void invert_affine(const float* mf, float* inv_out, float* nmat_out, float* det_
     *det_out = (float)det;
 }
 
+uint32_t leaf_size(uint32_t knob, uint32_t dflt) { return knob ? knob : dflt; }
+
 int treelet_passes(uint32_t knob, int dflt) {
     return knob == SNK_TREELET_PASSES_NONE ? 0 : (knob ? (int)knob : dflt);
 }
@@ -244,7 +246,7 @@ Status build_meshes(snk_pt_ctx* ctx) {
         BuildResult br;
         SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, mi.num_triangles, ctx->d_blas.p,
                                node_base, prim_base, ctx->d_prim_order.p, st, &br,
-                               treelet_passes(ctx->tune.bvh_treelet_passes, 3)));
+                               treelet_passes(ctx->tune.bvh_treelet_passes, 3), leaf_size(ctx->tune.bvh_leaf_max, 1)));
         SNK_TRY(launch_fill_triangles(ctx->d_prim_order.p, mi.num_triangles, ctx->d_pos.p, ctx->d_idx.p,
                                       mi.vertex_offset, mi.index_offset, ctx->d_tris.p + prim_base, st));
         mi.blas_root = node_base;
@@ -418,7 +420,8 @@ Status build_instances(snk_pt_ctx* ctx) {
             SNK_TRY_CUDA(ctx->d_tlas_order.reserve(n));
             SNK_TRY(build_wide_bvh_small(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
                                          ctx->d_tlas_order.p, passes, ctx->d_small_out.p, ctx->d_err.p,
-                                         ctx->d_tlas_box.p, ctx->d_tlas_depth.p, st));
+                                         ctx->d_tlas_box.p, ctx->d_tlas_depth.p, st,
+                                         leaf_size(ctx->tune.tlas_leaf_max, 1)));
             SNK_TRY(launch_map_prims(ctx->d_tlas_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
             ctx->tlas_nodes = n + 1;
             ctx->tlas_small = true;
@@ -431,7 +434,7 @@ Status build_instances(snk_pt_ctx* ctx) {
         } else {
             BuildResult br;
             SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
-                                   ctx->d_prim_order.p, st, &br, passes));
+                                   ctx->d_prim_order.p, st, &br, passes, leaf_size(ctx->tune.tlas_leaf_max, 1)));
             ctx->tlas_nodes = br.num_nodes;
             ctx->tlas_small = false;
             ctx->tlas_builds++;
@@ -985,7 +988,8 @@ int snk_pt_set_tuning(snk_pt_ctx* ctx, const snk_tuning* t) {
     if (t->trace_blocks_per_sm > 64 || t->shade_blocks_per_sm > 64 || t->ray_chunk > 4096 || t->refill_idle > 32 ||
         t->prim_bias > 64 || t->trace_variant > 2 || 
         (t->bvh_treelet_passes > 16 && t->bvh_treelet_passes != SNK_TREELET_PASSES_NONE) ||
-        (t->tlas_treelet_passes > 16 && t->tlas_treelet_passes != SNK_TREELET_PASSES_NONE))
+        (t->tlas_treelet_passes > 16 && t->tlas_treelet_passes != SNK_TREELET_PASSES_NONE) ||
+        t->bvh_leaf_max > LEAF_MAX_LIMIT || t->tlas_leaf_max > LEAF_MAX_LIMIT)
         return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: knob out of range");
     ctx->tune = *t;
     return SNK_OK;

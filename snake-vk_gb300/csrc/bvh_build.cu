@@ -206,7 +206,6 @@ constexpr int TL_SUBSETS = 1 << TL_LEAVES;
 constexpr int TL_WARPS = BLK / 32;
 constexpr float SAH_CI = 1.2f;   // binary internal node
 constexpr float SAH_CT = 1.0f;   // primitive
-constexpr uint32_t LEAF_MAX = 3; // subtrees the collapse turns into leaves
 
 struct TreeletSmem {
     float area[TL_SUBSETS];
@@ -220,14 +219,15 @@ struct TreeletSmem {
     int inner[TL_LEAVES - 1];
 };
 
-__device__ __forceinline__ float node_cost(float area, uint32_t cnt, float split_cost) {
-    return cnt <= LEAF_MAX ? SAH_CT * area * (float)cnt : SAH_CI * area + split_cost;
+// subtrees of at most leaf_max primitives become leaves of the wide BVH
+__device__ __forceinline__ float node_cost(float area, uint32_t cnt, float split_cost, uint32_t leaf_max) {
+    return cnt <= leaf_max ? SAH_CT * area * (float)cnt : SAH_CI * area + split_cost;
 }
 
 // Optimises the treelet rooted at `root` (all 32 lanes of the warp call this).
 template <bool G>
 __device__ void treelet_optimise(int root, int nl, int2* children, int* parent, float4* node_lo, float4* node_hi,
-                                 uint32_t* leaf_count, float* cost, TreeletSmem& T) {
+                                 uint32_t* leaf_count, float* cost, TreeletSmem& T, uint32_t leaf_max) {
     const int lane = threadIdx.x & 31;
     const uint32_t total = ldx<G>(&leaf_count[root]);
     if (total < (uint32_t)TL_LEAVES) {
@@ -235,7 +235,7 @@ __device__ void treelet_optimise(int root, int nl, int2* children, int* parent, 
         if (lane == 0) {
             int2 ch = ldx<G>(&children[root]);
             float c = ldx<G>(&cost[ch.x]) + ldx<G>(&cost[ch.y]);
-            cost[root] = node_cost(half_area(ldx<G>(&node_lo[root]), ldx<G>(&node_hi[root])), total, c);
+            cost[root] = node_cost(half_area(ldx<G>(&node_lo[root]), ldx<G>(&node_hi[root])), total, c, leaf_max);
         }
         __syncwarp();
         return;
@@ -303,7 +303,7 @@ __device__ void treelet_optimise(int root, int nl, int2* children, int* parent, 
                 if (c < best || (c == best && P < bp)) { best = c; bp = P; }
                 if (q == 0) break;
             }
-            T.cost[sub] = node_cost(T.area[sub], T.count[sub], best);
+            T.cost[sub] = node_cost(T.area[sub], T.count[sub], best, leaf_max);
             T.part[sub] = (uint8_t)bp;
         }
         __syncwarp();
@@ -324,7 +324,7 @@ __device__ void treelet_optimise(int root, int nl, int2* children, int* parent, 
             if (ob < best || (ob == best && op < bp)) { best = ob; bp = op; }
         }
         if (lane == 0) {
-            T.cost[full] = node_cost(T.area[full], T.count[full], best);
+            T.cost[full] = node_cost(T.area[full], T.count[full], best, leaf_max);
             T.part[full] = (uint8_t)bp;
         }
     }
@@ -372,7 +372,7 @@ __device__ void treelet_optimise(int root, int nl, int2* children, int* parent, 
 // hands that node's treelet to its whole warp.
 template <bool G>
 __device__ void treelet_climb(int j, int n, int2* children, int* parent, int* flags, float4* node_lo,
-                              float4* node_hi, uint32_t* leaf_count, float* cost, TreeletSmem& T) {
+                              float4* node_hi, uint32_t* leaf_count, float* cost, TreeletSmem& T, uint32_t leaf_max) {
     const int nl = n - 1;
     bool active = j < n;
     int cur = nl + j;
@@ -396,7 +396,7 @@ __device__ void treelet_climb(int j, int n, int2* children, int* parent, int* fl
             const int l = __ffs(m) - 1;
             m &= m - 1;
             const int root = __shfl_sync(0xFFFFFFFFu, p, l);
-            treelet_optimise<G>(root, nl, children, parent, node_lo, node_hi, leaf_count, cost, T);
+            treelet_optimise<G>(root, nl, children, parent, node_lo, node_hi, leaf_count, cost, T, leaf_max);
         }
         mem_fence<G>();
         if (ready) cur = p;
@@ -406,10 +406,10 @@ __device__ void treelet_climb(int j, int n, int2* children, int* parent, int* fl
 
 __global__ void __launch_bounds__(BLK) k_treelet_pass(int n, int2* children, int* parent, int* flags,
                                                       float4* node_lo, float4* node_hi, uint32_t* leaf_count,
-                                                      float* cost) {
+                                                      float* cost, uint32_t leaf_max) {
     __shared__ TreeletSmem smem[TL_WARPS];
     treelet_climb<true>(blockIdx.x * BLK + threadIdx.x, n, children, parent, flags, node_lo, node_hi, leaf_count,
-                        cost, smem[threadIdx.x >> 5]);
+                        cost, smem[threadIdx.x >> 5], leaf_max);
 }
 
 // smallest power-of-two exponent (biased) with 2^(e-127) >= x; at least 1
@@ -454,7 +454,8 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
                               const int2* __restrict__ children, const float4* __restrict__ node_lo,
                               const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
                               const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
-                              uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area) {
+                              uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area,
+                              uint32_t leaf_max) {
     int b = (int)task.x;
     uint32_t w = task.y;
     const int nl = n - 1;  // first leaf id
@@ -467,7 +468,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
         float best_a = -1.0f;
         for (int k = 0; k < nc; k++) {
             int c = C[k];
-            if (c < nl && leaf_count[c] > 3u) {
+            if (c < nl && leaf_count[c] > leaf_max) {
                 float a = half_area(node_lo[c], node_hi[c]);
                 if (a > best_a) { best_a = a; best = k; }
             }
@@ -514,7 +515,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
     for (int s = 0; s < 8; s++) {
         int c = slot_child[s];
         if (c < 0) continue;
-        if (c < nl && leaf_count[c] > 3u) n_int++;
+        if (c < nl && leaf_count[c] > leaf_max) n_int++;
         else n_prims += leaf_count[c];
     }
     uint32_t child_local = n_int ? atomicAdd(&counters[2], n_int) : 0u;
@@ -544,8 +545,8 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
         float4 a4 = node_lo[c], z4 = node_hi[c];
         quant_child(F, a4, z4, node, s);
         float ha = half_area(a4, z4) / root_half_area;
-        if (c < nl && leaf_count[c] > 3u) {
-            node.meta[s] = 0x80u;
+        if (c < nl && leaf_count[c] > leaf_max) {
+            node.meta[s] = (uint8_t)META_INTERNAL;
             node.imask |= (uint8_t)(1u << s);
             uint32_t slot_out = atomicAdd(&counters[1], 1u);
             if (slot_out < (uint32_t)n) tasks_out[slot_out] = make_uint2((uint32_t)c, node.child_base + rank);
@@ -555,8 +556,8 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
         } else {
             uint32_t cnt = leaf_count[c];
             node.meta[s] = (uint8_t)((cnt << 5) | off);
-            // collect the (<= 3) leaves of subtree c in order
-            int stk[4];
+            // collect the (<= leaf_max) leaves of subtree c in order
+            int stk[8];
             int sp = 0;
             stk[sp++] = c;
             uint32_t k = 0;
@@ -565,10 +566,12 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
                 if (x >= nl) {
                     if (k < cnt) prim_order[prim_local + off + k] = sorted[x - nl];
                     k++;
-                } else if (sp < 3) {
+                } else if (sp < 7) {
                     int2 ch = children[x];
                     stk[sp++] = ch.y;
                     stk[sp++] = ch.x;
+                } else {
+                    atomicOr(&counters[4], 4u);   // deeper than a subtree of leaf_max leaves can be
                 }
             }
             off += cnt;
@@ -585,11 +588,12 @@ __global__ void k_collapse(const uint2* __restrict__ tasks_in, uint32_t* counter
                            const int2* __restrict__ children, const float4* __restrict__ node_lo,
                            const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
                            const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
-                           uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area) {
+                           uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area,
+                           uint32_t leaf_max) {
     uint32_t ti = blockIdx.x * BLK + threadIdx.x;
     if (ti >= counters[0]) return;
     collapse_task(tasks_in[ti], counters, tasks_out, n, children, node_lo, node_hi, leaf_count, sorted, nodes,
-                  node_base, prim_base, prim_order, sah, root_half_area);
+                  node_base, prim_base, prim_order, sah, root_half_area, leaf_max);
 }
 
 // ---- single-CTA agglomerative builder for small primitive sets -----------------
@@ -662,7 +666,7 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warp_sums, 
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
 k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, int n, int passes, WideNode* nodes,
               uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, SmallBuildOut* out, unsigned* err_word,
-              float4* wide_box, uint32_t* wide_depth) {
+              float4* wide_box, uint32_t* wide_depth, uint32_t leaf_max) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmallSmem& S = *reinterpret_cast<SmallSmem*>(smem_raw);
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -855,7 +859,7 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
             if (tid < n) S.flags[tid] = 0;
             __syncthreads();
             treelet_climb<false>((tid & 31) * 32 + (tid >> 5), n, S.children, S.parent, S.flags, S.node_lo,
-                                 S.node_hi, S.leaf_count, S.cost, S.tl[tid >> 5]);
+                                 S.node_hi, S.leaf_count, S.cost, S.tl[tid >> 5], leaf_max);
             __syncthreads();
         }
     }
@@ -883,7 +887,7 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
                 wide_depth[local] = (uint32_t)level;
             }
             collapse_task(task, S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
-                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, &S.sah, rha);
+                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, &S.sah, rha, leaf_max);
         }
         __syncthreads();
         if (tid == 0) { S.counters[0] = S.counters[1]; S.counters[1] = 0u; }
@@ -930,7 +934,7 @@ k_refit_small(WideNode* nodes, uint32_t node_base, uint32_t prim_base, const Sma
                 clo[s] = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f);
                 chi[s] = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
                 if (meta == 0u) continue;
-                if (meta == 0x80u) {
+                if (meta == META_INTERNAL) {
                     const uint32_t child = node.child_base + (uint32_t)__popc(node.imask & ((1u << s) - 1u)) - node_base;
                     if (child >= nn) { bad = true; continue; }
                     clo[s] = wide_box[2 * child];
@@ -1035,7 +1039,8 @@ inline unsigned grid_for(uint32_t n) { return (n + BLK - 1) / BLK; }
 
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t st,
-                      BuildResult* out, int treelet_passes) {
+                      BuildResult* out, int treelet_passes, uint32_t leaf_max) {
+    if (leaf_max < 1 || leaf_max > LEAF_MAX_LIMIT) return Status::Err(1, "build_wide_bvh: leaf size out of range");
     if (n == 0) return Status::Err(1, "build_wide_bvh: no primitives");
     if (n > (1u << 30)) return Status::Err(1, "build_wide_bvh: too many primitives");
     SNK_TRY_CUDA(sc.keys.reserve(n));
@@ -1081,7 +1086,7 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
         for (int pass = 0; pass < treelet_passes; pass++) {
             SNK_TRY_CUDA(cudaMemsetAsync(sc.flags.p, 0, sizeof(int) * n, st));
             k_treelet_pass<<<g, BLK, 0, st>>>((int)n, sc.children.p, sc.parent.p, sc.flags.p, sc.node_lo.p,
-                                              sc.node_hi.p, sc.leaf_count.p, sc.cost.p);
+                                              sc.node_hi.p, sc.leaf_count.p, sc.cost.p, leaf_max);
             SNK_TRY_CUDA(cudaGetLastError());
         }
     }
@@ -1105,7 +1110,7 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
         if (level > 4096) return Status::Err(5, "build_wide_bvh: collapse did not terminate");
         k_collapse<<<grid_for(ntasks), BLK, 0, st>>>(tin, sc.counters.p, tout, (int)n, sc.children.p, sc.node_lo.p,
                                                      sc.node_hi.p, sc.leaf_count.p, sorted, nodes, node_base,
-                                                     prim_base, prim_order, sc.sah.p, rha);
+                                                     prim_base, prim_order, sc.sah.p, rha, leaf_max);
         SNK_TRY_CUDA(cudaGetLastError());
         uint32_t ctr[5];
         SNK_TRY_CUDA(cudaMemcpyAsync(ctr, sc.counters.p, sizeof(ctr), cudaMemcpyDeviceToHost, st));
@@ -1132,13 +1137,14 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
 Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                             uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
                             SmallBuildOut* out, unsigned* err_word, float4* wide_box, uint32_t* wide_depth,
-                            cudaStream_t st) {
+                            cudaStream_t st, uint32_t leaf_max) {
     if (n == 0 || n > (uint32_t)SMALL_BUILD_MAX) return Status::Err(1, "build_wide_bvh_small: bad primitive count");
+    if (leaf_max < 1 || leaf_max > LEAF_MAX_LIMIT) return Status::Err(1, "build_wide_bvh_small: leaf size out of range");
     SNK_TRY_CUDA(cudaFuncSetAttribute(k_build_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(SmallSmem)));
     k_build_small<<<1, SMALL_THREADS, sizeof(SmallSmem), st>>>(prim_lo, prim_hi, (int)n, treelet_passes, nodes,
                                                                 node_base, prim_base, prim_order, out, err_word,
-                                                                wide_box, wide_depth);
+                                                                wide_box, wide_depth, leaf_max);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }

@@ -218,9 +218,12 @@ SNK_HD V3 f0_of(V3 albedo, float metallic) {
 //   w0: p.x p.y p.z | e.x e.y e.z imask (bytes)
 //   w1: child_base  | prim_base | meta[0..3] | meta[4..7]
 //   w2: qlo_x[8] qlo_y[8]   w3: qlo_z[8] qhi_x[8]   w4: qhi_y[8] qhi_z[8]
-// meta: 0 = empty slot; bit 7 = internal child; leaf = (count << 5) | offset
-// (count 1..3 primitives at prim_base + offset).  Internal children are stored
+// meta: 0 = empty slot; META_INTERNAL = internal child (also bit s of imask);
+// leaf = (count << 5) | offset: count 1..LEAF_MAX_LIMIT primitives at
+// prim_base + offset, offset + count <= 32.  Internal children are stored
 // contiguously from child_base in slot order.
+constexpr uint32_t META_INTERNAL = 0x1Fu;   // count 0: never a leaf
+constexpr uint32_t LEAF_MAX_LIMIT = 4;       // 8 leaves x 4 primitives = the 32 primitive hit bits
 struct alignas(16) WideNode {
     float px, py, pz;
     uint8_t ex, ey, ez, imask;

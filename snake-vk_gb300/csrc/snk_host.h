@@ -91,7 +91,7 @@ struct BuildResult {
 // the primitive id stored in slot prim_base + k.
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t stream,
-                      BuildResult* out, int treelet_passes);
+                      BuildResult* out, int treelet_passes, uint32_t leaf_max);
 
 // Single-launch build for n <= SMALL_BUILD_MAX primitives (one CTA, shared
 // memory, no host synchronisation); same algorithm and output layout as
@@ -108,7 +108,7 @@ struct SmallBuildOut {
 Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                             uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
                             SmallBuildOut* out, unsigned* err_word, float4* wide_box, uint32_t* wide_depth,
-                            cudaStream_t stream);
+                            cudaStream_t stream, uint32_t leaf_max);
 // Refit of a tree made by build_wide_bvh_small for the same n primitives in new
 // boxes (prim_order as that build wrote it; everything stays on the device).
 Status refit_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,

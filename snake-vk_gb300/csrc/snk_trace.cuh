@@ -12,9 +12,10 @@
 //
 // Traversal scheme (Ylitie, Karras, Laine, HPG 2017): the current node group
 // is (child_base, hit bits of internal children << 24 | imask) and the current
-// primitive group is (prim_base, 24 primitive hit bits).  Groups are kept on a
+// primitive group is (prim_base, 32 primitive hit bits).  Groups are kept on a
 // short per-thread stack in shared memory ([entry][thread] layout, conflict
-// free) that spills to local memory.  Children are visited in the order of the
+// free) that spills to local memory; primitive groups carry PRIM_GROUP in the
+// base word there.  Children are visited in the order of the
 // slot index xor the ray octant, which the builder makes approximately
 // front-to-back.  Leaves of the instance BVH hold instance ids: on reaching one
 // the ray is transformed into object space and the BLAS root is entered; when
@@ -27,6 +28,7 @@ namespace snk {
 constexpr int STACK_SH = 8;           // shared-memory entries per thread
 constexpr int STACK_MAX = 64;         // total entries (shared + local spill)
 constexpr uint32_t MAX_TRAVERSAL_STEPS = 1u << 16;   // node groups popped per ray
+constexpr uint32_t PRIM_GROUP = 0x80000000u;         // stack tag of a primitive group (bases are < 2^31)
 
 // device error word bits
 constexpr unsigned ERR_STACK_OVERFLOW = 1u;
@@ -95,9 +97,9 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
                          fminf(__fmaf_rn(byte_f(fz[h], k), az, bz), tmax));
         uint32_t m = (meta[h] >> (8 * k)) & 0xFFu;
         bool hit = (tn <= tf + ((fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f)) && m != 0u;
-        // internal children: meta 0x80 (count bits 0); leaves: (count << 5) | offset
-        hit_int |= (hit && (m & 0x80u)) ? (1u << ((uint32_t)s ^ r.oct)) : 0u;
-        hit_prim |= hit ? (((1u << ((m >> 5) & 3u)) - 1u) << (m & 31u)) : 0u;
+        // internal children: imask bit (meta META_INTERNAL, count 0); leaves: (count << 5) | offset
+        hit_int |= (hit && ((imask >> s) & 1u)) ? (1u << ((uint32_t)s ^ r.oct)) : 0u;
+        hit_prim |= hit ? (((1u << (m >> 5)) - 1u) << (m & 31u)) : 0u;
     }
     ngroup = make_uint2(__float_as_uint(w1.x), (hit_int << 24) | imask);
     tgroup = make_uint2(__float_as_uint(w1.y), hit_prim);
@@ -171,8 +173,8 @@ struct Traverser {
             if (level == 1 && st.sp == blas_sp) { level = 0; cr = make_node_ray(o, d); }
             if (st.sp == 0) { done = true; return; }
             uint2 g = st.pop();
-            if (g.y > 0x00FFFFFFu) ngroup = g;
-            else tgroup = g;
+            if (g.x & PRIM_GROUP) tgroup = make_uint2(g.x & ~PRIM_GROUP, g.y);
+            else ngroup = g;
         }
     }
 
@@ -180,7 +182,7 @@ struct Traverser {
         if (++steps > MAX_TRAVERSAL_STEPS) { fail(ERR_STEP_LIMIT); return; }
         // a pending primitive group is postponed onto the stack
         if (has_prim()) {
-            if (!st.push(tgroup)) { fail(ERR_STACK_OVERFLOW); return; }
+            if (!st.push(make_uint2(tgroup.x | PRIM_GROUP, tgroup.y))) { fail(ERR_STACK_OVERFLOW); return; }
             tgroup = make_uint2(0u, 0u);
         }
         uint32_t k = __ffs(ngroup.y >> 24) - 1;
@@ -205,7 +207,7 @@ struct Traverser {
             uint32_t inst = __ldg(&S.tlas_prims[pidx]);
             if (inst >= S.num_instances) { fail(ERR_BAD_INDEX); return; }
             if (has_prim()) {
-                if (!st.push(tgroup)) { fail(ERR_STACK_OVERFLOW); return; }
+                if (!st.push(make_uint2(tgroup.x | PRIM_GROUP, tgroup.y))) { fail(ERR_STACK_OVERFLOW); return; }
             }
             if (has_node()) {
                 if (!st.push(ngroup)) { fail(ERR_STACK_OVERFLOW); return; }
