@@ -267,8 +267,10 @@ typedef struct snk_tuning {
     uint32_t trace_variant;         /* registers: 0 <= 85 (6 blocks/SM), 1 <= 64, 2 unconstrained */
     uint32_t bvh_treelet_passes;    /* treelet restructuring passes of later mesh BVH builds (3);
                                        SNK_TREELET_PASSES_NONE builds the plain LBVH */
-    uint32_t tlas_treelet_passes;   /* the same for the per-frame instance BVH (1); up to 1024
-                                       instances it is built in one launch by locally-ordered
+    uint32_t tlas_treelet_passes;   /* the same for the per-frame instance BVH (0: with
+                                       single-instance leaves the clustered tree gains ~1 % of
+                                       trace time from a pass that costs more per rebuild); up to
+                                       1024 instances it is built in one launch by locally-ordered
                                        clustering, and the passes refine that tree */
     uint32_t tlas_refit_interval;   /* 0: rebuild the instance BVH on every instance update (as
                                        TlasSystem::BuildTlas, TlasSystem.cpp:16-20); k >= 1:

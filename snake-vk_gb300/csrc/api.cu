@@ -392,7 +392,7 @@ Status build_instances(snk_pt_ctx* ctx) {
         SNK_TRY_CUDA(ctx->d_tlas_prims.reserve(n));
         SNK_TRY(launch_instance_boxes(ctx->d_inst_list.p, n, ctx->d_inst_shade.p, ctx->d_meshes.p, ctx->d_box_lo.p,
                                       ctx->d_box_hi.p, st));
-        const int passes = treelet_passes(ctx->tune.tlas_treelet_passes, 1);
+        const int passes = treelet_passes(ctx->tune.tlas_treelet_passes, 0);
         std::vector<uint32_t> meshes_now(n);
         for (uint32_t k = 0; k < n; k++) meshes_now[k] = ctx->instances[list[k]].mesh_id;
         const uint32_t interval = ctx->tune.tlas_refit_interval;
