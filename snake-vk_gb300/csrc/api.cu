@@ -745,8 +745,11 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     const uint32_t n_render = (uint32_t)(n_pixels * spp);
     const uint32_t n_paths = n_render + n_train;
 
-    // per-view device descriptors (host outputs go through staging buffers)
+    // per-view device descriptors.  Host outputs in page-locked memory (cudaHostAlloc /
+    // cudaHostRegister) are written by the kernels in place over the CPU-GPU link;
+    // other host outputs go through device staging buffers and a copy back.
     std::vector<ViewDev> vd(num_views);
+    std::vector<uint32_t> direct(num_views, 0u);   // bit k: output k written in place
     uint64_t off = 0;
     Status sst = Status::Ok();
     for (uint32_t v = 0; v < num_views; v++) {
@@ -761,6 +764,14 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         for (int k = 0; k < NUM_OUT; k++) {
             if (!src[k]) continue;
             if (o.memory == SNK_MEM_HOST) {
+                cudaPointerAttributes pa;
+                if (cudaPointerGetAttributes(&pa, src[k]) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+                    pa.devicePointer && reinterpret_cast<uintptr_t>(pa.devicePointer) % 16 == 0) {
+                    dst[k] = pa.devicePointer;
+                    direct[v] |= 1u << k;
+                    continue;
+                }
+                cudaGetLastError();
                 dst[k] = stage(ctx, v, (uint32_t)k, np * OUT_BYTES[k], &sst);
                 if (!sst.ok()) return fail(ctx, sst);
             } else {
@@ -974,7 +985,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         void** dst = dev_slots(vd[v]);
         size_t np = (size_t)views[v].width * views[v].height;
         for (int k = 0; k < NUM_OUT; k++) {
-            if (!src[k]) continue;
+            if (!src[k] || (direct[v] >> k) & 1u) continue;
             if (cudaMemcpyAsync(src[k], dst[k], np * OUT_BYTES[k], cudaMemcpyDeviceToHost, st) != cudaSuccess)
                 return fail(ctx, SNK_ERR_CUDA, "render: output copy");
         }

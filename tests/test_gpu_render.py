@@ -106,6 +106,17 @@ def test_host_outputs_match_device_outputs(cuda, built_lib):
     for k in g:
         h = host[k].view(np.uint32) if k in ("mat_flags", "inst_id", "prim_id") else host[k]
         assert np.array_equal(g[k], h), k
+    # page-locked host outputs are written in place by the kernels (no staging copy)
+    import torch
+    pinned = {}
+    for k, a in snkpt.alloc_outputs(128, 128).items():
+        t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32, pin_memory=True)
+        t.fill_(-7)
+        pinned[k] = t.numpy()
+    pt.render([sc.views[0]], st, [pinned])
+    for k in g:
+        h = pinned[k].view(np.uint32) if k in ("mat_flags", "inst_id", "prim_id") else pinned[k]
+        assert np.array_equal(g[k], h), ("pinned", k)
 
 
 def test_fp64_accumulator(cuda, built_lib):
