@@ -56,6 +56,25 @@ __device__ __forceinline__ NodeRay make_node_ray(V3 o, V3 d) {
     return r;
 }
 
+// Three-input maximum / minimum (one instruction on sm_100 and later; NaN inputs
+// are ignored, as with fmaxf / fminf).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+// ((1 << len) - 1) << pos in one instruction
+__device__ __forceinline__ uint32_t bit_mask(uint32_t pos, uint32_t len) {
+    uint32_t d;
+    asm("bmsk.clamp.b32 %0, %1, %2;" : "=r"(d) : "r"(pos), "r"(len));
+    return d;
+}
+
 // Exact byte -> float: the byte is placed in the mantissa of 2^23 (one byte
 // permute) and 2^23 is subtracted (exact), keeping the conversion off the XU pipe.
 __device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) {
@@ -91,15 +110,15 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
 #pragma unroll
     for (int s = 0; s < 8; s++) {
         const int h = s >> 2, k = s & 3;
-        float tn = fmaxf(fmaxf(__fmaf_rn(byte_f(nx[h], k), ax, bx), __fmaf_rn(byte_f(ny[h], k), ay, by)),
+        float tn = max3f(__fmaf_rn(byte_f(nx[h], k), ax, bx), __fmaf_rn(byte_f(ny[h], k), ay, by),
                          fmaxf(__fmaf_rn(byte_f(nz[h], k), az, bz), tmin));
-        float tf = fminf(fminf(__fmaf_rn(byte_f(fx[h], k), ax, bx), __fmaf_rn(byte_f(fy[h], k), ay, by)),
+        float tf = min3f(__fmaf_rn(byte_f(fx[h], k), ax, bx), __fmaf_rn(byte_f(fy[h], k), ay, by),
                          fminf(__fmaf_rn(byte_f(fz[h], k), az, bz), tmax));
         uint32_t m = (meta[h] >> (8 * k)) & 0xFFu;
         bool hit = (tn <= tf + ((fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f)) && m != 0u;
         // internal children: imask bit (meta META_INTERNAL, count 0); leaves: (count << 5) | offset
         hit_int |= (hit && ((imask >> s) & 1u)) ? (1u << ((uint32_t)s ^ r.oct)) : 0u;
-        hit_prim |= hit ? (((1u << (m >> 5)) - 1u) << (m & 31u)) : 0u;
+        hit_prim |= hit ? bit_mask(m & 31u, m >> 5) : 0u;
     }
     ngroup = make_uint2(__float_as_uint(w1.x), (hit_int << 24) | imask);
     tgroup = make_uint2(__float_as_uint(w1.y), hit_prim);
