@@ -279,7 +279,8 @@ typedef struct snk_tuning {
                                        update (instance BVHs of up to 1024 instances) */
     uint32_t bvh_leaf_max;          /* primitives per leaf of later mesh BVH builds, 1..4 (1) */
     uint32_t tlas_leaf_max;         /* instances per leaf of the instance BVH, 1..4 (1) */
-    uint32_t reserved;
+    uint32_t bvh_leaf_pack;         /* largest mesh-BVH subtree a full node keeps as one leaf
+                                       (bvh_leaf_max..4; default bvh_leaf_max) */
 } snk_tuning;
 
 #define SNK_TREELET_PASSES_NONE 0xFFFFFFFFu

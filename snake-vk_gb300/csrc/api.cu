@@ -246,7 +246,8 @@ Status build_meshes(snk_pt_ctx* ctx) {
         BuildResult br;
         SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, mi.num_triangles, ctx->d_blas.p,
                                node_base, prim_base, ctx->d_prim_order.p, st, &br,
-                               treelet_passes(ctx->tune.bvh_treelet_passes, 3), leaf_size(ctx->tune.bvh_leaf_max, 1)));
+                               treelet_passes(ctx->tune.bvh_treelet_passes, 3), leaf_size(ctx->tune.bvh_leaf_max, 1),
+                               std::max(leaf_size(ctx->tune.bvh_leaf_pack, 1), leaf_size(ctx->tune.bvh_leaf_max, 1))));
         SNK_TRY(launch_fill_triangles(ctx->d_prim_order.p, mi.num_triangles, ctx->d_pos.p, ctx->d_idx.p,
                                       mi.vertex_offset, mi.index_offset, ctx->d_tris.p + prim_base, st));
         mi.blas_root = node_base;
@@ -434,7 +435,8 @@ Status build_instances(snk_pt_ctx* ctx) {
         } else {
             BuildResult br;
             SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
-                                   ctx->d_prim_order.p, st, &br, passes, leaf_size(ctx->tune.tlas_leaf_max, 1)));
+                                   ctx->d_prim_order.p, st, &br, passes, leaf_size(ctx->tune.tlas_leaf_max, 1),
+                                   leaf_size(ctx->tune.tlas_leaf_max, 1)));
             ctx->tlas_nodes = br.num_nodes;
             ctx->tlas_small = false;
             ctx->tlas_builds++;
@@ -1000,7 +1002,7 @@ int snk_pt_set_tuning(snk_pt_ctx* ctx, const snk_tuning* t) {
         t->prim_bias > 64 || t->trace_variant > 2 || 
         (t->bvh_treelet_passes > 16 && t->bvh_treelet_passes != SNK_TREELET_PASSES_NONE) ||
         (t->tlas_treelet_passes > 16 && t->tlas_treelet_passes != SNK_TREELET_PASSES_NONE) ||
-        t->bvh_leaf_max > LEAF_MAX_LIMIT || t->tlas_leaf_max > LEAF_MAX_LIMIT)
+        t->bvh_leaf_max > LEAF_MAX_LIMIT || t->tlas_leaf_max > LEAF_MAX_LIMIT || t->bvh_leaf_pack > LEAF_MAX_LIMIT)
         return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: knob out of range");
     ctx->tune = *t;
     return SNK_OK;

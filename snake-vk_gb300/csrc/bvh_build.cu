@@ -22,9 +22,11 @@
 //      finished subtrees, ties break on the lowest subset index).
 //   6. top-down collapse to 8-wide nodes, one thread per output node, level by
 //      level: a node's children start as its binary children; the internal child
-//      with the largest surface area and more than 3 leaves is replaced by its two
-//      children until 8 children exist or none can be opened.  Children with <= 3
-//      leaves become leaves.  Children are assigned to the 8 slots greedily by how
+//      with the largest surface area and more than leaf_max primitives is replaced
+//      by its two children until 8 children exist or none can be opened.  Children
+//      with <= leaf_pack primitives (leaf_max <= leaf_pack <= 4) become leaves: a
+//      full node keeps small subtrees as multi-primitive leaves instead of
+//      spending a sparsely filled child node on them.  Children are assigned to the 8 slots greedily by how
 //      well their centroid offset matches each octant corner, so that visiting
 //      slot ^ ray_octant in increasing order is roughly front to back.  Child boxes
 //      are quantised outwards to 8 bits per plane.
@@ -455,7 +457,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
                               const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
                               const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
                               uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area,
-                              uint32_t leaf_max) {
+                              uint32_t leaf_max, uint32_t leaf_pack) {
     int b = (int)task.x;
     uint32_t w = task.y;
     const int nl = n - 1;  // first leaf id
@@ -515,7 +517,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
     for (int s = 0; s < 8; s++) {
         int c = slot_child[s];
         if (c < 0) continue;
-        if (c < nl && leaf_count[c] > leaf_max) n_int++;
+        if (c < nl && leaf_count[c] > leaf_pack) n_int++;
         else n_prims += leaf_count[c];
     }
     uint32_t child_local = n_int ? atomicAdd(&counters[2], n_int) : 0u;
@@ -545,7 +547,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
         float4 a4 = node_lo[c], z4 = node_hi[c];
         quant_child(F, a4, z4, node, s);
         float ha = half_area(a4, z4) / root_half_area;
-        if (c < nl && leaf_count[c] > leaf_max) {
+        if (c < nl && leaf_count[c] > leaf_pack) {
             node.meta[s] = (uint8_t)META_INTERNAL;
             node.imask |= (uint8_t)(1u << s);
             uint32_t slot_out = atomicAdd(&counters[1], 1u);
@@ -556,7 +558,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
         } else {
             uint32_t cnt = leaf_count[c];
             node.meta[s] = (uint8_t)((cnt << 5) | off);
-            // collect the (<= leaf_max) leaves of subtree c in order
+            // collect the (<= leaf_pack) leaves of subtree c in order
             int stk[8];
             int sp = 0;
             stk[sp++] = c;
@@ -571,7 +573,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
                     stk[sp++] = ch.y;
                     stk[sp++] = ch.x;
                 } else {
-                    atomicOr(&counters[4], 4u);   // deeper than a subtree of leaf_max leaves can be
+                    atomicOr(&counters[4], 4u);   // deeper than a subtree of leaf_pack leaves can be
                 }
             }
             off += cnt;
@@ -589,11 +591,11 @@ __global__ void k_collapse(const uint2* __restrict__ tasks_in, uint32_t* counter
                            const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
                            const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
                            uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area,
-                           uint32_t leaf_max) {
+                           uint32_t leaf_max, uint32_t leaf_pack) {
     uint32_t ti = blockIdx.x * BLK + threadIdx.x;
     if (ti >= counters[0]) return;
     collapse_task(tasks_in[ti], counters, tasks_out, n, children, node_lo, node_hi, leaf_count, sorted, nodes,
-                  node_base, prim_base, prim_order, sah, root_half_area, leaf_max);
+                  node_base, prim_base, prim_order, sah, root_half_area, leaf_max, leaf_pack);
 }
 
 // ---- single-CTA agglomerative builder for small primitive sets -----------------
@@ -887,7 +889,8 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
                 wide_depth[local] = (uint32_t)level;
             }
             collapse_task(task, S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
-                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, &S.sah, rha, leaf_max);
+                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, &S.sah, rha, leaf_max,
+                          leaf_max);
         }
         __syncthreads();
         if (tid == 0) { S.counters[0] = S.counters[1]; S.counters[1] = 0u; }
@@ -1039,8 +1042,9 @@ inline unsigned grid_for(uint32_t n) { return (n + BLK - 1) / BLK; }
 
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t st,
-                      BuildResult* out, int treelet_passes, uint32_t leaf_max) {
-    if (leaf_max < 1 || leaf_max > LEAF_MAX_LIMIT) return Status::Err(1, "build_wide_bvh: leaf size out of range");
+                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack) {
+    if (leaf_max < 1 || leaf_max > LEAF_MAX_LIMIT || leaf_pack < leaf_max || leaf_pack > LEAF_MAX_LIMIT)
+        return Status::Err(1, "build_wide_bvh: leaf size out of range");
     if (n == 0) return Status::Err(1, "build_wide_bvh: no primitives");
     if (n > (1u << 30)) return Status::Err(1, "build_wide_bvh: too many primitives");
     SNK_TRY_CUDA(sc.keys.reserve(n));
@@ -1110,7 +1114,7 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
         if (level > 4096) return Status::Err(5, "build_wide_bvh: collapse did not terminate");
         k_collapse<<<grid_for(ntasks), BLK, 0, st>>>(tin, sc.counters.p, tout, (int)n, sc.children.p, sc.node_lo.p,
                                                      sc.node_hi.p, sc.leaf_count.p, sorted, nodes, node_base,
-                                                     prim_base, prim_order, sc.sah.p, rha, leaf_max);
+                                                     prim_base, prim_order, sc.sah.p, rha, leaf_max, leaf_pack);
         SNK_TRY_CUDA(cudaGetLastError());
         uint32_t ctr[5];
         SNK_TRY_CUDA(cudaMemcpyAsync(ctr, sc.counters.p, sizeof(ctr), cudaMemcpyDeviceToHost, st));

@@ -91,7 +91,7 @@ struct BuildResult {
 // the primitive id stored in slot prim_base + k.
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t stream,
-                      BuildResult* out, int treelet_passes, uint32_t leaf_max);
+                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack);
 
 // Single-launch build for n <= SMALL_BUILD_MAX primitives (one CTA, shared
 // memory, no host synchronisation); same algorithm and output layout as

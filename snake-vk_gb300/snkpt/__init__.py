@@ -54,9 +54,9 @@ class Tuning(C.Structure):
                 ("ray_chunk", C.c_uint32), ("refill_idle", C.c_uint32), ("prim_bias", C.c_uint32),
                 ("trace_variant", C.c_uint32), ("bvh_treelet_passes", C.c_uint32), ("tlas_treelet_passes", C.c_uint32),
                 ("tlas_refit_interval", C.c_uint32), ("bvh_leaf_max", C.c_uint32), ("tlas_leaf_max", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("bvh_leaf_pack", C.c_uint32)]
     KNOBS = ("trace_blocks_per_sm", "shade_blocks_per_sm", "ray_chunk", "refill_idle", "prim_bias", "trace_variant",
-             "bvh_treelet_passes", "tlas_treelet_passes", "tlas_refit_interval", "bvh_leaf_max", "tlas_leaf_max")
+             "bvh_treelet_passes", "tlas_treelet_passes", "tlas_refit_interval", "bvh_leaf_max", "tlas_leaf_max", "bvh_leaf_pack")
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k in self.KNOBS}
