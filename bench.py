@@ -340,6 +340,44 @@ def particle_bench(pt, abi, scene, device, n=100_000, steps=20, warmup=3):
             "note": "wall clock around the C-ABI call (synchronising), device buffers"}
 
 
+def restir_bench(snkpt, abi, scenes, device, stream, tuning, frames=16, warmup=3):
+    """ReSTIR DI on the stress scene (config 2: the 1080p sphere field + 4096
+    emissive quads, camera moving 0.05 units per frame): per frame the G-buffer
+    pass, 32 initial light candidates + 1 visibility ray with temporal reuse
+    (M cap 20), and spatial reuse over 5 neighbours in a 30-pixel radius.
+    Device-resident outputs; CUDA events on the library's stream."""
+    import torch
+    sc = scenes.config2(frames=frames)
+    pt = snkpt.PathTracer(device.index or 0, stream=stream)
+    pt.load_scene(sc)
+    if tuning:
+        pt.set_tuning(tuning)
+    out = snkpt.alloc_outputs(1920, 1080, device=device, names=("radiance", "albedo", "normal", "motion", "depth"))
+    for k in range(warmup):
+        pt.render([sc.views[0]], abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=k, seed=1), [out])
+        pt.stats()
+    ms, rays = 0.0, 0
+    per_stage = {}
+    for f in range(frames):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        pt.render([sc.views[f]], abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=warmup + f, seed=1,
+                                              flags=abi.RENDER_PROFILE), [out])
+        b.record(stream)
+        s = pt.stats()
+        b.synchronize()
+        ms += a.elapsed_time(b)
+        rays += s["rays_camera"] + s["rays_shadow"]
+        for k, v in s["stage_ms"].items():
+            if v > 0:
+                per_stage[k] = per_stage.get(k, 0.0) + v / frames
+    del pt, out
+    return {"workload": "config 2: ReSTIR DI, 1920x1080, 4096 emissive quads + 16 sphere lights + sun, 32 "
+                        "candidates, temporal (M cap 20) + 5 spatial neighbours in 30 px, camera +0.05/frame",
+            "frames": frames, "ms_per_frame": ms / frames, "Mrays_per_s": rays / (ms / 1e3) / 1e6,
+            "rays_per_frame": rays / frames, "stage_ms_per_frame": per_stage}
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -538,6 +576,7 @@ def run_ours(args):
             line["cpu_baseline"] = cpu_baseline(sc, view, settings(1, 0))
         line["taa"] = taa_bench(snkpt, dev, stream)
         line["particles"] = particle_bench(pt, abi, sc, dev)
+        line["restir"] = restir_bench(snkpt, abi, scenes, dev, stream, tuning)
         if not args.no_batched:
             line["batched_views"] = batched_views(snkpt, abi, scenes, dev, stream, tuning)
             line["batched_views_small"] = batched_views(snkpt, abi, scenes, dev, stream, tuning, frames=20, scale=8)
