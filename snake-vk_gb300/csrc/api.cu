@@ -30,6 +30,7 @@ struct RestirState {
     uint32_t w = 0, h = 0;
     DBuf<float4> g_pos, g_normal, g_albedo, g_misc, prev_normal;
     DBuf<float4> res_a, res_b, res_c;   // temporal, history, spatial (48 B = 3 float4 per pixel)
+    DBuf<float4> ris;                    // initial-pass state between its recording and replaying runs
     uint32_t history_valid = 0;
     uint32_t hist = 1, spat = 2;        // which of b/c holds history / receives spatial
 };
@@ -72,6 +73,9 @@ struct snk_pt_ctx {
     uint32_t n_emissive = 0, n_local = 0;
     DBuf<unsigned> d_err;
     DBuf<unsigned char> q_in, q_in2, q_out, q_out2;   // staging of the particle / contact queries
+    DBuf<float4> rq_rays;                              // ReSTIR visibility queue (slots x pixels x 2)
+    DBuf<uint8_t> rq_vis_a, rq_vis_b;                  // its results (initial / shading, spatial)
+    DBuf<uint32_t> rq_work;                            // work counters of the three visibility traces
     DBuf<SmallBuildOut> d_small_out;   // result record of the single-launch instance BVH build
     bool tlas_small = false;
     // instance BVH refit state: exact node boxes and depths, primitive order and
@@ -730,6 +734,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     const bool path_like = rs.mode == SNK_MODE_PATH || rs.mode == SNK_MODE_PATH_CACHE;
     if (path_like && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: spp must be >= 1 and 1 <= max_depth <= 16");
+    if (!path_like && (rs.restir_spatial < 0 || rs.restir_spatial > 32 || rs.restir_candidates > 4096))
+        return fail(ctx, SNK_ERR_INVALID_ARG, "render: restir_spatial must be 0..32, restir_candidates <= 4096");
     uint64_t n_pixels = 0;
     for (uint32_t v = 0; v < num_views; v++) {
         if (views[v].width == 0 || views[v].height == 0) return fail(ctx, SNK_ERR_INVALID_ARG, "render: empty view");
@@ -942,7 +948,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (R.w != w || R.h != h) {
                 if (R.g_pos.reserve(np) || R.g_normal.reserve(np) || R.g_albedo.reserve(np) || R.g_misc.reserve(np) ||
                     R.prev_normal.reserve(np) || R.res_a.reserve(3 * np) || R.res_b.reserve(3 * np) ||
-                    R.res_c.reserve(3 * np))
+                    R.res_c.reserve(3 * np) || R.ris.reserve(2 * np))
                     return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir buffers");
                 R.w = w; R.h = h; R.history_valid = 0; R.hist = 1; R.spat = 2;
             }
@@ -952,15 +958,43 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             RV.temporal = R.res_a.p;
             RV.history = R.hist == 1 ? R.res_b.p : R.res_c.p;
             RV.spatial = R.spat == 1 ? R.res_b.p : R.res_c.p;
+            RV.ris = R.ris.p;
             RV.history_valid = R.history_valid;
             RestirSettings s;
             s.frame_index = rs.frame_index; s.seed = rs.seed; s.candidates = rs.restir_candidates;
             s.mcap = rs.restir_mcap; s.temporal = rs.restir_temporal; s.spatial = rs.restir_spatial;
             s.radius = rs.restir_radius; s.pad = 0;
-            cudaError_t e = cudaSuccess;
-            for (int k = 0; k < 3 && e == cudaSuccess; k++)
-                e = staged(ctx, profile, SNK_STAGE_RESTIR_GBUFFER + k,
-                           [&] { return launch_restir_stage(k, F, v, RV, s, trace_grid(ctx), st); });
+            // visibility queues: initial (K1 slots per pixel), spatial (K2), final shading (K3)
+            const uint32_t K1 = RESTIR_INITIAL_SLOTS, K2 = restir_spatial_slots(s.spatial), K3 = RESTIR_SHADE_SLOTS;
+            if (ctx->rq_rays.reserve(2ull * std::max(K1, K2) * np) || ctx->rq_vis_a.reserve(std::max(K1, K3) * np) ||
+                ctx->rq_vis_b.reserve((size_t)K2 * np) || ctx->rq_work.reserve(3))
+                return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir visibility queues");
+            if (cudaMemsetAsync(ctx->rq_work.p, 0, 3 * sizeof(uint32_t), st) != cudaSuccess)
+                return fail(ctx, SNK_ERR_CUDA, "restir queue reset");
+            const RestirQueue q1{ctx->rq_rays.p, ctx->rq_vis_a.p, K1, 0u}, q2{ctx->rq_rays.p, ctx->rq_vis_b.p, K2, 0u},
+                q3{ctx->rq_rays.p, ctx->rq_vis_a.p, K3, 0u};
+            const int tg = trace_grid(ctx);
+            const SceneDev SD = scene_dev(ctx);
+            const TraceTuning tt = trace_tuning(ctx);
+            auto pass = [&](int stage, int phase, const RestirQueue& qa, const RestirQueue& qb) {
+                return staged(ctx, profile, SNK_STAGE_RESTIR_GBUFFER + stage,
+                              [&] { return launch_restir_stage(stage, phase, F, v, RV, s, qa, qb, tg, st); });
+            };
+            auto visibility = [&](uint32_t K, uint8_t* vis, int slot) {
+                return staged(ctx, profile, SNK_STAGE_TRACE_SHADOW, [&] {
+                    return launch_trace_visibility(SD, ctx->rq_rays.p, (uint32_t)(K * np), vis, ctx->rq_work.p + slot,
+                                                   tg, tt, st);
+                });
+            };
+            cudaError_t e = pass(0, 0, q1, q3);
+            if (e == cudaSuccess) e = pass(1, 0, q1, q3);
+            if (e == cudaSuccess) e = visibility(K1, ctx->rq_vis_a.p, 0);
+            if (e == cudaSuccess) e = pass(1, 1, q1, q3);
+            if (e == cudaSuccess) e = pass(2, 0, q2, q3);
+            if (e == cudaSuccess) e = visibility(K2, ctx->rq_vis_b.p, 1);
+            if (e == cudaSuccess) e = pass(2, 1, q2, q3);
+            if (e == cudaSuccess) e = visibility(K3, ctx->rq_vis_a.p, 2);
+            if (e == cudaSuccess) e = pass(2, 2, q2, q3);
             if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("restir launch: ") + cudaGetErrorString(e));
             std::swap(R.hist, R.spat);
             R.history_valid = 1;

@@ -25,6 +25,15 @@
 //     reuse compares against this frame's normals (the shader samples the
 //     previous frame's normal image at :490);
 //   - FindNeighbourPixelCoord's unbounded retry loop (:400) is bounded to 8 tries.
+//
+// Visibility rays are not traced inline: the initial and spatial passes run twice
+// (three times for the spatial pass) over the same pixels with the same random
+// streams.  The first run records every shadow ray into a per-pixel slot queue
+// (the rays' origins, directions and lengths never depend on earlier visibility
+// results, and neither does the number of random draws), the queue is traced by
+// the persistent any-hit kernel with ray replacement, and the next run replays
+// the results in the same order.  The final shading rays depend on which samples
+// the spatial reservoir kept, so they form a third queue.
 #include "snk_frame.h"
 #include "snk_trace.cuh"
 
@@ -63,17 +72,49 @@ __device__ __forceinline__ void res_store(void* base, uint32_t i, const Reservoi
     p[0] = q[0]; p[1] = q[1]; p[2] = q[2];
 }
 
-struct Ctx {   // per-thread traversal context
+// Per-pixel visibility context: records shadow rays into a queue, or replays
+// their results, in call order.
+struct Ctx {
     const SceneDev* S;
-    uint2* sh;
-    uint32_t shadow_rays;
+    uint32_t shadow_rays;   // rays recorded by this thread
+    float4* rays;           // recording
+    const uint8_t* vis;     // replaying
+    size_t base;
+    uint32_t k, cap;
+    bool overflow;
 };
 
+__device__ __forceinline__ void ctx_queue(Ctx& c, const RestirQueue& q, uint32_t pixel, bool record) {
+    c.rays = record ? q.rays : nullptr;
+    c.vis = record ? nullptr : q.vis;
+    c.base = (size_t)pixel * q.per_pixel;
+    c.k = 0;
+    c.cap = q.per_pixel;
+}
+
+// marks the slots a recording pass left unused as empty (tmax < 0)
+__device__ __forceinline__ void ctx_close(Ctx& c) {
+    if (!c.rays) return;
+    for (uint32_t k = c.k; k < c.cap; k++) c.rays[2 * (c.base + k) + 1] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+}
+
+// 1 when the segment is unoccluded (recording: always 1, the value is not used
+// for anything the replay would see differently)
 __device__ __noinline__ float shadow_test(Ctx& c, V3 o, V3 d, float tmax) {
-    TraceResult r;
-    c.shadow_rays++;
-    bool hit = trace_scene<true, false>(*c.S, o, d, SHADOW_TMIN, tmax, r, c.sh, threadIdx.x, RBLK, nullptr);
-    return hit ? 0.0f : 1.0f;
+    if (c.k >= c.cap) { c.overflow = true; return 0.0f; }
+    const size_t slot = c.base + c.k++;
+    if (c.rays) {
+        c.shadow_rays++;
+        c.rays[2 * slot] = make_float4(o.x, o.y, o.z, SHADOW_TMIN);
+        c.rays[2 * slot + 1] = make_float4(d.x, d.y, d.z, tmax);
+        return 1.0f;
+    }
+    return c.vis[slot] ? 1.0f : 0.0f;
+}
+
+__device__ __forceinline__ void ctx_check(Ctx& c) {
+    if (c.overflow && c.S->error_word) atomicOr(c.S->error_word, ERR_BAD_INDEX);
+    c.overflow = false;
 }
 
 __device__ __noinline__ bool trace_primary(const SceneDev& S, V3 o, V3 d, TraceResult& r, uint2* sh) {
@@ -230,60 +271,82 @@ __global__ void __launch_bounds__(RBLK) k_restir_gbuffer(FrameParams F, uint32_t
 }
 
 // WriteInitialReservoirs: initial RIS + temporal reuse
-__global__ void __launch_bounds__(RBLK) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs) {
-    __shared__ uint2 sh[STACK_SH * RBLK];
+__global__ void __launch_bounds__(RBLK) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
+                                                        RestirQueue q, int phase) {
     const ViewDev& V = F.views[vi];
     const SceneDev& S = F.S;
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
+    const bool record = phase == 0;
     Ctx c;
-    c.S = &F.S; c.sh = sh; c.shadow_rays = 0;
+    c.S = &F.S; c.shadow_rays = 0; c.overflow = false;
     for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
         uint32_t o = base + threadIdx.x;
         if (o >= n) continue;
         uint32_t x = o % W, y = o / W;
+        ctx_queue(c, q, o, record);
         float4 gp = R.g_pos[o];
-        if (gp.w != 1.0f) { res_store(R.temporal, o, res_init()); continue; }
+        if (gp.w != 1.0f) {
+            if (record) ctx_close(c);
+            else res_store(R.temporal, o, res_init());
+            continue;
+        }
         float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
         V3 nrm = v3(gn.x, gn.y, gn.z);
         Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
-        Pcg rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000001u, rs.seed);
-        Reservoir Rr = res_init();
+        Pcg rng;
+        Reservoir Rr;
         float phat_pl = 0.0f, phat_em = 0.0f;
-        const uint32_t npl = S.num_point_lights;
-        if (npl > 0) {
-            for (uint32_t i = 0; i < rs.candidates; i++) {
-                uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
-                if (idx > npl - 1) idx = npl - 1;
-                float p_hat = length(calc_pointlight(S.point_lights[idx], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
-                                                     sh.albedo));
-                float w = p_hat / (1.0f / (float)npl);
-                if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
+        if (!record) {
+            // the RIS result of the recording run: reservoir, target values and stream position
+            Rr = res_load(R.temporal, o);
+            const float4 a = R.ris[2ull * o], b = R.ris[2ull * o + 1];
+            phat_pl = a.x; phat_em = a.y;
+            rng.state = ((uint64_t)__float_as_uint(b.y) << 32) | __float_as_uint(b.x);
+            rng.inc = ((uint64_t)__float_as_uint(b.w) << 32) | __float_as_uint(b.z);
+        } else {
+            rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000001u, rs.seed);
+            Rr = res_init();
+            const uint32_t npl = S.num_point_lights;
+            if (npl > 0) {
+                for (uint32_t i = 0; i < rs.candidates; i++) {
+                    uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
+                    if (idx > npl - 1) idx = npl - 1;
+                    float p_hat = length(calc_pointlight(S.point_lights[idx], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
+                                                         sh.albedo));
+                    float w = p_hat / (1.0f / (float)npl);
+                    if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
+                }
             }
-        }
-        const uint32_t nem = S.num_emissive_instances;
-        if (nem > 0) {
-            for (uint32_t i = 0; i < rs.candidates; i++) {
-                uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
-                if (k > nem - 1) k = nem - 1;
-                uint32_t inst = S.emissive_instances[k];
-                const InstShade& I = S.inst_shade[inst];
-                const MeshInfo& M = S.meshes[I.mesh_id];
-                uint32_t ntri = M.num_triangles;
-                uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
-                if (tri > ntri - 1) tri = ntri - 1;
-                float bu = pcg_float(rng), bv = pcg_float(rng);
-                if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
-                const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
-                V3 p0 = load3(S.positions + 3ull * (M.vertex_offset + ix[0]));
-                V3 p1 = load3(S.positions + 3ull * (M.vertex_offset + ix[1]));
-                V3 p2 = load3(S.positions + 3ull * (M.vertex_offset + ix[2]));
-                float area = (I.det3 * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
-                V3 rad = tri_radiance(c, inst, tri, bu, bv, sh, false);
-                float p_hat = length(rad);
-                float pdf = 1.0f / ((float)(nem * ntri) * area);
-                float w = p_hat / pdf;
-                if (update_em(Rr, inst, tri, bu, bv, w, rng)) phat_em = p_hat;
+            const uint32_t nem = S.num_emissive_instances;
+            if (nem > 0) {
+                for (uint32_t i = 0; i < rs.candidates; i++) {
+                    uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
+                    if (k > nem - 1) k = nem - 1;
+                    uint32_t inst = S.emissive_instances[k];
+                    const InstShade& I = S.inst_shade[inst];
+                    const MeshInfo& M = S.meshes[I.mesh_id];
+                    uint32_t ntri = M.num_triangles;
+                    uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
+                    if (tri > ntri - 1) tri = ntri - 1;
+                    float bu = pcg_float(rng), bv = pcg_float(rng);
+                    if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
+                    const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
+                    V3 p0 = load3(S.positions + 3ull * (M.vertex_offset + ix[0]));
+                    V3 p1 = load3(S.positions + 3ull * (M.vertex_offset + ix[1]));
+                    V3 p2 = load3(S.positions + 3ull * (M.vertex_offset + ix[2]));
+                    float area = (I.det3 * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
+                    V3 rad = tri_radiance(c, inst, tri, bu, bv, sh, false);
+                    float p_hat = length(rad);
+                    float pdf = 1.0f / ((float)(nem * ntri) * area);
+                    float w = p_hat / pdf;
+                    if (update_em(Rr, inst, tri, bu, bv, w, rng)) phat_em = p_hat;
+                }
             }
+            res_store(R.temporal, o, Rr);
+            R.ris[2ull * o] = make_float4(phat_pl, phat_em, 0.0f, 0.0f);
+            R.ris[2ull * o + 1] =
+                make_float4(__uint_as_float((uint32_t)rng.state), __uint_as_float((uint32_t)(rng.state >> 32)),
+                            __uint_as_float((uint32_t)rng.inc), __uint_as_float((uint32_t)(rng.inc >> 32)));
         }
         if (Rr.pl_idx != INVALID) {
             V3 lp = load3(S.point_lights[Rr.pl_idx].pos);
@@ -331,28 +394,40 @@ __global__ void __launch_bounds__(RBLK) k_restir_initial(FrameParams F, uint32_t
                 }
             }
         }
-        res_store(R.temporal, o, out);
+        ctx_check(c);
+        if (record) ctx_close(c);
+        else res_store(R.temporal, o, out);
     }
     flush_rays(c.shadow_rays, &F.counters[CNT_SHADOW_RAYS]);
 }
 
 // ComputeAndWriteSpatialReservoirReuse + CalculateRadianceFromReservoirs + main
-__global__ void __launch_bounds__(RBLK) k_restir_spatial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs) {
-    __shared__ uint2 sh[STACK_SH * RBLK];
+// phase 0: record q (sun ray, combine rays); phase 1: replay q, write the spatial
+// reservoirs, record qs (final shading rays); phase 2: replay q's sun ray and qs,
+// write radiance, the FP64 accumulator and the next frame's history normals.
+__global__ void __launch_bounds__(RBLK) k_restir_spatial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
+                                                        RestirQueue q, RestirQueue qs, int phase) {
     const ViewDev& V = F.views[vi];
     const SceneDev& S = F.S;
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
     Ctx c;
-    c.S = &F.S; c.sh = sh; c.shadow_rays = 0;
+    c.S = &F.S; c.shadow_rays = 0; c.overflow = false;
     for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
         uint32_t o = base + threadIdx.x;
         if (o >= n) continue;
         uint32_t x = o % W, y = o / W;
         float4 gp = R.g_pos[o];
         float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
+        ctx_queue(c, q, o, phase == 0);
         V3 colour;
         if (gp.w != 1.0f) {
-            res_store(R.spatial, o, res_init());
+            if (phase == 0) { ctx_close(c); continue; }
+            if (phase == 1) {
+                res_store(R.spatial, o, res_init());
+                ctx_queue(c, qs, o, true);
+                ctx_close(c);
+                continue;
+            }
             colour = gp.w == 2.0f ? v3(ga.x, ga.y, ga.z) : v3(0.0f, 0.0f, 0.0f);
         } else {
             V3 nrm = v3(gn.x, gn.y, gn.z);
@@ -363,35 +438,44 @@ __global__ void __launch_bounds__(RBLK) k_restir_spatial(FrameParams F, uint32_t
                                           sh.metal, sh.albedo);
                 light = mul(cdl, shadow_test(c, sh.biased, load3(S.dir_light.dir), 1000.0f));
             }
-            Pcg rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000002u, rs.seed);
-            Reservoir Rr = res_init();
-            float phat_pl = 0.0f, phat_em = 0.0f;
-            Reservoir self = res_load(R.temporal, o);
-            combine(c, Rr, self, phat_pl, phat_em, sh, rng);
-            Rr.m_em += self.m_em;
-            Rr.pl_m += self.pl_m;
-            for (int i = 0; i < rs.spatial; i++) {
-                int nx = -1, ny = -1;
-                for (int tries = 0; tries < 8; tries++) {
-                    float ox = ((pcg_float(rng) - 0.5f) * 2.0f) * rs.radius;
-                    float oy = ((pcg_float(rng) - 0.5f) * 2.0f) * rs.radius;
-                    float fx = (float)x + ox, fy = (float)y + oy;
-                    if (fx >= 0.0f && fy >= 0.0f && fx < (float)W && fy < (float)H) { nx = (int)fx; ny = (int)fy; break; }
+            Reservoir Rr;
+            if (phase < 2) {
+                Pcg rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000002u, rs.seed);
+                Rr = res_init();
+                float phat_pl = 0.0f, phat_em = 0.0f;
+                Reservoir self = res_load(R.temporal, o);
+                combine(c, Rr, self, phat_pl, phat_em, sh, rng);
+                Rr.m_em += self.m_em;
+                Rr.pl_m += self.pl_m;
+                for (int i = 0; i < rs.spatial; i++) {
+                    int nx = -1, ny = -1;
+                    for (int tries = 0; tries < 8; tries++) {
+                        float ox = ((pcg_float(rng) - 0.5f) * 2.0f) * rs.radius;
+                        float oy = ((pcg_float(rng) - 0.5f) * 2.0f) * rs.radius;
+                        float fx = (float)x + ox, fy = (float)y + oy;
+                        if (fx >= 0.0f && fy >= 0.0f && fx < (float)W && fy < (float)H) { nx = (int)fx; ny = (int)fy; break; }
+                    }
+                    if (nx < 0) continue;
+                    uint32_t qi = (uint32_t)ny * W + (uint32_t)nx;
+                    float4 qp = R.g_pos[qi];
+                    float4 qn4 = R.g_normal[qi];
+                    V3 qn = qp.w == 1.0f ? v3(qn4.x, qn4.y, qn4.z) : v3(0.0f, 0.0f, 0.0f);
+                    if (dot(qn, nrm) < 0.95f) continue;
+                    Reservoir Q = res_load(R.temporal, qi);
+                    combine(c, Rr, Q, phat_pl, phat_em, sh, rng);
+                    Rr.m_em += Q.m_em;
+                    Rr.pl_m += Q.pl_m;
                 }
-                if (nx < 0) continue;
-                uint32_t q = (uint32_t)ny * W + (uint32_t)nx;
-                float4 qp = R.g_pos[q];
-                float4 qn4 = R.g_normal[q];
-                V3 qn = qp.w == 1.0f ? v3(qn4.x, qn4.y, qn4.z) : v3(0.0f, 0.0f, 0.0f);
-                if (dot(qn, nrm) < 0.95f) continue;
-                Reservoir Q = res_load(R.temporal, q);
-                combine(c, Rr, Q, phat_pl, phat_em, sh, rng);
-                Rr.m_em += Q.m_em;
-                Rr.pl_m += Q.pl_m;
+                Rr.w_em = phat_em > 0.0f ? (Rr.w_sum_em / phat_em) / (float)Rr.m_em : 0.0f;
+                Rr.w_pl = phat_pl > 0.0f ? (Rr.w_sum_pl / phat_pl) / (float)Rr.pl_m : 0.0f;
+                ctx_check(c);
+                if (phase == 0) { ctx_close(c); continue; }
+                res_store(R.spatial, o, Rr);
+                ctx_queue(c, qs, o, true);   // phase 1 records the final shading rays
+            } else {
+                Rr = res_load(R.spatial, o);
+                ctx_queue(c, qs, o, false);
             }
-            Rr.w_em = phat_em > 0.0f ? (Rr.w_sum_em / phat_em) / (float)Rr.m_em : 0.0f;
-            Rr.w_pl = phat_pl > 0.0f ? (Rr.w_sum_pl / phat_pl) / (float)Rr.pl_m : 0.0f;
-            res_store(R.spatial, o, Rr);
             V3 rad = v3(0.0f, 0.0f, 0.0f);
             if (S.num_point_lights > 0 && Rr.pl_idx != INVALID) {
                 const PointLightDev& L = S.point_lights[Rr.pl_idx];
@@ -406,6 +490,8 @@ __global__ void __launch_bounds__(RBLK) k_restir_spatial(FrameParams F, uint32_t
                 V3 e = tri_radiance(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, true);
                 rad = add(rad, mul(e, Rr.w_em));
             }
+            ctx_check(c);
+            if (phase == 1) { ctx_close(c); continue; }
             colour = add(light, rad);
         }
         float4 r4 = make_float4(colour.x, colour.y, colour.z, 1.0f);
@@ -425,11 +511,12 @@ __global__ void __launch_bounds__(RBLK) k_restir_spatial(FrameParams F, uint32_t
 
 }  // namespace
 
-cudaError_t launch_restir_stage(int stage, const FrameParams& F, uint32_t vi, const RestirView& R,
-                                const RestirSettings& rs, int grid, cudaStream_t s) {
+cudaError_t launch_restir_stage(int stage, int phase, const FrameParams& F, uint32_t vi, const RestirView& R,
+                                const RestirSettings& rs, const RestirQueue& q, const RestirQueue& qs, int grid,
+                                cudaStream_t s) {
     if (stage == 0) k_restir_gbuffer<<<grid, RBLK, 0, s>>>(F, vi, R);
-    else if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs);
-    else k_restir_spatial<<<grid, RBLK, 0, s>>>(F, vi, R, rs);
+    else if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, phase);
+    else k_restir_spatial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs, phase);
     return cudaGetLastError();
 }
 

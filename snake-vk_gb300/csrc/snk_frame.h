@@ -69,6 +69,9 @@ cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid,
 cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
 cudaError_t launch_trace_rays(const SceneDev& S, const float4* rays, uint32_t n, HitDev* hits, bool any,
                               uint32_t* work_counter, int grid, const TraceTuning& tune, cudaStream_t s);
+// vis[i] = 1 when segment i (origin, tmin | direction, tmax; tmax < 0: empty) is unoccluded
+cudaError_t launch_trace_visibility(const SceneDev& S, const float4* rays, uint32_t n, uint8_t* vis,
+                                    uint32_t* work_counter, int grid, const TraceTuning& tune, cudaStream_t s);
 
 // ReSTIR DI state of one view
 struct RestirView {
@@ -80,6 +83,7 @@ struct RestirView {
     void* temporal;     // reservoirs (48 bytes per pixel)
     void* history;      // final reservoirs of the previous frame
     void* spatial;      // final reservoirs of this frame
+    float4* ris;        // 2 per pixel: the initial pass's RIS state between its two runs
     uint32_t history_valid;
 };
 
@@ -90,9 +94,30 @@ struct RestirSettings {
     uint32_t pad;
 };
 
-// stage 0: primary G-buffer, 1: initial + temporal reuse, 2: spatial reuse + shading
-cudaError_t launch_restir_stage(int stage, const FrameParams& F, uint32_t view_index, const RestirView& R,
-                                const RestirSettings& rs, int grid, cudaStream_t s);
+// Visibility rays of a ReSTIR pass: per pixel `per_pixel` slots of 2 float4
+// (origin, tmin | direction, tmax) at rays[2 * (pixel * per_pixel + k)].  A pass
+// either records its rays into `rays` or replays their results from `vis`.
+struct RestirQueue {
+    float4* rays;
+    const uint8_t* vis;
+    uint32_t per_pixel;
+    uint32_t pad;
+};
+// slots per pixel of the passes
+constexpr uint32_t RESTIR_INITIAL_SLOTS = 6;   // 2 visibility + 2 x 2 temporal combine
+__host__ __device__ constexpr uint32_t restir_spatial_slots(int spatial) {
+    return 1u + 2u * (1u + (uint32_t)(spatial > 0 ? spatial : 0));   // sun + 2 x (self + neighbours)
+}
+constexpr uint32_t RESTIR_SHADE_SLOTS = 2;
+
+// stage 0: primary G-buffer
+// stage 1: initial RIS + temporal reuse: phase 0 records q's rays, phase 1 replays them
+// stage 2: spatial reuse + shading: phase 0 records q's rays; phase 1 replays q,
+//          writes the spatial reservoirs and records qs's (final shading) rays;
+//          phase 2 replays the sun ray of q and qs, writes the frame's outputs
+cudaError_t launch_restir_stage(int stage, int phase, const FrameParams& F, uint32_t view_index, const RestirView& R,
+                                const RestirSettings& rs, const RestirQueue& q, const RestirQueue& qs, int grid,
+                                cudaStream_t s);
 
 // Read-only view of a context (defined in api.cu) for entry points that live in
 // other translation units.

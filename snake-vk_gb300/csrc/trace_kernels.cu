@@ -206,6 +206,51 @@ __global__ void __launch_bounds__(256) k_accum_shadow(FrameParams F, uint32_t d)
     }
 }
 
+// visibility of a queue of segments: vis[i] = 1 when nothing is hit in (tmin, tmax),
+// 0 when something is; entries with tmax < 0 are empty (vis 1, no traversal).
+// The ReSTIR passes queue their visibility rays here instead of tracing inline.
+template <int MINB>
+__global__ void __launch_bounds__(TBLK, MINB) k_trace_visibility(SceneDev S, const float4* __restrict__ rays,
+                                                                 uint32_t n, uint8_t* vis, uint32_t* work,
+                                                                 TraceTuning tune) {
+    const Knobs kn(tune);
+    __shared__ uint2 sh_stack[STACK_SH * TBLK];
+    const uint32_t lane = threadIdx.x & 31u;
+    Traverser<true, false> tv;
+    uint2 spill[STACK_MAX - STACK_SH];
+    RayFeed feed;
+    feed.init();
+    bool active = false;
+    uint32_t ri = 0;
+    for (;;) {
+        unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+        if (__popc(~act) >= kn.refill_idle && !feed.done()) {
+            uint32_t i = feed.refill(~act, lane, work, n, kn.chunk);
+            if (i != INVALID) {
+                float4 b = __ldg(rays + 2ull * i + 1);
+                if (b.w < 0.0f) {
+                    vis[i] = 1u;
+                } else {
+                    float4 a = __ldg(rays + 2ull * i);
+                    tv.init(S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
+                    ri = i;
+                    active = true;
+                }
+            }
+            act = __ballot_sync(0xFFFFFFFFu, active);
+        }
+        if (act == 0) {
+            if (feed.done()) break;
+            continue;
+        }
+        if (warp_step(tv, active, S, nullptr, kn.prim_bias)) {
+            TraceResult r;
+            vis[ri] = tv.finish(S, r) ? 0u : 1u;
+            active = false;
+        }
+    }
+}
+
 // generic trace of an array of rays (the snk_pt_trace_rays test hook)
 template <bool ANY>
 __global__ void __launch_bounds__(TBLK, 6) k_trace_rays(SceneDev S, const float4* __restrict__ rays, uint32_t n,
@@ -280,6 +325,14 @@ cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, 
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_accum_shadow<<<grid / 2 > 0 ? grid / 2 : 1, 256, 0, s>>>(F, depth);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_visibility(const SceneDev& S, const float4* rays, uint32_t n, uint8_t* vis, uint32_t* work,
+                                    int grid, const TraceTuning& tune, cudaStream_t s) {
+    if (tune.variant == 1) k_trace_visibility<8><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+    else if (tune.variant == 2) k_trace_visibility<4><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+    else k_trace_visibility<6><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
     return cudaGetLastError();
 }
 
