@@ -54,6 +54,22 @@ def dist_info():
     return ws, rank, local
 
 
+def over_ranks(seconds: float, units: float, ws: int, device=None) -> tuple:
+    """(max of `seconds`, sum of `units`) over the ranks of the job: the job takes as
+    long as its slowest rank, and its work is every rank's.  Uses the default
+    process group (NCCL with CUDA tensors in the benchmark; gloo with CPU tensors
+    in the tests)."""
+    if ws <= 1:
+        return float(seconds), float(units)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(u)
+    return float(t.item()), float(u.item())
+
+
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
 
@@ -489,16 +505,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier()
     total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        r = torch.tensor([rays], device=dev, dtype=torch.float64)
-        dist.all_reduce(r)
-        rays_all = float(r.item())
-    else:
-        rays_all = float(rays)
+    total_ms, rays_all = over_ranks(total_ms, rays, ws, dev)
     value = rays_all / (total_ms / 1e3) / 1e6
 
     # roofline of the dominant kernel
@@ -536,12 +543,14 @@ def run_ours(args):
         s = pt.stats()
         e2e_rays += s["rays_camera"] + s["rays_extension"] + s["rays_shadow"]
     e2e_s = time.perf_counter() - t0
-    e2e_value = e2e_rays * ws / e2e_s / 1e6
+    e2e_s, e2e_rays_all = over_ranks(e2e_s, e2e_rays, ws, dev)
+    e2e_value = e2e_rays_all / e2e_s / 1e6
     # the same, refitting the instance BVH between full rebuilds every 16 updates
     pt.set_tuning(dict(tuning, tlas_refit_interval=16))
     for k in range(max(1, args.warmup)):
         pt.set_instances(inst)
         pt.render([view], settings(2000 + k, 0), [{"radiance": host_rad}])
+    barrier()
     t0 = time.perf_counter()
     refit_rays = 0
     for k in range(args.steps):
@@ -550,6 +559,7 @@ def run_ours(args):
         s = pt.stats()
         refit_rays += s["rays_camera"] + s["rays_extension"] + s["rays_shadow"]
     refit_s = time.perf_counter() - t0
+    refit_s, refit_rays = over_ranks(refit_s, refit_rays, ws, dev)
     pt.set_tuning(tuning)
     clk = clocks.stop()   # sampled over the device-timed and the end-to-end frames
     h2d = inst.nbytes + abi.VIEW_DTYPE.itemsize + abi.SETTINGS_DTYPE.itemsize
@@ -565,7 +575,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": e2e_s / args.steps * 1e3},
-            "e2e_instance_refit": {"value": refit_rays * ws / refit_s / 1e6, "unit": UNIT,
+            "e2e_instance_refit": {"value": refit_rays / refit_s / 1e6, "unit": UNIT,
                                    "ms_per_step": refit_s / args.steps * 1e3,
                                    "note": "as e2e, instance BVH refitted, rebuilt every 16th update"},
             "roofline": roofline}
