@@ -49,40 +49,63 @@ __device__ __forceinline__ int wrap_repeat(int i, int n) {
     return r < 0 ? r + n : r;
 }
 
-// texture() with a linear filter and repeat addressing, in FP32
-template <class T, int C>
-__device__ __forceinline__ void bilinear(const T* img, int w, int h, float cu, float cv, float* o) {
-    const float u = cu * (float)w - 0.5f, v = cv * (float)h - 0.5f;
-    const float fu = floorf(u), fv = floorf(v);
-    const float a = u - fu, b = v - fv;
-    const int i0 = wrap_repeat((int)fu, w), i1 = wrap_repeat((int)fu + 1, w);
-    const int j0 = wrap_repeat((int)fv, h), j1 = wrap_repeat((int)fv + 1, h);
-    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
-    const float* t00 = reinterpret_cast<const float*>(&img[(size_t)j0 * w + i0]);
-    const float* t10 = reinterpret_cast<const float*>(&img[(size_t)j0 * w + i1]);
-    const float* t01 = reinterpret_cast<const float*>(&img[(size_t)j1 * w + i0]);
-    const float* t11 = reinterpret_cast<const float*>(&img[(size_t)j1 * w + i1]);
-    for (int c = 0; c < C; c++) o[c] = ((w00 * t00[c] + w10 * t10[c]) + w01 * t01[c]) + w11 * t11[c];
-}
+// texture() with a linear filter and repeat addressing, in FP32: the four texels
+// are fetched first (so that their loads are in flight together with the
+// frame's tile), the weights are applied later
+template <class T>
+struct Bilinear {
+    T t00, t10, t01, t11;
+    float w00, w10, w01, w11;
+    __device__ __forceinline__ void fetch(const T* __restrict__ img, int w, int h, float cu, float cv) {
+        const float u = cu * (float)w - 0.5f, v = cv * (float)h - 0.5f;
+        const float fu = floorf(u), fv = floorf(v);
+        const float a = u - fu, b = v - fv;
+        const int i0 = wrap_repeat((int)fu, w), i1 = wrap_repeat((int)fu + 1, w);
+        const int j0 = wrap_repeat((int)fv, h), j1 = wrap_repeat((int)fv + 1, h);
+        w00 = (1.0f - a) * (1.0f - b); w10 = a * (1.0f - b); w01 = (1.0f - a) * b; w11 = a * b;
+        t00 = img[(size_t)j0 * w + i0];
+        t10 = img[(size_t)j0 * w + i1];
+        t01 = img[(size_t)j1 * w + i0];
+        t11 = img[(size_t)j1 * w + i1];
+    }
+    template <int C>
+    __device__ __forceinline__ void apply(float* o) const {
+        const float* a = reinterpret_cast<const float*>(&t00);
+        const float* b = reinterpret_cast<const float*>(&t10);
+        const float* c = reinterpret_cast<const float*>(&t01);
+        const float* d = reinterpret_cast<const float*>(&t11);
+        for (int k = 0; k < C; k++) o[k] = ((w00 * a[k] + w10 * b[k]) + w01 * c[k]) + w11 * d[k];
+    }
+};
 
 __global__ void __launch_bounds__(TX * TY) k_taa_resolve(TaaImages I) {
     __shared__ float4 tile[TY + 2][TX + 2];
     const int bx = blockIdx.x * TX, by = blockIdx.y * TY;
     const int t = threadIdx.y * TX + threadIdx.x;
+    const int x = bx + threadIdx.x, y = by + threadIdx.y;
+    const bool inside = x < I.w && y < I.h;
+    const size_t pix = inside ? (size_t)y * I.w + x : 0;
+    // this pixel's reprojected history and previous-velocity texels, fetched
+    // before the tile so that all of the thread's loads overlap
+    float2 vel = make_float2(0.0f, 0.0f);
+    Bilinear<float4> hb;
+    Bilinear<float2> pb;
+    if (inside) {
+        vel = I.motion[pix];
+        float hx = ((float)x + 0.5f) / (float)I.w + vel.x;
+        float hy = ((float)y + 0.5f) / (float)I.h + vel.y;
+        hx = fminf(fmaxf(hx, 0.0f), 1.0f);
+        hy = fminf(fmaxf(hy, 0.0f), 1.0f);
+        hb.fetch(I.hist, I.w, I.h, hx, hy);
+        pb.fetch(I.pmot, I.w, I.h, hx, hy);
+    }
     for (int k = t; k < (TX + 2) * (TY + 2); k += TX * TY) {
         const int ly = k / (TX + 2), lx = k % (TX + 2);
         const int gx = min(max(bx + lx - 1, 0), I.w - 1), gy = min(max(by + ly - 1, 0), I.h - 1);
         tile[ly][lx] = I.cur[(size_t)gy * I.w + gx];
     }
     __syncthreads();
-    const int x = bx + threadIdx.x, y = by + threadIdx.y;
-    if (x >= I.w || y >= I.h) return;
-    const size_t pix = (size_t)y * I.w + x;
-    const float2 vel = I.motion[pix];
-    float hx = ((float)x + 0.5f) / (float)I.w + vel.x;
-    float hy = ((float)y + 0.5f) / (float)I.h + vel.y;
-    hx = fminf(fmaxf(hx, 0.0f), 1.0f);
-    hy = fminf(fmaxf(hy, 0.0f), 1.0f);
+    if (!inside) return;
     const float4 cur4 = tile[threadIdx.y + 1][threadIdx.x + 1];
     const float cur[3] = {cur4.x, cur4.y, cur4.z};
     float mn[3] = {9999.0f, 9999.0f, 9999.0f}, mx[3] = {-9999.0f, -9999.0f, -9999.0f};
@@ -110,7 +133,7 @@ __global__ void __launch_bounds__(TX * TY) k_taa_resolve(TaaImages I) {
         p[c] = fminf(fmaxf(mu[c], mn[c]), mx[c]);
     }
     float hist[3];
-    bilinear<float4, 3>(I.hist, I.w, I.h, hx, hy, hist);
+    hb.apply<3>(hist);
     // clip_aabb(minc, maxc, vec4(p, 1), vec4(hist, 1)); r.w stays 0
     float r[3];
     for (int c = 0; c < 3; c++) r[c] = fmaxf(hist[c], 0.0f) - p[c];
@@ -129,7 +152,7 @@ __global__ void __launch_bounds__(TX * TY) k_taa_resolve(TaaImages I) {
         }
     }
     float pv[2];
-    bilinear<float2, 2>(I.pmot, I.w, I.h, hx, hy, pv);
+    pb.apply<2>(pv);
     const float vx = pv[0] + vel.x, vy = pv[1] + vel.y;
     const float vlen = sqrtf(vx * vx + vy * vy);
     const float dis = fminf(fmaxf((vlen - 0.001f) * 10.0f, 0.0f), 1.0f);
