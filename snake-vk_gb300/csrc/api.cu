@@ -26,6 +26,13 @@ struct HostMesh {
     bool has_normals = false;
 };
 
+// Host copy of the last bytes uploaded into a device buffer, so that per-frame
+// scene updates skip re-uploading tables that did not change.
+struct UploadMemo {
+    std::vector<unsigned char> bytes;
+    const void* dev = nullptr;
+};
+
 struct RestirState {
     uint32_t w = 0, h = 0;
     DBuf<float4> g_pos, g_normal, g_albedo, g_misc, prev_normal;
@@ -76,6 +83,7 @@ struct snk_pt_ctx {
     DBuf<float4> rq_rays;                              // ReSTIR visibility queue (slots x pixels x 2)
     DBuf<uint8_t> rq_vis_a, rq_vis_b;                  // its results (initial / shading, spatial)
     DBuf<uint32_t> rq_work;                            // work counters of the three visibility traces
+    UploadMemo memo[7];                // instance trace/shade records, emissive list, lights, CDF, PMF, BVH list
     DBuf<SmallBuildOut> d_small_out;   // result record of the single-launch instance BVH build
     bool tlas_small = false;
     // instance BVH refit state: exact node boxes and depths, primitive order and
@@ -159,6 +167,20 @@ int fail(snk_pt_ctx* c, const Status& s) { return fail(c, s.code, s.msg); }
 
 Status set_device(snk_pt_ctx* ctx) {
     SNK_TRY_CUDA(cudaSetDevice(ctx->device));
+    return Status::Ok();
+}
+
+template <class T>
+Status upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s);
+
+template <class T>
+Status upload_changed(DBuf<T>& b, UploadMemo& memo, const T* src, size_t n, cudaStream_t s) {
+    const size_t bytes = n * sizeof(T);
+    if (b.p && memo.dev == b.p && memo.bytes.size() == bytes && (bytes == 0 || !std::memcmp(memo.bytes.data(), src, bytes)))
+        return Status::Ok();
+    SNK_TRY(upload(b, src, n, s));
+    memo.bytes.assign(reinterpret_cast<const unsigned char*>(src), reinterpret_cast<const unsigned char*>(src) + bytes);
+    memo.dev = b.p;
     return Status::Ok();
 }
 
@@ -317,9 +339,9 @@ Status build_instances(snk_pt_ctx* ctx) {
             ctx->scene_hi[r] = list.empty() ? 1.0f : (float)hi[r];
         }
     }
-    SNK_TRY(upload(ctx->d_inst_trace, it.data(), it.size(), st));
-    SNK_TRY(upload(ctx->d_inst_shade, is.data(), is.size(), st));
-    SNK_TRY(upload(ctx->d_emissive, emissive.data(), emissive.size(), st));
+    SNK_TRY(upload_changed(ctx->d_inst_trace, ctx->memo[0], it.data(), it.size(), st));
+    SNK_TRY(upload_changed(ctx->d_inst_shade, ctx->memo[1], is.data(), is.size(), st));
+    SNK_TRY(upload_changed(ctx->d_emissive, ctx->memo[2], emissive.data(), emissive.size(), st));
     ctx->n_emissive = (uint32_t)emissive.size();
 
     // path-tracer local lights: sphere lights, then every emissive triangle,
@@ -376,9 +398,9 @@ Status build_instances(snk_pt_ctx* ctx) {
     }
     if (!w.empty() && total > 0) cdf.back() = 1.0f;
     ctx->n_local = total > 0 ? (uint32_t)lights.size() : 0u;
-    SNK_TRY(upload(ctx->d_lights, lights.data(), lights.size(), st));
-    SNK_TRY(upload(ctx->d_cdf, cdf.data(), cdf.size(), st));
-    SNK_TRY(upload(ctx->d_pmf, pmf.data(), pmf.size(), st));
+    SNK_TRY(upload_changed(ctx->d_lights, ctx->memo[3], lights.data(), lights.size(), st));
+    SNK_TRY(upload_changed(ctx->d_cdf, ctx->memo[4], cdf.data(), cdf.size(), st));
+    SNK_TRY(upload_changed(ctx->d_pmf, ctx->memo[5], pmf.data(), pmf.size(), st));
 
     // instance BVH (rebuilt whenever instances change, as TlasSystem::BuildTlas,
     // or refitted when the tuning asks for it and the topology allows it)
@@ -389,7 +411,7 @@ Status build_instances(snk_pt_ctx* ctx) {
     ctx->tlas_prim_count = 0;
     const uint32_t n = (uint32_t)list.size();
     if (n > 0) {
-        SNK_TRY(upload(ctx->d_inst_list, list.data(), list.size(), st));
+        SNK_TRY(upload_changed(ctx->d_inst_list, ctx->memo[6], list.data(), list.size(), st));
         SNK_TRY_CUDA(ctx->d_box_lo.reserve(n));
         SNK_TRY_CUDA(ctx->d_box_hi.reserve(n));
         SNK_TRY_CUDA(ctx->d_prim_order.reserve(n));

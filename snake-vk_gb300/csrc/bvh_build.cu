@@ -546,7 +546,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
         }
         float4 a4 = node_lo[c], z4 = node_hi[c];
         quant_child(F, a4, z4, node, s);
-        float ha = half_area(a4, z4) / root_half_area;
+        const float ha = sah ? half_area(a4, z4) / root_half_area : 0.0f;
         if (c < nl && leaf_count[c] > leaf_pack) {
             node.meta[s] = (uint8_t)META_INTERNAL;
             node.imask |= (uint8_t)(1u << s);
@@ -580,7 +580,7 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
             local_sah += (double)ha * (double)cnt;   // primitive tests
         }
     }
-    atomicAdd(sah, local_sah);
+    if (sah) atomicAdd(sah, local_sah);
     uint4* dst = reinterpret_cast<uint4*>(nodes + w);
     const uint4* src = reinterpret_cast<const uint4*>(&node);
     for (int k = 0; k < 5; k++) dst[k] = src[k];
@@ -888,8 +888,9 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
                 wide_box[2 * local + 1] = S.node_hi[task.x];
                 wide_depth[local] = (uint32_t)level;
             }
+            // (no SAH statistic: the per-frame build skips its double-precision atomics)
             collapse_task(task, S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
-                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, &S.sah, rha, leaf_max,
+                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, nullptr, rha, leaf_max,
                           leaf_max);
         }
         __syncthreads();
@@ -905,7 +906,7 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
         out->prims = S.counters[3];
         out->error = e;
         out->max_depth = level > 0 ? (uint32_t)(level - 1) : 0u;
-        out->sah = 1.0 + S.sah;
+        out->sah = 0.0;
         out->lo[0] = rlo.x; out->lo[1] = rlo.y; out->lo[2] = rlo.z; out->lo[3] = 0.0f;
         out->hi[0] = rhi.x; out->hi[1] = rhi.y; out->hi[2] = rhi.z; out->hi[3] = 0.0f;
         if (e && err_word) atomicOr(err_word, 8u);

@@ -100,7 +100,7 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
 constexpr int SMALL_BUILD_MAX = 1024;
 struct SmallBuildOut {
     uint32_t num_nodes, prims, error, max_depth;
-    double sah;
+    double sah;   // not computed by the single-launch build (0)
     float lo[4], hi[4];
 };
 // wide_box (2 x (n + 1) float4: exact lo, hi per wide node) and wide_depth
