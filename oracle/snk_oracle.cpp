@@ -645,7 +645,8 @@ static void build_scene(Scene& S) {
         box_pad(w);
         I.wbox = w;
         ib[i] = w;
-        if (S.mats[I.in.material_id].flags & MAT_EMISSIVE) S.emissive_insts.push_back((uint32_t)i);
+        // (instances of empty meshes have no triangle to sample: left out of the list)
+        if ((S.mats[I.in.material_id].flags & MAT_EMISSIVE) && M.nt > 0) S.emissive_insts.push_back((uint32_t)i);
     }
     S.tlas.build(ib);
     // local light table for the path tracer: sphere lights, then emissive triangles

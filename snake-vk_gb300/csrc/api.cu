@@ -317,7 +317,9 @@ Status build_instances(snk_pt_ctx* ctx) {
         T.material_id = in.material_id;
         T.pad = 0;
         if (T.blas_root != INVALID) list.push_back((uint32_t)i);
-        if (ctx->materials[in.material_id].flags & SNK_MAT_EMISSIVE) emissive.push_back((uint32_t)i);
+        // (instances of empty meshes have no triangle to sample: left out of the list)
+        if ((ctx->materials[in.material_id].flags & SNK_MAT_EMISSIVE) && T.blas_root != INVALID)
+            emissive.push_back((uint32_t)i);
     }
     {   // world bounds of the scene (positions of the radiance cache are normalised to them)
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};

@@ -202,3 +202,55 @@ def test_graph_replay_matches_stream_launches(cuda, built_lib):
     assert np.array_equal(weights[0][0], weights[1][0])
     for a, b in zip(weights[0][1], weights[1][1]):
         assert np.array_equal(a, b)
+
+
+def test_full_size_eight_view_batch_sampled_pixels(cuda, built_lib):
+    """The largest workload in one call: config 3's eight views (640x360 .. 3840x2160,
+    19,238,400 pixels, depth 6) rendered together; 1500 seeded pixels of every view
+    against the oracle, and the ray count against the per-view pixel counts."""
+    sc = scenes.config3()
+    st = abi.settings(spp=1, max_depth=6, rr_depth=3, seed=17)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    outs = [snkpt.alloc_outputs(int(v["width"]), int(v["height"]), device=cuda,
+                                names=("radiance", "albedo", "normal", "depth", "inst_id", "prim_id"))
+            for v in sc.views]
+    pt.render(sc.views, st, outs)
+    pt.synchronize()
+    assert pt.stats()["rays_camera"] == sum(int(v["width"]) * int(v["height"]) for v in sc.views) == 19_238_400
+    osc = O.OracleScene(sc)
+    rng = np.random.default_rng(99)
+    base = 0
+    for v, o in zip(sc.views, outs):
+        n = int(v["width"]) * int(v["height"])
+        px = np.sort(rng.choice(n, 1500, replace=False)).astype(np.uint32)
+        r = osc.render_path(v, st, pixels=px, pixel_base=base)
+        g = {k: t.cpu().numpy() for k, t in o.items()}
+        for k in ("inst_id", "prim_id"):
+            assert np.array_equal(g[k].view(np.uint32)[px], r[k]), (int(v["width"]), k)
+        for k in ("albedo", "normal", "depth"):
+            assert np.array_equal(g[k][px], r[k]), (int(v["width"]), k)
+        m = max_rel(g["radiance"][px, :3], r["radiance"][:, :3])
+        assert m <= RTOL, (int(v["width"]), m)
+        base += n
+
+
+def test_instances_of_empty_meshes_are_skipped(cuda, built_lib):
+    """A scene mixing empty meshes (0 triangles) with real ones renders as if the
+    empty instances were absent."""
+    sc = scenes.config0(width=96, height=96)
+    empty = scenes.Mesh(np.zeros((0, 3), np.float32), None, np.zeros((0, 3), np.uint32))
+    meshes = list(sc.meshes) + [empty]
+    inst = np.concatenate([sc.instances, scenes.make_instances([(scenes.affine(t=(1.0, 2.0, 3.0)), len(meshes) - 1, 0)])])
+    mixed = scenes.Scene(meshes, inst, sc.materials, sc.dir_light, sc.point_lights, sc.views, "mixed")
+    st = abi.settings(spp=1, max_depth=3, seed=2)
+    a = _gpu_frame(_tracer(mixed), [sc.views[0]], st, cuda)[0]
+    b = _gpu_frame(_tracer(sc), [sc.views[0]], st, cuda)[0]
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def _tracer(sc):
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    return pt
