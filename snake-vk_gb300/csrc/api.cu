@@ -553,7 +553,8 @@ Status check_device_error(snk_pt_ctx* ctx) {
     if (e) {
         SNK_TRY_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
         return Status::Err(SNK_ERR_LIMIT, std::string("device traversal bound hit (error word ") + std::to_string(e) +
-                                              "): bit 1 stack depth, bit 2 step limit, bit 4 bad index, bit 8 instance BVH build");
+                                              "): bit 1 stack depth, bit 2 step limit, bit 4 bad index, bit 8 instance BVH build, "
+                                              "bit 16 tensor-core wait");
     }
     return Status::Ok();
 }
@@ -918,7 +919,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             const EncodeParams ep = cache_encode_params(ctx);
             e = staged(ctx, profile, SNK_STAGE_CACHE_INFER, [&] {
                 Status s = mlp_infer(ctx->mlp, F.qrec, F.counters + CNT_CACHE_QUERIES, 0u, ep, nullptr, F.qbeta, F.L,
-                                     grid_of(ctx, 4), st);
+                                     grid_of(ctx, 4), ctx->d_err.p, st);
                 return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
             });
         }
@@ -1260,11 +1261,12 @@ int snk_pt_cache_infer(snk_pt_ctx* ctx, const float* records, uint32_t n, float*
         out = ctx->cache_out.p;
     }
     API_TRY(mlp_infer(ctx->mlp, rec, nullptr, n, cache_encode_params(ctx), out, nullptr, nullptr, grid_of(ctx, 4),
-                      ctx->stream));
+                      ctx->d_err.p, ctx->stream));
     if (memory == SNK_MEM_HOST &&
         cudaMemcpyAsync(outp, out, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream))
         return fail(ctx, SNK_ERR_CUDA, "cache_infer: copy");
     if (cudaStreamSynchronize(ctx->stream)) return fail(ctx, SNK_ERR_CUDA, "cache_infer: sync");
+    API_TRY(check_device_error(ctx));
     return SNK_OK;
 }
 

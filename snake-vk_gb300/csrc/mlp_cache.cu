@@ -19,6 +19,14 @@
 // writes its dW partial; the Adam kernel sums the partials in a fixed order, so
 // training is deterministic.
 //
+// Inference runs on the fifth-generation tensor cores: one CTA of 128 threads
+// takes 128 queries, writes their encodings into shared memory in the tcgen05
+// operand layout, and chains the 5 layers as 128x64x64 (last 128x16x64)
+// tcgen05.mma issued by one thread, accumulating in tensor memory; after each
+// layer every thread reads its row back with tcgen05.ld, applies the ReLU and
+// stores the BF16 row as the next layer's operand.  Waits on the MMA completion
+// barrier are bounded (a give-up sets a status bit, read by the host).
+//
 // Input encoding (64 features, from a 64-byte query record: position, outgoing
 // direction, shading normal, roughness, albedo, metallic):
 //   0..35   position normalised to the scene box, per axis 6 octaves of
@@ -158,7 +166,189 @@ __device__ __forceinline__ void forward_tile(const uint2* wf, uint32_t (&a)[4][4
     }
 }
 
+// ---- tcgen05 helpers ---------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (row r, k) of an N x 64 K-major operand (no swizzle)
+__host__ __device__ __forceinline__ uint32_t tc_off(uint32_t r, uint32_t k) {
+    return (r >> 3) * 1024u + (k >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// shared-memory matrix descriptor: start address, leading (K) and stride (M/N)
+// byte offsets between core matrices, fixed version bits 0b001, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(128u >> 4) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor: D FP32, A and B BF16, both K-major, M = 128
+__device__ __forceinline__ uint32_t tc_idesc(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+// D[tmem] (+)= A[128 x 64] B^T (B: n x 64), four K = 16 steps, then a commit to mbar
+__device__ __forceinline__ void tc_gemm_k64(uint32_t tmem, uint32_t a_addr, uint32_t b_addr, uint32_t n,
+                                            uint32_t mbar) {
+    const uint32_t idesc = tc_idesc(n);
+#pragma unroll
+    for (uint32_t ks = 0; ks < 4; ks++) {
+        const uint64_t da = tc_desc(a_addr + ks * 256u), db = tc_desc(b_addr + ks * 256u);
+        const uint32_t acc = ks > 0 ? 1u : 0u;
+        asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                     :: "r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar));
+}
+
+// bounded wait for the barrier phase `parity`; false when it gave up
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (int it = 0; it < (1 << 24); it++) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(mbar), "r"(parity));
+        if (done) return true;
+    }
+    return false;
+}
+
+#define SNK_TC_LD16(base, r, o)                                                                        \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "                                             \
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"                   \
+                 : "=r"(r[o + 0]), "=r"(r[o + 1]), "=r"(r[o + 2]), "=r"(r[o + 3]), "=r"(r[o + 4]),   \
+                   "=r"(r[o + 5]), "=r"(r[o + 6]), "=r"(r[o + 7]), "=r"(r[o + 8]), "=r"(r[o + 9]),   \
+                   "=r"(r[o + 10]), "=r"(r[o + 11]), "=r"(r[o + 12]), "=r"(r[o + 13]),              \
+                   "=r"(r[o + 14]), "=r"(r[o + 15])                                                  \
+                 : "r"(base))
+
+constexpr int INFER_THREADS = 128;
+
+struct InferSmem {
+    unsigned short w[MLP_TC_ELEMS];   // the 5 layers, tcgen05 operand layout
+    unsigned short a[128 * 64];       // this tile's activations (A operand)
+    unsigned long long mbar;
+    uint32_t tmem;
+    uint32_t failed;
+};
+
 // ---- inference -------------------------------------------------------------------
+// records: 4 float4 per query.  Result y (3 floats) goes to out[3i..] when out is
+// given; otherwise, in render mode, L[path] += beta * max(y, 0) (one query per path).
+__global__ void __launch_bounds__(INFER_THREADS) k_mlp_infer_tc(const unsigned short* __restrict__ wtc_g,
+                                                                const float4* __restrict__ rec,
+                                                                const uint32_t* __restrict__ n_ptr, uint32_t n_const,
+                                                                EncodeParams ep, float* out,
+                                                                const float4* __restrict__ beta, float4* L,
+                                                                unsigned* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(wtc_g);
+        uint4* dst = reinterpret_cast<uint4*>(S.w);
+        for (int i = tid; i < MLP_TC_ELEMS / 8; i += INFER_THREADS) dst[i] = src[i];
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&S.mbar)));
+        S.failed = 0u;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" :: "r"(smem_u32(&S.tmem)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = S.tmem, mbar = smem_u32(&S.mbar), a_addr = smem_u32(S.a), w_addr = smem_u32(S.w);
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes (rows)
+    const uint32_t n = n_ptr ? *n_ptr : n_const;
+    uint32_t parity = 0;
+    unsigned char* arow = reinterpret_cast<unsigned char*>(S.a);
+    for (uint32_t tile = blockIdx.x; tile * 128u < n; tile += gridDim.x) {
+        const uint32_t i = tile * 128u + (uint32_t)tid;
+        {   // encode this thread's query into its row of the A operand
+            float f[64];
+            if (i < n) {
+                const float4* r = rec + 4ull * i;
+                const float4 q0 = r[0], q1 = r[1], q2 = r[2], q3 = r[3];
+                encode_half(q0, q1, q2, q3, ep, 0, f);
+                encode_half(q0, q1, q2, q3, ep, 1, f + 32);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 64; j++) f[j] = 0.0f;
+            }
+#pragma unroll
+            for (int kb = 0; kb < 8; kb++) {
+                uint4 v = make_uint4(pack_bf16(f[8 * kb], f[8 * kb + 1]), pack_bf16(f[8 * kb + 2], f[8 * kb + 3]),
+                                     pack_bf16(f[8 * kb + 4], f[8 * kb + 5]), pack_bf16(f[8 * kb + 6], f[8 * kb + 7]));
+                *reinterpret_cast<uint4*>(arow + tc_off((uint32_t)tid, 8u * kb)) = v;
+            }
+        }
+        float y[3] = {0.0f, 0.0f, 0.0f};
+        bool ok = true;
+#pragma unroll 1
+        for (int l = 0; l < 5 && ok; l++) {
+            asm volatile("fence.proxy.async.shared::cta;");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                tc_gemm_k64(tmem, a_addr, w_addr + (uint32_t)l * 8192u, l < 4 ? 64u : 16u, mbar);
+                if (!mbar_wait(mbar, parity)) S.failed = 1u;
+            }
+            parity ^= 1u;
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            ok = S.failed == 0u;
+            if (!ok) break;
+            if (l < 4) {
+                uint32_t r[64];
+                SNK_TC_LD16(taddr + 0u, r, 0);
+                SNK_TC_LD16(taddr + 16u, r, 16);
+                SNK_TC_LD16(taddr + 32u, r, 32);
+                SNK_TC_LD16(taddr + 48u, r, 48);
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                for (int kb = 0; kb < 8; kb++) {
+                    float v[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) v[j] = fmaxf(__uint_as_float(r[8 * kb + j]), 0.0f);
+                    uint4 pk = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                                          pack_bf16(v[6], v[7]));
+                    *reinterpret_cast<uint4*>(arow + tc_off((uint32_t)tid, 8u * kb)) = pk;
+                }
+            } else {
+                uint32_t r[16];
+                SNK_TC_LD16(taddr, r, 0);
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                y[0] = __uint_as_float(r[0]); y[1] = __uint_as_float(r[1]); y[2] = __uint_as_float(r[2]);
+            }
+        }
+        if (!ok) break;
+        if (i < n) {
+            if (out) {
+                out[3ull * i] = y[0]; out[3ull * i + 1] = y[1]; out[3ull * i + 2] = y[2];
+            } else {
+                const uint32_t p = __float_as_uint(rec[4ull * i + 3].w);
+                float4 b = beta[i], l = L[p];
+                L[p] = make_float4(l.x + b.x * fmaxf(y[0], 0.0f), l.y + b.y * fmaxf(y[1], 0.0f),
+                                   l.z + b.z * fmaxf(y[2], 0.0f), 0.0f);
+            }
+        }
+    }
+    if (tid == 0 && S.failed && status) atomicOr(status, 16u);   // bit 16: a tensor-core wait gave up
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" :: "r"(tmem));
+}
+
+// ---- inference (mma.sync) --------------------------------------------------------
+// records: 4 float4 per query.  Result y (3 floats) goes to out[3i..] when out is
+// given; otherwise, in render mode, L[path] += beta * max(y, 0) (one query per path).
 // records: 4 float4 per query.  Result y (3 floats) goes to out[3i..] when out is
 // given; otherwise, in render mode, L[path] += beta * max(y, 0) (one query per path).
 __global__ void __launch_bounds__(128) k_mlp_infer(const uint2* __restrict__ wf_g, const float4* __restrict__ rec,
@@ -455,7 +645,8 @@ __device__ __forceinline__ int frag_index(int block_words_off, int ntiles, int k
 
 // sums the CTA partials in a fixed order, one Adam step in FP32, BF16 copies
 __global__ void k_mlp_adam(const float* __restrict__ part, uint32_t nparts, float* w, float* m, float* v,
-                           AdamParams ap, unsigned short* wf, unsigned short* wb, float* grad_out) {
+                           AdamParams ap, unsigned short* wf, unsigned short* wb, unsigned short* wtc,
+                           float* grad_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= MLP_NW) return;
     float gsum = 0.0f;
@@ -476,6 +667,7 @@ __global__ void k_mlp_adam(const float* __restrict__ part, uint32_t nparts, floa
     else { l = 4; in = (i - 4 * 4096) / 3; out = (i - 4 * 4096) % 3; }
     wf[frag_index(MLP_FWD_OFF(l), l < 4 ? 8 : 1, in, out)] = b;
     if (l >= 1) wb[frag_index(MLP_BWD_OFF(l), 8, out, in)] = b;
+    wtc[l * 4096 + tc_off((uint32_t)out, (uint32_t)in) / 2] = b;   // N = out, K = in
 }
 
 }  // namespace
@@ -487,7 +679,9 @@ Status mlp_init(MlpState& M, const float* w_host, cudaStream_t st) {
     SNK_TRY_CUDA(M.v.reserve(MLP_NW));
     SNK_TRY_CUDA(M.wf.reserve(MLP_FWD_WORDS));
     SNK_TRY_CUDA(M.wb.reserve(MLP_BWD_WORDS));
+    SNK_TRY_CUDA(M.wtc.reserve(MLP_TC_ELEMS));
     SNK_TRY_CUDA(cudaMemcpyAsync(M.w.p, w_host, MLP_NW * sizeof(float), cudaMemcpyHostToDevice, st));
+    SNK_TRY_CUDA(cudaMemsetAsync(M.wtc.p, 0, MLP_TC_ELEMS * sizeof(unsigned short), st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.m.p, 0, MLP_NW * sizeof(float), st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.v.p, 0, MLP_NW * sizeof(float), st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.wf.p, 0, MLP_FWD_WORDS * sizeof(uint2), st));
@@ -496,10 +690,12 @@ Status mlp_init(MlpState& M, const float* w_host, cudaStream_t st) {
     // per launch, so frames can be captured into CUDA graphs)
     SNK_TRY_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(TrainSmem)));
+    SNK_TRY_CUDA(cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(InferSmem)));
     AdamParams ap{};   // lr 0: only refresh the BF16 copies
     k_mlp_adam<<<(MLP_NW + 255) / 256, 256, 0, st>>>(M.w.p, 0, M.w.p, M.m.p, M.v.p, ap,
                                                      reinterpret_cast<unsigned short*>(M.wf.p),
-                                                     reinterpret_cast<unsigned short*>(M.wb.p), nullptr);
+                                                     reinterpret_cast<unsigned short*>(M.wb.p), M.wtc.p, nullptr);
     SNK_TRY_CUDA(cudaGetLastError());
     M.step = 0;
     M.ready = true;
@@ -507,8 +703,9 @@ Status mlp_init(MlpState& M, const float* w_host, cudaStream_t st) {
 }
 
 Status mlp_infer(const MlpState& M, const float4* rec, const uint32_t* n_dev, uint32_t n, const EncodeParams& ep,
-                 float* out, const float4* beta, float4* L, int grid, cudaStream_t st) {
-    k_mlp_infer<<<grid, 128, 0, st>>>(M.wf.p, rec, n_dev, n, ep, out, beta, L);
+                 float* out, const float4* beta, float4* L, int grid, unsigned* err_word, cudaStream_t st) {
+    k_mlp_infer_tc<<<grid, INFER_THREADS, sizeof(InferSmem), st>>>(M.wtc.p, rec, n_dev, n, ep, out, beta, L,
+                                                                     err_word);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }
@@ -545,7 +742,7 @@ Status mlp_train_step(MlpState& M, const float4* samples, uint32_t n, const Enco
     ap.c2 = (float)(1.0 - std::pow(0.99, (double)M.step));
     k_mlp_adam<<<(MLP_NW + 255) / 256, 256, 0, st>>>(M.part.p, ctas, M.w.p, M.m.p, M.v.p, ap,
                                                      reinterpret_cast<unsigned short*>(M.wf.p),
-                                                     reinterpret_cast<unsigned short*>(M.wb.p), grad_out);
+                                                     reinterpret_cast<unsigned short*>(M.wb.p), M.wtc.p, grad_out);
     SNK_TRY_CUDA(cudaGetLastError());
     if (loss_host) {
         std::vector<float> lp(ctas);

@@ -15,6 +15,11 @@ constexpr int MLP_NW = 4 * 64 * 64 + 64 * 3;   // master weights (FP32)
 constexpr int MLP_FWD_WORDS = 4096 + 128;
 #define MLP_BWD_OFF(l) ((l) < 4 ? ((l) - 1) * 1024 : 3072) // transposed layers 1..3, then layer 4 (1 x 8 x 32)
 constexpr int MLP_BWD_WORDS = 3072 + 256;
+// BF16 copy in the tcgen05 shared-memory operand layout (K-major, no swizzle: 8x8
+// core matrices of 128 contiguous bytes): layer l < 4 as N = 64 outputs x K = 64
+// inputs at element offset l * 4096, layer 4 as N = 16 (3 outputs + 13 zero rows)
+// x K = 64 at 4 * 4096
+constexpr int MLP_TC_ELEMS = 4 * 4096 + 16 * 64;
 
 struct EncodeParams {
     float lo[3];        // scene box the positions are normalised to
@@ -28,6 +33,7 @@ struct AdamParams {
 struct MlpState {
     DBuf<float> w, m, v;             // FP32 master weights and Adam moments
     DBuf<uint2> wf, wb;              // BF16 forward / transposed copies (fragment order)
+    DBuf<unsigned short> wtc;        // BF16 forward copy in the tcgen05 operand layout (inference)
     DBuf<float> part, loss;          // per-CTA gradient partials and losses
     uint32_t step = 0;
     bool ready = false;
@@ -35,8 +41,9 @@ struct MlpState {
 
 Status mlp_init(MlpState& M, const float* w_host, cudaStream_t st);
 // records: 4 float4 per query (position+roughness, direction+metallic, normal, albedo+path id)
+// (tcgen05 kernel; a give-up of its bounded tensor-core waits sets bit 16 of *err_word)
 Status mlp_infer(const MlpState& M, const float4* rec, const uint32_t* n_dev, uint32_t n, const EncodeParams& ep,
-                 float* out, const float4* beta, float4* L, int grid, cudaStream_t st);
+                 float* out, const float4* beta, float4* L, int grid, unsigned* err_word, cudaStream_t st);
 Status mlp_encode(const float4* rec, uint32_t n, const EncodeParams& ep, float* out, cudaStream_t st);
 // samples: 5 float4 each (the 4 record words, then target rgb + weight)
 // grows the per-CTA gradient/loss buffers for batches of up to n samples (call
