@@ -935,7 +935,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 const uint32_t b = k * chunk, cnt = b < total ? std::min(chunk, total - b) : 0u;
                 if (cnt == 0) break;
                 e = staged(ctx, profile, SNK_STAGE_CACHE_TRAIN, [&] {
-                    Status s = mlp_train_step(ctx->mlp, F.samples + 5ull * b, cnt, ep, lr, nullptr, nullptr, st);
+                    Status s = mlp_train_step(ctx->mlp, F.samples + 5ull * b, cnt, ep, lr, nullptr, nullptr,
+                                              ctx->d_err.p, st);
                     return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
                 });
             }
@@ -1282,10 +1283,11 @@ int snk_pt_cache_train(snk_pt_ctx* ctx, const float* samples, uint32_t n, float 
     if (grad && ctx->cache_grad.reserve(MLP_NW)) return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "cache_train: buffer");
     float l = 0.0f;
     API_TRY(mlp_train_step(ctx->mlp, s, n, cache_encode_params(ctx), lr, grad ? ctx->cache_grad.p : nullptr, &l,
-                           ctx->stream));
+                           ctx->d_err.p, ctx->stream));
     if (grad && (cudaMemcpyAsync(grad, ctx->cache_grad.p, MLP_NW * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream) ||
                  cudaStreamSynchronize(ctx->stream)))
         return fail(ctx, SNK_ERR_CUDA, "cache_train: copy");
+    API_TRY(check_device_error(ctx));
     if (loss) *loss = l;
     return SNK_OK;
 }

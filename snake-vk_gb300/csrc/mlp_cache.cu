@@ -1,31 +1,28 @@
 // mlp_cache.cu -- the online-trained MLP radiance cache: input encoding, fused
-// inference, fused forward+backward training and the Adam update, on BF16
-// tensor cores (mma.sync m16n8k16, FP32 accumulation).  There is no
-// counterpart in the reference; this is the learned part of the path tracer
-// (cache queries replace path tails, radiance-caching style, Mueller et al. 2021).
+// inference, fused forward+backward training and the Adam update, on the
+// fifth-generation BF16 tensor cores (tcgen05.mma, FP32 accumulation in tensor
+// memory).  There is no counterpart in the reference; this is the learned part
+// of the path tracer (cache queries replace path tails, radiance-caching style,
+// Mueller et al. 2021).
 //
 // Network: 64 encoded inputs -> 4 x (64, ReLU) -> 3 linear outputs, no biases
 // (the encoding carries a constant 1).  FP32 master weights W_l[in][out]
 // (4 x 64x64 then 64x3 = 16576 values) with Adam moments; the tensor cores read
-// BF16 copies stored in MMA-fragment order, so a lane loads its B fragment with
-// one 8-byte shared-memory load:
-//   forward block (layer l, k-tile kt, n-tile nt), lane (g = lane/4, t = lane%4):
-//     b0 = (W[16kt+2t][8nt+g], W[16kt+2t+1][8nt+g]), b1 = same at rows +8
-//   transposed block (for dX = dY W^T) is the same with W replaced by W^T.
-// Activations stay in registers between layers: the D fragment of one layer is
-// the A fragment of the next.  Training keeps the post-ReLU activations and the
-// back-propagated gradients transposed ([feature][sample]) in shared memory, so
-// dW = act^T g runs as a CTA-wide GEMM with 4-byte operand loads.  Each CTA
-// writes its dW partial; the Adam kernel sums the partials in a fixed order, so
-// training is deterministic.
+// BF16 copies that the Adam kernel writes in the tcgen05 shared-memory operand
+// layout (K-major, no swizzle: 8x8 core matrices of 128 contiguous bytes), one
+// with N = outputs (forward) and one with N = inputs (input gradients).
 //
-// Inference runs on the fifth-generation tensor cores: one CTA of 128 threads
-// takes 128 queries, writes their encodings into shared memory in the tcgen05
-// operand layout, and chains the 5 layers as 128x64x64 (last 128x16x64)
-// tcgen05.mma issued by one thread, accumulating in tensor memory; after each
-// layer every thread reads its row back with tcgen05.ld, applies the ReLU and
-// stores the BF16 row as the next layer's operand.  Waits on the MMA completion
-// barrier are bounded (a give-up sets a status bit, read by the host).
+// Inference: one CTA of 128 threads takes 128 queries, writes their encodings
+// into shared memory in the operand layout, and chains the 5 layers as 128x64x64
+// (last 128x16x64) tcgen05.mma issued by one thread, accumulating in tensor
+// memory; after each layer every thread reads its row back with tcgen05.ld,
+// applies the ReLU and stores the BF16 row as the next layer's operand.
+// Training does the same forward pass for 128 samples, then the backward pass as
+// tcgen05 GEMMs as well (input gradients M = 128, weight gradients M = 64 from
+// the stored activations read as MN-major operands).  Each CTA writes its dW
+// partial; the Adam kernel sums the partials in a fixed order, so training is
+// deterministic.  Waits on the MMA completion barrier are bounded (a give-up sets
+// a status bit, read by the host).
 //
 // Input encoding (64 features, from a 64-byte query record: position, outgoing
 // direction, shading normal, roughness, albedo, metallic):
@@ -41,9 +38,7 @@
 namespace snk {
 namespace {
 
-constexpr int ROW_PAD = 72;     // bf16 row stride of a [16][64] tile (conflict-free 4-byte loads)
-constexpr int TS = 136;         // sample stride of transposed [64][128] tiles
-constexpr int TRAIN_ROWS = 128; // samples per training CTA (8 warps x 16)
+constexpr int TRAIN_ROWS = 128; // samples per training CTA (one per thread)
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -53,14 +48,6 @@ __device__ __forceinline__ float bf16_bits_to_float(unsigned short b) { return _
 __device__ __forceinline__ unsigned short float_to_bf16_bits(float f) {
     __nv_bfloat16 h = __float2bfloat16_rn(f);
     return *reinterpret_cast<unsigned short*>(&h);
-}
-
-__device__ __forceinline__ void mma16816(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
 // Features [32*half, 32*half + 32) of one query record.
@@ -109,60 +96,6 @@ __device__ __forceinline__ void encode_half(const float4 q0, const float4 q1, co
         f[29] = 0.04f * om + q3.y * q1.w;
         f[30] = 0.04f * om + q3.z * q1.w;
         f[31] = 1.0f;
-    }
-}
-
-// ---- weights to shared memory -------------------------------------------------
-__device__ __forceinline__ void load_words(uint2* dst, const uint2* __restrict__ src, int n) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
-}
-
-// forward pass of one warp's 16-row tile whose A fragments are in a[4][4];
-// returns the output fragment c5 (row g: cols 2t,2t+1; row g+8: cols 2t,2t+1)
-template <bool STORE_ACT>
-__device__ __forceinline__ void forward_tile(const uint2* wf, uint32_t (&a)[4][4], float (&c5)[4],
-                                             unsigned short* actT, int row0) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int l = 0; l < 4; l++) {
-        float c[8][4];
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
-#pragma unroll
-        for (int kt = 0; kt < 4; kt++)
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                uint2 b = wf[MLP_FWD_OFF(l) + (kt * 8 + nt) * 32 + lane];
-                mma16816(c[nt], a[kt], b.x, b.y);
-            }
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++)
-#pragma unroll
-            for (int r = 0; r < 4; r++) c[nt][r] = fmaxf(c[nt][r], 0.0f);
-        if (STORE_ACT) {
-            unsigned short* A = actT + l * 64 * TS;
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                int f = 8 * nt + 2 * t;
-                A[f * TS + row0 + g] = float_to_bf16_bits(c[nt][0]);
-                A[(f + 1) * TS + row0 + g] = float_to_bf16_bits(c[nt][1]);
-                A[f * TS + row0 + g + 8] = float_to_bf16_bits(c[nt][2]);
-                A[(f + 1) * TS + row0 + g + 8] = float_to_bf16_bits(c[nt][3]);
-            }
-        }
-#pragma unroll
-        for (int kt = 0; kt < 4; kt++) {
-            a[kt][0] = pack_bf16(c[2 * kt][0], c[2 * kt][1]);
-            a[kt][1] = pack_bf16(c[2 * kt][2], c[2 * kt][3]);
-            a[kt][2] = pack_bf16(c[2 * kt + 1][0], c[2 * kt + 1][1]);
-            a[kt][3] = pack_bf16(c[2 * kt + 1][2], c[2 * kt + 1][3]);
-        }
-    }
-    c5[0] = c5[1] = c5[2] = c5[3] = 0.0f;
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        uint2 b = wf[MLP_FWD_OFF(4) + kt * 32 + lane];
-        mma16816(c5, a[kt], b.x, b.y);
     }
 }
 
@@ -346,73 +279,267 @@ __global__ void __launch_bounds__(INFER_THREADS) k_mlp_infer_tc(const unsigned s
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" :: "r"(tmem));
 }
 
-// ---- inference (mma.sync) --------------------------------------------------------
-// records: 4 float4 per query.  Result y (3 floats) goes to out[3i..] when out is
-// given; otherwise, in render mode, L[path] += beta * max(y, 0) (one query per path).
-// records: 4 float4 per query.  Result y (3 floats) goes to out[3i..] when out is
-// given; otherwise, in render mode, L[path] += beta * max(y, 0) (one query per path).
-__global__ void __launch_bounds__(128) k_mlp_infer(const uint2* __restrict__ wf_g, const float4* __restrict__ rec,
-                                                   const uint32_t* __restrict__ n_ptr, uint32_t n_const,
-                                                   EncodeParams ep, float* out, const float4* __restrict__ beta,
-                                                   float4* L) {
-    __shared__ uint2 wf[MLP_FWD_WORDS];
-    __shared__ __align__(16) unsigned short X[4][16 * ROW_PAD];
-    load_words(wf, wf_g, MLP_FWD_WORDS);
+// ---- training on tcgen05: forward + backward of 128 samples per CTA -------------------
+// Sample s is owned by threads s and s + 128 (warps w and w + 4 share tensor-memory
+// lanes 32 (w % 4) ..); thread half h = tid / 128 handles features / columns
+// [32h, 32h + 32).  Every activation A_l (A_0 = encoded input, A_l = output of
+// layer l-1) and the running output gradient G are stored once, row s, in the
+// K-major operand layout of a 128 x 64 matrix.  The same bytes serve three GEMMs:
+//   forward       A_{l+1} = relu(A_l W_l)          M = 128, A_l K-major, W_l (N = out, K = in)
+//   input grad    G' = (G W_l^T) * [A_l > 0]        M = 128, G K-major, W_l^T (N = in, K = out)
+//   weight grad   dW_l = A_l^T G                    M = 64 (in), N = out, K = 128 samples:
+//                                                    A_l and G read as MN-major operands
+// so no transpose is ever written.  Read as an MN-major operand, such a buffer has
+// its 8-sample row groups (K direction) 1024 B apart, given as the leading byte
+// offset, and its 8-feature chunks (M/N direction) 128 B apart, given as the
+// stride byte offset: the two fields swap roles against the K-major descriptor
+// (measured on GB300 with a 64 x 64 x 128 product).  The M = 64 accumulator puts row m
+// in tensor-memory lane 32 (m / 16) + m % 16: warp w % 4, lanes 0..15 hold
+// in-features 16 (w % 4) .. + 15.  Tensor memory: columns 0..63 forward / input
+// gradient, 64..127 weight gradient.  The weights arrive by two bulk asynchronous
+// copies that overlap the input encoding; the ReLU masks of A_1..A_4 stay in
+// registers (32 bits per thread each).
+constexpr int TRAIN_TC_THREADS = 256;
+
+struct TrainTcSmem {
+    unsigned short wf[MLP_TC_ELEMS];     // W_l: N = out x K = in (layer 4: N = 16)
+    unsigned short wb[MLP_TCB_ELEMS];    // W_l^T, l = 1..4: N = in x K = out (layer 4: K = 3 of 16 used)
+    unsigned short act[5][128 * 64];     // A_0 .. A_4
+    unsigned short g[128 * 64];          // gradient at the current layer's output
+    unsigned long long mbar;             // MMA completion
+    unsigned long long wbar;             // weight copies
+    uint32_t tmem;
+    uint32_t failed;
+    float loss[8];
+};
+
+// descriptor of a 128-sample x 64-feature buffer read as an MN-major operand
+__device__ __forceinline__ uint64_t tc_desc_mn(uint32_t addr) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(1024u >> 4) << 16;   // K direction: next 8 samples
+    d |= (uint64_t)(128u >> 4) << 32;    // M/N direction: next 8 features
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor of the weight-gradient GEMM: M = 64, A and B MN-major
+__device__ __forceinline__ uint32_t tc_idesc_wgrad(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((n >> 3) << 17) | ((64u >> 4) << 24);
+}
+
+// D[tmem] = sum over ksteps of A B^T; operand addresses advance by kstride bytes per K = 16 step
+template <bool MN>
+__device__ __forceinline__ void tc_issue(uint32_t tmem, uint32_t a_addr, uint32_t b_addr, uint32_t idesc,
+                                         uint32_t ksteps, uint32_t kstride) {
+#pragma unroll 1
+    for (uint32_t ks = 0; ks < ksteps; ks++) {
+        const uint64_t da = MN ? tc_desc_mn(a_addr + ks * kstride) : tc_desc(a_addr + ks * kstride);
+        const uint64_t db = MN ? tc_desc_mn(b_addr + ks * kstride) : tc_desc(b_addr + ks * kstride);
+        const uint32_t acc = ks > 0 ? 1u : 0u;
+        asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                     :: "r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+    }
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar));
+}
+
+// global -> shared bulk copy (16-byte aligned, size a multiple of 16) completing on mbar
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
+}
+
+// 32 values into columns [col0, col0 + 32) of row `row` of a K-major 128 x 64
+// operand as BF16; returns the positive-value mask (bit j: value j > 0 after rounding)
+__device__ __forceinline__ uint32_t store_row32(unsigned char* base, uint32_t row, uint32_t col0, const float* v) {
+    uint32_t mask = 0;
+#pragma unroll
+    for (int kb = 0; kb < 4; kb++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            w[j] = pack_bf16(v[8 * kb + 2 * j], v[8 * kb + 2 * j + 1]);
+            if ((short)(w[j] & 0xFFFFu) > 0) mask |= 1u << (8 * kb + 2 * j);
+            if ((short)(w[j] >> 16) > 0) mask |= 1u << (8 * kb + 2 * j + 1);
+        }
+        *reinterpret_cast<uint4*>(base + tc_off(row, col0 + 8u * kb)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    return mask;
+}
+
+// samples: 5 float4 each (4 record words + (target rgb, weight)); part: per CTA
+// MLP_NW floats (W_l[in][out] order); loss_part: per CTA loss sum; norm = 1 / (3 * batch).
+// wtc_g / wtcb_g: 16-byte aligned.  A give-up of a bounded wait sets bit 16 of *status.
+__global__ void __launch_bounds__(TRAIN_TC_THREADS, 1) k_mlp_train_tc(const unsigned short* __restrict__ wtc_g,
+                                                                   const unsigned short* __restrict__ wtcb_g,
+                                                                   const float4* __restrict__ samples, uint32_t n,
+                                                                   EncodeParams ep, float norm, float* part_all,
+                                                                   float* loss_part, unsigned* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    TrainTcSmem& S = *reinterpret_cast<TrainTcSmem*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t row = (uint32_t)tid & 127u, half = (uint32_t)tid >> 7, col0 = 32u * half;
+    const uint32_t mbar = smem_u32(&S.mbar), wbar = smem_u32(&S.wbar);
+    constexpr uint32_t WF_BYTES = MLP_TC_ELEMS * 2, WB_BYTES = MLP_TCB_ELEMS * 2;
+    if (tid == 0) {
+        S.failed = 0u;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(mbar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(wbar));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(wbar), "r"(WF_BYTES + WB_BYTES)
+                     : "memory");
+        bulk_load(smem_u32(S.wf), wtc_g, WF_BYTES, wbar);
+        bulk_load(smem_u32(S.wb), wtcb_g, WB_BYTES, wbar);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" :: "r"(smem_u32(&S.tmem)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    const uint32_t i = blockIdx.x * 128u + row;
+    {   // encode this thread's half of its sample into A_0
+        float f[32];
+        if (i < n) {
+            const float4* r = samples + 5ull * i;
+            encode_half(r[0], r[1], r[2], r[3], ep, (int)half, f);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; j++) f[j] = 0.0f;
+        }
+        store_row32(reinterpret_cast<unsigned char*>(S.act[0]), row, col0, f);
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    const uint32_t n = n_ptr ? *n_ptr : n_const;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    unsigned short* Xw = X[warp];
-    const uint32_t tiles = (n + 15) / 16;
-    for (uint32_t tile = blockIdx.x * 4 + warp; tile < tiles; tile += gridDim.x * 4) {
-        const uint32_t row0 = tile * 16;
-        {   // encode: lane -> sample lane/2, half lane%2
-            const int sl = lane >> 1, half = lane & 1;
-            const uint32_t i = row0 + sl;
-            float f[32];
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = S.tmem, wf = smem_u32(S.wf), wb = smem_u32(S.wb), g_addr = smem_u32(S.g);
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    uint32_t parity = 0;
+    uint32_t msk[4] = {0u, 0u, 0u, 0u};   // positive masks of this thread's columns of A_1 .. A_4
+    float lsum = 0.0f;
+    bool ok = true;
+    if (tid == 0 && !mbar_wait(wbar, 0)) S.failed = 1u;   // the weights are in shared memory
+    // runs the GEMMs `issue` queues (thread 0), then waits for them with a bound
+    auto run = [&](auto issue) {
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        if (tid == 0 && S.failed == 0u) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            issue();
+            tc_commit(mbar);
+            if (!mbar_wait(mbar, parity)) S.failed = 1u;
+        }
+        parity ^= 1u;
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        return S.failed == 0u;
+    };
+    // forward
+#pragma unroll
+    for (int l = 0; l < 5; l++) {
+        if (!ok) break;
+        const uint32_t a_addr = smem_u32(S.act[l]);
+        ok = run([&] { tc_issue<false>(tmem, a_addr, wf + (uint32_t)l * 8192u, tc_idesc(l < 4 ? 64u : 16u), 4, 256); });
+        if (!ok) break;
+        if (l < 4) {
+            uint32_t r[32];
+            SNK_TC_LD16(lane_base + col0, r, 0);
+            SNK_TC_LD16(lane_base + col0 + 16u, r, 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            float v[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) v[j] = fmaxf(__uint_as_float(r[j]), 0.0f);
+            msk[l] = store_row32(reinterpret_cast<unsigned char*>(S.act[l + 1]), row, col0, v);
+        } else if (half == 0) {
+            uint32_t r[16];
+            SNK_TC_LD16(lane_base, r, 0);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            // relative L2 loss and its gradient at the 3 outputs (columns 3..15 of G zero)
+            float gy[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) gy[j] = 0.0f;
             if (i < n) {
-                const float4* r = rec + 4ull * i;
-                encode_half(r[0], r[1], r[2], r[3], ep, half, f);
-            } else {
+                const float4 tg = samples[5ull * i + 4];
+                const float target[3] = {tg.x, tg.y, tg.z};
 #pragma unroll
-                for (int j = 0; j < 32; j++) f[j] = 0.0f;
-            }
-            uint32_t* dst = reinterpret_cast<uint32_t*>(Xw + sl * ROW_PAD + 32 * half);
-#pragma unroll
-            for (int j = 0; j < 16; j++) dst[j] = pack_bf16(f[2 * j], f[2 * j + 1]);
-        }
-        __syncwarp();
-        uint32_t a[4][4];
-#pragma unroll
-        for (int kt = 0; kt < 4; kt++) {
-            a[kt][0] = *reinterpret_cast<const uint32_t*>(Xw + g * ROW_PAD + 16 * kt + 2 * t);
-            a[kt][1] = *reinterpret_cast<const uint32_t*>(Xw + (g + 8) * ROW_PAD + 16 * kt + 2 * t);
-            a[kt][2] = *reinterpret_cast<const uint32_t*>(Xw + g * ROW_PAD + 16 * kt + 8 + 2 * t);
-            a[kt][3] = *reinterpret_cast<const uint32_t*>(Xw + (g + 8) * ROW_PAD + 16 * kt + 8 + 2 * t);
-        }
-        __syncwarp();
-        float c5[4];
-        forward_tile<false>(wf, a, c5, nullptr, 0);
-        // outputs: lane (g,0) holds cols 0,1 of rows g, g+8; lane (g,1) holds col 2
-        float y2a = __shfl_down_sync(0xFFFFFFFFu, c5[0], 1);
-        float y2b = __shfl_down_sync(0xFFFFFFFFu, c5[2], 1);
-        if (t == 0) {
-            const float ya[3] = {c5[0], c5[1], y2a}, yb[3] = {c5[2], c5[3], y2b};
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const uint32_t i = row0 + g + 8 * h;
-                if (i >= n) continue;
-                const float* y = h ? yb : ya;
-                if (out) {
-                    out[3ull * i] = y[0]; out[3ull * i + 1] = y[1]; out[3ull * i + 2] = y[2];
-                } else {
-                    const uint32_t p = __float_as_uint(rec[4ull * i + 3].w);
-                    float4 b = beta[i], l = L[p];
-                    L[p] = make_float4(l.x + b.x * fmaxf(y[0], 0.0f), l.y + b.y * fmaxf(y[1], 0.0f),
-                                       l.z + b.z * fmaxf(y[2], 0.0f), 0.0f);
+                for (int c = 0; c < 3; c++) {
+                    const float y = __uint_as_float(r[c]), d = y - target[c], den = y * y + 0.01f;
+                    lsum += tg.w * d * d / den * norm;
+                    gy[c] = tg.w * 2.0f * d / den * norm;
                 }
             }
+            unsigned char* gb = reinterpret_cast<unsigned char*>(S.g);
+#pragma unroll
+            for (int kb = 0; kb < 2; kb++)
+                *reinterpret_cast<uint4*>(gb + tc_off(row, 8u * kb)) =
+                    make_uint4(pack_bf16(gy[8 * kb], gy[8 * kb + 1]), pack_bf16(gy[8 * kb + 2], gy[8 * kb + 3]),
+                               pack_bf16(gy[8 * kb + 4], gy[8 * kb + 5]), pack_bf16(gy[8 * kb + 6], gy[8 * kb + 7]));
         }
     }
+    // backward: layer l takes G (gradient at its output), writes dW_l and, for l >= 1,
+    // the gradient at its input into G
+    float* part = part_all + (size_t)blockIdx.x * MLP_NW;
+#pragma unroll
+    for (int l = 4; l >= 0; l--) {
+        if (!ok) break;
+        const uint32_t a_addr = smem_u32(S.act[l]);
+        ok = run([&] {
+            tc_issue<true>(tmem + 64u, a_addr, g_addr, tc_idesc_wgrad(l == 4 ? 16u : 64u), 8, 2048);
+            if (l >= 1) tc_issue<false>(tmem, g_addr, wb + (uint32_t)(l - 1) * 8192u, tc_idesc(64u), l == 4 ? 1u : 4u, 256);
+        });
+        if (!ok) break;
+        // dW_l: in-feature 16 (warp % 4) + lane on lanes 0..15, out-features col0 .. col0 + 31
+        if (l == 4) {
+            if (half == 0) {
+                uint32_t r[16];
+                SNK_TC_LD16(lane_base + 64u, r, 0);
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (lane < 16) {
+                    float* dst = part + MLP_OFF(4) + (16 * (warp & 3) + lane) * 3;
+                    dst[0] = __uint_as_float(r[0]); dst[1] = __uint_as_float(r[1]); dst[2] = __uint_as_float(r[2]);
+                }
+            }
+        } else {
+            uint32_t r[32];
+            SNK_TC_LD16(lane_base + 64u + col0, r, 0);
+            SNK_TC_LD16(lane_base + 80u + col0, r, 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (lane < 16) {
+                float4* dst = reinterpret_cast<float4*>(part + MLP_OFF(l) + (16 * (warp & 3) + lane) * 64 + col0);
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    dst[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                                         __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+            }
+        }
+        if (l >= 1) {   // G <- (G W_l^T) * [A_l > 0]
+            uint32_t r[32];
+            SNK_TC_LD16(lane_base + col0, r, 0);
+            SNK_TC_LD16(lane_base + col0 + 16u, r, 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            const uint32_t m = msk[l - 1];
+            float v[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) v[j] = (m >> j) & 1u ? __uint_as_float(r[j]) : 0.0f;
+            store_row32(reinterpret_cast<unsigned char*>(S.g), row, col0, v);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xFFFFFFFFu, lsum, o);
+    if (lane == 0) S.loss[warp] = lsum;
+    if (tid == 0 && S.failed && status) atomicOr(status, 16u);   // bit 16: a tensor-core wait gave up
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0) {
+        float t = 0.0f;
+        for (int w = 0; w < 8; w++) t += S.loss[w];
+        loss_part[blockIdx.x] = t;
+    }
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" :: "r"(tmem));
 }
 
 // encodings as floats (test hook): features of each record, bf16-rounded as the
@@ -428,225 +555,9 @@ __global__ void k_mlp_encode(const float4* __restrict__ rec, uint32_t n, EncodeP
     }
 }
 
-// ---- training: forward + backward of 128 samples per CTA -----------------------------
-struct TrainSmem {
-    uint2 wf[MLP_FWD_WORDS];
-    uint2 wb[MLP_BWD_WORDS];
-    unsigned short XT[64 * TS];
-    unsigned short actT[4 * 64 * TS];
-    unsigned short gT[64 * TS];
-    float loss[8];
-};
-
-// one warp's share of a CTA-wide dW = act^T (64 x 128) . g (128 x ncols) with the
-// result written to part[in * ncols + out]; warp w takes in-feature tile w>>1 and
-// output tiles (w&1)*4 .. +3 (ncols = 64), or tile w for ncols = 3 (warps 0..3)
-__device__ __forceinline__ void dw_gemm(const unsigned short* actT, const unsigned short* gT, int ncols,
-                                        float* part) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    int mt, nt0, ntn;
-    if (ncols == 64) { mt = warp >> 1; nt0 = (warp & 1) * 4; ntn = 4; }
-    else { if (warp >= 4) return; mt = warp; nt0 = 0; ntn = 1; }
-    float c[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.0f;
-#pragma unroll
-    for (int kt = 0; kt < 8; kt++) {
-        uint32_t a[4];
-        const unsigned short* A0 = actT + (16 * mt + g) * TS + 16 * kt + 2 * t;
-        const unsigned short* A1 = actT + (16 * mt + g + 8) * TS + 16 * kt + 2 * t;
-        a[0] = *reinterpret_cast<const uint32_t*>(A0);
-        a[1] = *reinterpret_cast<const uint32_t*>(A1);
-        a[2] = *reinterpret_cast<const uint32_t*>(A0 + 8);
-        a[3] = *reinterpret_cast<const uint32_t*>(A1 + 8);
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if (j >= ntn) break;
-            const unsigned short* B = gT + (8 * (nt0 + j) + g) * TS + 16 * kt + 2 * t;
-            mma16816(c[j], a, *reinterpret_cast<const uint32_t*>(B), *reinterpret_cast<const uint32_t*>(B + 8));
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        if (j >= ntn) break;
-        const int in0 = 16 * mt + g, out0 = 8 * (nt0 + j) + 2 * t;
-        const float v[4] = {c[j][0], c[j][1], c[j][2], c[j][3]};
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int in = in0 + (r >= 2 ? 8 : 0), out = out0 + (r & 1);
-            if (out < ncols) part[in * ncols + out] = v[r];
-        }
-    }
-}
-
-// dX for this warp's rows: g_next = (g . W^T) masked by act > 0, from A fragments
-// a (K = ktn 16-wide tiles) and transposed weight blocks at wb + off
-__device__ __forceinline__ void dx_tile(const uint2* wb, int off, int ktn, const uint32_t (*a)[4],
-                                        const unsigned short* act, int row0, float (&c)[8][4]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
-    for (int kt = 0; kt < ktn; kt++)
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            uint2 b = wb[off + (kt * 8 + nt) * 32 + lane];
-            mma16816(c[nt], a[kt], b.x, b.y);
-        }
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int f = 8 * nt + 2 * t;
-        // ReLU derivative: the stored bf16 activation is positive (sign bit clear, nonzero)
-        if ((short)act[f * TS + row0 + g] <= 0) c[nt][0] = 0.0f;
-        if ((short)act[(f + 1) * TS + row0 + g] <= 0) c[nt][1] = 0.0f;
-        if ((short)act[f * TS + row0 + g + 8] <= 0) c[nt][2] = 0.0f;
-        if ((short)act[(f + 1) * TS + row0 + g + 8] <= 0) c[nt][3] = 0.0f;
-    }
-}
-
-__device__ __forceinline__ void store_gT(unsigned short* gT, const float (&c)[8][4], int row0) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int f = 8 * nt + 2 * t;
-        gT[f * TS + row0 + g] = float_to_bf16_bits(c[nt][0]);
-        gT[(f + 1) * TS + row0 + g] = float_to_bf16_bits(c[nt][1]);
-        gT[f * TS + row0 + g + 8] = float_to_bf16_bits(c[nt][2]);
-        gT[(f + 1) * TS + row0 + g + 8] = float_to_bf16_bits(c[nt][3]);
-    }
-}
-
-__device__ __forceinline__ void frags_from_c(const float (&c)[8][4], uint32_t (&a)[4][4]) {
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        a[kt][0] = pack_bf16(c[2 * kt][0], c[2 * kt][1]);
-        a[kt][1] = pack_bf16(c[2 * kt][2], c[2 * kt][3]);
-        a[kt][2] = pack_bf16(c[2 * kt + 1][0], c[2 * kt + 1][1]);
-        a[kt][3] = pack_bf16(c[2 * kt + 1][2], c[2 * kt + 1][3]);
-    }
-}
-
-// samples: 5 float4 each (4 record words + (target rgb, weight)); part: per CTA
-// MLP_NW floats; loss_part: per CTA loss sum.  norm = 1 / (3 * batch).
-__global__ void __launch_bounds__(256) k_mlp_train(const uint2* __restrict__ wf_g, const uint2* __restrict__ wb_g,
-                                                   const float4* __restrict__ samples, uint32_t n, EncodeParams ep,
-                                                   float norm, float* part_all, float* loss_part) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
-    load_words(S.wf, wf_g, MLP_FWD_WORDS);
-    load_words(S.wb, wb_g, MLP_BWD_WORDS);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int row0 = 16 * warp;
-    const uint32_t base = blockIdx.x * TRAIN_ROWS;
-    float* part = part_all + (size_t)blockIdx.x * MLP_NW;
-    // encode this warp's 16 samples into XT (transposed)
-    {
-        const int sl = lane >> 1, half = lane & 1;
-        const uint32_t i = base + row0 + sl;
-        float f[32];
-        if (i < n) {
-            const float4* r = samples + 5ull * i;
-            encode_half(r[0], r[1], r[2], r[3], ep, half, f);
-        } else {
-#pragma unroll
-            for (int j = 0; j < 32; j++) f[j] = 0.0f;
-        }
-#pragma unroll
-        for (int j = 0; j < 32; j++) S.XT[(32 * half + j) * TS + row0 + sl] = float_to_bf16_bits(f[j]);
-    }
-    __syncthreads();
-    uint32_t a[4][4];
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        const int k0 = 16 * kt + 2 * t;
-        auto pk = [&](int k, int s) {
-            return (uint32_t)S.XT[k * TS + s] | ((uint32_t)S.XT[(k + 1) * TS + s] << 16);
-        };
-        a[kt][0] = pk(k0, row0 + g);
-        a[kt][1] = pk(k0, row0 + g + 8);
-        a[kt][2] = pk(k0 + 8, row0 + g);
-        a[kt][3] = pk(k0 + 8, row0 + g + 8);
-    }
-    float c5[4];
-    forward_tile<true>(S.wf, a, c5, S.actT, row0);
-    // relative L2 loss gradient at the outputs (lanes t = 0: cols 0,1; t = 1: col 2)
-    float lsum = 0.0f;
-    float gy[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (t < 2) {
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int col = 2 * t + (r & 1);
-            const uint32_t i = base + row0 + g + (r >= 2 ? 8 : 0);
-            if (col < 3 && i < n) {
-                const float4 tg = samples[5ull * i + 4];
-                const float target = col == 0 ? tg.x : (col == 1 ? tg.y : tg.z);
-                const float y = c5[r], d = y - target, den = y * y + 0.01f;
-                lsum += tg.w * d * d / den * norm;
-                gy[r] = tg.w * 2.0f * d / den * norm;
-            }
-        }
-    }
-    // g_out into gT rows 0..15 (rows 3..15 zero: they pad the 16-wide k tile)
-    for (int f = lane; f < 16 * 16; f += 32) S.gT[(f >> 4) * TS + row0 + (f & 15)] = 0;
-    __syncwarp();
-    if (t < 2) {
-        S.gT[(2 * t) * TS + row0 + g] = float_to_bf16_bits(gy[0]);
-        S.gT[(2 * t + 1) * TS + row0 + g] = float_to_bf16_bits(gy[1]);
-        S.gT[(2 * t) * TS + row0 + g + 8] = float_to_bf16_bits(gy[2]);
-        S.gT[(2 * t + 1) * TS + row0 + g + 8] = float_to_bf16_bits(gy[3]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xFFFFFFFFu, lsum, o);
-    if (lane == 0) S.loss[warp] = lsum;
-    __syncthreads();
-    // dW4 = act3^T g_out (in-features x 3)
-    dw_gemm(S.actT + 3 * 64 * TS, S.gT, 3, part + MLP_OFF(4));
-    // g3 = (g_out W4^T) * (act3 > 0): A = g_out rows (k = outputs 0..15, only 0..2 nonzero)
-    float c[8][4];
-    {
-        uint32_t ag[1][4];
-        auto pk = [&](int k, int s) {
-            return (uint32_t)S.gT[k * TS + s] | ((uint32_t)S.gT[(k + 1) * TS + s] << 16);
-        };
-        ag[0][0] = pk(2 * t, row0 + g);
-        ag[0][1] = pk(2 * t, row0 + g + 8);
-        ag[0][2] = pk(2 * t + 8, row0 + g);
-        ag[0][3] = pk(2 * t + 8, row0 + g + 8);
-        dx_tile(S.wb, MLP_BWD_OFF(4), 1, ag, S.actT + 3 * 64 * TS, row0, c);
-    }
-    __syncthreads();   // every warp has read g_out
-    store_gT(S.gT, c, row0);
-    frags_from_c(c, a);
-    __syncthreads();
-    // layers 3, 2, 1: dW_l = act_{l-1}^T g_l ; g_{l-1} = (g_l W_l^T) * (act_{l-1} > 0)
-#pragma unroll 1
-    for (int l = 3; l >= 1; l--) {
-        dw_gemm(S.actT + (l - 1) * 64 * TS, S.gT, 64, part + MLP_OFF(l));
-        dx_tile(S.wb, MLP_BWD_OFF(l), 4, a, S.actT + (l - 1) * 64 * TS, row0, c);
-        __syncthreads();
-        store_gT(S.gT, c, row0);
-        frags_from_c(c, a);
-        __syncthreads();
-    }
-    // dW0 = X^T g_0
-    dw_gemm(S.XT, S.gT, 64, part + MLP_OFF(0));
-    if (threadIdx.x == 0) {
-        float s = 0.0f;
-        for (int w = 0; w < 8; w++) s += S.loss[w];
-        loss_part[blockIdx.x] = s;
-    }
-}
-
-// position of master weight (layer l, in i, out o) in the fragment-ordered bf16 buffers
-__device__ __forceinline__ int frag_index(int block_words_off, int ntiles, int k, int n) {
-    const int kt = k >> 4, rem = k & 15, reg = rem >> 3, t = (rem & 7) >> 1, hi = rem & 1;
-    const int nt = n >> 3, g = n & 7, lane = g * 4 + t;
-    return ((block_words_off + (kt * ntiles + nt) * 32 + lane) * 2 + reg) * 2 + hi;
-}
-
-// sums the CTA partials in a fixed order, one Adam step in FP32, BF16 copies
+// sums the CTA partials in a fixed order, one Adam step in FP32, the two BF16 operand copies
 __global__ void k_mlp_adam(const float* __restrict__ part, uint32_t nparts, float* w, float* m, float* v,
-                           AdamParams ap, unsigned short* wf, unsigned short* wb, unsigned short* wtc,
-                           float* grad_out) {
+                           AdamParams ap, unsigned short* wtc, unsigned short* wtcb, float* grad_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= MLP_NW) return;
     float gsum = 0.0f;
@@ -665,9 +576,8 @@ __global__ void k_mlp_adam(const float* __restrict__ part, uint32_t nparts, floa
     int l, in, out;
     if (i < 4 * 4096) { l = i >> 12; in = (i >> 6) & 63; out = i & 63; }
     else { l = 4; in = (i - 4 * 4096) / 3; out = (i - 4 * 4096) % 3; }
-    wf[frag_index(MLP_FWD_OFF(l), l < 4 ? 8 : 1, in, out)] = b;
-    if (l >= 1) wb[frag_index(MLP_BWD_OFF(l), 8, out, in)] = b;
-    wtc[l * 4096 + tc_off((uint32_t)out, (uint32_t)in) / 2] = b;   // N = out, K = in
+    wtc[l * 4096 + tc_off((uint32_t)out, (uint32_t)in) / 2] = b;                        // N = out, K = in
+    if (l >= 1) wtcb[(l - 1) * 4096 + tc_off((uint32_t)in, (uint32_t)out) / 2] = b;   // N = in, K = out
 }
 
 }  // namespace
@@ -677,25 +587,22 @@ Status mlp_init(MlpState& M, const float* w_host, cudaStream_t st) {
     SNK_TRY_CUDA(M.w.reserve(MLP_NW));
     SNK_TRY_CUDA(M.m.reserve(MLP_NW));
     SNK_TRY_CUDA(M.v.reserve(MLP_NW));
-    SNK_TRY_CUDA(M.wf.reserve(MLP_FWD_WORDS));
-    SNK_TRY_CUDA(M.wb.reserve(MLP_BWD_WORDS));
     SNK_TRY_CUDA(M.wtc.reserve(MLP_TC_ELEMS));
+    SNK_TRY_CUDA(M.wtcb.reserve(MLP_TCB_ELEMS));
     SNK_TRY_CUDA(cudaMemcpyAsync(M.w.p, w_host, MLP_NW * sizeof(float), cudaMemcpyHostToDevice, st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.wtc.p, 0, MLP_TC_ELEMS * sizeof(unsigned short), st));
+    SNK_TRY_CUDA(cudaMemsetAsync(M.wtcb.p, 0, MLP_TCB_ELEMS * sizeof(unsigned short), st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.m.p, 0, MLP_NW * sizeof(float), st));
     SNK_TRY_CUDA(cudaMemsetAsync(M.v.p, 0, MLP_NW * sizeof(float), st));
-    SNK_TRY_CUDA(cudaMemsetAsync(M.wf.p, 0, MLP_FWD_WORDS * sizeof(uint2), st));
-    SNK_TRY_CUDA(cudaMemsetAsync(M.wb.p, 0, MLP_BWD_WORDS * sizeof(uint2), st));
-    // the training kernel's shared memory exceeds the default limit (set here, not
-    // per launch, so frames can be captured into CUDA graphs)
-    SNK_TRY_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(TrainSmem)));
+    // the kernels' shared memory exceeds the default limit (set here, not per
+    // launch, so frames can be captured into CUDA graphs)
+    SNK_TRY_CUDA(cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(TrainTcSmem)));
     SNK_TRY_CUDA(cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(InferSmem)));
     AdamParams ap{};   // lr 0: only refresh the BF16 copies
-    k_mlp_adam<<<(MLP_NW + 255) / 256, 256, 0, st>>>(M.w.p, 0, M.w.p, M.m.p, M.v.p, ap,
-                                                     reinterpret_cast<unsigned short*>(M.wf.p),
-                                                     reinterpret_cast<unsigned short*>(M.wb.p), M.wtc.p, nullptr);
+    k_mlp_adam<<<(MLP_NW + 255) / 256, 256, 0, st>>>(M.w.p, 0, M.w.p, M.m.p, M.v.p, ap, M.wtc.p, M.wtcb.p,
+                                                     nullptr);
     SNK_TRY_CUDA(cudaGetLastError());
     M.step = 0;
     M.ready = true;
@@ -724,13 +631,13 @@ Status mlp_train_reserve(MlpState& M, uint32_t n) {
 }
 
 Status mlp_train_step(MlpState& M, const float4* samples, uint32_t n, const EncodeParams& ep, float lr,
-                      float* grad_out, float* loss_host, cudaStream_t st) {
+                      float* grad_out, float* loss_host, unsigned* err_word, cudaStream_t st) {
     if (n == 0) return Status::Ok();
     const uint32_t ctas = (n + TRAIN_ROWS - 1) / TRAIN_ROWS;
     Status rs = mlp_train_reserve(M, n);
     if (!rs.ok()) return rs;
-    k_mlp_train<<<ctas, 256, sizeof(TrainSmem), st>>>(M.wf.p, M.wb.p, samples, n, ep, 1.0f / (3.0f * (float)n),
-                                                      M.part.p, M.loss.p);
+    k_mlp_train_tc<<<ctas, TRAIN_TC_THREADS, sizeof(TrainTcSmem), st>>>(
+        M.wtc.p, M.wtcb.p, samples, n, ep, 1.0f / (3.0f * (float)n), M.part.p, M.loss.p, err_word);
     SNK_TRY_CUDA(cudaGetLastError());
     M.step++;
     AdamParams ap;
@@ -740,9 +647,8 @@ Status mlp_train_step(MlpState& M, const float4* samples, uint32_t n, const Enco
     ap.eps = 1e-8f;
     ap.c1 = (float)(1.0 - std::pow(0.9, (double)M.step));
     ap.c2 = (float)(1.0 - std::pow(0.99, (double)M.step));
-    k_mlp_adam<<<(MLP_NW + 255) / 256, 256, 0, st>>>(M.part.p, ctas, M.w.p, M.m.p, M.v.p, ap,
-                                                     reinterpret_cast<unsigned short*>(M.wf.p),
-                                                     reinterpret_cast<unsigned short*>(M.wb.p), M.wtc.p, grad_out);
+    k_mlp_adam<<<(MLP_NW + 255) / 256, 256, 0, st>>>(M.part.p, ctas, M.w.p, M.m.p, M.v.p, ap, M.wtc.p, M.wtcb.p,
+                                                     grad_out);
     SNK_TRY_CUDA(cudaGetLastError());
     if (loss_host) {
         std::vector<float> lp(ctas);

@@ -10,16 +10,15 @@ namespace snk {
 constexpr int MLP_NW = 4 * 64 * 64 + 64 * 3;   // master weights (FP32)
 // master weight offset of layer l (W_l[in][out], row major)
 #define MLP_OFF(l) ((l) * 4096)
-// fragment-ordered BF16 copies, in uint2 words (one B fragment per lane per tile)
-#define MLP_FWD_OFF(l) ((l) < 4 ? (l) * 1024 : 4096)      // 4 x (4 k-tiles x 8 n-tiles x 32), then 4 x 1 x 32
-constexpr int MLP_FWD_WORDS = 4096 + 128;
-#define MLP_BWD_OFF(l) ((l) < 4 ? ((l) - 1) * 1024 : 3072) // transposed layers 1..3, then layer 4 (1 x 8 x 32)
-constexpr int MLP_BWD_WORDS = 3072 + 256;
 // BF16 copy in the tcgen05 shared-memory operand layout (K-major, no swizzle: 8x8
 // core matrices of 128 contiguous bytes): layer l < 4 as N = 64 outputs x K = 64
 // inputs at element offset l * 4096, layer 4 as N = 16 (3 outputs + 13 zero rows)
 // x K = 64 at 4 * 4096
 constexpr int MLP_TC_ELEMS = 4 * 4096 + 16 * 64;
+// BF16 transposed copy in the same layout, for the input-gradient GEMMs: layer
+// l = 1..4 as N = 64 inputs x K = 64 outputs at element offset (l - 1) * 4096
+// (layer 4: outputs 0..2, zero beyond)
+constexpr int MLP_TCB_ELEMS = 4 * 4096;
 
 struct EncodeParams {
     float lo[3];        // scene box the positions are normalised to
@@ -32,8 +31,7 @@ struct AdamParams {
 
 struct MlpState {
     DBuf<float> w, m, v;             // FP32 master weights and Adam moments
-    DBuf<uint2> wf, wb;              // BF16 forward / transposed copies (fragment order)
-    DBuf<unsigned short> wtc;        // BF16 forward copy in the tcgen05 operand layout (inference)
+    DBuf<unsigned short> wtc, wtcb;  // BF16 forward / transposed copies in the tcgen05 operand layout
     DBuf<float> part, loss;          // per-CTA gradient partials and losses
     uint32_t step = 0;
     bool ready = false;
@@ -47,9 +45,10 @@ Status mlp_infer(const MlpState& M, const float4* rec, const uint32_t* n_dev, ui
 Status mlp_encode(const float4* rec, uint32_t n, const EncodeParams& ep, float* out, cudaStream_t st);
 // samples: 5 float4 each (the 4 record words, then target rgb + weight)
 // grows the per-CTA gradient/loss buffers for batches of up to n samples (call
-// before a stream capture: the training step itself then allocates nothing)
+// before a stream capture: the training step itself then allocates nothing);
+// a give-up of the training kernel's bounded tensor-core waits sets bit 16 of *err_word
 Status mlp_train_reserve(MlpState& M, uint32_t n);
 Status mlp_train_step(MlpState& M, const float4* samples, uint32_t n, const EncodeParams& ep, float lr,
-                      float* grad_out, float* loss_host, cudaStream_t st);
+                      float* grad_out, float* loss_host, unsigned* err_word, cudaStream_t st);
 
 }  // namespace snk
