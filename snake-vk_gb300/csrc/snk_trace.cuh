@@ -83,9 +83,11 @@ __device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) {
 
 // Tests the 8 children of node idx.  ngroup <- (child_base, internal hits << 24 | imask)
 // with internal hit bits at position (slot ^ oct); tgroup <- (prim_base, primitive hits).
-// Near/far planes are swapped once per node by the ray octant, the hit masks are
-// built without branches, and a slack of 1e-5 of the entry/exit distances keeps
-// the test conservative.
+// Near/far planes are swapped once per node by the ray octant and a slack of 1e-5
+// of the entry/exit distances keeps the test conservative.  The 8 box tests only
+// set one bit each; the internal-child bits are then moved into visiting order
+// with three conditional swaps (bit s -> s ^ oct), and only the hit leaf slots
+// are expanded into primitive bits.
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ nodes, uint32_t idx, const NodeRay& r,
                                                float tmin, float tmax, uint2& ngroup, uint2& tgroup) {
     const float4* np = reinterpret_cast<const float4*>(nodes + idx);
@@ -105,8 +107,8 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
     uint32_t nx[2] = {sx ? hx0 : lx0, sx ? hx1 : lx1}, fx[2] = {sx ? lx0 : hx0, sx ? lx1 : hx1};
     uint32_t ny[2] = {sy ? hy0 : ly0, sy ? hy1 : ly1}, fy[2] = {sy ? ly0 : hy0, sy ? ly1 : hy1};
     uint32_t nz[2] = {sz ? hz0 : lz0, sz ? hz1 : lz1}, fz[2] = {sz ? lz0 : hz0, sz ? lz1 : hz1};
-    uint32_t meta[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
-    uint32_t hit_int = 0, hit_prim = 0;
+    const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
+    uint32_t hits = 0;   // bit s: the box of slot s is hit
 #pragma unroll
     for (int s = 0; s < 8; s++) {
         const int h = s >> 2, k = s & 3;
@@ -114,13 +116,22 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
                          fmaxf(__fmaf_rn(byte_f(nz[h], k), az, bz), tmin));
         float tf = min3f(__fmaf_rn(byte_f(fx[h], k), ax, bx), __fmaf_rn(byte_f(fy[h], k), ay, by),
                          fminf(__fmaf_rn(byte_f(fz[h], k), az, bz), tmax));
-        uint32_t m = (meta[h] >> (8 * k)) & 0xFFu;
-        bool hit = (tn <= tf + ((fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f)) && m != 0u;
-        // internal children: imask bit (meta META_INTERNAL, count 0); leaves: (count << 5) | offset
-        hit_int |= (hit && ((imask >> s) & 1u)) ? (1u << ((uint32_t)s ^ r.oct)) : 0u;
-        hit_prim |= hit ? bit_mask(m & 31u, m >> 5) : 0u;
+        hits |= (tn <= tf + ((fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f)) ? (1u << s) : 0u;
     }
-    ngroup = make_uint2(__float_as_uint(w1.x), (hit_int << 24) | imask);
+    // internal children (imask bits) in visiting order: bit s moves to s ^ oct
+    uint32_t x = hits & imask;
+    x = (r.oct & 1u) ? (((x & 0x55u) << 1) | ((x >> 1) & 0x55u)) : x;
+    x = (r.oct & 2u) ? (((x & 0x33u) << 2) | ((x >> 2) & 0x33u)) : x;
+    x = (r.oct & 4u) ? (((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu)) : x;
+    // leaf children: (count << 5) | offset -> primitive bits; an empty slot (meta 0) adds none
+    uint32_t leaves = hits & ~imask, hit_prim = 0;
+    while (leaves) {
+        const uint32_t s = __ffs(leaves) - 1;
+        leaves &= leaves - 1u;
+        const uint32_t m = __byte_perm(meta0, meta1, s) & 0xFFu;
+        hit_prim |= bit_mask(m & 31u, m >> 5);
+    }
+    ngroup = make_uint2(__float_as_uint(w1.x), (x << 24) | imask);
     tgroup = make_uint2(__float_as_uint(w1.y), hit_prim);
 }
 

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 def scenes_loaded(cuda, built_lib):
     out = {}
     for cfg, kw in [(0, {}), (1, {"width": 1920, "height": 1080}), (2, {"width": 640, "height": 360, "frames": 1}),
-                    (3, {"resolutions": [(1280, 720)]})]:
+                    (3, {"resolutions": [(1280, 720)]}), (4, {"width": 960, "height": 540, "frames": 2})]:
         sc = scenes.make(cfg, **kw)
         pt = snkpt.PathTracer(0)
         pt.load_scene(sc)
@@ -23,7 +23,9 @@ def scenes_loaded(cuda, built_lib):
     return out
 
 
-@pytest.mark.parametrize("cfg,n_rand", [(0, 600_000), (1, 600_000), (2, 200_000), (3, 200_000)])
+# at least 1M rays per configuration: every camera ray of the view (400k sampled
+# at 1080p) plus random rays through the scene box
+@pytest.mark.parametrize("cfg,n_rand", [(0, 1_000_000), (1, 600_000), (2, 800_000), (3, 200_000), (4, 600_000)])
 def test_closest_hit_bit_exact(scenes_loaded, cfg, n_rand):
     sc, pt, osc = scenes_loaded[cfg]
     rng = np.random.default_rng(100 + cfg)
@@ -31,13 +33,14 @@ def test_closest_hit_bit_exact(scenes_loaded, cfg, n_rand):
     npix = int(v["width"]) * int(v["height"])
     cam = camera_rays(v) if npix <= 1 << 20 else camera_rays(v, 400_000, rng)
     rays = np.concatenate([cam, random_rays(sc, n_rand, rng)])
+    assert len(rays) >= 1_000_000
     gpu = pt.trace_rays(rays)
     ref = osc.trace(rays)
     assert_hits_equal(gpu, ref, f"config {cfg} closest")
     assert (ref["flags"] == 1).mean() > 0.3   # the ray sets actually hit geometry
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_any_hit_bit_exact(scenes_loaded, cfg):
     sc, pt, osc = scenes_loaded[cfg]
     rng = np.random.default_rng(200 + cfg)
