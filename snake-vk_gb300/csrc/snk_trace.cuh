@@ -15,9 +15,9 @@
 // primitive group is (prim_base, 32 primitive hit bits).  Groups are kept on a
 // short per-thread stack in shared memory ([entry][thread] layout, conflict
 // free) that spills to local memory; primitive groups carry PRIM_GROUP in the
-// base word there.  Children are visited in the order of the
-// slot index xor the ray octant, which the builder makes approximately
-// front-to-back.  Leaves of the instance BVH hold instance ids: on reaching one
+// base word there.  Closest-hit rays visit children in the order of the slot
+// index xor the ray octant, which the builder makes approximately front to back;
+// any-hit rays visit them in slot order.  Leaves of the instance BVH hold instance ids: on reaching one
 // the ray is transformed into object space and the BLAS root is entered; when
 // the stack unwinds to the entry depth, the world ray is restored.
 #pragma once
@@ -82,12 +82,15 @@ __device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) {
 }
 
 // Tests the 8 children of node idx.  ngroup <- (child_base, internal hits << 24 | imask)
-// with internal hit bits at position (slot ^ oct); tgroup <- (prim_base, primitive hits).
+// with internal hit bit of slot s at position s ^ oct (ORDERED) or s; tgroup <- (prim_base,
+// primitive hits).
 // Near/far planes are swapped once per node by the ray octant and a slack of 1e-5
 // of the entry/exit distances keeps the test conservative.  The 8 box tests only
 // set one bit each; the internal-child bits are then moved into visiting order
-// with three conditional swaps (bit s -> s ^ oct), and only the hit leaf slots
-// are expanded into primitive bits.
+// with three conditional swaps (bit s -> s ^ oct) when the order matters (closest
+// hit; an any-hit ray stops at whichever occluder it meets first and skips the
+// swaps), and only the hit leaf slots are expanded into primitive bits.
+template <bool ORDERED>
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ nodes, uint32_t idx, const NodeRay& r,
                                                float tmin, float tmax, uint2& ngroup, uint2& tgroup) {
     const float4* np = reinterpret_cast<const float4*>(nodes + idx);
@@ -120,9 +123,11 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
     }
     // internal children (imask bits) in visiting order: bit s moves to s ^ oct
     uint32_t x = hits & imask;
-    x = (r.oct & 1u) ? (((x & 0x55u) << 1) | ((x >> 1) & 0x55u)) : x;
-    x = (r.oct & 2u) ? (((x & 0x33u) << 2) | ((x >> 2) & 0x33u)) : x;
-    x = (r.oct & 4u) ? (((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu)) : x;
+    if (ORDERED) {
+        x = (r.oct & 1u) ? (((x & 0x55u) << 1) | ((x >> 1) & 0x55u)) : x;
+        x = (r.oct & 2u) ? (((x & 0x33u) << 2) | ((x >> 2) & 0x33u)) : x;
+        x = (r.oct & 4u) ? (((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu)) : x;
+    }
     // leaf children: (count << 5) | offset -> primitive bits; an empty slot (meta 0) adds none
     uint32_t leaves = hits & ~imask, hit_prim = 0;
     while (leaves) {
@@ -168,6 +173,7 @@ struct ShortStack {
 //                when its part of the stack is used up; true when finished
 template <bool ANY, bool COUNT>
 struct Traverser {
+    static constexpr bool ORD = !ANY;   // visit children front to back (closest hit only)
     V3 o, d;             // world-space ray
     float tmin, tmax;
     NodeRay cr;          // ray of the current level (world or object space)
@@ -188,7 +194,7 @@ struct Traverser {
         best_t = tmax; best_u = 0.0f; best_v = 0.0f; best_inst = INVALID; best_prim = INVALID;
         level = 0; blas_sp = 0; cur_inst = 0; steps = 0; err = 0; done = false;
         st.sh = sh; st.spill = spill; st.tid = tid; st.nthreads = nthreads; st.sp = 0;
-        ngroup = S.tlas_root == INVALID ? make_uint2(0u, 0u) : make_uint2(S.tlas_root, (1u << (24 + cr.oct)) | 1u);
+        ngroup = S.tlas_root == INVALID ? make_uint2(0u, 0u) : make_uint2(S.tlas_root, (1u << (24 + (ORD ? cr.oct : 0u))) | 1u);
         tgroup = make_uint2(0u, 0u);
     }
 
@@ -217,14 +223,14 @@ struct Traverser {
         }
         uint32_t k = __ffs(ngroup.y >> 24) - 1;
         ngroup.y &= ~(1u << (24 + k));
-        uint32_t slot = k ^ cr.oct;
+        uint32_t slot = ORD ? k ^ cr.oct : k;
         uint32_t child = ngroup.x + __popc(ngroup.y & ((1u << slot) - 1u) & 0xFFu);
         if (has_node()) {
             if (!st.push(ngroup)) { fail(ERR_STACK_OVERFLOW); return; }
         }
         if (COUNT) ctr->nodes++;
         if (child >= (level ? S.num_blas_nodes : S.num_tlas_nodes)) { fail(ERR_BAD_INDEX); return; }
-        intersect_node(level ? S.blas_nodes : S.tlas_nodes, child, cr, tmin, best_t, ngroup, tgroup);
+        intersect_node<ORD>(level ? S.blas_nodes : S.tlas_nodes, child, cr, tmin, best_t, ngroup, tgroup);
     }
 
     __device__ __forceinline__ void prim_step(const SceneDev& S, TraceCounters* ctr) {
@@ -253,7 +259,7 @@ struct Traverser {
             blas_sp = st.sp;
             level = 1;
             cur_inst = inst;
-            ngroup = make_uint2(root, (1u << (24 + cr.oct)) | 1u);
+            ngroup = make_uint2(root, (1u << (24 + (ORD ? cr.oct : 0u))) | 1u);
             tgroup = make_uint2(0u, 0u);
         } else {
             if (pidx >= S.num_tris) { fail(ERR_BAD_INDEX); return; }
