@@ -631,6 +631,7 @@ struct SmallSmem {
     unsigned cb[6];
     double sah;
     TreeletSmem tl[SMALL_THREADS / 32];
+    WideNode stage[SMALL_THREADS / 32];        // per-warp staging of collapsed nodes
 };
 static_assert(sizeof(SmallSmem) <= 227 * 1024, "single-CTA builder exceeds shared memory");
 
@@ -663,6 +664,168 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warp_sums, 
     *total = warp_sums[31];
     __syncthreads();
     return r;
+}
+
+// float -> unsigned with the same order (for warp max reductions)
+__device__ __forceinline__ unsigned order_f(float f) {
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// collapse_task for a whole warp (every lane passes the same task): the same
+// greedy choices, made with warp reductions instead of one thread's loops.
+// Lane k < nc holds candidate child k while the node is opened; the 64 (child,
+// slot) pairs p = 8k + s of the slot assignment are spread two per lane; lane s
+// < 8 then builds slot s.  Ties go to the lowest child / pair index, as in the
+// sequential loops.  stage: this warp's 80-byte staging node in shared memory.
+__device__ void collapse_task_warp(uint2 task, uint32_t* counters, uint2* tasks_out, int n, const int2* children,
+                                   const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count,
+                                   const uint32_t* sorted, WideNode* nodes, WideNode* stage, uint32_t node_base,
+                                   uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack) {
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const int b = (int)task.x;
+    const uint32_t w = task.y;
+    const int nl = n - 1;   // first leaf id
+    int c = -1, nc;
+    if (b >= nl) {
+        nc = 1;
+        if (lane == 0) c = b;
+    } else {
+        const int2 ch = children[b];
+        nc = 2;
+        c = lane == 0 ? ch.x : (lane == 1 ? ch.y : -1);
+    }
+    // open the largest internal candidate (more than leaf_max primitives) until 8 children
+    while (nc < 8) {
+        const bool elig = lane < nc && c < nl && leaf_count[c] > leaf_max;
+        const unsigned key = elig ? __float_as_uint(half_area(node_lo[c], node_hi[c])) + 1u : 0u;   // areas >= 0
+        const unsigned mx = __reduce_max_sync(FULL, key);
+        if (mx == 0u) break;
+        const int best = __ffs(__ballot_sync(FULL, key == mx)) - 1;
+        const int cb = __shfl_sync(FULL, c, best);
+        const int2 ch = children[cb];
+        if (lane == best) c = ch.x;
+        if (lane == nc) c = ch.y;
+        nc++;
+    }
+    // parent box (min / max are exact, so the reduction order does not matter)
+    float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+    float4 clo = lo, chi = hi;
+    if (lane < nc) { clo = node_lo[c]; chi = node_hi[c]; lo = clo; hi = chi; }
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        lo.x = fminf(lo.x, __shfl_xor_sync(FULL, lo.x, o)); lo.y = fminf(lo.y, __shfl_xor_sync(FULL, lo.y, o));
+        lo.z = fminf(lo.z, __shfl_xor_sync(FULL, lo.z, o));
+        hi.x = fmaxf(hi.x, __shfl_xor_sync(FULL, hi.x, o)); hi.y = fmaxf(hi.y, __shfl_xor_sync(FULL, hi.y, o));
+        hi.z = fmaxf(hi.z, __shfl_xor_sync(FULL, hi.z, o));
+    }
+    const float4 plo = make_float4(__shfl_sync(FULL, lo.x, 0), __shfl_sync(FULL, lo.y, 0), __shfl_sync(FULL, lo.z, 0), 0.0f);
+    const float4 phi = make_float4(__shfl_sync(FULL, hi.x, 0), __shfl_sync(FULL, hi.y, 0), __shfl_sync(FULL, hi.z, 0), 0.0f);
+    const float pcx = 0.5f * (plo.x + phi.x), pcy = 0.5f * (plo.y + phi.y), pcz = 0.5f * (plo.z + phi.z);
+    const float cx = 0.5f * (clo.x + chi.x) - pcx, cy = 0.5f * (clo.y + chi.y) - pcy, cz = 0.5f * (clo.z + chi.z) - pcz;
+    // greedy slot assignment over the pairs p0 = lane, p1 = lane + 32 (child p >> 3, slot p & 7)
+    const int s_ = lane & 7, k0 = lane >> 3, k1 = 4 + (lane >> 3);
+    float sc[2];
+    {
+        const float x0 = __shfl_sync(FULL, cx, k0), y0 = __shfl_sync(FULL, cy, k0), z0 = __shfl_sync(FULL, cz, k0);
+        const float x1 = __shfl_sync(FULL, cx, k1), y1 = __shfl_sync(FULL, cy, k1), z1 = __shfl_sync(FULL, cz, k1);
+        sc[0] = ((s_ & 1) ? x0 : -x0) + ((s_ & 2) ? y0 : -y0) + ((s_ & 4) ? z0 : -z0);
+        sc[1] = ((s_ & 1) ? x1 : -x1) + ((s_ & 2) ? y1 : -y1) + ((s_ & 4) ? z1 : -z1);
+    }
+    uint32_t used_c = 0, used_s = 0;
+    int slot_c = -1;   // lane s < 8: the child in slot s
+    for (int it = 0; it < nc; it++) {
+        const bool v0 = k0 < nc && !((used_c >> k0) & 1u) && !((used_s >> s_) & 1u);
+        const bool v1 = k1 < nc && !((used_c >> k1) & 1u) && !((used_s >> s_) & 1u);
+        const bool take1 = v1 && (!v0 || sc[1] > sc[0]);
+        const bool has = v0 || v1;
+        const unsigned key = has ? order_f(take1 ? sc[1] : sc[0]) : 0u;
+        const uint32_t p = take1 ? (uint32_t)lane + 32u : (uint32_t)lane;
+        const unsigned mx = __reduce_max_sync(FULL, key);
+        const uint32_t pm = __reduce_min_sync(FULL, (has && key == mx) ? p : 0xFFFFFFFFu);
+        const int bk = (int)(pm >> 3), bs = (int)(pm & 7u);
+        used_c |= 1u << bk;
+        used_s |= 1u << bs;
+        const int cb = __shfl_sync(FULL, c, bk);
+        if (lane == bs) slot_c = cb;
+    }
+    // classify and allocate
+    const bool mine = lane < 8 && slot_c >= 0;
+    const bool is_int = mine && slot_c < nl && leaf_count[slot_c] > leaf_pack;
+    const uint32_t cnt = (mine && !is_int) ? leaf_count[slot_c] : 0u;
+    const unsigned int_mask = __ballot_sync(FULL, is_int);
+    const uint32_t n_int = (uint32_t)__popc(int_mask);
+    uint32_t off = cnt;   // inclusive scan of the leaf counts over the slots, then exclusive
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, off, o);
+        if (lane >= o) off += t;
+    }
+    const uint32_t n_prims = __shfl_sync(FULL, off, 7);
+    off -= cnt;
+    uint32_t child_local = 0, prim_local = 0, task_base = 0;
+    if (lane == 0) {
+        child_local = n_int ? atomicAdd(&counters[2], n_int) : 0u;
+        prim_local = n_prims ? atomicAdd(&counters[3], n_prims) : 0u;
+    }
+    child_local = __shfl_sync(FULL, child_local, 0);
+    prim_local = __shfl_sync(FULL, prim_local, 0);
+    // capacity checks (never exceeded by a correct tree; a violation is recorded,
+    // the node is not written and no child task is queued)
+    if (child_local + n_int > (uint32_t)n + 1u || prim_local + n_prims > (uint32_t)n || w - node_base > (uint32_t)n) {
+        if (lane == 0) atomicOr(&counters[4], 1u);
+        return;
+    }
+    if (lane == 0 && n_int) task_base = atomicAdd(&counters[1], n_int);
+    task_base = __shfl_sync(FULL, task_base, 0);
+    const QuantFrame F = quant_frame(plo, phi);
+    if (lane == 0) {
+        stage->px = plo.x; stage->py = plo.y; stage->pz = plo.z;
+        stage->ex = (uint8_t)F.eb[0]; stage->ey = (uint8_t)F.eb[1]; stage->ez = (uint8_t)F.eb[2];
+        stage->imask = (uint8_t)(int_mask & 0xFFu);
+        stage->child_base = node_base + child_local;
+        stage->prim_base = prim_base + prim_local;
+    }
+    if (lane < 8) {
+        const int s = lane;
+        if (slot_c < 0) {
+            stage->meta[s] = 0;
+            for (int a = 0; a < 3; a++) { stage->qlo[a][s] = 0; stage->qhi[a][s] = 0; }
+        } else {
+            quant_child(F, node_lo[slot_c], node_hi[slot_c], *stage, s);
+            if (is_int) {
+                const uint32_t rank = (uint32_t)__popc(int_mask & ((1u << s) - 1u));
+                stage->meta[s] = (uint8_t)META_INTERNAL;
+                const uint32_t slot_out = task_base + rank;
+                if (slot_out < (uint32_t)n) tasks_out[slot_out] = make_uint2((uint32_t)slot_c, node_base + child_local + rank);
+                else atomicOr(&counters[4], 2u);
+            } else {
+                stage->meta[s] = (uint8_t)((cnt << 5) | off);
+                // the (<= leaf_pack) leaves of subtree slot_c, in order
+                int stk[8];
+                int sp = 0;
+                stk[sp++] = slot_c;
+                uint32_t k = 0;
+                while (sp > 0) {
+                    const int x = stk[--sp];
+                    if (x >= nl) {
+                        if (k < cnt) prim_order[prim_local + off + k] = sorted[x - nl];
+                        k++;
+                    } else if (sp < 7) {
+                        const int2 ch = children[x];
+                        stk[sp++] = ch.y;
+                        stk[sp++] = ch.x;
+                    } else {
+                        atomicOr(&counters[4], 4u);
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (lane < 5) reinterpret_cast<uint4*>(nodes + w)[lane] = reinterpret_cast<const uint4*>(stage)[lane];
+    __syncwarp();
 }
 
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
@@ -732,6 +895,34 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
     uint32_t m = (uint32_t)n;
     uint32_t next_id = n > 1 ? (uint32_t)(n - 2) : 0u;
     while (m > 32 && rounds < SMALL_BUILD_MAX) {
+        // nearest neighbour of every position within PLOC_RADIUS: a group of tpc
+        // threads per position splits the 2 * PLOC_RADIUS candidates, then takes
+        // the minimum of (area, position), so ties keep the lower position
+        {
+            int tpc = 2 * PLOC_RADIUS;
+            while (tpc > 1 && (uint32_t)tpc * m > (uint32_t)SMALL_THREADS) tpc >>= 1;
+            const int g = tid / tpc, sub = tid % tpc;
+            float best = 3.4e38f;
+            uint32_t nn = 0xFFFFFFFFu;
+            if (g < (int)m) {
+                const int cg = S.clusters[cur][g];
+                const float4 glo = S.node_lo[cg], ghi = S.node_hi[cg];
+                for (int u = sub; u < 2 * PLOC_RADIUS; u += tpc) {
+                    const int j = g + (u < PLOC_RADIUS ? u - PLOC_RADIUS : u - PLOC_RADIUS + 1);
+                    if (j < 0 || j >= (int)m) continue;
+                    const int cj = S.clusters[cur][j];
+                    const float a = half_area(f4min(glo, S.node_lo[cj]), f4max(ghi, S.node_hi[cj]));
+                    if (a < best) { best = a; nn = (uint32_t)j; }   // increasing j within the thread
+                }
+            }
+            for (int o = 1; o < tpc; o <<= 1) {
+                const float ob = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+                const uint32_t on = __shfl_xor_sync(0xFFFFFFFFu, nn, o);
+                if (ob < best || (ob == best && on < nn)) { best = ob; nn = on; }
+            }
+            if (sub == 0 && g < (int)m) S.tasks[0][g].x = nn;   // scratch: nearest neighbour per position
+        }
+        __syncthreads();
         const int i = tid;
         int nn = -1;
         float4 mylo = make_float4(0.f, 0.f, 0.f, 0.f), myhi = mylo;
@@ -739,17 +930,8 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
             const int ci = S.clusters[cur][i];
             mylo = S.node_lo[ci];
             myhi = S.node_hi[ci];
-            float best = 3.4e38f;
-            const int j0 = max(0, i - PLOC_RADIUS), j1 = min((int)m - 1, i + PLOC_RADIUS);
-            for (int j = j0; j <= j1; j++) {
-                if (j == i) continue;
-                const int cj = S.clusters[cur][j];
-                const float a = half_area(f4min(mylo, S.node_lo[cj]), f4max(myhi, S.node_hi[cj]));
-                if (a < best) { best = a; nn = j; }   // increasing j: ties keep the lower position
-            }
+            nn = (int)S.tasks[0][i].x;
         }
-        S.tasks[0][tid].x = (uint32_t)nn;   // scratch: nearest neighbour per position
-        __syncthreads();
         bool merge = false, keep = false;
         if (i < (int)m) {
             const bool mutual = nn >= 0 && (int)S.tasks[0][nn].x == i;
@@ -793,13 +975,12 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
             const bool live = lane < (int)m;
             float best = 3.4e38f;
             int nn = -1;
+            // every live cluster's box is stored at its node id (merges write it before
+            // the __syncwarp that ends a round)
             for (int j = 0; j < (int)m; j++) {
-                const float4 ol = make_float4(__shfl_sync(0xFFFFFFFFu, lo.x, j), __shfl_sync(0xFFFFFFFFu, lo.y, j),
-                                              __shfl_sync(0xFFFFFFFFu, lo.z, j), 0.0f);
-                const float4 oh = make_float4(__shfl_sync(0xFFFFFFFFu, hi.x, j), __shfl_sync(0xFFFFFFFFu, hi.y, j),
-                                              __shfl_sync(0xFFFFFFFFu, hi.z, j), 0.0f);
+                const int idj = __shfl_sync(0xFFFFFFFFu, id, j);
                 if (j == lane || !live) continue;
-                const float a = half_area(f4min(lo, ol), f4max(hi, oh));
+                const float a = half_area(f4min(lo, S.node_lo[idj]), f4max(hi, S.node_hi[idj]));
                 if (a < best) { best = a; nn = j; }
             }
             const int nn_of_nn = __shfl_sync(0xFFFFFFFFu, nn, nn < 0 ? lane : nn);
@@ -839,6 +1020,7 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
                              __shfl_sync(0xFFFFFFFFu, hi.z, k), 0.0f);
             cnt = __shfl_sync(0xFFFFFFFFu, cnt, k);
             m = (uint32_t)__popc(km);
+            __syncwarp();
         }
         if (lane == 0) S.clusters[cur][0] = id;
         if (lane == 0 && m != 1u) S.counters[6] |= 16u;
@@ -877,21 +1059,21 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
     __syncthreads();
     int cc = 0, level = 0;
     for (; level < 4096; level++) {
-        const uint32_t nin = S.counters[0];
-        if (nin == 0) break;
-        for (uint32_t t = tid; t < nin; t += nt) {
+        const uint32_t nin = min(S.counters[0], (uint32_t)n);   // the task arrays hold n entries
+        if (nin == 0 || S.counters[4] != 0u) break;               // done, or a capacity error
+        // one warp per wide node (no SAH statistic: the per-frame build skips it)
+        for (uint32_t t = (uint32_t)(tid >> 5); t < nin; t += (uint32_t)(nt >> 5)) {
             const uint2 task = S.tasks[cc][t];
             // refit data: exact box and depth of every wide node
             const uint32_t local = task.y - node_base;
-            if (local <= (uint32_t)n) {
+            if ((tid & 31) == 0 && local <= (uint32_t)n) {
                 wide_box[2 * local] = S.node_lo[task.x];
                 wide_box[2 * local + 1] = S.node_hi[task.x];
                 wide_depth[local] = (uint32_t)level;
             }
-            // (no SAH statistic: the per-frame build skips its double-precision atomics)
-            collapse_task(task, S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
-                          S.leaf_count, S.vals, nodes, node_base, prim_base, prim_order, nullptr, rha, leaf_max,
-                          leaf_max);
+            collapse_task_warp(task, S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi, S.leaf_count,
+                               S.vals, nodes, &S.stage[tid >> 5], node_base, prim_base, prim_order, leaf_max,
+                               leaf_max);
         }
         __syncthreads();
         if (tid == 0) { S.counters[0] = S.counters[1]; S.counters[1] = 0u; }
