@@ -75,17 +75,17 @@ __device__ __forceinline__ uint32_t bit_mask(uint32_t pos, uint32_t len) {
     return d;
 }
 
-// Exact byte -> float: the byte is placed in the mantissa of 2^23 (one byte
-// permute) and 2^23 is subtracted (exact), keeping the conversion off the XU pipe.
-__device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k)) - 8388608.0f;
+// Byte k of w as 1 + q 2^-15 (bits 8..15 of the mantissa of 1.0f): one byte permute.
+__device__ __forceinline__ float byte_m(uint32_t w, uint32_t k) {
+    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (k << 4)));
 }
 
 // Tests the 8 children of node idx.  ngroup <- (child_base, internal hits << 24 | imask)
 // with internal hit bit of slot s at position s ^ oct (ORDERED) or s; tgroup <- (prim_base,
 // primitive hits).
-// Near/far planes are swapped once per node by the ray octant and a slack of 1e-5
-// of the entry/exit distances keeps the test conservative.  The 8 box tests only
+// Near/far planes are swapped once per node by the ray octant; each plane costs a
+// byte permute and one FMA, and a slack of 1e-5 of the entry/exit distances (on
+// top of the per-axis widening below) keeps the test conservative.  The 8 box tests only
 // set one bit each; the internal-child bits are then moved into visiting order
 // with three conditional swaps (bit s -> s ^ oct) when the order matters (closest
 // hit; an any-hit ray stops at whichever occluder it meets first and skips the
@@ -96,11 +96,18 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
     const float4* np = reinterpret_cast<const float4*>(nodes + idx);
     float4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
     uint32_t e = __float_as_uint(w0.w);
-    float ax = __uint_as_float((e & 0xFFu) << 23) * r.idx;
-    float ay = __uint_as_float(((e >> 8) & 0xFFu) << 23) * r.idy;
-    float az = __uint_as_float(((e >> 16) & 0xFFu) << 23) * r.idz;
+    // per axis A = 2^15 x (grid step) / d, B = (p - o) / d - A rounded once; a plane
+    // byte q decodes as x = 1 + q 2^-15 (one byte permute), so t = fma(x, A, B).
+    // B's rounding (at most |A| 2^-24) is covered with room to spare by moving the
+    // near planes down and the far planes up by |A| 2^-21 (1/64 of a grid step).
+    const float ax = __uint_as_float(((e & 0xFFu) + 15u) << 23) * r.idx;
+    const float ay = __uint_as_float((((e >> 8) & 0xFFu) + 15u) << 23) * r.idy;
+    const float az = __uint_as_float((((e >> 16) & 0xFFu) + 15u) << 23) * r.idz;
     uint32_t imask = e >> 24;
-    float bx = (w0.x - r.ox) * r.idx, by = (w0.y - r.oy) * r.idy, bz = (w0.z - r.oz) * r.idz;
+    const float bx = __fmaf_rn(w0.x - r.ox, r.idx, -ax), by = __fmaf_rn(w0.y - r.oy, r.idy, -ay),
+                bz = __fmaf_rn(w0.z - r.oz, r.idz, -az);
+    const float mx = fabsf(ax) * 4.76837158e-7f, my = fabsf(ay) * 4.76837158e-7f, mz = fabsf(az) * 4.76837158e-7f;
+    const float bnx = bx - mx, bfx = bx + mx, bny = by - my, bfy = by + my, bnz = bz - mz, bfz = bz + mz;
     const bool sx = r.oct & 1u, sy = r.oct & 2u, sz = r.oct & 4u;
     uint32_t lx0 = __float_as_uint(w2.x), lx1 = __float_as_uint(w2.y), ly0 = __float_as_uint(w2.z),
              ly1 = __float_as_uint(w2.w), lz0 = __float_as_uint(w3.x), lz1 = __float_as_uint(w3.y),
@@ -115,10 +122,10 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
 #pragma unroll
     for (int s = 0; s < 8; s++) {
         const int h = s >> 2, k = s & 3;
-        float tn = max3f(__fmaf_rn(byte_f(nx[h], k), ax, bx), __fmaf_rn(byte_f(ny[h], k), ay, by),
-                         fmaxf(__fmaf_rn(byte_f(nz[h], k), az, bz), tmin));
-        float tf = min3f(__fmaf_rn(byte_f(fx[h], k), ax, bx), __fmaf_rn(byte_f(fy[h], k), ay, by),
-                         fminf(__fmaf_rn(byte_f(fz[h], k), az, bz), tmax));
+        float tn = max3f(__fmaf_rn(byte_m(nx[h], k), ax, bnx), __fmaf_rn(byte_m(ny[h], k), ay, bny),
+                         fmaxf(__fmaf_rn(byte_m(nz[h], k), az, bnz), tmin));
+        float tf = min3f(__fmaf_rn(byte_m(fx[h], k), ax, bfx), __fmaf_rn(byte_m(fy[h], k), ay, bfy),
+                         fminf(__fmaf_rn(byte_m(fz[h], k), az, bfz), tmax));
         hits |= (tn <= tf + ((fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f)) ? (1u << s) : 0u;
     }
     // internal children (imask bits) in visiting order: bit s moves to s ^ oct

@@ -5,7 +5,7 @@ import pytest
 
 import oracle as O
 import snkpt
-from helpers import assert_hits_equal, camera_rays, random_rays, shadow_rays
+from helpers import assert_hits_equal, camera_rays, random_rays, scene_bounds, shadow_rays
 from snkpt import abi, scenes
 
 pytestmark = pytest.mark.gpu
@@ -88,6 +88,44 @@ def test_degenerate_rays(scenes_loaded):
     r["tmax"][2048:3072] = 1e-6
     assert_hits_equal(pt.trace_rays(r), osc.trace(r), "degenerate rays")
     assert (pt.trace_rays(r)["flags"][1024:2048] == 0).all()
+
+
+def test_box_test_edge_cases(scenes_loaded):
+    """Rays that stress the rounding of the quantised box test: origins far
+    outside the scene, origins on mesh vertices with axis-parallel directions,
+    and rays grazing the ground plane (y = 0) from points on it."""
+    sc, pt, osc = scenes_loaded[1]
+    rng = np.random.default_rng(21)
+    lo, hi = scene_bounds(sc)
+    n = 100_000
+    # far origins (1e4 outside the box) aimed at random points inside it
+    target = rng.uniform(lo, hi, (n, 3))
+    d = rng.normal(size=(n, 3)); d /= np.linalg.norm(d, axis=1, keepdims=True)
+    far = np.zeros(n, abi.RAY_DTYPE)
+    far["o"] = target - 1e4 * d
+    far["d"] = d
+    far["tmax"] = 3e4
+    # world-space vertices of random instances, axis-parallel directions
+    verts = []
+    for i in rng.integers(0, len(sc.instances), 64):
+        m = sc.meshes[int(sc.instances[i]["mesh_id"])]
+        M = sc.instances[i]["transform"].reshape(3, 4).astype(np.float64)
+        p = m.positions[rng.integers(0, len(m.positions), n // 64)].astype(np.float64)
+        verts.append(p @ M[:, :3].T + M[:, 3])
+    verts = np.concatenate(verts)
+    axis = np.zeros(len(verts), abi.RAY_DTYPE)
+    axis["o"] = verts
+    axis["d"] = np.eye(3)[rng.integers(0, 3, len(verts))] * rng.choice([-1.0, 1.0], (len(verts), 1))
+    axis["tmax"] = 1e4
+    # grazing: from points of the ground plane, nearly parallel to it
+    g = np.zeros(n, abi.RAY_DTYPE)
+    g["o"] = np.stack([rng.uniform(lo[0], hi[0], n), np.zeros(n), rng.uniform(lo[2], hi[2], n)], 1)
+    phi = rng.uniform(0, 2 * np.pi, n)
+    elev = rng.choice([-1.0, 1.0], n) * 10.0 ** rng.uniform(-7, -2, n)
+    g["d"] = np.stack([np.cos(phi), elev, np.sin(phi)], 1) / np.sqrt(1 + elev ** 2)[:, None]
+    g["tmax"] = 1e4
+    for name, rays in (("far origins", far), ("vertex origins, axis-parallel", axis), ("grazing", g)):
+        assert_hits_equal(pt.trace_rays(rays), osc.trace(rays), name)
 
 
 def test_empty_scene(cuda, built_lib):
