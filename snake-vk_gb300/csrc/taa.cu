@@ -18,8 +18,9 @@
 //     undefined).
 //
 // Kernel: 32x8 pixels per block, the 34x10 halo tile of the current frame staged
-// in shared memory (coalesced float4 loads), history and previous velocity
-// fetched through L1 (neighbouring pixels share texels).  HBM bound: 88 B per
+// in shared memory (coalesced float4 loads, issued first and held in registers
+// until the motion-dependent gathers are in flight), history and previous
+// velocity fetched through L1 (neighbouring pixels share texels).  HBM bound: 88 B per
 // pixel (16 current + 8 motion + 16 history + 8 previous motion in; 16 out, 16
 // next history, 8 next previous motion).
 #include <cstring>
@@ -85,8 +86,19 @@ __global__ void __launch_bounds__(TX * TY) k_taa_resolve(TaaImages I) {
     const int x = bx + threadIdx.x, y = by + threadIdx.y;
     const bool inside = x < I.w && y < I.h;
     const size_t pix = inside ? (size_t)y * I.w + x : 0;
-    // this pixel's reprojected history and previous-velocity texels, fetched
-    // before the tile so that all of the thread's loads overlap
+    // the tile's texels first (independent loads, into registers), then this
+    // pixel's motion and its reprojected history and previous-velocity texels
+    constexpr int TN = ((TX + 2) * (TY + 2) + TX * TY - 1) / (TX * TY);
+    float4 tv[TN];
+#pragma unroll
+    for (int q = 0; q < TN; q++) {
+        const int k = t + q * TX * TY;
+        if (k < (TX + 2) * (TY + 2)) {
+            const int ly = k / (TX + 2), lx = k % (TX + 2);
+            const int gx = min(max(bx + lx - 1, 0), I.w - 1), gy = min(max(by + ly - 1, 0), I.h - 1);
+            tv[q] = I.cur[(size_t)gy * I.w + gx];
+        }
+    }
     float2 vel = make_float2(0.0f, 0.0f);
     Bilinear<float4> hb;
     Bilinear<float2> pb;
@@ -99,10 +111,10 @@ __global__ void __launch_bounds__(TX * TY) k_taa_resolve(TaaImages I) {
         hb.fetch(I.hist, I.w, I.h, hx, hy);
         pb.fetch(I.pmot, I.w, I.h, hx, hy);
     }
-    for (int k = t; k < (TX + 2) * (TY + 2); k += TX * TY) {
-        const int ly = k / (TX + 2), lx = k % (TX + 2);
-        const int gx = min(max(bx + lx - 1, 0), I.w - 1), gy = min(max(by + ly - 1, 0), I.h - 1);
-        tile[ly][lx] = I.cur[(size_t)gy * I.w + gx];
+#pragma unroll
+    for (int q = 0; q < TN; q++) {
+        const int k = t + q * TX * TY;
+        if (k < (TX + 2) * (TY + 2)) tile[k / (TX + 2)][k % (TX + 2)] = tv[q];
     }
     __syncthreads();
     if (!inside) return;
