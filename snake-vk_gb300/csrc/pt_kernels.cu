@@ -89,7 +89,10 @@ __device__ __forceinline__ void write_gbuffer_miss(const ViewDev& V, uint32_t o)
     if (V.prim_id) V.prim_id[o] = INVALID;
 }
 
-__global__ void __launch_bounds__(BLK) k_shade(FrameParams F, uint32_t d) {
+// 4 resident blocks per SM (64 registers): the kernel is bound by the latency of
+// its dependent loads (path id -> hit -> triangle -> material), and twice the
+// resident warps of the unconstrained 93-register build outweigh a few spills
+__global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
     const uint32_t cur = d & 1u, nxt = cur ^ 1u;
     const uint32_t n = F.counters[CNT_QUEUE + d];
     const uint32_t lane = threadIdx.x & 31u;

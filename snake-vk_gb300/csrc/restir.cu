@@ -271,7 +271,9 @@ __global__ void __launch_bounds__(RBLK) k_restir_gbuffer(FrameParams F, uint32_t
 }
 
 // WriteInitialReservoirs: initial RIS + temporal reuse
-__global__ void __launch_bounds__(RBLK) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
+// RIS/temporal and spatial passes: 8 resident blocks per SM (64 registers); their
+// light and reservoir loads are latency bound and the extra warps outweigh the spills
+__global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
                                                         RestirQueue q, int phase) {
     const ViewDev& V = F.views[vi];
     const SceneDev& S = F.S;
@@ -405,7 +407,7 @@ __global__ void __launch_bounds__(RBLK) k_restir_initial(FrameParams F, uint32_t
 // phase 0: record q (sun ray, combine rays); phase 1: replay q, write the spatial
 // reservoirs, record qs (final shading rays); phase 2: replay q's sun ray and qs,
 // write radiance, the FP64 accumulator and the next frame's history normals.
-__global__ void __launch_bounds__(RBLK) k_restir_spatial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
+__global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
                                                         RestirQueue q, RestirQueue qs, int phase) {
     const ViewDev& V = F.views[vi];
     const SceneDev& S = F.S;
