@@ -141,6 +141,13 @@ class OracleScene:
         except Exception:
             pass
 
+    def set_instances(self, instances):
+        """Replaces the instance list and rebuilds (as snk_pt_set_instances + snk_pt_build)."""
+        inst = np.ascontiguousarray(instances)
+        self._keep.append(inst)
+        assert lib().snko_set_instances(self._h, _p(inst), len(inst)) == 0
+        assert lib().snko_build(self._h) == 0
+
     def num_local_lights(self) -> int:
         return int(lib().snko_num_local_lights(self._h))
 

@@ -1139,6 +1139,9 @@ static Reservoir restir_initial_temporal(const Scene& S, const View& vw, const S
             const float* pn = &prev_normals[4 * (hy * W + hx)];
             if (dot(load3(pn), g.n) > 0.95f) {
                 Reservoir Hh = history[hy * W + hx];
+                // a history of an earlier scene: lights or instances that no longer exist are dropped
+                if (Hh.pl_idx != INVALID && Hh.pl_idx >= (uint32_t)S.pls.size()) Hh.pl_idx = INVALID;
+                if (Hh.em_inst != INVALID && Hh.em_inst >= (uint32_t)S.insts.size()) Hh.em_inst = INVALID;
                 float mcap = (float)st.restir_mcap;
                 if ((float)Hh.pl_m > mcap * (float)R.pl_m) {
                     Hh.w_sum_pl = Hh.w_sum_pl * ((mcap * (float)R.pl_m) / (float)Hh.pl_m);

@@ -375,6 +375,9 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
                 float4 pn = R.prev_normal[hy * W + hx];
                 if (dot(v3(pn.x, pn.y, pn.z), nrm) > 0.95f) {
                     Reservoir Hh = res_load(R.history, hy * W + hx);
+                    // a history of an earlier scene: lights or instances that no longer exist are dropped
+                    if (Hh.pl_idx != INVALID && Hh.pl_idx >= S.num_point_lights) Hh.pl_idx = INVALID;
+                    if (Hh.em_inst != INVALID && Hh.em_inst >= S.num_instances) Hh.em_inst = INVALID;
                     float mcap = (float)rs.mcap;
                     if ((float)Hh.pl_m > mcap * (float)Rr.pl_m) {
                         Hh.w_sum_pl = Hh.w_sum_pl * ((mcap * (float)Rr.pl_m) / (float)Hh.pl_m);

@@ -154,6 +154,28 @@ def test_restir_config2_frames(cuda, built_lib):
         assert g["radiance"][:, :3].mean() > 0.0
 
 
+def test_restir_history_of_a_larger_scene(cuda, built_lib):
+    """Frames after the instance list shrinks: history reservoirs that point at
+    instances which no longer exist are dropped, on the GPU as in the oracle."""
+    W, H, F = 128, 72, 4
+    sc = scenes.config2(width=W, height=H, frames=F)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    osc = O.OracleScene(sc)
+    ors = O.OracleRestir(osc, W, H)
+    smaller = np.ascontiguousarray(sc.instances[:len(sc.instances) - 4000])   # most emissive quads removed
+    for f in range(F):
+        if f == 2:
+            pt.set_instances(smaller)
+            pt.build()
+            osc.set_instances(smaller)
+        st = abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=f, seed=1)
+        g = _gpu_frame(pt, [sc.views[f]], st, cuda)[0]
+        r, _ = ors.frame(sc.views[f], st)
+        _compare(g, r, f"ReSTIR frame {f}")
+    pt.synchronize()   # no device error
+
+
 def test_launch_knobs_do_not_change_results(cuda, built_lib):
     """Every autotuner candidate must render the same bits (the knobs only move work)."""
     sc = scenes.config1(width=320, height=180)
