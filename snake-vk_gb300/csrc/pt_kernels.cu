@@ -91,154 +91,194 @@ __device__ __forceinline__ void write_gbuffer_miss(const ViewDev& V, uint32_t o)
 
 // 4 resident blocks per SM (64 registers): the kernel is bound by the latency of
 // its dependent loads (path id -> hit -> triangle -> material), and twice the
-// resident warps of the unconstrained 93-register build outweigh a few spills
+// resident warps of the unconstrained 93-register build outweigh a few spills.
+// Misses end in a first pass over each chunk of 32 queue entries (their shadow
+// slots are marked empty and, on the first segment, the G-buffer gets a miss);
+// hits are collected in a per-warp ring in shared memory and shaded 32 at a
+// time, so the surface shading runs with full warps even when most rays of a
+// bounce leave the scene.  Every output is indexed by queue entry or path, so
+// the order in which entries are shaded does not change any result.
 __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
+    __shared__ uint32_t ring[BLK / 32][64];
     const uint32_t cur = d & 1u, nxt = cur ^ 1u;
     const uint32_t n = F.counters[CNT_QUEUE + d];
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp_global = (blockIdx.x * BLK + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * BLK) >> 5;
     const SceneDev& S = F.S;
-    for (uint32_t base = warp_global * 32u; base < n; base += nwarps * 32u) {
-        const uint32_t i = base + lane;
-        bool cont = false, sv0 = false, sv1 = false, query = false;
-        uint32_t p = 0;
-        float4 nr0 = make_float4(0, 0, 0, 0), nr1 = make_float4(0, 0, 0, 0);
-        float4 q0, q1, q2, q3, qb;
-        if (i < n) {
-            p = F.path_ids[cur][i];
-            uint32_t gpix, s, vi, x, y;
-            const bool train = decode_path(F, p, &gpix, &s, &vi, &x, &y);
-            const ViewDev& V = F.views[vi];
-            const uint32_t o = y * V.v.width + x;
-            float4 rd4 = F.rays[cur][2ull * i + 1];
-            V3 rd = v3(rd4.x, rd4.y, rd4.z);
-            HitDev h = F.hits[i];
-            float4* sr = F.shadow_rays + 4ull * i;
-            sr[1].w = -1.0f;
-            sr[3].w = -1.0f;
-            Pcg rng = pcg_stream(gpix, s, d, F.seed);
-            if (d == 0) { pcg_next(rng); pcg_next(rng); }
-            const bool gbuf = d == 0 && s == 0 && !train;
-            if (!h.flags) {
-                if (gbuf) write_gbuffer_miss(V, o);
-            } else {
-                Surface sf = surface_at(S, h.inst, h.prim, h.u, h.v, rd);
-                if (gbuf) write_gbuffer_hit(V, o, sf, h.t, motion_of(S, V.v, sf, x, y));
-                float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
-                float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
-                float u_lobe = pcg_float(rng);
-                float4 b4 = F.beta[p];
-                V3 beta = v3(b4.x, b4.y, b4.z);
-                bool to_cache = false;
-                if (F.cache) {
-                    // path spread (Mueller et al. 2021): a0 = t^2 / (4 pi cos) at the primary
-                    // vertex; later vertices add sqrt(t^2 / (pdf cos)); the path is handed
-                    // to the cache once spread^2 > c a0
-                    float2 sp = F.spread[p];
-                    const float cosv = fmax_(fabsf(dot(sf.n, rd)), 1e-6f);
-                    if (d == 0) sp = make_float2((h.t * h.t) / ((4.0f * PI) * cosv), 0.0f);
-                    else sp.y = sp.y + sqrtf((h.t * h.t) / (fmax_(b4.w, 1e-6f) * cosv));
-                    F.spread[p] = sp;
-                    to_cache = !train && d >= 1 && !(sf.flags & MAT_EMISSIVE) && (sp.y * sp.y > F.spread_c * sp.x);
-                    if (train && d < TRAIN_V && !(sf.flags & MAT_EMISSIVE)) {
-                        const uint32_t slot = (p - F.n_render) * TRAIN_V + d;
-                        float4* r = F.train_rec + 4ull * slot;
-                        r[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, sf.roughness);
-                        r[1] = make_float4(-rd.x, -rd.y, -rd.z, sf.metallic);
-                        r[2] = make_float4(sf.n.x, sf.n.y, sf.n.z, 0.0f);
-                        r[3] = make_float4(sf.albedo.x, sf.albedo.y, sf.albedo.z, 0.0f);
-                        F.train_beta[slot] = make_float4(beta.x, beta.y, beta.z, 1.0f);
-                    }
-                }
-                if (to_cache) {
-                    q0 = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, sf.roughness);
-                    q1 = make_float4(-rd.x, -rd.y, -rd.z, sf.metallic);
-                    q2 = make_float4(sf.n.x, sf.n.y, sf.n.z, 0.0f);
-                    q3 = make_float4(sf.albedo.x, sf.albedo.y, sf.albedo.z, __uint_as_float(p));
-                    qb = make_float4(beta.x, beta.y, beta.z, 0.0f);
-                    query = true;
-                } else if (sf.flags & MAT_EMISSIVE) {
+    uint32_t* hq = ring[threadIdx.x >> 5];
+    uint32_t head = 0, cnt = 0;   // hits waiting in the ring (at most 63)
+    for (uint32_t base = warp_global * 32u;; base += nwarps * 32u) {
+        const bool more = base < n;
+        if (more) {
+            const uint32_t i = base + lane;
+            bool hit = false;
+            if (i < n) {
+                hit = F.hits[i].flags != 0u;
+                if (!hit) {
+                    float4* sr = F.shadow_rays + 4ull * i;
+                    sr[1].w = -1.0f;
+                    sr[3].w = -1.0f;
                     if (d == 0) {
-                        float4 l4 = F.L[p];
-                        V3 Lp = add(v3(l4.x, l4.y, l4.z), cmul(beta, sf.albedo));
-                        F.L[p] = make_float4(Lp.x, Lp.y, Lp.z, 0.0f);
-                    }
-                } else {
-                    V3 v = neg(rd);
-                    V3 f0 = f0_of(sf.albedo, sf.metallic);
-                    V3 xb = add(sf.pos, mul(sf.n, SURFACE_BIAS));
-                    if (S.dir_light.enabled) {
-                        V3 c = calc_directional(load3(S.dir_light.dir), load3(S.dir_light.colour), v, f0, sf.n,
-                                                sf.roughness, sf.metallic, sf.albedo);
-                        if (maxc(c) > 0.0f) {
-                            V3 cb = cmul(beta, c);
-                            sr[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
-                            sr[1] = make_float4(S.dir_light.dir[0], S.dir_light.dir[1], S.dir_light.dir[2], T_FAR);
-                            F.shadow_contrib[2ull * i] = make_float4(cb.x, cb.y, cb.z, 0.0f);
-                            sv0 = true;
-                        }
-                    }
-                    V3 c, ldir;
-                    float ltmax;
-                    if (sample_local(S, sf, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
-                        V3 cb = cmul(beta, c);
-                        sr[2] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
-                        sr[3] = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
-                        F.shadow_contrib[2ull * i + 1] = make_float4(cb.x, cb.y, cb.z, 0.0f);
-                        sv1 = true;
-                    }
-                    bool alive = d + 1 < F.max_depth;
-                    if (alive && d + 1 >= F.rr_depth) {
-                        float ps = fmin_(maxc(beta), 0.95f);
-                        if (u_rr < ps) beta = v3(beta.x / ps, beta.y / ps, beta.z / ps);
-                        else alive = false;
-                    }
-                    if (alive) {
-                        V3 wi, w;
-                        float pdf;
-                        if (sample_continuation(sf, v, f0, u_lobe, u_d1, u_d2, &wi, &w, &pdf)) {
-                            beta = cmul(beta, w);
-                            // w: pdf of the sampled direction, used by the spread heuristic
-                            F.beta[p] = make_float4(beta.x, beta.y, beta.z, pdf);
-                            nr0 = make_float4(xb.x, xb.y, xb.z, EXT_TMIN);
-                            nr1 = make_float4(wi.x, wi.y, wi.z, T_FAR);
-                            cont = true;
+                        uint32_t gpix, s, vi, x, y;
+                        const bool train = decode_path(F, F.path_ids[cur][i], &gpix, &s, &vi, &x, &y);
+                        if (s == 0 && !train) {
+                            const ViewDev& V = F.views[vi];
+                            write_gbuffer_miss(V, y * V.v.width + x);
                         }
                     }
                 }
             }
+            const unsigned hm = __ballot_sync(0xFFFFFFFFu, hit);
+            if (hit) hq[(head + cnt + (uint32_t)__popc(hm & ((1u << lane) - 1u))) & 63u] = i;
+            cnt += (uint32_t)__popc(hm);
+            __syncwarp();
         }
-        // warp-ballot compaction of the continuing paths into the next queue
-        const unsigned full = 0xFFFFFFFFu;
-        unsigned m = __ballot_sync(full, cont);
-        unsigned sm = __popc(__ballot_sync(full, sv0)) + __popc(__ballot_sync(full, sv1));
-        uint32_t slot_base = 0;
-        if (lane == 0) {
-            if (m) slot_base = atomicAdd(&F.counters[CNT_QUEUE + d + 1], (uint32_t)__popc(m));
-            if (sm) atomicAdd(&F.counters[CNT_SHADOW_RAYS], sm);
-        }
-        slot_base = __shfl_sync(full, slot_base, 0);
-        if (cont) {
-            uint32_t j = slot_base + __popc(m & ((1u << lane) - 1u));
-            F.rays[nxt][2ull * j] = nr0;
-            F.rays[nxt][2ull * j + 1] = nr1;
-            F.path_ids[nxt][j] = p;
-        }
-        if (F.cache) {
-            const unsigned qm = __ballot_sync(full, query);
-            uint32_t qbase = 0;
-            if (lane == 0 && qm) qbase = atomicAdd(&F.counters[CNT_CACHE_QUERIES], (uint32_t)__popc(qm));
-            qbase = __shfl_sync(full, qbase, 0);
-            if (query) {
-                const uint32_t j = qbase + __popc(qm & ((1u << lane) - 1u));
-                F.qrec[4ull * j] = q0;
-                F.qrec[4ull * j + 1] = q1;
-                F.qrec[4ull * j + 2] = q2;
-                F.qrec[4ull * j + 3] = q3;
-                F.qbeta[j] = qb;
+        while (cnt >= 32u || (!more && cnt > 0u)) {
+            const uint32_t take = cnt < 32u ? cnt : 32u;
+            const bool have = lane < take;
+            const uint32_t i = have ? hq[(head + lane) & 63u] : 0u;
+            head = (head + take) & 63u;
+            cnt -= take;
+            __syncwarp();
+            bool cont = false, sv0 = false, sv1 = false, query = false;
+            uint32_t p = 0;
+            float4 nr0 = make_float4(0, 0, 0, 0), nr1 = make_float4(0, 0, 0, 0);
+            float4 q0, q1, q2, q3, qb;
+            if (have) {
+                p = F.path_ids[cur][i];
+                uint32_t gpix, s, vi, x, y;
+                const bool train = decode_path(F, p, &gpix, &s, &vi, &x, &y);
+                const ViewDev& V = F.views[vi];
+                const uint32_t o = y * V.v.width + x;
+                float4 rd4 = F.rays[cur][2ull * i + 1];
+                V3 rd = v3(rd4.x, rd4.y, rd4.z);
+                HitDev h = F.hits[i];
+                float4* sr = F.shadow_rays + 4ull * i;
+                sr[1].w = -1.0f;
+                sr[3].w = -1.0f;
+                Pcg rng = pcg_stream(gpix, s, d, F.seed);
+                if (d == 0) { pcg_next(rng); pcg_next(rng); }
+                const bool gbuf = d == 0 && s == 0 && !train;
+                {   // a hit (misses ended in the first pass)
+                    Surface sf = surface_at(S, h.inst, h.prim, h.u, h.v, rd);
+                    if (gbuf) write_gbuffer_hit(V, o, sf, h.t, motion_of(S, V.v, sf, x, y));
+                    float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
+                    float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
+                    float u_lobe = pcg_float(rng);
+                    float4 b4 = F.beta[p];
+                    V3 beta = v3(b4.x, b4.y, b4.z);
+                    bool to_cache = false;
+                    if (F.cache) {
+                        // path spread (Mueller et al. 2021): a0 = t^2 / (4 pi cos) at the primary
+                        // vertex; later vertices add sqrt(t^2 / (pdf cos)); the path is handed
+                        // to the cache once spread^2 > c a0
+                        float2 sp = F.spread[p];
+                        const float cosv = fmax_(fabsf(dot(sf.n, rd)), 1e-6f);
+                        if (d == 0) sp = make_float2((h.t * h.t) / ((4.0f * PI) * cosv), 0.0f);
+                        else sp.y = sp.y + sqrtf((h.t * h.t) / (fmax_(b4.w, 1e-6f) * cosv));
+                        F.spread[p] = sp;
+                        to_cache = !train && d >= 1 && !(sf.flags & MAT_EMISSIVE) && (sp.y * sp.y > F.spread_c * sp.x);
+                        if (train && d < TRAIN_V && !(sf.flags & MAT_EMISSIVE)) {
+                            const uint32_t slot = (p - F.n_render) * TRAIN_V + d;
+                            float4* r = F.train_rec + 4ull * slot;
+                            r[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, sf.roughness);
+                            r[1] = make_float4(-rd.x, -rd.y, -rd.z, sf.metallic);
+                            r[2] = make_float4(sf.n.x, sf.n.y, sf.n.z, 0.0f);
+                            r[3] = make_float4(sf.albedo.x, sf.albedo.y, sf.albedo.z, 0.0f);
+                            F.train_beta[slot] = make_float4(beta.x, beta.y, beta.z, 1.0f);
+                        }
+                    }
+                    if (to_cache) {
+                        q0 = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, sf.roughness);
+                        q1 = make_float4(-rd.x, -rd.y, -rd.z, sf.metallic);
+                        q2 = make_float4(sf.n.x, sf.n.y, sf.n.z, 0.0f);
+                        q3 = make_float4(sf.albedo.x, sf.albedo.y, sf.albedo.z, __uint_as_float(p));
+                        qb = make_float4(beta.x, beta.y, beta.z, 0.0f);
+                        query = true;
+                    } else if (sf.flags & MAT_EMISSIVE) {
+                        if (d == 0) {
+                            float4 l4 = F.L[p];
+                            V3 Lp = add(v3(l4.x, l4.y, l4.z), cmul(beta, sf.albedo));
+                            F.L[p] = make_float4(Lp.x, Lp.y, Lp.z, 0.0f);
+                        }
+                    } else {
+                        V3 v = neg(rd);
+                        V3 f0 = f0_of(sf.albedo, sf.metallic);
+                        V3 xb = add(sf.pos, mul(sf.n, SURFACE_BIAS));
+                        if (S.dir_light.enabled) {
+                            V3 c = calc_directional(load3(S.dir_light.dir), load3(S.dir_light.colour), v, f0, sf.n,
+                                                    sf.roughness, sf.metallic, sf.albedo);
+                            if (maxc(c) > 0.0f) {
+                                V3 cb = cmul(beta, c);
+                                sr[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
+                                sr[1] = make_float4(S.dir_light.dir[0], S.dir_light.dir[1], S.dir_light.dir[2], T_FAR);
+                                F.shadow_contrib[2ull * i] = make_float4(cb.x, cb.y, cb.z, 0.0f);
+                                sv0 = true;
+                            }
+                        }
+                        V3 c, ldir;
+                        float ltmax;
+                        if (sample_local(S, sf, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
+                            V3 cb = cmul(beta, c);
+                            sr[2] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
+                            sr[3] = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
+                            F.shadow_contrib[2ull * i + 1] = make_float4(cb.x, cb.y, cb.z, 0.0f);
+                            sv1 = true;
+                        }
+                        bool alive = d + 1 < F.max_depth;
+                        if (alive && d + 1 >= F.rr_depth) {
+                            float ps = fmin_(maxc(beta), 0.95f);
+                            if (u_rr < ps) beta = v3(beta.x / ps, beta.y / ps, beta.z / ps);
+                            else alive = false;
+                        }
+                        if (alive) {
+                            V3 wi, w;
+                            float pdf;
+                            if (sample_continuation(sf, v, f0, u_lobe, u_d1, u_d2, &wi, &w, &pdf)) {
+                                beta = cmul(beta, w);
+                                // w: pdf of the sampled direction, used by the spread heuristic
+                                F.beta[p] = make_float4(beta.x, beta.y, beta.z, pdf);
+                                nr0 = make_float4(xb.x, xb.y, xb.z, EXT_TMIN);
+                                nr1 = make_float4(wi.x, wi.y, wi.z, T_FAR);
+                                cont = true;
+                            }
+                        }
+                    }
+                }
+            }
+            // warp-ballot compaction of the continuing paths into the next queue
+            const unsigned full = 0xFFFFFFFFu;
+            unsigned m = __ballot_sync(full, cont);
+            unsigned sm = __popc(__ballot_sync(full, sv0)) + __popc(__ballot_sync(full, sv1));
+            uint32_t slot_base = 0;
+            if (lane == 0) {
+                if (m) slot_base = atomicAdd(&F.counters[CNT_QUEUE + d + 1], (uint32_t)__popc(m));
+                if (sm) atomicAdd(&F.counters[CNT_SHADOW_RAYS], sm);
+            }
+            slot_base = __shfl_sync(full, slot_base, 0);
+            if (cont) {
+                uint32_t j = slot_base + __popc(m & ((1u << lane) - 1u));
+                F.rays[nxt][2ull * j] = nr0;
+                F.rays[nxt][2ull * j + 1] = nr1;
+                F.path_ids[nxt][j] = p;
+            }
+            if (F.cache) {
+                const unsigned qm = __ballot_sync(full, query);
+                uint32_t qbase = 0;
+                if (lane == 0 && qm) qbase = atomicAdd(&F.counters[CNT_CACHE_QUERIES], (uint32_t)__popc(qm));
+                qbase = __shfl_sync(full, qbase, 0);
+                if (query) {
+                    const uint32_t j = qbase + __popc(qm & ((1u << lane) - 1u));
+                    F.qrec[4ull * j] = q0;
+                    F.qrec[4ull * j + 1] = q1;
+                    F.qrec[4ull * j + 2] = q2;
+                    F.qrec[4ull * j + 3] = q3;
+                    F.qbeta[j] = qb;
+                }
             }
         }
+        if (!more) break;
     }
 }
 

@@ -281,127 +281,153 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
     const bool record = phase == 0;
     Ctx c;
     c.S = &F.S; c.shadow_rays = 0; c.overflow = false;
-    for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
-        uint32_t o = base + threadIdx.x;
-        if (o >= n) continue;
-        uint32_t x = o % W, y = o / W;
-        ctx_queue(c, q, o, record);
-        float4 gp = R.g_pos[o];
-        if (gp.w != 1.0f) {
+    // background pixels end in a first pass over each warp's 32 pixels; surface
+    // pixels wait in a per-warp ring and are processed 32 at a time
+    __shared__ uint32_t ring[RBLK / 32][64];
+    uint32_t* hq = ring[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t head = 0, cnt = 0;
+    for (uint32_t base = blockIdx.x * RBLK + (threadIdx.x & ~31u);; base += gridDim.x * RBLK) {
+        const bool more = base < n;
+        if (more) {
+            const uint32_t o = base + lane;
+            bool surf = false;
+            if (o < n) {
+                surf = R.g_pos[o].w == 1.0f;
+                if (!surf) {
+                    ctx_queue(c, q, o, record);
+                    if (record) ctx_close(c);
+                    else res_store(R.temporal, o, res_init());
+                }
+            }
+            const unsigned sm = __ballot_sync(0xFFFFFFFFu, surf);
+            if (surf) hq[(head + cnt + (uint32_t)__popc(sm & ((1u << lane) - 1u))) & 63u] = o;
+            cnt += (uint32_t)__popc(sm);
+            __syncwarp();
+        }
+        while (cnt >= 32u || (!more && cnt > 0u)) {
+            const uint32_t take = cnt < 32u ? cnt : 32u;
+            const bool have = lane < take;
+            const uint32_t o = have ? hq[(head + lane) & 63u] : 0u;
+            head = (head + take) & 63u;
+            cnt -= take;
+            __syncwarp();
+            if (!have) continue;
+            uint32_t x = o % W, y = o / W;
+            ctx_queue(c, q, o, record);
+            float4 gp = R.g_pos[o];
+            float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
+            V3 nrm = v3(gn.x, gn.y, gn.z);
+            Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
+            Pcg rng;
+            Reservoir Rr;
+            float phat_pl = 0.0f, phat_em = 0.0f;
+            if (!record) {
+                // the RIS result of the recording run: reservoir, target values and stream position
+                Rr = res_load(R.temporal, o);
+                const float4 a = R.ris[2ull * o], b = R.ris[2ull * o + 1];
+                phat_pl = a.x; phat_em = a.y;
+                rng.state = ((uint64_t)__float_as_uint(b.y) << 32) | __float_as_uint(b.x);
+                rng.inc = ((uint64_t)__float_as_uint(b.w) << 32) | __float_as_uint(b.z);
+            } else {
+                rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000001u, rs.seed);
+                Rr = res_init();
+                const uint32_t npl = S.num_point_lights;
+                if (npl > 0) {
+                    for (uint32_t i = 0; i < rs.candidates; i++) {
+                        uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
+                        if (idx > npl - 1) idx = npl - 1;
+                        float p_hat = length(calc_pointlight(S.point_lights[idx], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
+                                                             sh.albedo));
+                        float w = p_hat / (1.0f / (float)npl);
+                        if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
+                    }
+                }
+                const uint32_t nem = S.num_emissive_instances;
+                if (nem > 0) {
+                    for (uint32_t i = 0; i < rs.candidates; i++) {
+                        uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
+                        if (k > nem - 1) k = nem - 1;
+                        uint32_t inst = S.emissive_instances[k];
+                        const InstShade& I = S.inst_shade[inst];
+                        const MeshInfo& M = S.meshes[I.mesh_id];
+                        uint32_t ntri = M.num_triangles;
+                        uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
+                        if (tri > ntri - 1) tri = ntri - 1;
+                        float bu = pcg_float(rng), bv = pcg_float(rng);
+                        if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
+                        const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
+                        V3 p0 = load3(S.positions + 3ull * (M.vertex_offset + ix[0]));
+                        V3 p1 = load3(S.positions + 3ull * (M.vertex_offset + ix[1]));
+                        V3 p2 = load3(S.positions + 3ull * (M.vertex_offset + ix[2]));
+                        float area = (I.det3 * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
+                        V3 rad = tri_radiance(c, inst, tri, bu, bv, sh, false);
+                        float p_hat = length(rad);
+                        float pdf = 1.0f / ((float)(nem * ntri) * area);
+                        float w = p_hat / pdf;
+                        if (update_em(Rr, inst, tri, bu, bv, w, rng)) phat_em = p_hat;
+                    }
+                }
+                res_store(R.temporal, o, Rr);
+                R.ris[2ull * o] = make_float4(phat_pl, phat_em, 0.0f, 0.0f);
+                R.ris[2ull * o + 1] =
+                    make_float4(__uint_as_float((uint32_t)rng.state), __uint_as_float((uint32_t)(rng.state >> 32)),
+                                __uint_as_float((uint32_t)rng.inc), __uint_as_float((uint32_t)(rng.inc >> 32)));
+            }
+            if (Rr.pl_idx != INVALID) {
+                V3 lp = load3(S.point_lights[Rr.pl_idx].pos);
+                float dist = length(sub(lp, sh.biased));
+                float vis = shadow_test(c, sh.biased, divs(sub(lp, sh.biased), dist), dist);
+                Rr.w_pl = vis * ((Rr.w_sum_pl / (float)Rr.pl_m) / phat_pl);
+            } else {
+                Rr.w_pl = 0.0f;
+            }
+            if (Rr.em_inst != INVALID) {
+                float vis = tri_shadow(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh.biased);
+                Rr.w_em = vis * ((Rr.w_sum_em / (float)Rr.m_em) / phat_em);
+            } else {
+                Rr.w_em = 0.0f;
+            }
+            Reservoir out = Rr;
+            if (R.history_valid && rs.temporal != 0 && V.v.prev_valid) {
+                float hu = ((float)x + 0.5f) / (float)W + gm.y;
+                float hv = ((float)y + 0.5f) / (float)H + gm.z;
+                if (hu > 0.0f && hv > 0.0f && hu < 1.0f && hv < 1.0f) {
+                    uint32_t hx = (uint32_t)(hu * (float)W), hy = (uint32_t)(hv * (float)H);
+                    if (hx > W - 1) hx = W - 1;
+                    if (hy > H - 1) hy = H - 1;
+                    float4 pn = R.prev_normal[hy * W + hx];
+                    if (dot(v3(pn.x, pn.y, pn.z), nrm) > 0.95f) {
+                        Reservoir Hh = res_load(R.history, hy * W + hx);
+                        // a history of an earlier scene: lights or instances that no longer exist are dropped
+                        if (Hh.pl_idx != INVALID && Hh.pl_idx >= S.num_point_lights) Hh.pl_idx = INVALID;
+                        if (Hh.em_inst != INVALID && Hh.em_inst >= S.num_instances) Hh.em_inst = INVALID;
+                        float mcap = (float)rs.mcap;
+                        if ((float)Hh.pl_m > mcap * (float)Rr.pl_m) {
+                            Hh.w_sum_pl = Hh.w_sum_pl * ((mcap * (float)Rr.pl_m) / (float)Hh.pl_m);
+                            Hh.pl_m = rs.mcap * Rr.pl_m;
+                        }
+                        if ((float)Hh.m_em > mcap * (float)Rr.m_em) {
+                            Hh.w_sum_em = Hh.w_sum_em * ((mcap * (float)Rr.m_em) / (float)Hh.m_em);
+                            Hh.m_em = rs.mcap * Rr.m_em;
+                        }
+                        Reservoir T = res_init();
+                        float tp_pl = 0.0f, tp_em = 0.0f;
+                        combine(c, T, Rr, tp_pl, tp_em, sh, rng);
+                        combine(c, T, Hh, tp_pl, tp_em, sh, rng);
+                        T.m_em = Hh.m_em + Rr.m_em;
+                        T.pl_m = Hh.pl_m + Rr.pl_m;
+                        T.w_em = tp_em > 0.0f ? (T.w_sum_em / (float)T.m_em) / tp_em : 0.0f;
+                        T.w_pl = tp_pl > 0.0f ? (T.w_sum_pl / (float)T.pl_m) / tp_pl : 0.0f;
+                        out = T;
+                    }
+                }
+            }
+            ctx_check(c);
             if (record) ctx_close(c);
-            else res_store(R.temporal, o, res_init());
-            continue;
+            else res_store(R.temporal, o, out);
         }
-        float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
-        V3 nrm = v3(gn.x, gn.y, gn.z);
-        Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
-        Pcg rng;
-        Reservoir Rr;
-        float phat_pl = 0.0f, phat_em = 0.0f;
-        if (!record) {
-            // the RIS result of the recording run: reservoir, target values and stream position
-            Rr = res_load(R.temporal, o);
-            const float4 a = R.ris[2ull * o], b = R.ris[2ull * o + 1];
-            phat_pl = a.x; phat_em = a.y;
-            rng.state = ((uint64_t)__float_as_uint(b.y) << 32) | __float_as_uint(b.x);
-            rng.inc = ((uint64_t)__float_as_uint(b.w) << 32) | __float_as_uint(b.z);
-        } else {
-            rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000001u, rs.seed);
-            Rr = res_init();
-            const uint32_t npl = S.num_point_lights;
-            if (npl > 0) {
-                for (uint32_t i = 0; i < rs.candidates; i++) {
-                    uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
-                    if (idx > npl - 1) idx = npl - 1;
-                    float p_hat = length(calc_pointlight(S.point_lights[idx], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
-                                                         sh.albedo));
-                    float w = p_hat / (1.0f / (float)npl);
-                    if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
-                }
-            }
-            const uint32_t nem = S.num_emissive_instances;
-            if (nem > 0) {
-                for (uint32_t i = 0; i < rs.candidates; i++) {
-                    uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
-                    if (k > nem - 1) k = nem - 1;
-                    uint32_t inst = S.emissive_instances[k];
-                    const InstShade& I = S.inst_shade[inst];
-                    const MeshInfo& M = S.meshes[I.mesh_id];
-                    uint32_t ntri = M.num_triangles;
-                    uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
-                    if (tri > ntri - 1) tri = ntri - 1;
-                    float bu = pcg_float(rng), bv = pcg_float(rng);
-                    if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
-                    const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
-                    V3 p0 = load3(S.positions + 3ull * (M.vertex_offset + ix[0]));
-                    V3 p1 = load3(S.positions + 3ull * (M.vertex_offset + ix[1]));
-                    V3 p2 = load3(S.positions + 3ull * (M.vertex_offset + ix[2]));
-                    float area = (I.det3 * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
-                    V3 rad = tri_radiance(c, inst, tri, bu, bv, sh, false);
-                    float p_hat = length(rad);
-                    float pdf = 1.0f / ((float)(nem * ntri) * area);
-                    float w = p_hat / pdf;
-                    if (update_em(Rr, inst, tri, bu, bv, w, rng)) phat_em = p_hat;
-                }
-            }
-            res_store(R.temporal, o, Rr);
-            R.ris[2ull * o] = make_float4(phat_pl, phat_em, 0.0f, 0.0f);
-            R.ris[2ull * o + 1] =
-                make_float4(__uint_as_float((uint32_t)rng.state), __uint_as_float((uint32_t)(rng.state >> 32)),
-                            __uint_as_float((uint32_t)rng.inc), __uint_as_float((uint32_t)(rng.inc >> 32)));
-        }
-        if (Rr.pl_idx != INVALID) {
-            V3 lp = load3(S.point_lights[Rr.pl_idx].pos);
-            float dist = length(sub(lp, sh.biased));
-            float vis = shadow_test(c, sh.biased, divs(sub(lp, sh.biased), dist), dist);
-            Rr.w_pl = vis * ((Rr.w_sum_pl / (float)Rr.pl_m) / phat_pl);
-        } else {
-            Rr.w_pl = 0.0f;
-        }
-        if (Rr.em_inst != INVALID) {
-            float vis = tri_shadow(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh.biased);
-            Rr.w_em = vis * ((Rr.w_sum_em / (float)Rr.m_em) / phat_em);
-        } else {
-            Rr.w_em = 0.0f;
-        }
-        Reservoir out = Rr;
-        if (R.history_valid && rs.temporal != 0 && V.v.prev_valid) {
-            float hu = ((float)x + 0.5f) / (float)W + gm.y;
-            float hv = ((float)y + 0.5f) / (float)H + gm.z;
-            if (hu > 0.0f && hv > 0.0f && hu < 1.0f && hv < 1.0f) {
-                uint32_t hx = (uint32_t)(hu * (float)W), hy = (uint32_t)(hv * (float)H);
-                if (hx > W - 1) hx = W - 1;
-                if (hy > H - 1) hy = H - 1;
-                float4 pn = R.prev_normal[hy * W + hx];
-                if (dot(v3(pn.x, pn.y, pn.z), nrm) > 0.95f) {
-                    Reservoir Hh = res_load(R.history, hy * W + hx);
-                    // a history of an earlier scene: lights or instances that no longer exist are dropped
-                    if (Hh.pl_idx != INVALID && Hh.pl_idx >= S.num_point_lights) Hh.pl_idx = INVALID;
-                    if (Hh.em_inst != INVALID && Hh.em_inst >= S.num_instances) Hh.em_inst = INVALID;
-                    float mcap = (float)rs.mcap;
-                    if ((float)Hh.pl_m > mcap * (float)Rr.pl_m) {
-                        Hh.w_sum_pl = Hh.w_sum_pl * ((mcap * (float)Rr.pl_m) / (float)Hh.pl_m);
-                        Hh.pl_m = rs.mcap * Rr.pl_m;
-                    }
-                    if ((float)Hh.m_em > mcap * (float)Rr.m_em) {
-                        Hh.w_sum_em = Hh.w_sum_em * ((mcap * (float)Rr.m_em) / (float)Hh.m_em);
-                        Hh.m_em = rs.mcap * Rr.m_em;
-                    }
-                    Reservoir T = res_init();
-                    float tp_pl = 0.0f, tp_em = 0.0f;
-                    combine(c, T, Rr, tp_pl, tp_em, sh, rng);
-                    combine(c, T, Hh, tp_pl, tp_em, sh, rng);
-                    T.m_em = Hh.m_em + Rr.m_em;
-                    T.pl_m = Hh.pl_m + Rr.pl_m;
-                    T.w_em = tp_em > 0.0f ? (T.w_sum_em / (float)T.m_em) / tp_em : 0.0f;
-                    T.w_pl = tp_pl > 0.0f ? (T.w_sum_pl / (float)T.pl_m) / tp_pl : 0.0f;
-                    out = T;
-                }
-            }
-        }
-        ctx_check(c);
-        if (record) ctx_close(c);
-        else res_store(R.temporal, o, out);
+        if (!more) break;
     }
     flush_rays(c.shadow_rays, &F.counters[CNT_SHADOW_RAYS]);
 }
@@ -417,24 +443,66 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
     Ctx c;
     c.S = &F.S; c.shadow_rays = 0; c.overflow = false;
-    for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
-        uint32_t o = base + threadIdx.x;
-        if (o >= n) continue;
-        uint32_t x = o % W, y = o / W;
-        float4 gp = R.g_pos[o];
-        float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
-        ctx_queue(c, q, o, phase == 0);
-        V3 colour;
-        if (gp.w != 1.0f) {
-            if (phase == 0) { ctx_close(c); continue; }
-            if (phase == 1) {
-                res_store(R.spatial, o, res_init());
-                ctx_queue(c, qs, o, true);
-                ctx_close(c);
-                continue;
+    // radiance, FP64 accumulation and the next frame's history normal of pixel o
+    auto write_out = [&](uint32_t o, V3 colour, float4 hist_normal) {
+        float4 r4 = make_float4(colour.x, colour.y, colour.z, 1.0f);
+        if (V.radiance) V.radiance[o] = r4;
+        if (F.accumulate && vi == 0) {
+            double2 a0 = F.accum[2ull * o], a1 = F.accum[2ull * o + 1];
+            a0.x += (double)r4.x; a0.y += (double)r4.y; a1.x += (double)r4.z; a1.y += 1.0;
+            F.accum[2ull * o] = a0;
+            F.accum[2ull * o + 1] = a1;
+        }
+        // this frame's normals become the next frame's history normals (the
+        // initial pass of this frame has already consumed the previous ones)
+        R.prev_normal[o] = hist_normal;
+    };
+    // background pixels end in a first pass over each warp's 32 pixels; surface
+    // pixels wait in a per-warp ring and are processed 32 at a time
+    __shared__ uint32_t ring[RBLK / 32][64];
+    uint32_t* hq = ring[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t head = 0, cnt = 0;
+    for (uint32_t base = blockIdx.x * RBLK + (threadIdx.x & ~31u);; base += gridDim.x * RBLK) {
+        const bool more = base < n;
+        if (more) {
+            const uint32_t o = base + lane;
+            bool surf = false;
+            if (o < n) {
+                const float4 gp = R.g_pos[o];
+                surf = gp.w == 1.0f;
+                if (!surf) {
+                    ctx_queue(c, q, o, phase == 0);
+                    if (phase == 0) {
+                        ctx_close(c);
+                    } else if (phase == 1) {
+                        res_store(R.spatial, o, res_init());
+                        ctx_queue(c, qs, o, true);
+                        ctx_close(c);
+                    } else {
+                        const float4 ga = R.g_albedo[o];
+                        write_out(o, gp.w == 2.0f ? v3(ga.x, ga.y, ga.z) : v3(0.0f, 0.0f, 0.0f),
+                                  make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+                    }
+                }
             }
-            colour = gp.w == 2.0f ? v3(ga.x, ga.y, ga.z) : v3(0.0f, 0.0f, 0.0f);
-        } else {
+            const unsigned sm = __ballot_sync(0xFFFFFFFFu, surf);
+            if (surf) hq[(head + cnt + (uint32_t)__popc(sm & ((1u << lane) - 1u))) & 63u] = o;
+            cnt += (uint32_t)__popc(sm);
+            __syncwarp();
+        }
+        while (cnt >= 32u || (!more && cnt > 0u)) {
+            const uint32_t take = cnt < 32u ? cnt : 32u;
+            const bool have = lane < take;
+            const uint32_t o = have ? hq[(head + lane) & 63u] : 0u;
+            head = (head + take) & 63u;
+            cnt -= take;
+            __syncwarp();
+            if (!have) continue;
+            uint32_t x = o % W, y = o / W;
+            float4 gp = R.g_pos[o];
+            float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
+            ctx_queue(c, q, o, phase == 0);
             V3 nrm = v3(gn.x, gn.y, gn.z);
             Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
             V3 light = v3(0.0f, 0.0f, 0.0f);
@@ -497,19 +565,9 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
             }
             ctx_check(c);
             if (phase == 1) { ctx_close(c); continue; }
-            colour = add(light, rad);
+            write_out(o, add(light, rad), make_float4(gn.x, gn.y, gn.z, 0.0f));
         }
-        float4 r4 = make_float4(colour.x, colour.y, colour.z, 1.0f);
-        if (V.radiance) V.radiance[o] = r4;
-        if (F.accumulate && vi == 0) {
-            double2 a0 = F.accum[2ull * o], a1 = F.accum[2ull * o + 1];
-            a0.x += (double)r4.x; a0.y += (double)r4.y; a1.x += (double)r4.z; a1.y += 1.0;
-            F.accum[2ull * o] = a0;
-            F.accum[2ull * o + 1] = a1;
-        }
-        // this frame's normals become the next frame's history normals (the
-        // initial pass of this frame has already consumed the previous ones)
-        R.prev_normal[o] = gp.w == 1.0f ? make_float4(gn.x, gn.y, gn.z, 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!more) break;
     }
     flush_rays(c.shadow_rays, &F.counters[CNT_SHADOW_RAYS]);
 }
