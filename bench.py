@@ -356,6 +356,49 @@ def particle_bench(pt, abi, scene, device, n=100_000, steps=20, warmup=3):
             "note": "wall clock around the C-ABI call (synchronising), device buffers"}
 
 
+def bvh_bench(snkpt, scenes, device, stream, reps=3):
+    """BVH builds (wall clock around synchronising C-ABI calls, median of reps):
+    the mesh BVHs of config 3 (a 131,072-triangle terrain tile and a 1,280-triangle
+    icosphere: Morton sort, hierarchy, 3 treelet passes, 8-wide collapse) from
+    uploaded meshes, and one per-frame instance-BVH rebuild (set_instances + build)
+    at config 1's 201 instances (single-launch builder) and config 2's 4,297
+    instances (multi-launch builder)."""
+    import torch
+    sc3 = scenes.config3(resolutions=[(64, 36)])
+    tris = int(sum(m.num_triangles for m in sc3.meshes))
+    mesh_ms = []
+    for _ in range(reps):
+        pt = snkpt.PathTracer(device.index or 0, stream=stream)
+        pt.upload_meshes(sc3.meshes)
+        pt.set_materials(sc3.materials)
+        pt.set_lights(sc3.dir_light, sc3.point_lights)
+        pt.set_instances(sc3.instances[:1])
+        pt.synchronize()
+        t0 = time.perf_counter()
+        pt.build()
+        pt.synchronize()
+        mesh_ms.append((time.perf_counter() - t0) * 1e3)
+        del pt
+    out = {"mesh_bvh": {"workload": "config 3 meshes: 131,072 + 1,280 triangles", "triangles": tris,
+                        "ms": float(np.median(mesh_ms)), "Mtris_per_s": tris / (float(np.median(mesh_ms)) / 1e3) / 1e6}}
+    for name, sc in (("instance_bvh_201", scenes.config1(width=64, height=36)),
+                     ("instance_bvh_4297", scenes.config2(width=64, height=36, frames=1))):
+        pt = snkpt.PathTracer(device.index or 0, stream=stream)
+        pt.load_scene(sc)
+        inst = np.ascontiguousarray(sc.instances)
+        for _ in range(3):
+            pt.set_instances(inst); pt.build(); pt.synchronize()
+        ms = []
+        for _ in range(20):
+            t0 = time.perf_counter()
+            pt.set_instances(inst); pt.build(); pt.synchronize()
+            ms.append((time.perf_counter() - t0) * 1e3)
+        out[name] = {"instances": len(inst), "ms_per_rebuild": float(np.median(ms))}
+        del pt
+    torch.cuda.synchronize()
+    return out
+
+
 def restir_bench(snkpt, abi, scenes, device, stream, tuning, frames=16, warmup=3):
     """ReSTIR DI on the stress scene (config 2: the 1080p sphere field + 4096
     emissive quads, camera moving 0.05 units per frame): per frame the G-buffer
@@ -587,6 +630,7 @@ def run_ours(args):
         line["taa"] = taa_bench(snkpt, dev, stream)
         line["particles"] = particle_bench(pt, abi, sc, dev)
         line["restir"] = restir_bench(snkpt, abi, scenes, dev, stream, tuning)
+        line["bvh_build"] = bvh_bench(snkpt, scenes, dev, stream)
         if not args.no_batched:
             line["batched_views"] = batched_views(snkpt, abi, scenes, dev, stream, tuning)
             line["batched_views_small"] = batched_views(snkpt, abi, scenes, dev, stream, tuning, frames=20, scale=8)

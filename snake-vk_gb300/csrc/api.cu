@@ -461,11 +461,11 @@ Status build_instances(snk_pt_ctx* ctx) {
             ctx->tlas_prim_count = n;
             return Status::Ok();
         } else {
-            BuildResult br;
-            SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
-                                   ctx->d_prim_order.p, st, &br, passes, leaf_size(ctx->tune.tlas_leaf_max, 1),
-                                   leaf_size(ctx->tune.tlas_leaf_max, 1)));
-            ctx->tlas_nodes = br.num_nodes;
+            // multi-launch build, also without a host round trip (node count bounded by n + 1)
+            SNK_TRY(build_wide_bvh_device(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
+                                          ctx->d_prim_order.p, ctx->d_err.p, st, passes,
+                                          leaf_size(ctx->tune.tlas_leaf_max, 1), leaf_size(ctx->tune.tlas_leaf_max, 1)));
+            ctx->tlas_nodes = n + 1;
             ctx->tlas_small = false;
             ctx->tlas_builds++;
         }

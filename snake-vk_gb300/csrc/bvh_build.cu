@@ -674,11 +674,14 @@ __device__ __forceinline__ unsigned order_f(float f) {
 
 // collapse_task for a whole warp (every lane passes the same task): the same
 // greedy choices, made with warp reductions instead of one thread's loops.
+// counters: [2] wide nodes, [3] primitive slots, [4] capacity error bits;
+// next_tasks counts the child tasks queued in tasks_out.
 // Lane k < nc holds candidate child k while the node is opened; the 64 (child,
 // slot) pairs p = 8k + s of the slot assignment are spread two per lane; lane s
 // < 8 then builds slot s.  Ties go to the lowest child / pair index, as in the
 // sequential loops.  stage: this warp's 80-byte staging node in shared memory.
-__device__ void collapse_task_warp(uint2 task, uint32_t* counters, uint2* tasks_out, int n, const int2* children,
+__device__ void collapse_task_warp(uint2 task, uint32_t* counters, uint32_t* next_tasks, uint2* tasks_out, int n,
+                                   const int2* children,
                                    const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count,
                                    const uint32_t* sorted, WideNode* nodes, WideNode* stage, uint32_t node_base,
                                    uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack) {
@@ -777,7 +780,7 @@ __device__ void collapse_task_warp(uint2 task, uint32_t* counters, uint2* tasks_
         if (lane == 0) atomicOr(&counters[4], 1u);
         return;
     }
-    if (lane == 0 && n_int) task_base = atomicAdd(&counters[1], n_int);
+    if (lane == 0 && n_int) task_base = atomicAdd(next_tasks, n_int);
     task_base = __shfl_sync(FULL, task_base, 0);
     const QuantFrame F = quant_frame(plo, phi);
     if (lane == 0) {
@@ -1071,9 +1074,9 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
                 wide_box[2 * local + 1] = S.node_hi[task.x];
                 wide_depth[local] = (uint32_t)level;
             }
-            collapse_task_warp(task, S.counters, S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi, S.leaf_count,
-                               S.vals, nodes, &S.stage[tid >> 5], node_base, prim_base, prim_order, leaf_max,
-                               leaf_max);
+            collapse_task_warp(task, S.counters, &S.counters[1], S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
+                               S.leaf_count, S.vals, nodes, &S.stage[tid >> 5], node_base, prim_base, prim_order,
+                               leaf_max, leaf_max);
         }
         __syncthreads();
         if (tid == 0) { S.counters[0] = S.counters[1]; S.counters[1] = 0u; }
@@ -1092,6 +1095,66 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
         out->lo[0] = rlo.x; out->lo[1] = rlo.y; out->lo[2] = rlo.z; out->lo[3] = 0.0f;
         out->hi[0] = rhi.x; out->hi[1] = rhi.y; out->hi[2] = rhi.z; out->hi[3] = 0.0f;
         if (e && err_word) atomicOr(err_word, 8u);
+    }
+}
+
+// ---- collapse without host round trips (multi-launch builds of per-frame trees) ----------
+// level_tasks[l] counts the tasks of wide level l (tasks of even levels in
+// tasks_a, odd levels in tasks_b); counters: [2] wide nodes, [3] primitive
+// slots, [4] capacity error bits.  A few launches of k_collapse_level take the
+// usual depths with every SM; k_collapse_finish takes whatever is left in one
+// block, so no level count has to come back to the host.
+constexpr int COLLAPSE_MAX_LEVELS = 128;
+constexpr int COLLAPSE_FAST_LEVELS = 8;
+constexpr int LEVEL_WARPS = 8;
+
+__global__ void k_collapse_init(uint2* tasks_a, uint32_t* counters, uint32_t* level_tasks, uint32_t node_base) {
+    for (int l = threadIdx.x; l <= COLLAPSE_MAX_LEVELS; l += blockDim.x) level_tasks[l] = l == 0 ? 1u : 0u;
+    if (threadIdx.x == 0) {
+        tasks_a[0] = make_uint2(0u, node_base);
+        counters[2] = 1u;
+        counters[3] = 0u;
+        counters[4] = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(32 * LEVEL_WARPS) k_collapse_level(
+    int level, uint2* tasks_a, uint2* tasks_b, uint32_t* level_tasks, uint32_t* counters, int n, const int2* children,
+    const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count, const uint32_t* sorted, WideNode* nodes,
+    uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack) {
+    __shared__ WideNode stage[LEVEL_WARPS];
+    const uint32_t nin = min(level_tasks[level], (uint32_t)n);   // the task arrays hold n entries
+    if (nin == 0 || counters[4] != 0u) return;
+    const uint2* tin = (level & 1) ? tasks_b : tasks_a;
+    uint2* tout = (level & 1) ? tasks_a : tasks_b;
+    const uint32_t w = threadIdx.x >> 5;
+    for (uint32_t t = blockIdx.x * LEVEL_WARPS + w; t < nin; t += gridDim.x * LEVEL_WARPS)
+        collapse_task_warp(tin[t], counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi, leaf_count,
+                           sorted, nodes, &stage[w], node_base, prim_base, prim_order, leaf_max, leaf_pack);
+}
+
+__global__ void __launch_bounds__(1024) k_collapse_finish(
+    int first_level, uint2* tasks_a, uint2* tasks_b, uint32_t* level_tasks, uint32_t* counters, int n,
+    const int2* children, const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count,
+    const uint32_t* sorted, WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
+    uint32_t leaf_max, uint32_t leaf_pack, unsigned* err_word) {
+    __shared__ WideNode stage[32];
+    const uint32_t w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int level = first_level;
+    for (; level < COLLAPSE_MAX_LEVELS; level++) {
+        const uint32_t nin = min(level_tasks[level], (uint32_t)n);
+        if (nin == 0 || counters[4] != 0u) break;
+        const uint2* tin = (level & 1) ? tasks_b : tasks_a;
+        uint2* tout = (level & 1) ? tasks_a : tasks_b;
+        for (uint32_t t = w; t < nin; t += nw)
+            collapse_task_warp(tin[t], counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi,
+                               leaf_count, sorted, nodes, &stage[w], node_base, prim_base, prim_order, leaf_max,
+                               leaf_pack);
+        __syncthreads();   // this level's child tasks and their count are complete
+    }
+    if (threadIdx.x == 0) {
+        const bool unfinished = level >= COLLAPSE_MAX_LEVELS && level_tasks[COLLAPSE_MAX_LEVELS] != 0u;
+        if ((counters[4] != 0u || unfinished || counters[3] != (uint32_t)n) && err_word) atomicOr(err_word, 8u);
     }
 }
 
@@ -1223,9 +1286,12 @@ inline unsigned grid_for(uint32_t n) { return (n + BLK - 1) / BLK; }
 
 }  // namespace
 
-Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
-                      uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t st,
-                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack) {
+namespace {
+// the binary tree of build_wide_bvh and build_wide_bvh_device (Morton codes, radix
+// sort, Karras hierarchy, bottom-up boxes, treelet passes); *sorted_out receives
+// the primitive of each sorted position
+Status build_binary_tree(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, cudaStream_t st,
+                         int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack, const uint32_t** sorted_out) {
     if (leaf_max < 1 || leaf_max > LEAF_MAX_LIMIT || leaf_pack < leaf_max || leaf_pack > LEAF_MAX_LIMIT)
         return Status::Err(1, "build_wide_bvh: leaf size out of range");
     if (n == 0) return Status::Err(1, "build_wide_bvh: no primitives");
@@ -1261,6 +1327,7 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
     SNK_TRY_CUDA(cub::DeviceRadixSort::SortPairs(sc.cub_tmp.p, tmp_bytes, dk, dv, (int)n, 0, 63, st));
     const unsigned long long* keys = dk.Current();
     const uint32_t* sorted = dv.Current();
+    *sorted_out = sorted;
 
     SNK_TRY_CUDA(cudaMemsetAsync(sc.flags.p, 0, sizeof(int) * n, st));
     int minus1 = -1;
@@ -1277,7 +1344,15 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
             SNK_TRY_CUDA(cudaGetLastError());
         }
     }
+    return Status::Ok();
+}
+}  // namespace
 
+Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
+                      uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t st,
+                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack) {
+    const uint32_t* sorted = nullptr;
+    SNK_TRY(build_binary_tree(sc, prim_lo, prim_hi, n, st, treelet_passes, leaf_max, leaf_pack, &sorted));
     float4 rlo, rhi;
     SNK_TRY_CUDA(cudaMemcpyAsync(&rlo, sc.node_lo.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
     SNK_TRY_CUDA(cudaMemcpyAsync(&rhi, sc.node_hi.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
@@ -1318,6 +1393,30 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
     out->sah = 1.0 + sah;
     out->lo[0] = rlo.x; out->lo[1] = rlo.y; out->lo[2] = rlo.z;
     out->hi[0] = rhi.x; out->hi[1] = rhi.y; out->hi[2] = rhi.z;
+    return Status::Ok();
+}
+
+Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n,
+                             WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
+                             unsigned* err_word, cudaStream_t st, int treelet_passes, uint32_t leaf_max,
+                             uint32_t leaf_pack) {
+    const uint32_t* sorted = nullptr;
+    SNK_TRY(build_binary_tree(sc, prim_lo, prim_hi, n, st, treelet_passes, leaf_max, leaf_pack, &sorted));
+    SNK_TRY_CUDA(sc.level_tasks.reserve(COLLAPSE_MAX_LEVELS + 1));
+    k_collapse_init<<<1, 128, 0, st>>>(sc.tasks_a.p, sc.counters.p, sc.level_tasks.p, node_base);
+    // enough warps for the widest level of a typical tree, at most 1024 blocks
+    uint32_t grid = (n + 8u * LEVEL_WARPS - 1u) / (8u * LEVEL_WARPS);
+    grid = grid < 1u ? 1u : (grid > 1024u ? 1024u : grid);
+    for (int level = 0; level < COLLAPSE_FAST_LEVELS; level++)
+        k_collapse_level<<<grid, 32 * LEVEL_WARPS, 0, st>>>(level, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
+                                                            sc.counters.p, (int)n, sc.children.p, sc.node_lo.p,
+                                                            sc.node_hi.p, sc.leaf_count.p, sorted, nodes, node_base,
+                                                            prim_base, prim_order, leaf_max, leaf_pack);
+    k_collapse_finish<<<1, 1024, 0, st>>>(COLLAPSE_FAST_LEVELS, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
+                                          sc.counters.p, (int)n, sc.children.p, sc.node_lo.p, sc.node_hi.p,
+                                          sc.leaf_count.p, sorted, nodes, node_base, prim_base, prim_order, leaf_max,
+                                          leaf_pack, err_word);
+    SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }
 

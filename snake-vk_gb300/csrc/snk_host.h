@@ -76,6 +76,7 @@ struct BuildScratch {
     DBuf<unsigned> cbounds;       // centroid bounds, order-preserving encoded
     DBuf<unsigned char> cub_tmp;
     DBuf<double> sah;             // SAH accumulator
+    DBuf<uint32_t> level_tasks;   // task count per wide level (device-driven collapse)
     size_t cap = 0;
 };
 
@@ -92,6 +93,15 @@ struct BuildResult {
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t stream,
                       BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack);
+
+// The same tree without host round trips (for per-frame rebuilds): the collapse
+// runs level by level on the device, nothing is read back, and a build error
+// (never seen for a correct tree) sets bit 8 of *err_word.  The node count is
+// not reported; at most n + 1 nodes are written.
+Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n,
+                             WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
+                             unsigned* err_word, cudaStream_t stream, int treelet_passes, uint32_t leaf_max,
+                             uint32_t leaf_pack);
 
 // Single-launch build for n <= SMALL_BUILD_MAX primitives (one CTA, shared
 // memory, no host synchronisation); same algorithm and output layout as
