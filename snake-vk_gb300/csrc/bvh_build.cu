@@ -1407,12 +1407,17 @@ Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const floa
     // enough warps for the widest level of a typical tree, at most 1024 blocks
     uint32_t grid = (n + 8u * LEVEL_WARPS - 1u) / (8u * LEVEL_WARPS);
     grid = grid < 1u ? 1u : (grid > 1024u ? 1024u : grid);
-    for (int level = 0; level < COLLAPSE_FAST_LEVELS; level++)
+    // multi-block launches for about the depth of a balanced 8-wide tree; deeper
+    // levels (unbalanced trees) go to the single-block finish
+    int fast = 1;
+    for (uint64_t cap = 8; cap < n && fast < COLLAPSE_FAST_LEVELS; cap *= 8) fast++;
+    fast = fast + 1 < COLLAPSE_FAST_LEVELS ? fast + 1 : COLLAPSE_FAST_LEVELS;
+    for (int level = 0; level < fast; level++)
         k_collapse_level<<<grid, 32 * LEVEL_WARPS, 0, st>>>(level, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
                                                             sc.counters.p, (int)n, sc.children.p, sc.node_lo.p,
                                                             sc.node_hi.p, sc.leaf_count.p, sorted, nodes, node_base,
                                                             prim_base, prim_order, leaf_max, leaf_pack);
-    k_collapse_finish<<<1, 1024, 0, st>>>(COLLAPSE_FAST_LEVELS, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
+    k_collapse_finish<<<1, 1024, 0, st>>>(fast, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
                                           sc.counters.p, (int)n, sc.children.p, sc.node_lo.p, sc.node_hi.p,
                                           sc.leaf_count.p, sorted, nodes, node_base, prim_base, prim_order, leaf_max,
                                           leaf_pack, err_word);

@@ -128,6 +128,40 @@ def test_box_test_edge_cases(scenes_loaded):
         assert_hits_equal(pt.trace_rays(rays), osc.trace(rays), name)
 
 
+def test_deep_instance_bvh(cuda, built_lib):
+    """More than 1024 instances (the multi-launch instance BVH) in a layout whose
+    Morton hierarchy is deep: 40 cubes at halving distances along the diagonal
+    (1e5 down to 1e-7) plus 1,100 small cubes in a cluster.  The collapse then
+    runs past its multi-block levels into the single-block finish; hits must
+    still equal the oracle's and no device error may be reported."""
+    rng = np.random.default_rng(31)
+    cube = scenes.cube_mesh()
+    rows = []
+    for k in range(40):
+        c = 1e5 * 0.5 ** k
+        rows.append((scenes.affine(scale=(0.3 * 0.5 ** k,) * 3, t=(c, c, c)), 0, 0))
+    for p in rng.uniform(-2.0, 2.0, (1100, 3)):
+        rows.append((scenes.affine(scale=(0.05, 0.05, 0.05), t=tuple(p)), 0, 0))
+    sc = scenes.Scene([cube], scenes.make_instances(rows), scenes.make_materials([((0.5, 0.5, 0.5), 0.5, 0.0, 0)]),
+                      scenes.no_dir_light(), scenes.point_lights([]), [], "deep")
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    osc = O.OracleScene(sc)
+    n = 200_000
+    rays = np.zeros(n, abi.RAY_DTYPE)
+    # half the rays aim at the diagonal chain, half at the cluster
+    tgt = np.concatenate([np.repeat(1e5 * 0.5 ** rng.uniform(0.0, 20.0, (n // 2, 1)), 3, 1),
+                          rng.uniform(-2.0, 2.0, (n // 2, 3))])
+    d = rng.normal(size=(n, 3)); d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays["o"] = tgt - 0.5 * np.linalg.norm(tgt, axis=1, keepdims=True).clip(4.0, None) * d
+    rays["d"] = d
+    rays["tmax"] = 1e6
+    h = pt.trace_rays(rays)
+    assert_hits_equal(h, osc.trace(rays), "deep instance BVH")
+    assert (h["flags"] == 1).mean() > 0.05
+    pt.synchronize()   # raises on a device error (bit 8: instance BVH build)
+
+
 def test_empty_scene(cuda, built_lib):
     pt = snkpt.PathTracer(0)
     pt.upload_meshes([scenes.Mesh(np.zeros((0, 3), np.float32), None, np.zeros((0, 3), np.uint32))])
