@@ -126,9 +126,11 @@ struct snk_pt_ctx {
 
     // per-launch profiling (SNK_RENDER_PROFILE): event pairs and their stage
     std::vector<cudaEvent_t> prof_ev;
-    std::vector<int> prof_stage;
+    struct ProfInterval { uint32_t begin, end; int stage; };
+    std::vector<ProfInterval> prof_iv;   // stage timings of the last profiled frame (event indices)
     size_t prof_used = 0;
     bool prof_pending = false;
+    bool prof_chain = false;   // the last recorded event ended a stage and nothing was enqueued since
     double stage_ms[SNK_NUM_STAGES] = {0};
     uint64_t stage_launches[SNK_NUM_STAGES] = {0};
 
@@ -587,6 +589,9 @@ TraceTuning trace_tuning(snk_pt_ctx* ctx) {
 
 // Runs one kernel launch; with profiling on, brackets it with an event pair.
 template <class Fn>
+// Runs one stage's launches; when profiling, CUDA events bracket them.  Stages
+// enqueued back to back share the event between them (the end of one is the
+// start of the next), so a profiled frame records one event per stage boundary.
 cudaError_t staged(snk_pt_ctx* ctx, bool profile, int stage, Fn&& fn) {
     ctx->stage_launches[stage]++;
     if (!profile) return fn();
@@ -597,13 +602,19 @@ cudaError_t staged(snk_pt_ctx* ctx, bool profile, int stage, Fn&& fn) {
             if (r != cudaSuccess) return r;
             ctx->prof_ev.push_back(e);
         }
-        ctx->prof_stage.resize(ctx->prof_ev.size() / 2);
     }
-    cudaEventRecord(ctx->prof_ev[ctx->prof_used], ctx->stream);
+    uint32_t b;
+    if (ctx->prof_chain && ctx->prof_used > 0) {
+        b = (uint32_t)(ctx->prof_used - 1);
+    } else {
+        b = (uint32_t)ctx->prof_used++;
+        cudaEventRecord(ctx->prof_ev[b], ctx->stream);
+    }
     cudaError_t r = fn();
-    cudaEventRecord(ctx->prof_ev[ctx->prof_used + 1], ctx->stream);
-    ctx->prof_stage[ctx->prof_used / 2] = stage;
-    ctx->prof_used += 2;
+    const uint32_t e = (uint32_t)ctx->prof_used++;
+    cudaEventRecord(ctx->prof_ev[e], ctx->stream);
+    ctx->prof_iv.push_back({b, e, stage});
+    ctx->prof_chain = true;
     return r;
 }
 
@@ -831,6 +842,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     const bool profile = (rs.flags & SNK_RENDER_PROFILE) != 0;
     if (ctx->prof_pending) cudaStreamSynchronize(st);   // events of the previous frame are reused
     ctx->prof_used = 0;
+    ctx->prof_iv.clear();
+    ctx->prof_chain = false;
     ctx->prof_pending = profile;
     for (int k = 0; k < SNK_NUM_STAGES; k++) ctx->stage_launches[k] = 0;
 
@@ -995,6 +1008,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (ctx->rq_rays.reserve(2ull * std::max(K1, K2) * np) || ctx->rq_vis_a.reserve(std::max(K1, K3) * np) ||
                 ctx->rq_vis_b.reserve((size_t)K2 * np) || ctx->rq_work.reserve(3))
                 return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir visibility queues");
+            ctx->prof_chain = false;   // the queue reset below is not part of a stage
             if (cudaMemsetAsync(ctx->rq_work.p, 0, 3 * sizeof(uint32_t), st) != cudaSuccess)
                 return fail(ctx, SNK_ERR_CUDA, "restir queue reset");
             const RestirQueue q1{ctx->rq_rays.p, ctx->rq_vis_a.p, K1, 0u}, q2{ctx->rq_rays.p, ctx->rq_vis_b.p, K2, 0u},
@@ -1452,10 +1466,10 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     out->shadow_triangle_tests = ctx->last_count_nodes ? ctx->h_trav[3] : 0;
     if (ctx->prof_pending) {
         for (int k = 0; k < SNK_NUM_STAGES; k++) ctx->stage_ms[k] = 0.0;
-        for (size_t i = 0; i + 1 < ctx->prof_used; i += 2) {
+        for (const auto& iv : ctx->prof_iv) {
             float ms = 0.0f;
-            cudaEventElapsedTime(&ms, ctx->prof_ev[i], ctx->prof_ev[i + 1]);
-            ctx->stage_ms[ctx->prof_stage[i / 2]] += ms;
+            cudaEventElapsedTime(&ms, ctx->prof_ev[iv.begin], ctx->prof_ev[iv.end]);
+            ctx->stage_ms[iv.stage] += ms;
         }
         ctx->prof_pending = false;
     }
