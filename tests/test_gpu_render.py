@@ -154,6 +154,28 @@ def test_restir_config2_frames(cuda, built_lib):
         assert g["radiance"][:, :3].mean() > 0.0
 
 
+def test_restir_two_views_per_call(cuda, built_lib):
+    """Two views of different sizes rendered by one call in ReSTIR mode: each view
+    keeps its own reservoirs, and the second view's random streams are keyed by
+    its global pixel offset (the width x height of the first)."""
+    F = 3
+    a = scenes.config2(width=160, height=90, frames=F)
+    b = scenes.config2(width=96, height=54, frames=F)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(a)
+    osc = O.OracleScene(a)
+    ra, rb = O.OracleRestir(osc, 160, 90), O.OracleRestir(osc, 96, 54)
+    for f in range(F):
+        st = abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=f, seed=1)
+        ga, gb = _gpu_frame(pt, [a.views[f], b.views[f]], st, cuda)
+        ca, cb = np.zeros(5, np.uint64), np.zeros(5, np.uint64)
+        oa, _ = ra.frame(a.views[f], st, pixel_base=0, counters=ca)
+        ob, _ = rb.frame(b.views[f], st, pixel_base=160 * 90, counters=cb)
+        _compare(ga, oa, f"ReSTIR view 0 frame {f}")
+        _compare(gb, ob, f"ReSTIR view 1 frame {f}")
+        assert pt.stats()["rays_shadow"] == int(ca[2] + cb[2])
+
+
 def test_restir_history_of_a_larger_scene(cuda, built_lib):
     """Frames after the instance list shrinks: history reservoirs that point at
     instances which no longer exist are dropped, on the GPU as in the oracle."""
