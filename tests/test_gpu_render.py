@@ -80,10 +80,11 @@ def test_path_config1_1080p_sampled_pixels_and_determinism(cuda, built_lib):
     _compare(sub, r, "config 1 1080p (20k sampled pixels)")
 
 
-def test_path_multi_view_batch(cuda, built_lib):
+@pytest.mark.parametrize("spp", [1, 3])
+def test_path_multi_view_batch(cuda, built_lib, spp):
     res = [(160, 90), (96, 54), (200, 120)]
     sc = scenes.config3(resolutions=res)
-    st = abi.settings(spp=1, max_depth=6, rr_depth=3, seed=3)
+    st = abi.settings(spp=spp, max_depth=6, rr_depth=3, seed=3)
     pt = snkpt.PathTracer(0)
     pt.load_scene(sc)
     gs = _gpu_frame(pt, sc.views, st, cuda)
