@@ -38,6 +38,8 @@ struct RestirState {
     DBuf<float4> g_pos, g_normal, g_albedo, g_misc, prev_normal;
     DBuf<float4> res_a, res_b, res_c;   // temporal, history, spatial (48 B = 3 float4 per pixel)
     DBuf<float4> ris;                    // initial-pass state between its recording and replaying runs
+    DBuf<uint4> memo_keys;               // initial-pass visibility tests reused by the spatial pass
+    DBuf<uint32_t> plan;                 // final-shading answers, spatial phase 1 -> 2
     uint32_t history_valid = 0;
     uint32_t hist = 1, spat = 2;        // which of b/c holds history / receives spatial
 };
@@ -987,7 +989,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (R.w != w || R.h != h) {
                 if (R.g_pos.reserve(np) || R.g_normal.reserve(np) || R.g_albedo.reserve(np) || R.g_misc.reserve(np) ||
                     R.prev_normal.reserve(np) || R.res_a.reserve(3 * np) || R.res_b.reserve(3 * np) ||
-                    R.res_c.reserve(3 * np) || R.ris.reserve(2 * np))
+                    R.res_c.reserve(3 * np) || R.ris.reserve(2 * np) || R.memo_keys.reserve(4 * np) ||
+                    R.plan.reserve(np))
                     return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir buffers");
                 R.w = w; R.h = h; R.history_valid = 0; R.hist = 1; R.spat = 2;
             }
@@ -998,6 +1001,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             RV.history = R.hist == 1 ? R.res_b.p : R.res_c.p;
             RV.spatial = R.spat == 1 ? R.res_b.p : R.res_c.p;
             RV.ris = R.ris.p;
+            RV.memo_keys = R.memo_keys.p; RV.plan = R.plan.p;
             RV.history_valid = R.history_valid;
             RestirSettings s;
             s.frame_index = rs.frame_index; s.seed = rs.seed; s.candidates = rs.restir_candidates;
@@ -1451,6 +1455,7 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     const uint32_t* c = ctx->h_counters;
     out->cache_queries = ctx->last_mode == SNK_MODE_PATH_CACHE ? c[CNT_CACHE_QUERIES] : 0;
     out->cache_samples = ctx->last_mode == SNK_MODE_PATH_CACHE ? ctx->last_cache_samples : 0;
+    out->shadow_tests_reused = ctx->last_mode == SNK_MODE_RESTIR_DI ? c[CNT_SHADOW_REUSED] : 0;
     if (ctx->last_mode == SNK_MODE_PATH || ctx->last_mode == SNK_MODE_PATH_CACHE) {
         out->rays_camera = ctx->last_paths;
         uint64_t ext = 0;

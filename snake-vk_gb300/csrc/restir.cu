@@ -72,16 +72,40 @@ __device__ __forceinline__ void res_store(void* base, uint32_t i, const Reservoi
     p[0] = q[0]; p[1] = q[1]; p[2] = q[2];
 }
 
+// A shadow test of one pixel and frame is fixed by what its ray is aimed at:
+// the origin (the pixel's biased surface point) is the same in every pass, so
+// a point light with its distance variant, or an emissive sample (instance,
+// triangle, barycentrics), determines the ray bit for bit.  Repeats of a test
+// reuse it instead of tracing again: its known result, or its slot in the
+// queue being recorded.
+constexpr uint32_t MEMO_KNOWN = 0x100;  // answer code: MEMO_KNOWN | visibility, else a slot of the current queue
+constexpr uint32_t MEMO_NONE = 0xFFFF;  // plan code of a test that was not made
+constexpr int MEMO_PL = 4, MEMO_EM = 4;
+// Tests already made for this pixel and frame, by what they aim at: the point
+// light tested at its full distance, point lights tested at distance - 0.001,
+// and emissive samples (instance, triangle, barycentric bits).
+struct Memo {
+    uint32_t pla_idx, pla_code;
+    uint32_t n_pl, n_em;
+    uint32_t pl_idx[MEMO_PL], pl_code[MEMO_PL];
+    uint4 em_key[MEMO_EM];
+    uint32_t em_code[MEMO_EM];
+};
+__device__ __forceinline__ void memo_clear(Memo& m) { m.pla_idx = INVALID; m.n_pl = 0; m.n_em = 0; }
+
 // Per-pixel visibility context: records shadow rays into a queue, or replays
 // their results, in call order.
 struct Ctx {
     const SceneDev* S;
     uint32_t shadow_rays;   // rays recorded by this thread
+    uint32_t reused;        // tests answered by an earlier identical test (counted when recording)
     float4* rays;           // recording
     const uint8_t* vis;     // replaying
     size_t base;
     uint32_t k, cap;
     bool overflow;
+    Memo* m;                // tests made so far (null: no reuse)
+    uint32_t last;          // code of the last keyed test: MEMO_KNOWN | visibility or its slot
 };
 
 __device__ __forceinline__ void ctx_queue(Ctx& c, const RestirQueue& q, uint32_t pixel, bool record) {
@@ -110,6 +134,106 @@ __device__ __noinline__ float shadow_test(Ctx& c, V3 o, V3 d, float tmax) {
         return 1.0f;
     }
     return c.vis[slot] ? 1.0f : 0.0f;
+}
+
+// answer of an earlier test (recording: the result is not needed yet)
+__device__ __forceinline__ float memo_answer(Ctx& c, uint32_t code) {
+    if (c.rays) c.reused++;
+    c.last = code;
+    if (code & MEMO_KNOWN) return (code & 1u) ? 1.0f : 0.0f;
+    return c.rays ? 1.0f : (c.vis[c.base + code] ? 1.0f : 0.0f);
+}
+
+// shadow test toward point light idx at its full distance (minus == false) or at
+// distance - 0.001, reusing an identical earlier test of this pixel
+__device__ __noinline__ float shadow_test_pl(Ctx& c, uint32_t idx, bool minus, V3 o, V3 d, float tmax) {
+    Memo* m = c.m;
+    if (m) {
+        if (!minus && m->pla_idx == idx) return memo_answer(c, m->pla_code);
+        if (minus)
+            for (uint32_t j = 0; j < m->n_pl; j++)
+                if (m->pl_idx[j] == idx) return memo_answer(c, m->pl_code[j]);
+    }
+    const uint32_t k = c.k;
+    const float r = shadow_test(c, o, d, tmax);
+    c.last = k;
+    if (m && c.k == k + 1) {
+        if (!minus) { m->pla_idx = idx; m->pla_code = k; }
+        else if (m->n_pl < MEMO_PL) { m->pl_idx[m->n_pl] = idx; m->pl_code[m->n_pl] = k; m->n_pl++; }
+    }
+    return r;
+}
+
+// shadow test toward an emissive sample, reusing an identical earlier test of this pixel
+__device__ __noinline__ float shadow_test_em(Ctx& c, uint4 key, V3 o, V3 d, float tmax) {
+    Memo* m = c.m;
+    if (m)
+        for (uint32_t j = 0; j < m->n_em; j++) {
+            const uint4 e = m->em_key[j];
+            if (e.x == key.x && e.y == key.y && e.z == key.z && e.w == key.w) return memo_answer(c, m->em_code[j]);
+        }
+    const uint32_t k = c.k;
+    const float r = shadow_test(c, o, d, tmax);
+    c.last = k;
+    if (m && c.k == k + 1 && m->n_em < MEMO_EM) {
+        m->em_key[m->n_em] = key;
+        m->em_code[m->n_em] = k;
+        m->n_em++;
+    }
+    return r;
+}
+
+__device__ __forceinline__ uint4 key_em(uint32_t inst, uint32_t tri, float u, float v) {
+    return make_uint4(inst, tri, __float_as_uint(u), __float_as_uint(v));
+}
+
+// after a replay: tests still pointing at slots of the replayed queue get their results
+__device__ __forceinline__ uint32_t resolve_code(const Ctx& c, uint32_t code) {
+    return (code & MEMO_KNOWN) ? code : (MEMO_KNOWN | (c.vis[c.base + code] ? 1u : 0u));
+}
+__device__ __forceinline__ void memo_resolve(Ctx& c) {
+    Memo* m = c.m;
+    if (!m || !c.vis) return;
+    if (m->pla_idx != INVALID) m->pla_code = resolve_code(c, m->pla_code);
+    for (uint32_t j = 0; j < m->n_pl; j++) m->pl_code[j] = resolve_code(c, m->pl_code[j]);
+    for (uint32_t j = 0; j < m->n_em; j++) m->em_code[j] = resolve_code(c, m->em_code[j]);
+}
+
+// the initial pass's tests of pixel o (all answers known) for the spatial pass:
+// 3 uint4 per pixel: (pla idx, visibility bits, counts, -), point-light indices, and
+// two emissive keys
+__device__ __forceinline__ void memo_store(const Memo& m, const RestirView& R, uint32_t o) {
+    const uint32_t npl = m.n_pl < 4u ? m.n_pl : 4u, nem = m.n_em < 2u ? m.n_em : 2u;
+    uint32_t vis = (m.pla_idx != INVALID ? (m.pla_code & 1u) : 0u);
+    uint4 pl = make_uint4(INVALID, INVALID, INVALID, INVALID);
+    uint32_t* plw = &pl.x;
+    for (uint32_t j = 0; j < npl; j++) { plw[j] = m.pl_idx[j]; vis |= (m.pl_code[j] & 1u) << (1 + j); }
+    for (uint32_t j = 0; j < nem; j++) vis |= (m.em_code[j] & 1u) << (5 + j);
+    uint4* dst = R.memo_keys + 4ull * o;
+    dst[0] = make_uint4(m.pla_idx, vis, npl | (nem << 8), 0u);
+    dst[1] = pl;
+    if (nem > 0) dst[2] = m.em_key[0];
+    if (nem > 1) dst[3] = m.em_key[1];
+}
+__device__ __forceinline__ void memo_load(Memo& m, const RestirView& R, uint32_t o) {
+    const uint4* src = R.memo_keys + 4ull * o;
+    const uint4 h = src[0];
+    const uint32_t vis = h.y;
+    m.pla_idx = h.x;
+    m.pla_code = MEMO_KNOWN | (vis & 1u);
+    m.n_pl = min(h.z & 0xFFu, (uint32_t)MEMO_PL);
+    m.n_em = min((h.z >> 8) & 0xFFu, 2u);
+    const uint4 pl = src[1];
+    const uint32_t plw[4] = {pl.x, pl.y, pl.z, pl.w};
+    for (uint32_t j = 0; j < m.n_pl; j++) { m.pl_idx[j] = plw[j]; m.pl_code[j] = MEMO_KNOWN | ((vis >> (1 + j)) & 1u); }
+    for (uint32_t j = 0; j < m.n_em; j++) { m.em_key[j] = src[2 + j]; m.em_code[j] = MEMO_KNOWN | ((vis >> (5 + j)) & 1u); }
+}
+
+// visibility of a test answered by a plan code (a known result or a slot of the replayed queue)
+__device__ __forceinline__ float plan_vis(const Ctx& c, uint32_t code) {
+    if (code & MEMO_KNOWN) return (code & 1u) ? 1.0f : 0.0f;
+    if (code >= c.cap || !c.vis) return 0.0f;
+    return c.vis[c.base + code] ? 1.0f : 0.0f;
 }
 
 __device__ __forceinline__ void ctx_check(Ctx& c) {
@@ -167,7 +291,7 @@ __device__ __forceinline__ float tri_shadow(Ctx& c, uint32_t inst, uint32_t tri,
     V3 target = add(p, mul(pn, 0.01f));
     float dist = length(sub(surface_pos, target));
     V3 dir = divs(sub(target, surface_pos), dist);
-    return shadow_test(c, surface_pos, dir, dist);
+    return shadow_test_em(c, key_em(inst, tri, bu, bv), surface_pos, dir, dist);
 }
 
 __device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, const Shade& sh,
@@ -185,7 +309,7 @@ __device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, flo
         V3 target = add(p, mul(pn, 0.01f));
         float dist = length(sub(sh.biased, target));
         V3 dir = divs(sub(target, sh.biased), dist);
-        rad = mul(rad, shadow_test(c, sh.biased, dir, dist));
+        rad = mul(rad, shadow_test_em(c, key_em(inst, tri, bu, bv), sh.biased, dir, dist));
     }
     return rad;
 }
@@ -197,7 +321,7 @@ __device__ __noinline__ void combine(Ctx& c, Reservoir& cur, const Reservoir& nb
         const PointLightDev& L = S.point_lights[nb.pl_idx];
         V3 lp = load3(L.pos);
         float ld = length(sub(lp, sh.biased));
-        float vis = shadow_test(c, sh.biased, divs(sub(lp, sh.biased), ld), ld - 0.001f);
+        float vis = shadow_test_pl(c, nb.pl_idx, true, sh.biased, divs(sub(lp, sh.biased), ld), ld - 0.001f);
         float p_hat = length(calc_pointlight(L, sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal, sh.albedo)) * vis;
         float w = (p_hat * (float)nb.pl_m) * nb.w_pl;
         if (update_pl(cur, nb.pl_idx, w, rng)) phat_pl = p_hat;
@@ -280,7 +404,8 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
     const bool record = phase == 0;
     Ctx c;
-    c.S = &F.S; c.shadow_rays = 0; c.overflow = false;
+    c.S = &F.S; c.shadow_rays = 0; c.reused = 0; c.overflow = false; c.m = nullptr; c.last = MEMO_NONE;
+    Memo memo;
     // background pixels end in a first pass over each warp's 32 pixels; surface
     // pixels wait in a per-warp ring and are processed 32 at a time
     __shared__ uint32_t ring[RBLK / 32][64];
@@ -315,6 +440,8 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
             if (!have) continue;
             uint32_t x = o % W, y = o / W;
             ctx_queue(c, q, o, record);
+            memo_clear(memo);
+            c.m = &memo;
             float4 gp = R.g_pos[o];
             float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
             V3 nrm = v3(gn.x, gn.y, gn.z);
@@ -377,7 +504,7 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
             if (Rr.pl_idx != INVALID) {
                 V3 lp = load3(S.point_lights[Rr.pl_idx].pos);
                 float dist = length(sub(lp, sh.biased));
-                float vis = shadow_test(c, sh.biased, divs(sub(lp, sh.biased), dist), dist);
+                float vis = shadow_test_pl(c, Rr.pl_idx, false, sh.biased, divs(sub(lp, sh.biased), dist), dist);
                 Rr.w_pl = vis * ((Rr.w_sum_pl / (float)Rr.pl_m) / phat_pl);
             } else {
                 Rr.w_pl = 0.0f;
@@ -424,12 +551,18 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
                 }
             }
             ctx_check(c);
-            if (record) ctx_close(c);
-            else res_store(R.temporal, o, out);
+            if (record) {
+                ctx_close(c);
+            } else {
+                res_store(R.temporal, o, out);
+                memo_resolve(c);
+                memo_store(memo, R, o);
+            }
         }
         if (!more) break;
     }
     flush_rays(c.shadow_rays, &F.counters[CNT_SHADOW_RAYS]);
+    flush_rays(c.reused, &F.counters[CNT_SHADOW_REUSED]);
 }
 
 // ComputeAndWriteSpatialReservoirReuse + CalculateRadianceFromReservoirs + main
@@ -442,7 +575,8 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
     const SceneDev& S = F.S;
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
     Ctx c;
-    c.S = &F.S; c.shadow_rays = 0; c.overflow = false;
+    c.S = &F.S; c.shadow_rays = 0; c.reused = 0; c.overflow = false; c.m = nullptr; c.last = MEMO_NONE;
+    Memo memo;
     // radiance, FP64 accumulation and the next frame's history normal of pixel o
     auto write_out = [&](uint32_t o, V3 colour, float4 hist_normal) {
         float4 r4 = make_float4(colour.x, colour.y, colour.z, 1.0f);
@@ -503,6 +637,12 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
             float4 gp = R.g_pos[o];
             float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
             ctx_queue(c, q, o, phase == 0);
+            // the initial pass's tests are known; the combines add theirs (phases 0 and 1 alike)
+            c.m = nullptr;
+            if (phase < 2) {
+                memo_load(memo, R, o);
+                c.m = &memo;
+            }
             V3 nrm = v3(gn.x, gn.y, gn.z);
             Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
             V3 light = v3(0.0f, 0.0f, 0.0f);
@@ -544,32 +684,55 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
                 ctx_check(c);
                 if (phase == 0) { ctx_close(c); continue; }
                 res_store(R.spatial, o, Rr);
+                memo_resolve(c);             // the combines' results are known now
                 ctx_queue(c, qs, o, true);   // phase 1 records the final shading rays
             } else {
                 Rr = res_load(R.spatial, o);
                 ctx_queue(c, qs, o, false);
             }
+            // phase 1 makes the final tests (reusing earlier ones) and writes how each is
+            // answered; phase 2 reads the answers through that plan
+            const uint32_t plan = phase == 2 ? R.plan[o] : 0u;
+            uint32_t code_pl = MEMO_NONE, code_em = MEMO_NONE;
             V3 rad = v3(0.0f, 0.0f, 0.0f);
             if (S.num_point_lights > 0 && Rr.pl_idx != INVALID) {
                 const PointLightDev& L = S.point_lights[Rr.pl_idx];
                 V3 lp = load3(L.pos);
                 float ld = length(sub(lp, sh.biased));
                 V3 cpl = calc_pointlight(L, sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal, sh.albedo);
-                cpl = mul(cpl, shadow_test(c, sh.biased, divs(sub(lp, sh.biased), ld), ld));
+                float vis;
+                if (phase == 1) {
+                    vis = shadow_test_pl(c, Rr.pl_idx, false, sh.biased, divs(sub(lp, sh.biased), ld), ld);
+                    code_pl = c.last;
+                } else {
+                    vis = plan_vis(c, plan & 0xFFFFu);
+                }
+                cpl = mul(cpl, vis);
                 cpl = mul(cpl, Rr.w_pl);
                 rad = add(rad, cpl);
             }
             if (S.num_emissive_instances > 0 && Rr.em_inst != INVALID) {
-                V3 e = tri_radiance(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, true);
+                V3 e;
+                if (phase == 1) {
+                    e = tri_radiance(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, true);
+                    code_em = c.last;
+                } else {
+                    e = mul(tri_radiance(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, false), plan_vis(c, plan >> 16));
+                }
                 rad = add(rad, mul(e, Rr.w_em));
             }
             ctx_check(c);
-            if (phase == 1) { ctx_close(c); continue; }
+            if (phase == 1) {
+                R.plan[o] = (code_pl & 0xFFFFu) | (code_em << 16);
+                ctx_close(c);
+                continue;
+            }
             write_out(o, add(light, rad), make_float4(gn.x, gn.y, gn.z, 0.0f));
         }
         if (!more) break;
     }
     flush_rays(c.shadow_rays, &F.counters[CNT_SHADOW_RAYS]);
+    flush_rays(c.reused, &F.counters[CNT_SHADOW_REUSED]);
 }
 
 }  // namespace

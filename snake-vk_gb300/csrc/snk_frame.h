@@ -15,6 +15,7 @@ constexpr uint32_t CNT_WORK_TRACE = 16;   // [d]: work fetch of the closest-hit 
 constexpr uint32_t CNT_WORK_SHADOW = 32;  // [d]: work fetch of the shadow pass of segment d
 constexpr uint32_t CNT_SHADOW_RAYS = 48;  // valid shadow rays
 constexpr uint32_t CNT_CACHE_QUERIES = 49; // paths terminated into the radiance cache
+constexpr uint32_t CNT_SHADOW_REUSED = 50;  // ReSTIR visibility tests answered by an identical earlier test
 constexpr uint32_t CNT_TOTAL = 64;
 constexpr uint32_t TRAIN_V = 4;           // recorded vertices per cache training path
 
@@ -84,6 +85,8 @@ struct RestirView {
     void* history;      // final reservoirs of the previous frame
     void* spatial;      // final reservoirs of this frame
     float4* ris;        // 2 per pixel: the initial pass's RIS state between its two runs
+    uint4* memo_keys;   // 4 per pixel: the initial pass's visibility tests and their results
+    uint32_t* plan;     // per pixel: how the final shading's two tests are answered (codes, 16 bits each)
     uint32_t history_valid;
 };
 

@@ -151,7 +151,11 @@ def test_restir_config2_frames(cuda, built_lib):
         r, _ = ors.frame(sc.views[f], st, counters=ctr)
         _compare(g, r, f"ReSTIR frame {f}")
         s = pt.stats()
-        assert s["rays_shadow"] == int(ctr[2]), f"frame {f}: shadow ray count {s['rays_shadow']} vs {int(ctr[2])}"
+        # every visibility test of the oracle is either traced or answered by an identical earlier test
+        tests = s["rays_shadow"] + s["shadow_tests_reused"]
+        assert tests == int(ctr[2]), f"frame {f}: visibility tests {tests} vs {int(ctr[2])}"
+        if f > 0:
+            assert s["shadow_tests_reused"] > 0.15 * tests
         assert g["radiance"][:, :3].mean() > 0.0
 
 
@@ -174,7 +178,8 @@ def test_restir_two_views_per_call(cuda, built_lib):
         ob, _ = rb.frame(b.views[f], st, pixel_base=160 * 90, counters=cb)
         _compare(ga, oa, f"ReSTIR view 0 frame {f}")
         _compare(gb, ob, f"ReSTIR view 1 frame {f}")
-        assert pt.stats()["rays_shadow"] == int(ca[2] + cb[2])
+        s = pt.stats()
+        assert s["rays_shadow"] + s["shadow_tests_reused"] == int(ca[2] + cb[2])
 
 
 def test_restir_history_of_a_larger_scene(cuda, built_lib):
