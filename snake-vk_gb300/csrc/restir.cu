@@ -200,8 +200,8 @@ __device__ __forceinline__ void memo_resolve(Ctx& c) {
 }
 
 // the initial pass's tests of pixel o (all answers known) for the spatial pass:
-// 3 uint4 per pixel: (pla idx, visibility bits, counts, -), point-light indices, and
-// two emissive keys
+// 4 uint4 per pixel: (full-distance light, visibility bits, counts, -), the
+// indices of up to 4 lights tested at distance - 0.001, and up to 2 emissive keys
 __device__ __forceinline__ void memo_store(const Memo& m, const RestirView& R, uint32_t o) {
     const uint32_t npl = m.n_pl < 4u ? m.n_pl : 4u, nem = m.n_em < 2u ? m.n_em : 2u;
     uint32_t vis = (m.pla_idx != INVALID ? (m.pla_code & 1u) : 0u);
@@ -231,6 +231,7 @@ __device__ __forceinline__ void memo_load(Memo& m, const RestirView& R, uint32_t
 
 // visibility of a test answered by a plan code (a known result or a slot of the replayed queue)
 __device__ __forceinline__ float plan_vis(const Ctx& c, uint32_t code) {
+    if (code == MEMO_NONE) return 0.0f;   // (phase 2 only asks for tests phase 1 made)
     if (code & MEMO_KNOWN) return (code & 1u) ? 1.0f : 0.0f;
     if (code >= c.cap || !c.vis) return 0.0f;
     return c.vis[c.base + code] ? 1.0f : 0.0f;
