@@ -159,6 +159,26 @@ def test_restir_config2_frames(cuda, built_lib):
         assert g["radiance"][:, :3].mean() > 0.0
 
 
+@pytest.mark.parametrize("temporal,spatial", [(0, 0), (1, 3), (0, 5)])
+def test_restir_reuse_settings(cuda, built_lib, temporal, spatial):
+    """The reference's RtSettings (num_temporal_resamples, num_spatial_resamples):
+    no reuse, its defaults (temporal on, 3 neighbours), spatial reuse only."""
+    W, H, F = 128, 72, 3
+    sc = scenes.config2(width=W, height=H, frames=F)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    ors = O.OracleRestir(O.OracleScene(sc), W, H)
+    for f in range(F):
+        st = abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=f, seed=4, restir_temporal=temporal,
+                          restir_spatial=spatial)
+        g = _gpu_frame(pt, [sc.views[f]], st, cuda)[0]
+        ctr = np.zeros(5, np.uint64)
+        r, _ = ors.frame(sc.views[f], st, counters=ctr)
+        _compare(g, r, f"ReSTIR temporal {temporal} spatial {spatial} frame {f}")
+        s = pt.stats()
+        assert s["rays_shadow"] + s["shadow_tests_reused"] == int(ctr[2])
+
+
 def test_restir_two_views_per_call(cuda, built_lib):
     """Two views of different sizes rendered by one call in ReSTIR mode: each view
     keeps its own reservoirs, and the second view's random streams are keyed by
