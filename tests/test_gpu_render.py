@@ -51,6 +51,23 @@ def test_path_config0_full(cuda, built_lib):
     assert g["radiance"][:, :3].mean() > 0.0
 
 
+@pytest.mark.parametrize("max_depth,rr_depth", [(1, 1), (8, 2)])
+def test_path_depth_and_roulette(cuda, built_lib, max_depth, rr_depth):
+    """Direct light only (one segment) and long paths with early Russian roulette."""
+    sc = scenes.config0(width=96, height=96)
+    st = abi.settings(spp=2, max_depth=max_depth, rr_depth=rr_depth, seed=9)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    ctr = np.zeros(5, np.uint64)
+    r = O.OracleScene(sc).render_path(sc.views[0], st, counters=ctr)
+    _compare(g, r, f"depth {max_depth}, roulette from {rr_depth}")
+    s = pt.stats()
+    assert (s["rays_camera"], s["rays_extension"], s["rays_shadow"]) == tuple(int(x) for x in ctr[:3])
+    if max_depth == 1:
+        assert s["rays_extension"] == 0
+
+
 def test_path_config1_reduced_full_frame(cuda, built_lib):
     sc = scenes.config1(width=480, height=270)
     st = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=1)
