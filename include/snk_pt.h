@@ -217,7 +217,8 @@ typedef struct snk_view_outputs {
     uint32_t  pad;
 } snk_view_outputs;
 
-/* A ray: origin, tmin, direction, tmax (32 bytes). */
+/* A ray: origin, tmin, direction, tmax (32 bytes).  Hits have tmin < t < tmax; a
+ * negative (or NaN) tmin is taken as 0, as traceRayEXT requires tmin >= 0. */
 typedef struct snk_ray {
     float ox, oy, oz, tmin;
     float dx, dy, dz, tmax;

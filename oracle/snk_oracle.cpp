@@ -571,6 +571,8 @@ static bool traverse(const Bvh& B, const double o[3], const double id[3], double
 }
 
 static bool trace(const Scene& S, V3 o, V3 d, float tmin, float tmax, bool any, HitRec* out, Counters* ctr) {
+    // traceRayEXT requires tmin >= 0: a negative (or NaN) tmin is taken as 0
+    tmin = std::fmax(tmin, 0.0f);
     HitRec best{0, INVALID, INVALID, 0, 0, false};
     double wo[3] = {o.x, o.y, o.z}, wid[3] = {1.0 / (double)d.x, 1.0 / (double)d.y, 1.0 / (double)d.z};
     auto lim = [&]() { return best.hit ? (double)best.t : (double)tmax; };

@@ -8,7 +8,9 @@
 //                 with tmin < t < tmax under the watertight test;
 //   any hit     = whether such a triangle exists.
 // Box tests are only required to be conservative: child boxes are quantised
-// outwards and accepted with a relative slack of 1e-5 in t.
+// outwards and accepted with a slack of BOX_SLACK_ULPS units in the last place
+// of the exit distance.  tmin below 0 (or NaN) is taken as 0, as traceRayEXT
+// requires tmin >= 0; entry distances are then never negative.
 //
 // Traversal scheme (Ylitie, Karras, Laine, HPG 2017): the current node group
 // is (child_base, hit bits of internal children << 24 | imask) and the current
@@ -29,6 +31,13 @@ constexpr int STACK_SH = 8;           // shared-memory entries per thread
 constexpr int STACK_MAX = 64;         // total entries (shared + local spill)
 constexpr uint32_t MAX_TRAVERSAL_STEPS = 1u << 16;   // node groups popped per ray
 constexpr uint32_t PRIM_GROUP = 0x80000000u;         // stack tag of a primitive group (bases are < 2^31)
+// A child box is accepted when bits(t_enter) <= bits(t_exit) + BOX_SLACK_ULPS as
+// signed integers.  With t_enter >= tmin >= 0 this orders like the floats, and
+// the slack (>= 2^-19 of t_exit) covers the 2-ulp reciprocal of the direction and
+// the final rounding of each plane distance (about 6 ulps of t in all); a
+// negative t_exit (box behind the origin) compares below every t_enter.  The
+// absolute rounding of the plane offsets is covered by the per-axis widening.
+constexpr int BOX_SLACK_ULPS = 32;
 
 // device error word bits
 constexpr unsigned ERR_STACK_OVERFLOW = 1u;
@@ -42,7 +51,7 @@ struct NodeRay {
 };
 
 // Reciprocal for box tests only (they need to be conservative, not exact): the
-// fast approximate division is within 2 ulp, far inside the 1e-5 slack.
+// fast approximate division is within 2 ulp, inside BOX_SLACK_ULPS.
 __device__ __forceinline__ float safe_rcp(float d) {
     return __fdividef(1.0f, fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d));
 }
@@ -84,8 +93,8 @@ __device__ __forceinline__ float byte_m(uint32_t w, uint32_t k) {
 // with internal hit bit of slot s at position s ^ oct (ORDERED) or s; tgroup <- (prim_base,
 // primitive hits).
 // Near/far planes are swapped once per node by the ray octant; each plane costs a
-// byte permute and one FMA, and a slack of 1e-5 of the entry/exit distances (on
-// top of the per-axis widening below) keeps the test conservative.  The 8 box tests only
+// byte permute and one FMA, and an integer compare with BOX_SLACK_ULPS of slack
+// (on top of the per-axis widening below) keeps the test conservative.  The 8 box tests only
 // set one bit each; the internal-child bits are then moved into visiting order
 // with three conditional swaps (bit s -> s ^ oct) when the order matters (closest
 // hit; an any-hit ray stops at whichever occluder it meets first and skips the
@@ -126,7 +135,7 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
                          fmaxf(__fmaf_rn(byte_m(nz[h], k), az, bnz), tmin));
         float tf = min3f(__fmaf_rn(byte_m(fx[h], k), ax, bfx), __fmaf_rn(byte_m(fy[h], k), ay, bfy),
                          fminf(__fmaf_rn(byte_m(fz[h], k), az, bfz), tmax));
-        hits |= (tn <= tf + ((fabsf(tn) + fabsf(tf)) * 1e-5f + 1e-7f)) ? (1u << s) : 0u;
+        hits |= (__float_as_int(tn) <= __float_as_int(tf) + BOX_SLACK_ULPS) ? (1u << s) : 0u;
     }
     // internal children (imask bits) in visiting order: bit s moves to s ^ oct
     uint32_t x = hits & imask;
@@ -196,7 +205,7 @@ struct Traverser {
 
     __device__ __forceinline__ void init(const SceneDev& S, V3 o_, V3 d_, float tmin_, float tmax_, uint2* sh,
                                          uint2* spill, uint32_t tid, uint32_t nthreads) {
-        o = o_; d = d_; tmin = tmin_; tmax = tmax_;
+        o = o_; d = d_; tmin = fmaxf(tmin_, 0.0f); tmax = tmax_;
         cr = make_node_ray(o, d);
         best_t = tmax; best_u = 0.0f; best_v = 0.0f; best_inst = INVALID; best_prim = INVALID;
         level = 0; blas_sp = 0; cur_inst = 0; steps = 0; err = 0; done = false;

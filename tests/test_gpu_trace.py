@@ -86,8 +86,15 @@ def test_degenerate_rays(scenes_loaded):
     r["tmin"][1024:2048] = 5.0
     r["tmax"][1024:2048] = 5.0
     r["tmax"][2048:3072] = 1e-6
-    assert_hits_equal(pt.trace_rays(r), osc.trace(r), "degenerate rays")
-    assert (pt.trace_rays(r)["flags"][1024:2048] == 0).all()
+    # negative and NaN tmin (taken as 0, as traceRayEXT requires tmin >= 0)
+    r["tmin"][3072:3584] = -1.0
+    r["tmin"][3584:] = np.nan
+    h = pt.trace_rays(r)
+    assert_hits_equal(h, osc.trace(r), "degenerate rays")
+    assert (h["flags"][1024:2048] == 0).all()
+    r0 = r[3072:].copy()
+    r0["tmin"] = 0.0
+    assert_hits_equal(h[3072:], pt.trace_rays(r0), "tmin below 0 as 0")
 
 
 def test_box_test_edge_cases(scenes_loaded):

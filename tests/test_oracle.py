@@ -218,6 +218,18 @@ def test_oracle_deterministic_hits(cfg):
     assert_hits_equal(osc.trace(rays, nthreads=1), osc.trace(rays, nthreads=8), "thread count")
 
 
+def test_oracle_negative_tmin_is_zero():
+    """A negative or NaN tmin is taken as 0 (traceRayEXT requires tmin >= 0)."""
+    sc = scenes.make(1, width=32, height=18)
+    osc = O.OracleScene(sc)
+    rays = random_rays(sc, 2000, np.random.default_rng(4))
+    ref = osc.trace(rays)
+    for v in (-1.0, -1e30, np.nan):
+        r = rays.copy()
+        r["tmin"] = v
+        assert_hits_equal(osc.trace(r), ref, f"tmin {v}")
+
+
 def test_taa_oracle_matches_golden_restatement():
     """The oracle's TAA resolve equals the independent numpy binary32 restatement
     (tests/golden/make_taa_golden.py) bit for bit over a 3-frame sequence."""
