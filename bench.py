@@ -9,8 +9,9 @@ is Mrays/s = (camera + extension + shadow rays) / device time.
 
   value  device-resident inputs, CUDA events on the library's stream around each
          frame; L2 flushed (256 MiB memset, untimed) between frames
-  e2e    the same frames through the C ABI with host buffers: per frame the
-         instance table goes host->device (instance BVH rebuilt, as the reference's
+  e2e    the same frames through the C ABI with host buffers: per frame every
+         instance moves, the instance table goes host->device (instance records,
+         light tables and instance BVH rebuilt, as the reference's
          TlasSystem::BuildTlas does every frame) and the HDR radiance image comes
          back device->host; wall clock around the frames
   roofline  the dominant kernel's algorithmic bytes per launch / its average
@@ -362,7 +363,8 @@ def bvh_bench(snkpt, scenes, device, stream, reps=3):
     icosphere: Morton sort, hierarchy, 3 treelet passes, 8-wide collapse) from
     uploaded meshes, and one per-frame instance-BVH rebuild (set_instances + build)
     at config 1's 201 instances (single-launch builder) and config 2's 4,297
-    instances (multi-launch builder)."""
+    instances (multi-launch builder), every instance moved between rebuilds
+    (instance records, emissive-light records, light CDF and the BVH all redone)."""
     import torch
     sc3 = scenes.config3(resolutions=[(64, 36)])
     tris = int(sum(m.num_triangles for m in sc3.meshes))
@@ -385,15 +387,17 @@ def bvh_bench(snkpt, scenes, device, stream, reps=3):
                      ("instance_bvh_4297", scenes.config2(width=64, height=36, frames=1))):
         pt = snkpt.PathTracer(device.index or 0, stream=stream)
         pt.load_scene(sc)
-        inst = np.ascontiguousarray(sc.instances)
+        inst = np.array(sc.instances, copy=True)
         for _ in range(3):
             pt.set_instances(inst); pt.build(); pt.synchronize()
         ms = []
-        for _ in range(20):
+        for k in range(20):
+            # every instance moves (all table rows and boxes change, as in an animated frame)
+            inst["transform"][:, [3, 7, 11]] += 1e-3 if k % 2 == 0 else -1e-3
             t0 = time.perf_counter()
             pt.set_instances(inst); pt.build(); pt.synchronize()
             ms.append((time.perf_counter() - t0) * 1e3)
-        out[name] = {"instances": len(inst), "ms_per_rebuild": float(np.median(ms))}
+        out[name] = {"instances": len(inst), "ms_per_rebuild": float(np.median(ms)), "note": "every instance moved"}
         del pt
     torch.cuda.synchronize()
     return out
@@ -573,14 +577,22 @@ def run_ours(args):
 
     # end to end through the C ABI with host buffers
     host_rad = torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True).numpy()
-    inst = np.ascontiguousarray(sc.instances)
+    inst = np.array(sc.instances, copy=True)
     e2e_rays = 0
+
+    def move(k):
+        # every instance moves by 1e-3 each frame (back and forth), so the instance
+        # table really crosses to the device and every derived table is redone
+        inst["transform"][:, [3, 7, 11]] += 1e-3 if k % 2 == 0 else -1e-3
+        inst["prev_transform"][:, [3, 7, 11]] = inst["transform"][:, [3, 7, 11]]
     for k in range(max(1, args.warmup)):
+        move(k)
         pt.set_instances(inst)
         pt.render([view], settings(2000 + k, 0), [{"radiance": host_rad}])
     barrier()
     t0 = time.perf_counter()
     for k in range(args.steps):
+        move(k)
         pt.set_instances(inst)
         pt.render([view], settings(3000 + k, 0), [{"radiance": host_rad}])
         s = pt.stats()
@@ -591,12 +603,14 @@ def run_ours(args):
     # the same, refitting the instance BVH between full rebuilds every 16 updates
     pt.set_tuning(dict(tuning, tlas_refit_interval=16))
     for k in range(max(1, args.warmup)):
+        move(k)
         pt.set_instances(inst)
         pt.render([view], settings(2000 + k, 0), [{"radiance": host_rad}])
     barrier()
     t0 = time.perf_counter()
     refit_rays = 0
     for k in range(args.steps):
+        move(k)
         pt.set_instances(inst)
         pt.render([view], settings(3000 + k, 0), [{"radiance": host_rad}])
         s = pt.stats()

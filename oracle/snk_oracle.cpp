@@ -685,17 +685,25 @@ static void build_scene(Scene& S) {
             w.push_back(2.0 * M_PI * (double)L.area * (0.2126 * Le.x + 0.7152 * Le.y + 0.0722 * Le.z));
         }
     }
-    double total = 0;
-    for (double x : w) total += x;
+    // CDF over integer weights q = max(1, round(w / w_max * 2^40)) (0 for w <= 0):
+    // integer prefix sums are exact, so any summation order gives these values
+    double wmax = 0.0;
+    for (double x : w)
+        if (x > 0.0 && x > wmax) wmax = x;
+    std::vector<uint64_t> q(w.size());
+    uint64_t total = 0;
+    for (size_t k = 0; k < w.size(); k++) {
+        q[k] = (w[k] > 0.0 && wmax > 0.0) ? std::max<uint64_t>(1, (uint64_t)std::llrint(w[k] / wmax * 1099511627776.0)) : 0;
+        total += q[k];
+    }
     S.light_cdf.resize(w.size());
     S.light_pmf.resize(w.size());
-    double acc = 0;
+    uint64_t acc = 0;
     for (size_t k = 0; k < w.size(); k++) {
-        acc += w[k];
-        S.light_cdf[k] = total > 0 ? (float)(acc / total) : 0.0f;
-        S.light_pmf[k] = total > 0 ? (float)(w[k] / total) : 0.0f;
+        acc += q[k];
+        S.light_cdf[k] = total ? (k + 1 == w.size() ? 1.0f : (float)((double)acc / (double)total)) : 0.0f;
+        S.light_pmf[k] = total ? (float)((double)q[k] / (double)total) : 0.0f;
     }
-    if (!w.empty() && total > 0) S.light_cdf.back() = 1.0f;
     S.built = true;
 }
 

@@ -77,15 +77,21 @@ struct snk_pt_ctx {
     DBuf<MaterialDev> d_mats;
     DBuf<PointLightDev> d_pls;
     DBuf<uint32_t> d_emissive;
+    DBuf<snk_instance> d_inst_raw;     // the caller's instance records, as given
+    DBuf<uint32_t> d_em_first;         // first NEE record of each emissive instance's triangles
     DBuf<LocalLight> d_lights;
+    DBuf<double> d_light_w;            // selection weight of every NEE record
     DBuf<float> d_cdf, d_pmf;
+    LightCdfScratch cdf_scratch;
+    bool inst_tables_valid = false;    // instance and NEE records match the uploaded inputs
+    bool lights_changed = true;        // point lights or materials changed since the NEE records
     uint32_t n_emissive = 0, n_local = 0;
     DBuf<unsigned> d_err;
     DBuf<unsigned char> q_in, q_in2, q_out, q_out2;   // staging of the particle / contact queries
     DBuf<float4> rq_rays;                              // ReSTIR visibility queue (slots x pixels x 2)
     DBuf<uint8_t> rq_vis_a, rq_vis_b;                  // its results (initial / shading, spatial)
     DBuf<uint32_t> rq_work;                            // work counters of the three visibility traces
-    UploadMemo memo[7];                // instance trace/shade records, emissive list, lights, CDF, PMF, BVH list
+    UploadMemo memo[7];                // raw instances, emissive firsts, emissive list, -, -, -, BVH list
     DBuf<SmallBuildOut> d_small_out;   // result record of the single-launch instance BVH build
     bool tlas_small = false;
     // instance BVH refit state: exact node boxes and depths, primitive order and
@@ -145,6 +151,7 @@ struct snk_pt_ctx {
     EncodeParams cache_ep{};
     bool cache_bounds_set = false;
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {1, 1, 1};
+    bool scene_bounds_dirty = true;    // recomputed on the host when the cache needs them
     DBuf<float4> cache_in;
     DBuf<float> cache_out, cache_grad;
     DBuf<float2> c_spread;
@@ -178,10 +185,12 @@ template <class T>
 Status upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s);
 
 template <class T>
-Status upload_changed(DBuf<T>& b, UploadMemo& memo, const T* src, size_t n, cudaStream_t s) {
+Status upload_changed(DBuf<T>& b, UploadMemo& memo, const T* src, size_t n, cudaStream_t s, bool* changed = nullptr) {
     const size_t bytes = n * sizeof(T);
+    if (changed) *changed = false;
     if (b.p && memo.dev == b.p && memo.bytes.size() == bytes && (bytes == 0 || !std::memcmp(memo.bytes.data(), src, bytes)))
         return Status::Ok();
+    if (changed) *changed = true;
     SNK_TRY(upload(b, src, n, s));
     memo.bytes.assign(reinterpret_cast<const unsigned char*>(src), reinterpret_cast<const unsigned char*>(src) + bytes);
     memo.dev = b.p;
@@ -193,36 +202,6 @@ Status upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s) {
     SNK_TRY_CUDA(b.reserve(n ? n : 1));
     if (n) SNK_TRY_CUDA(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
     return Status::Ok();
-}
-
-// inverse of a row-major 3x4 affine transform in double rounded to float, the
-// normal matrix transpose(inverse(mat3)) and determinant(mat3).  The CPU oracle
-// evaluates the same expressions in the same order.
-void invert_affine(const float* mf, float* inv_out, float* nmat_out, float* det_out) {
-    double a[3][3], t[3];
-    for (int r = 0; r < 3; r++) { for (int c = 0; c < 3; c++) a[r][c] = mf[4 * r + c]; t[r] = mf[4 * r + 3]; }
-    double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
-    double c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
-    double c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
-    double det = (a[0][0] * c00 + a[0][1] * c01) + a[0][2] * c02;
-    double inv[3][3];
-    inv[0][0] = c00 / det;
-    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
-    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
-    inv[1][0] = c01 / det;
-    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
-    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
-    inv[2][0] = c02 / det;
-    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
-    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
-    for (int r = 0; r < 3; r++) {
-        double it = -((inv[r][0] * t[0] + inv[r][1] * t[1]) + inv[r][2] * t[2]);
-        for (int c = 0; c < 3; c++) inv_out[4 * r + c] = (float)inv[r][c];
-        inv_out[4 * r + 3] = (float)it;
-    }
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) nmat_out[3 * r + c] = (float)inv[c][r];
-    *det_out = (float)det;
 }
 
 uint32_t leaf_size(uint32_t knob, uint32_t dflt) { return knob ? knob : dflt; }
@@ -295,65 +274,62 @@ Status build_meshes(snk_pt_ctx* ctx) {
     return Status::Ok();
 }
 
+// World bounds of the listed instances (positions of the radiance cache are
+// normalised to them); computed on the host when the cache asks for them.
+void update_scene_bounds(snk_pt_ctx* ctx) {
+    if (!ctx->scene_bounds_dirty) return;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    bool any = false;
+    for (const snk_instance& in : ctx->instances) {
+        if (in.mesh_id >= ctx->h_meshes.size()) continue;
+        const MeshInfo& M = ctx->h_meshes[in.mesh_id];
+        if (M.blas_root == INVALID) continue;
+        any = true;
+        for (int c = 0; c < 8; c++) {
+            double p[3] = {(c & 1) ? M.hi[0] : M.lo[0], (c & 2) ? M.hi[1] : M.lo[1], (c & 4) ? M.hi[2] : M.lo[2]};
+            for (int r = 0; r < 3; r++) {
+                double v = in.transform[4 * r] * p[0] + in.transform[4 * r + 1] * p[1] + in.transform[4 * r + 2] * p[2] +
+                           in.transform[4 * r + 3];
+                lo[r] = std::min(lo[r], v);
+                hi[r] = std::max(hi[r], v);
+            }
+        }
+    }
+    for (int r = 0; r < 3; r++) {
+        ctx->scene_lo[r] = any ? (float)lo[r] : 0.0f;
+        ctx->scene_hi[r] = any ? (float)hi[r] : 1.0f;
+    }
+    ctx->scene_bounds_dirty = false;
+}
+
 Status build_instances(snk_pt_ctx* ctx) {
     cudaStream_t st = ctx->stream;
     const size_t ni = ctx->instances.size();
-    std::vector<InstTrace> it(ni);
-    std::vector<InstShade> is(ni);
-    std::vector<uint32_t> list;
-    std::vector<uint32_t> emissive;
+    // host: index checks and the two instance lists (instances of empty meshes have
+    // no triangle to hit or sample and are left out of both)
+    std::vector<uint32_t> list, emissive, em_first;
+    list.reserve(ni);
+    uint64_t n_em_tris = 0;
     for (size_t i = 0; i < ni; i++) {
         const snk_instance& in = ctx->instances[i];
         if (in.mesh_id >= ctx->meshes.size()) return Status::Err(SNK_ERR_INVALID_ARG, "instance mesh_id out of range");
         if (in.material_id >= ctx->materials.size())
             return Status::Err(SNK_ERR_INVALID_ARG, "instance material_id out of range");
-        InstShade& S = is[i];
-        std::memcpy(S.m, in.transform, sizeof(S.m));
-        std::memcpy(S.pm, in.prev_transform, sizeof(S.pm));
-        float inv[12];
-        invert_affine(in.transform, inv, S.nmat, &S.det3);
-        S.mesh_id = in.mesh_id;
-        S.material_id = in.material_id;
-        InstTrace& T = it[i];
-        std::memcpy(T.inv, inv, sizeof(inv));
-        T.blas_root = ctx->h_meshes[in.mesh_id].blas_root;
-        T.mesh_id = in.mesh_id;
-        T.material_id = in.material_id;
-        T.pad = 0;
-        if (T.blas_root != INVALID) list.push_back((uint32_t)i);
-        // (instances of empty meshes have no triangle to sample: left out of the list)
-        if ((ctx->materials[in.material_id].flags & SNK_MAT_EMISSIVE) && T.blas_root != INVALID)
+        const MeshInfo& M = ctx->h_meshes[in.mesh_id];
+        if (M.blas_root == INVALID) continue;
+        list.push_back((uint32_t)i);
+        if (ctx->materials[in.material_id].flags & SNK_MAT_EMISSIVE) {
             emissive.push_back((uint32_t)i);
-    }
-    {   // world bounds of the scene (positions of the radiance cache are normalised to them)
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        for (uint32_t i : list) {
-            const snk_instance& in = ctx->instances[i];
-            const MeshInfo& M = ctx->h_meshes[in.mesh_id];
-            for (int c = 0; c < 8; c++) {
-                double p[3] = {(c & 1) ? M.hi[0] : M.lo[0], (c & 2) ? M.hi[1] : M.lo[1], (c & 4) ? M.hi[2] : M.lo[2]};
-                for (int r = 0; r < 3; r++) {
-                    double v = in.transform[4 * r] * p[0] + in.transform[4 * r + 1] * p[1] + in.transform[4 * r + 2] * p[2] +
-                               in.transform[4 * r + 3];
-                    lo[r] = std::min(lo[r], v);
-                    hi[r] = std::max(hi[r], v);
-                }
-            }
-        }
-        for (int r = 0; r < 3; r++) {
-            ctx->scene_lo[r] = list.empty() ? 0.0f : (float)lo[r];
-            ctx->scene_hi[r] = list.empty() ? 1.0f : (float)hi[r];
+            em_first.push_back((uint32_t)n_em_tris);
+            n_em_tris += M.num_triangles;
         }
     }
-    SNK_TRY(upload_changed(ctx->d_inst_trace, ctx->memo[0], it.data(), it.size(), st));
-    SNK_TRY(upload_changed(ctx->d_inst_shade, ctx->memo[1], is.data(), is.size(), st));
-    SNK_TRY(upload_changed(ctx->d_emissive, ctx->memo[2], emissive.data(), emissive.size(), st));
-    ctx->n_emissive = (uint32_t)emissive.size();
+    ctx->scene_bounds_dirty = true;
 
-    // path-tracer local lights: sphere lights, then every emissive triangle,
-    // selected in proportion to emitted power
-    std::vector<LocalLight> lights;
-    std::vector<double> w;
+    // path-tracer local lights: sphere lights (host, few), then every emissive
+    // triangle (device), selected in proportion to emitted power
+    std::vector<LocalLight> spheres;
+    std::vector<double> sw;
     for (size_t k = 0; k < ctx->point_lights.size(); k++) {
         const snk_point_light& P = ctx->point_lights[k];
         if (!(P.radius > 0.0f)) continue;
@@ -366,47 +342,55 @@ Status build_instances(snk_pt_ctx* ctx) {
         L.L[0] = (float)(P.colour[0] * inv_area);
         L.L[1] = (float)(P.colour[1] * inv_area);
         L.L[2] = (float)(P.colour[2] * inv_area);
-        lights.push_back(L);
-        w.push_back(4.0 * M_PI * (0.2126 * P.colour[0] + 0.7152 * P.colour[1] + 0.0722 * P.colour[2]));
+        spheres.push_back(L);
+        sw.push_back(4.0 * M_PI * (0.2126 * P.colour[0] + 0.7152 * P.colour[1] + 0.0722 * P.colour[2]));
     }
-    for (uint32_t ii : emissive) {
-        const snk_instance& in = ctx->instances[ii];
-        const HostMesh& M = ctx->meshes[in.mesh_id];
-        V3 Le = load3(ctx->materials[in.material_id].albedo);
-        for (uint32_t t = 0; t < M.nt; t++) {
-            LocalLight L{};
-            L.kind = 1;
-            L.index = ii;
-            V3 p0 = xform_point(in.transform, load3(&M.pos[3ull * M.idx[3ull * t + 0]]));
-            V3 p1 = xform_point(in.transform, load3(&M.pos[3ull * M.idx[3ull * t + 1]]));
-            V3 p2 = xform_point(in.transform, load3(&M.pos[3ull * M.idx[3ull * t + 2]]));
-            V3 nl = cross(sub(p1, p0), sub(p2, p0));
-            float len = length(nl);
-            float area = 0.5f * len;
-            V3 n = len > 0.0f ? divs(nl, len) : v3(0.0f, 1.0f, 0.0f);
-            L.p0[0] = p0.x; L.p0[1] = p0.y; L.p0[2] = p0.z;
-            L.p1[0] = p1.x; L.p1[1] = p1.y; L.p1[2] = p1.z;
-            L.p2[0] = p2.x; L.p2[1] = p2.y; L.p2[2] = p2.z;
-            L.n[0] = n.x; L.n[1] = n.y; L.n[2] = n.z;
-            L.L[0] = Le.x; L.L[1] = Le.y; L.L[2] = Le.z; L.L[3] = area;
-            lights.push_back(L);
-            w.push_back(2.0 * M_PI * (double)area * (0.2126 * Le.x + 0.7152 * Le.y + 0.0722 * Le.z));
+    const uint64_t n_lights = spheres.size() + n_em_tris;
+    if (n_lights > 0x7FFFFFFFull) return Status::Err(SNK_ERR_INVALID_ARG, "too many emissive triangles");
+
+    // device: instance records and NEE records, redone when their inputs changed
+    bool raw_changed = false, em_changed = false, first_changed = false;
+    SNK_TRY(upload_changed(ctx->d_inst_raw, ctx->memo[0], ctx->instances.data(), ni, st, &raw_changed));
+    SNK_TRY(upload_changed(ctx->d_emissive, ctx->memo[2], emissive.data(), emissive.size(), st, &em_changed));
+    SNK_TRY(upload_changed(ctx->d_em_first, ctx->memo[1], em_first.data(), em_first.size(), st, &first_changed));
+    ctx->n_emissive = (uint32_t)emissive.size();
+    const bool redo = raw_changed || em_changed || first_changed || !ctx->inst_tables_valid;
+    ctx->inst_tables_valid = false;
+    if (redo) {
+        SNK_TRY_CUDA(ctx->d_inst_trace.reserve(ni));
+        SNK_TRY_CUDA(ctx->d_inst_shade.reserve(ni));
+        SNK_TRY(launch_instance_records(ctx->d_inst_raw.p, (uint32_t)ni, ctx->d_meshes.p, ctx->d_inst_trace.p,
+                                        ctx->d_inst_shade.p, st));
+    }
+    SNK_TRY_CUDA(ctx->d_lights.reserve(n_lights));
+    SNK_TRY_CUDA(ctx->d_cdf.reserve(n_lights));
+    SNK_TRY_CUDA(ctx->d_pmf.reserve(n_lights));
+    if (n_em_tris == 0) {
+        // sphere lights only: the whole table is known here (nothing to launch)
+        std::vector<float> cdf(sw.size()), pmf(sw.size());
+        light_cdf_host(sw.data(), (uint32_t)sw.size(), cdf.data(), pmf.data());
+        SNK_TRY(upload_changed(ctx->d_lights, ctx->memo[3], spheres.data(), spheres.size(), st));
+        SNK_TRY(upload_changed(ctx->d_cdf, ctx->memo[4], cdf.data(), cdf.size(), st));
+        SNK_TRY(upload_changed(ctx->d_pmf, ctx->memo[5], pmf.data(), pmf.size(), st));
+    } else if (redo || ctx->lights_changed) {
+        for (int k = 3; k <= 5; k++) ctx->memo[k] = UploadMemo{};
+        SNK_TRY_CUDA(ctx->d_light_w.reserve(n_lights));
+        if (!spheres.empty()) {
+            SNK_TRY_CUDA(cudaMemcpyAsync(ctx->d_lights.p, spheres.data(), spheres.size() * sizeof(LocalLight),
+                                         cudaMemcpyHostToDevice, st));
+            SNK_TRY_CUDA(
+                cudaMemcpyAsync(ctx->d_light_w.p, sw.data(), sw.size() * sizeof(double), cudaMemcpyHostToDevice, st));
         }
+        SNK_TRY(launch_emissive_lights(ctx->d_inst_raw.p, ctx->d_emissive.p, ctx->d_em_first.p,
+                                       (uint32_t)emissive.size(), (uint32_t)n_em_tris, ctx->d_meshes.p, ctx->d_pos.p,
+                                       ctx->d_idx.p, ctx->d_mats.p, ctx->d_lights.p + spheres.size(),
+                                       ctx->d_light_w.p + spheres.size(), st));
+        SNK_TRY(launch_light_cdf(ctx->d_light_w.p, (uint32_t)n_lights, ctx->cdf_scratch, ctx->d_cdf.p, ctx->d_pmf.p, st));
     }
-    double total = 0.0;
-    for (double x : w) total += x;
-    std::vector<float> cdf(w.size()), pmf(w.size());
-    double acc = 0.0;
-    for (size_t k = 0; k < w.size(); k++) {
-        acc += w[k];
-        cdf[k] = total > 0 ? (float)(acc / total) : 0.0f;
-        pmf[k] = total > 0 ? (float)(w[k] / total) : 0.0f;
-    }
-    if (!w.empty() && total > 0) cdf.back() = 1.0f;
-    ctx->n_local = total > 0 ? (uint32_t)lights.size() : 0u;
-    SNK_TRY(upload_changed(ctx->d_lights, ctx->memo[3], lights.data(), lights.size(), st));
-    SNK_TRY(upload_changed(ctx->d_cdf, ctx->memo[4], cdf.data(), cdf.size(), st));
-    SNK_TRY(upload_changed(ctx->d_pmf, ctx->memo[5], pmf.data(), pmf.size(), st));
+    ctx->lights_changed = false;
+    ctx->inst_tables_valid = true;
+    // (a table whose weights are all zero has pmf 0 everywhere: no record is ever used)
+    ctx->n_local = (uint32_t)n_lights;
 
     // instance BVH (rebuilt whenever instances change, as TlasSystem::BuildTlas,
     // or refitted when the tuning asks for it and the topology allows it)
@@ -486,6 +470,7 @@ Status build_all(snk_pt_ctx* ctx) {
         SNK_TRY(build_meshes(ctx));
         ctx->meshes_dirty = false;
         ctx->inst_dirty = true;
+        ctx->inst_tables_valid = false;
     }
     if (ctx->mats_dirty) {
         std::vector<MaterialDev> m(ctx->materials.size());
@@ -494,6 +479,7 @@ Status build_all(snk_pt_ctx* ctx) {
         SNK_TRY(upload(ctx->d_mats, m.data(), m.size(), ctx->stream));
         ctx->mats_dirty = false;
         ctx->inst_dirty = true;
+        ctx->inst_tables_valid = false;
     }
     if (ctx->lights_dirty) {
         static_assert(sizeof(PointLightDev) == sizeof(snk_point_light), "point light layout");
@@ -501,6 +487,7 @@ Status build_all(snk_pt_ctx* ctx) {
                        ctx->point_lights.size(), ctx->stream));
         ctx->lights_dirty = false;
         ctx->inst_dirty = true;
+        ctx->lights_changed = true;
     }
     if (ctx->inst_dirty) {
         SNK_TRY(build_instances(ctx));
@@ -1167,6 +1154,7 @@ namespace {
 
 EncodeParams cache_encode_params(snk_pt_ctx* ctx) {
     EncodeParams ep;
+    if (!ctx->cache_bounds_set) update_scene_bounds(ctx);
     const float* lo = ctx->cache_bounds_set ? ctx->cache_ep.lo : ctx->scene_lo;
     for (int a = 0; a < 3; a++) {
         ep.lo[a] = lo[a];

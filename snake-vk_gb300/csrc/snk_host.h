@@ -8,6 +8,7 @@
 #include <utility>
 
 #include "snk_device.cuh"
+#include "snk_pt.h"
 
 namespace snk {
 
@@ -135,6 +136,24 @@ Status launch_fill_triangles(const uint32_t* prim_order, uint32_t n, const float
 // World boxes of the listed instances (transform of the mesh bounds) for the instance BVH.
 Status launch_instance_boxes(const uint32_t* inst_list, uint32_t n, const InstShade* inst, const MeshInfo* meshes,
                              float4* lo, float4* hi, cudaStream_t s);
+// ---- per-frame scene tables (scene_tables.cu) ---------------------------------
+struct LightCdfScratch {
+    DBuf<unsigned long long> acc, wmax;
+    DBuf<unsigned char> tmp;
+};
+// traversal and shading records of n instances from their raw records
+Status launch_instance_records(const snk_instance* raw, uint32_t n, const MeshInfo* meshes, InstTrace* it,
+                               InstShade* is, cudaStream_t st);
+// NEE records and weights of the n_tri triangles of the emissive instances em_list[0..n_em)
+// (em_first: prefix sums of their triangle counts)
+Status launch_emissive_lights(const snk_instance* raw, const uint32_t* em_list, const uint32_t* em_first, uint32_t n_em,
+                              uint32_t n_tri, const MeshInfo* meshes, const float* pos, const uint32_t* idx,
+                              const MaterialDev* mats, LocalLight* lights, double* w, cudaStream_t st);
+// light-selection CDF and PMF of n weights (quantised to integers, exact prefix sums)
+Status launch_light_cdf(const double* w, uint32_t n, LightCdfScratch& sc, float* cdf, float* pmf, cudaStream_t st);
+// the same table computed on the host (for tables whose weights are all known there)
+void light_cdf_host(const double* w, uint32_t n, float* cdf, float* pmf);
+
 // tlas_prims[k] = inst_list[prim_order[k]]
 Status launch_map_prims(const uint32_t* prim_order, const uint32_t* inst_list, uint32_t n, uint32_t* out,
                         cudaStream_t s);

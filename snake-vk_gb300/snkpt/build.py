@@ -35,6 +35,7 @@ UNITS = {
     "taa.cu": True,
     "meshdata.cpp": False,
     "particles.cu": True,
+    "scene_tables.cu": True,
 }
 
 

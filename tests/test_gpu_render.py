@@ -68,6 +68,35 @@ def test_path_depth_and_roulette(cuda, built_lib, max_depth, rr_depth):
         assert s["rays_extension"] == 0
 
 
+def test_light_tables_follow_instance_updates(cuda, built_lib):
+    """Instance and light tables across rebuilds of one context: emissive
+    instances present (device-built triangle lights), removed (sphere-light
+    table built on the host), back and moved, and set again unchanged (tables
+    kept); every frame matches the oracle scene with the same instances."""
+    sc = scenes.config1(width=64, height=48)
+    em_mat = len(sc.materials)
+    mats = np.concatenate([sc.materials, sc.materials[:1]])
+    mats["flags"][-1] |= abi.MAT_EMISSIVE
+    mats["albedo"][-1][:3] = (3.0, 2.5, 2.0)
+    sc.materials = mats
+    base = np.array(sc.instances, copy=True)
+    lamps = np.array(base[1:5], copy=True)   # four icospheres turned into emitters
+    lamps["material_id"] = em_mat
+    with_lamps = np.concatenate([base, lamps])
+    moved = np.array(with_lamps, copy=True)
+    moved["transform"][-4:, [3, 7, 11]] += 0.25
+    st = abi.settings(spp=1, max_depth=3, rr_depth=3, seed=5)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    osc = O.OracleScene(sc)
+    for step, inst in enumerate((with_lamps, base, moved, moved)):
+        pt.set_instances(inst)
+        osc.set_instances(inst)
+        g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+        r = osc.render_path(sc.views[0], st)
+        _compare(g, r, f"update {step}")
+
+
 def test_path_config1_reduced_full_frame(cuda, built_lib):
     sc = scenes.config1(width=480, height=270)
     st = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=1)
