@@ -7,7 +7,7 @@ import pytest
 
 import oracle as O
 import snkpt
-from helpers import max_rel
+from helpers import assert_hits_equal, camera_rays, max_rel, random_rays
 from snkpt import abi, scenes
 
 pytestmark = pytest.mark.gpu
@@ -370,3 +370,55 @@ def _tracer(sc):
     pt = snkpt.PathTracer(0)
     pt.load_scene(sc)
     return pt
+
+
+def _odd_geometry_scene():
+    """Config 1 (reduced) with transforms and triangles the regular scenes do not
+    have: mirrored, non-uniformly scaled and sheared icospheres; a mesh of
+    degenerate triangles (repeated vertex, collinear, a sliver) with a triangle
+    listed twice; and two coincident instances of it (ties in t broken by
+    instance, then triangle index)."""
+    sc = scenes.config1(width=96, height=64)
+    inst = np.array(sc.instances, copy=True)
+    odd = {1: scenes.affine(scale=(-1.0, 1.0, 1.0)), 2: scenes.affine(scale=(2.0, 0.5, 1.0)),
+           3: scenes.affine(R=[[1.0, 0.6, 0.0], [0.0, 1.0, 0.0], [0.0, 0.3, 1.0]]),
+           4: scenes.affine(scale=(-1.5, -0.7, 1.2))}
+    for i, m in odd.items():
+        t = inst["transform"][i].reshape(3, 4).astype(np.float64)
+        m = m.astype(np.float64)
+        # keep the instance where it was, change the linear part
+        new = np.concatenate([m[:, :3] @ t[:, :3], t[:, 3:]], 1).astype(np.float32)
+        inst["transform"][i] = new.reshape(12)
+        inst["prev_transform"][i] = new.reshape(12)
+    p = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [2, 0, 0], [1, 1e-7, 0], [0, 2, 0], [1, 1, 0]], np.float32)
+    tri = np.array([[0, 1, 2], [0, 0, 1], [0, 1, 3], [1, 4, 3], [2, 1, 6], [0, 1, 2], [2, 5, 6]], np.uint32)
+    nrm = np.tile(np.array([[0, 0, 1]], np.float32), (len(p), 1))
+    sc.meshes.append(scenes.Mesh(p, nrm, tri))
+    mid = len(sc.meshes) - 1
+    extra = np.zeros(3, inst.dtype)
+    for k, (x, z) in enumerate([(0.0, 2.0), (1.5, 3.0), (1.5, 3.0)]):
+        m = scenes.affine(R=scenes.rot_x(-0.4), scale=(1.5, 1.5, 1.5), t=(x, 0.5, z)).reshape(12)
+        extra[k]["transform"] = m
+        extra[k]["prev_transform"] = m
+        extra[k]["mesh_id"] = mid
+        extra[k]["material_id"] = k % len(sc.materials)
+    sc.instances = np.concatenate([inst, extra])
+    return sc
+
+
+def test_odd_transforms_and_degenerate_triangles(cuda, built_lib):
+    sc = _odd_geometry_scene()
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    osc = O.OracleScene(sc)
+    st = abi.settings(spp=2, max_depth=3, rr_depth=3, seed=13)
+    g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    r = osc.render_path(sc.views[0], st)
+    _compare(g, r, "odd transforms / degenerate triangles")
+    rays = np.concatenate([camera_rays(sc.views[0]), random_rays(sc, 200_000, np.random.default_rng(31))])
+    assert_hits_equal(pt.trace_rays(rays), osc.trace(rays), "odd geometry closest")
+    assert_hits_equal(pt.trace_rays(rays, any_hit=True), osc.trace(rays, any_hit=True), "odd geometry any")
+    # the coincident instances: every hit on either is reported on the lower instance index
+    n = len(sc.instances)
+    h = osc.trace(rays)
+    assert not (h["inst"] == n - 1).any() and (h["inst"] == n - 2).any()
