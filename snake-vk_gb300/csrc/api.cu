@@ -40,6 +40,7 @@ struct RestirState {
     DBuf<float4> ris;                    // initial-pass state between its recording and replaying runs
     DBuf<uint4> memo_keys;               // initial-pass visibility tests reused by the spatial pass
     DBuf<uint32_t> plan;                 // final-shading answers, spatial phase 1 -> 2
+    DBuf<float4> combo;                  // combine targets between the recording and replaying runs
     uint32_t history_valid = 0;
     uint32_t hist = 1, spat = 2;        // which of b/c holds history / receives spatial
 };
@@ -989,6 +990,9 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             RV.spatial = R.spat == 1 ? R.res_b.p : R.res_c.p;
             RV.ris = R.ris.p;
             RV.memo_keys = R.memo_keys.p; RV.plan = R.plan.p;
+            if (R.combo.reserve((RESTIR_TEMPORAL_COMBOS + 1u + (uint32_t)std::max(rs.restir_spatial, 0)) * np))
+                return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir buffers");
+            RV.combo = R.combo.p;
             RV.history_valid = R.history_valid;
             RestirSettings s;
             s.frame_index = rs.frame_index; s.seed = rs.seed; s.candidates = rs.restir_candidates;

@@ -296,7 +296,7 @@ __device__ __forceinline__ float tri_shadow(Ctx& c, uint32_t inst, uint32_t tri,
 }
 
 __device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, const Shade& sh,
-                                        bool shadow) {
+                                        bool shadow, V3* unshadowed = nullptr) {
     const SceneDev& S = *c.S;
     V3 p, pn;
     tri_point(S, inst, tri, bu, bv, &p, &pn);
@@ -306,6 +306,7 @@ __device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, flo
     float d2 = fabsf(dot(dd, dd));
     V3 rad = v3(((em.x * sh.albedo.x) * brdf.x) / d2, ((em.y * sh.albedo.y) * brdf.y) / d2,
                 ((em.z * sh.albedo.z) * brdf.z) / d2);
+    if (unshadowed) *unshadowed = rad;
     if (shadow) {
         V3 target = add(p, mul(pn, 0.01f));
         float dist = length(sub(sh.biased, target));
@@ -315,24 +316,58 @@ __device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, flo
     return rad;
 }
 
+// Unshadowed target values of a pixel's combines, kept between the recording and
+// the replaying run of a pass: slot j (the pixel's j-th combine) holds
+// (|point-light radiance|, emissive radiance) at p[j * stride].  The recording run
+// fills the slots; the replaying run reads them instead of evaluating the lights
+// again and only applies the visibility it now knows.
+struct ComboSlots {
+    float4* p;
+    size_t stride;
+    uint32_t j, cap;
+    bool fill, use;
+};
+
 __device__ __noinline__ void combine(Ctx& c, Reservoir& cur, const Reservoir& nb, float& phat_pl, float& phat_em,
-                                     const Shade& sh, Pcg& rng) {
+                                     const Shade& sh, Pcg& rng, ComboSlots& cs) {
     const SceneDev& S = *c.S;
+    float4* slot = (cs.p && cs.j < cs.cap) ? cs.p + cs.j * cs.stride : nullptr;
+    cs.j++;
+    const bool use = cs.use && slot;
+    float4 cv = use ? *slot : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const V3 none = v3(0.0f, 0.0f, 0.0f);   // (a replayed test needs no ray)
     if (nb.pl_idx != INVALID) {
-        const PointLightDev& L = S.point_lights[nb.pl_idx];
-        V3 lp = load3(L.pos);
-        float ld = length(sub(lp, sh.biased));
-        float vis = shadow_test_pl(c, nb.pl_idx, true, sh.biased, divs(sub(lp, sh.biased), ld), ld - 0.001f);
-        float p_hat = length(calc_pointlight(L, sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal, sh.albedo)) * vis;
+        float vis, len;
+        if (use) {
+            vis = shadow_test_pl(c, nb.pl_idx, true, none, none, 0.0f);
+            len = cv.x;
+        } else {
+            const PointLightDev& L = S.point_lights[nb.pl_idx];
+            V3 lp = load3(L.pos);
+            float ld = length(sub(lp, sh.biased));
+            vis = shadow_test_pl(c, nb.pl_idx, true, sh.biased, divs(sub(lp, sh.biased), ld), ld - 0.001f);
+            len = length(calc_pointlight(L, sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal, sh.albedo));
+            cv.x = len;
+        }
+        float p_hat = len * vis;
         float w = (p_hat * (float)nb.pl_m) * nb.w_pl;
         if (update_pl(cur, nb.pl_idx, w, rng)) phat_pl = p_hat;
     }
     if (nb.em_inst != INVALID) {
-        V3 rad = tri_radiance(c, nb.em_inst, nb.em_tri, nb.em_u, nb.em_v, sh, true);
+        V3 rad;
+        if (use) {
+            rad = mul(v3(cv.y, cv.z, cv.w),
+                      shadow_test_em(c, key_em(nb.em_inst, nb.em_tri, nb.em_u, nb.em_v), none, none, 0.0f));
+        } else {
+            V3 un;
+            rad = tri_radiance(c, nb.em_inst, nb.em_tri, nb.em_u, nb.em_v, sh, true, &un);
+            cv.y = un.x; cv.z = un.y; cv.w = un.z;
+        }
         float p_hat = length(rad);
         float w = (p_hat * nb.w_em) * (float)nb.m_em;
         if (update_em(cur, nb.em_inst, nb.em_tri, nb.em_u, nb.em_v, w, rng)) phat_em = p_hat;
     }
+    if (cs.fill && slot) *slot = cv;
 }
 
 __device__ __forceinline__ Shade shade_of(const ViewParams& vw, V3 pos, V3 n, V3 albedo, float rough, float metal) {
@@ -541,8 +576,9 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
                         }
                         Reservoir T = res_init();
                         float tp_pl = 0.0f, tp_em = 0.0f;
-                        combine(c, T, Rr, tp_pl, tp_em, sh, rng);
-                        combine(c, T, Hh, tp_pl, tp_em, sh, rng);
+                        ComboSlots cs{R.combo + o, n, 0u, RESTIR_TEMPORAL_COMBOS, record, !record};
+                        combine(c, T, Rr, tp_pl, tp_em, sh, rng, cs);
+                        combine(c, T, Hh, tp_pl, tp_em, sh, rng, cs);
                         T.m_em = Hh.m_em + Rr.m_em;
                         T.pl_m = Hh.pl_m + Rr.pl_m;
                         T.w_em = tp_em > 0.0f ? (T.w_sum_em / (float)T.m_em) / tp_em : 0.0f;
@@ -658,7 +694,9 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
                 Rr = res_init();
                 float phat_pl = 0.0f, phat_em = 0.0f;
                 Reservoir self = res_load(R.temporal, o);
-                combine(c, Rr, self, phat_pl, phat_em, sh, rng);
+                ComboSlots cs{R.combo + (size_t)RESTIR_TEMPORAL_COMBOS * n + o, n, 0u, 1u + (uint32_t)rs.spatial,
+                              phase == 0, phase == 1};
+                combine(c, Rr, self, phat_pl, phat_em, sh, rng, cs);
                 Rr.m_em += self.m_em;
                 Rr.pl_m += self.pl_m;
                 for (int i = 0; i < rs.spatial; i++) {
@@ -676,7 +714,7 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
                     V3 qn = qp.w == 1.0f ? v3(qn4.x, qn4.y, qn4.z) : v3(0.0f, 0.0f, 0.0f);
                     if (dot(qn, nrm) < 0.95f) continue;
                     Reservoir Q = res_load(R.temporal, qi);
-                    combine(c, Rr, Q, phat_pl, phat_em, sh, rng);
+                    combine(c, Rr, Q, phat_pl, phat_em, sh, rng, cs);
                     Rr.m_em += Q.m_em;
                     Rr.pl_m += Q.pl_m;
                 }

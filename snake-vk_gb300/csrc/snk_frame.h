@@ -87,8 +87,12 @@ struct RestirView {
     float4* ris;        // 2 per pixel: the initial pass's RIS state between its two runs
     uint4* memo_keys;   // 4 per pixel: the initial pass's visibility tests and their results
     uint32_t* plan;     // per pixel: how the final shading's two tests are answered (codes, 16 bits each)
+    float4* combo;      // unshadowed combine targets, slot-major (slot * pixels + pixel): the temporal
+                        // pass's RESTIR_TEMPORAL_COMBOS slots, then the spatial pass's 1 + spatial
     uint32_t history_valid;
 };
+
+constexpr uint32_t RESTIR_TEMPORAL_COMBOS = 2;   // current + history reservoir
 
 struct RestirSettings {
     uint32_t frame_index, seed, candidates, mcap;
