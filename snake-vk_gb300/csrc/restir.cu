@@ -295,17 +295,40 @@ __device__ __forceinline__ float tri_shadow(Ctx& c, uint32_t inst, uint32_t tri,
     return shadow_test_em(c, key_em(inst, tri, bu, bv), surface_pos, dir, dist);
 }
 
+// ComputeTriangleRadiance without the shadow test: emission of instance inst
+// arriving from world point p at the shading point (no light-side cosine)
+__device__ __forceinline__ V3 emitted_at(const SceneDev& S, uint32_t inst, V3 p, const Shade& sh) {
+    V3 em = load3(S.materials[S.inst_shade[inst].material_id].albedo);
+    V3 brdf = cook_torrance(brdf_terms(normalize(sub(p, sh.ro)), sh.v, sh.f0, sh.n, sh.rough, sh.metal));
+    V3 dd = sub(sh.ro, p);
+    float d2 = fabsf(dot(dd, dd));
+    return v3(((em.x * sh.albedo.x) * brdf.x) / d2, ((em.y * sh.albedo.y) * brdf.y) / d2,
+              ((em.z * sh.albedo.z) * brdf.z) / d2);
+}
+
+// The unshadowed radiance of sample (bu, bv) of the triangle and, when asked
+// for, the triangle's world-space area (det(mat3) x object area), from one fetch
+// of its vertices (the sample's normal is not needed: no shadow ray is aimed)
+__device__ __noinline__ V3 tri_candidate(const SceneDev& S, uint32_t inst, uint32_t tri, float bu, float bv,
+                                         const Shade& sh, float* area) {
+    const InstShade& I = S.inst_shade[inst];
+    const MeshInfo& M = S.meshes[I.mesh_id];
+    const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
+    V3 p0 = load3(S.positions + 3ull * (M.vertex_offset + ix[0]));
+    V3 p1 = load3(S.positions + 3ull * (M.vertex_offset + ix[1]));
+    V3 p2 = load3(S.positions + 3ull * (M.vertex_offset + ix[2]));
+    if (area) *area = (I.det3 * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
+    float bz = (1.0f - bu) - bv;
+    V3 q = add(add(mul(p0, bu), mul(p1, bv)), mul(p2, bz));
+    return emitted_at(S, inst, xform_point(I.m, q), sh);
+}
+
 __device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, const Shade& sh,
                                         bool shadow, V3* unshadowed = nullptr) {
     const SceneDev& S = *c.S;
     V3 p, pn;
     tri_point(S, inst, tri, bu, bv, &p, &pn);
-    V3 em = load3(S.materials[S.inst_shade[inst].material_id].albedo);
-    V3 brdf = cook_torrance(brdf_terms(normalize(sub(p, sh.ro)), sh.v, sh.f0, sh.n, sh.rough, sh.metal));
-    V3 dd = sub(sh.ro, p);
-    float d2 = fabsf(dot(dd, dd));
-    V3 rad = v3(((em.x * sh.albedo.x) * brdf.x) / d2, ((em.y * sh.albedo.y) * brdf.y) / d2,
-                ((em.z * sh.albedo.z) * brdf.z) / d2);
+    V3 rad = emitted_at(S, inst, p, sh);
     if (unshadowed) *unshadowed = rad;
     if (shadow) {
         V3 target = add(p, mul(pn, 0.01f));
@@ -519,12 +542,8 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
                         if (tri > ntri - 1) tri = ntri - 1;
                         float bu = pcg_float(rng), bv = pcg_float(rng);
                         if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
-                        const uint32_t* ix = S.indices + M.index_offset + 3ull * tri;
-                        V3 p0 = load3(S.positions + 3ull * (M.vertex_offset + ix[0]));
-                        V3 p1 = load3(S.positions + 3ull * (M.vertex_offset + ix[1]));
-                        V3 p2 = load3(S.positions + 3ull * (M.vertex_offset + ix[2]));
-                        float area = (I.det3 * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
-                        V3 rad = tri_radiance(c, inst, tri, bu, bv, sh, false);
+                        float area;
+                        V3 rad = tri_candidate(S, inst, tri, bu, bv, sh, &area);
                         float p_hat = length(rad);
                         float pdf = 1.0f / ((float)(nem * ntri) * area);
                         float w = p_hat / pdf;
@@ -756,7 +775,8 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
                     e = tri_radiance(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, true);
                     code_em = c.last;
                 } else {
-                    e = mul(tri_radiance(c, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, false), plan_vis(c, plan >> 16));
+                    e = mul(tri_candidate(S, Rr.em_inst, Rr.em_tri, Rr.em_u, Rr.em_v, sh, nullptr),
+                            plan_vis(c, plan >> 16));
                 }
                 rad = add(rad, mul(e, Rr.w_em));
             }
