@@ -80,6 +80,7 @@ struct snk_pt_ctx {
     DBuf<uint32_t> d_emissive;
     DBuf<snk_instance> d_inst_raw;     // the caller's instance records, as given
     DBuf<uint32_t> d_em_first;         // first NEE record of each emissive instance's triangles
+    DBuf<EmissiveRec> d_em_recs;       // ReSTIR candidate record of each emissive instance
     DBuf<LocalLight> d_lights;
     DBuf<double> d_light_w;            // selection weight of every NEE record
     DBuf<float> d_cdf, d_pmf;
@@ -362,6 +363,9 @@ Status build_instances(snk_pt_ctx* ctx) {
         SNK_TRY_CUDA(ctx->d_inst_shade.reserve(ni));
         SNK_TRY(launch_instance_records(ctx->d_inst_raw.p, (uint32_t)ni, ctx->d_meshes.p, ctx->d_inst_trace.p,
                                         ctx->d_inst_shade.p, st));
+        SNK_TRY_CUDA(ctx->d_em_recs.reserve(emissive.size()));
+        SNK_TRY(launch_emissive_records(ctx->d_emissive.p, (uint32_t)emissive.size(), ctx->d_inst_shade.p,
+                                        ctx->d_meshes.p, ctx->d_mats.p, ctx->d_em_recs.p, st));
     }
     SNK_TRY_CUDA(ctx->d_lights.reserve(n_lights));
     SNK_TRY_CUDA(ctx->d_cdf.reserve(n_lights));
@@ -519,6 +523,7 @@ SceneDev scene_dev(snk_pt_ctx* ctx) {
     S.num_point_lights = (uint32_t)ctx->point_lights.size();
     S.num_emissive_instances = ctx->n_emissive;
     S.emissive_instances = ctx->d_emissive.p;
+    S.emissive_recs = ctx->d_em_recs.p;
     S.local_lights = ctx->d_lights.p;
     S.light_cdf = ctx->d_cdf.p;
     S.light_pmf = ctx->d_pmf.p;

@@ -323,6 +323,29 @@ __device__ __noinline__ V3 tri_candidate(const SceneDev& S, uint32_t inst, uint3
     return emitted_at(S, inst, xform_point(I.m, q), sh);
 }
 
+// tri_candidate for an initial RIS candidate, reading the emissive instance's record
+__device__ __noinline__ V3 rec_candidate(const SceneDev& S, const EmissiveRec* E, uint32_t tri, float bu, float bv,
+                                         const Shade& sh, float* area) {
+    const float4* rp = reinterpret_cast<const float4*>(E);
+    const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3], r4 = rp[4];
+    const float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+    const uint32_t index_offset = __float_as_uint(r3.w), vertex_offset = __float_as_uint(r4.x);
+    const uint32_t* ix = S.indices + index_offset + 3ull * tri;
+    V3 p0 = load3(S.positions + 3ull * (vertex_offset + ix[0]));
+    V3 p1 = load3(S.positions + 3ull * (vertex_offset + ix[1]));
+    V3 p2 = load3(S.positions + 3ull * (vertex_offset + ix[2]));
+    *area = (r3.x * 0.5f) * length(cross(sub(p1, p0), sub(p1, p2)));
+    float bz = (1.0f - bu) - bv;
+    V3 q = add(add(mul(p0, bu), mul(p1, bv)), mul(p2, bz));
+    V3 p = xform_point(m, q);
+    V3 em = v3(r4.y, r4.z, r4.w);
+    V3 brdf = cook_torrance(brdf_terms(normalize(sub(p, sh.ro)), sh.v, sh.f0, sh.n, sh.rough, sh.metal));
+    V3 dd = sub(sh.ro, p);
+    float d2 = fabsf(dot(dd, dd));
+    return v3(((em.x * sh.albedo.x) * brdf.x) / d2, ((em.y * sh.albedo.y) * brdf.y) / d2,
+              ((em.z * sh.albedo.z) * brdf.z) / d2);
+}
+
 __device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, const Shade& sh,
                                         bool shadow, V3* unshadowed = nullptr) {
     const SceneDev& S = *c.S;
@@ -534,16 +557,14 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
                     for (uint32_t i = 0; i < rs.candidates; i++) {
                         uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
                         if (k > nem - 1) k = nem - 1;
-                        uint32_t inst = S.emissive_instances[k];
-                        const InstShade& I = S.inst_shade[inst];
-                        const MeshInfo& M = S.meshes[I.mesh_id];
-                        uint32_t ntri = M.num_triangles;
+                        const EmissiveRec* E = S.emissive_recs + k;
+                        const uint32_t inst = E->inst, ntri = E->ntri;
                         uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
                         if (tri > ntri - 1) tri = ntri - 1;
                         float bu = pcg_float(rng), bv = pcg_float(rng);
                         if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
                         float area;
-                        V3 rad = tri_candidate(S, inst, tri, bu, bv, sh, &area);
+                        V3 rad = rec_candidate(S, E, tri, bu, bv, sh, &area);
                         float p_hat = length(rad);
                         float pdf = 1.0f / ((float)(nem * ntri) * area);
                         float w = p_hat / pdf;

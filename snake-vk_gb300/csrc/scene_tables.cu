@@ -85,6 +85,25 @@ __global__ void k_instance_records(const snk_instance* __restrict__ raw, uint32_
     is[i] = S;
 }
 
+__global__ void k_emissive_records(const uint32_t* __restrict__ em_list, uint32_t n_em,
+                                   const InstShade* __restrict__ is, const MeshInfo* __restrict__ meshes,
+                                   const MaterialDev* __restrict__ mats, EmissiveRec* __restrict__ recs) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_em) return;
+    const uint32_t ii = em_list[e];
+    const InstShade& I = is[ii];
+    const MeshInfo& M = meshes[I.mesh_id];
+    EmissiveRec r;
+    for (int k = 0; k < 12; k++) r.m[k] = I.m[k];
+    r.det3 = I.det3;
+    r.inst = ii;
+    r.ntri = M.num_triangles;
+    r.index_offset = M.index_offset;
+    r.vertex_offset = M.vertex_offset;
+    for (int k = 0; k < 3; k++) r.albedo[k] = mats[I.material_id].albedo[k];
+    recs[e] = r;
+}
+
 // one thread per emissive triangle j: emissive instance e = the last with
 // first[e] <= j, triangle j - first[e] of its mesh
 __global__ void k_emissive_lights(const snk_instance* __restrict__ raw, const uint32_t* __restrict__ em_list,
@@ -173,6 +192,14 @@ Status launch_instance_records(const snk_instance* raw, uint32_t n, const MeshIn
                                InstShade* is, cudaStream_t st) {
     if (n == 0) return Status::Ok();
     k_instance_records<<<blocks_for(n, 128), 128, 0, st>>>(raw, n, meshes, it, is);
+    SNK_TRY_CUDA(cudaGetLastError());
+    return Status::Ok();
+}
+
+Status launch_emissive_records(const uint32_t* em_list, uint32_t n_em, const InstShade* is, const MeshInfo* meshes,
+                               const MaterialDev* mats, EmissiveRec* recs, cudaStream_t st) {
+    if (n_em == 0) return Status::Ok();
+    k_emissive_records<<<blocks_for(n_em, 128), 128, 0, st>>>(em_list, n_em, is, meshes, mats, recs);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }

@@ -270,6 +270,18 @@ struct LocalLight {     // path-tracer NEE table: sphere lights, then emissive t
     float L[4];                  // radiance (w = area)
 };
 
+// per emissive instance (ReSTIR candidate sampling): copies of what one candidate
+// reads from the instance, mesh and material records, so a candidate costs one
+// record fetch before its triangle's indices
+struct alignas(16) EmissiveRec {
+    float m[12];                 // object -> world (the instance's transform)
+    float det3;                  // determinant(mat3(m))
+    uint32_t inst, ntri, index_offset;
+    uint32_t vertex_offset;
+    float albedo[3];             // emitted radiance (the material's albedo)
+};
+static_assert(sizeof(EmissiveRec) == 80, "emissive record is 80 bytes");
+
 struct DirLightDev { float dir[3]; uint32_t enabled; float colour[3]; float pad; };
 
 // device pointers of the whole scene, passed by value to kernels
@@ -291,6 +303,7 @@ struct SceneDev {
     uint32_t num_point_lights;
     uint32_t num_emissive_instances;
     const uint32_t* emissive_instances;
+    const EmissiveRec* emissive_recs;   // one per entry of emissive_instances
     const LocalLight* local_lights;
     const float* light_cdf;
     const float* light_pmf;

@@ -144,6 +144,9 @@ struct LightCdfScratch {
 // traversal and shading records of n instances from their raw records
 Status launch_instance_records(const snk_instance* raw, uint32_t n, const MeshInfo* meshes, InstTrace* it,
                                InstShade* is, cudaStream_t st);
+// ReSTIR candidate records of the emissive instances em_list[0..n_em) (after their instance records)
+Status launch_emissive_records(const uint32_t* em_list, uint32_t n_em, const InstShade* is, const MeshInfo* meshes,
+                               const MaterialDev* mats, EmissiveRec* recs, cudaStream_t st);
 // NEE records and weights of the n_tri triangles of the emissive instances em_list[0..n_em)
 // (em_first: prefix sums of their triangle counts)
 Status launch_emissive_lights(const snk_instance* raw, const uint32_t* em_list, const uint32_t* em_first, uint32_t n_em,
