@@ -1011,8 +1011,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             ctx->prof_chain = false;   // the queue reset below is not part of a stage
             if (cudaMemsetAsync(ctx->rq_work.p, 0, 3 * sizeof(uint32_t), st) != cudaSuccess)
                 return fail(ctx, SNK_ERR_CUDA, "restir queue reset");
-            const RestirQueue q1{ctx->rq_rays.p, ctx->rq_vis_a.p, K1, 0u}, q2{ctx->rq_rays.p, ctx->rq_vis_b.p, K2, 0u},
-                q3{ctx->rq_rays.p, ctx->rq_vis_a.p, K3, 0u};
+            const RestirQueue q1{ctx->rq_rays.p, ctx->rq_vis_a.p, K1, (uint32_t)np},
+                q2{ctx->rq_rays.p, ctx->rq_vis_b.p, K2, (uint32_t)np}, q3{ctx->rq_rays.p, ctx->rq_vis_a.p, K3, (uint32_t)np};
             const int tg = trace_grid(ctx);
             const SceneDev SD = scene_dev(ctx);
             const TraceTuning tt = trace_tuning(ctx);

@@ -101,7 +101,8 @@ struct Ctx {
     uint32_t reused;        // tests answered by an earlier identical test (counted when recording)
     float4* rays;           // recording
     const uint8_t* vis;     // replaying
-    size_t base;
+    size_t base;            // the pixel: slot k is entry base + k * stride
+    size_t stride;          // pixels of the view
     uint32_t k, cap;
     bool overflow;
     Memo* m;                // tests made so far (null: no reuse)
@@ -111,7 +112,8 @@ struct Ctx {
 __device__ __forceinline__ void ctx_queue(Ctx& c, const RestirQueue& q, uint32_t pixel, bool record) {
     c.rays = record ? q.rays : nullptr;
     c.vis = record ? nullptr : q.vis;
-    c.base = (size_t)pixel * q.per_pixel;
+    c.base = pixel;
+    c.stride = q.pixels;
     c.k = 0;
     c.cap = q.per_pixel;
 }
@@ -119,14 +121,14 @@ __device__ __forceinline__ void ctx_queue(Ctx& c, const RestirQueue& q, uint32_t
 // marks the slots a recording pass left unused as empty (tmax < 0)
 __device__ __forceinline__ void ctx_close(Ctx& c) {
     if (!c.rays) return;
-    for (uint32_t k = c.k; k < c.cap; k++) c.rays[2 * (c.base + k) + 1] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    for (uint32_t k = c.k; k < c.cap; k++) c.rays[2 * (c.base + k * c.stride) + 1] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
 }
 
 // 1 when the segment is unoccluded (recording: always 1, the value is not used
 // for anything the replay would see differently)
 __device__ __noinline__ float shadow_test(Ctx& c, V3 o, V3 d, float tmax) {
     if (c.k >= c.cap) { c.overflow = true; return 0.0f; }
-    const size_t slot = c.base + c.k++;
+    const size_t slot = c.base + (size_t)c.k++ * c.stride;
     if (c.rays) {
         c.shadow_rays++;
         c.rays[2 * slot] = make_float4(o.x, o.y, o.z, SHADOW_TMIN);
@@ -141,7 +143,7 @@ __device__ __forceinline__ float memo_answer(Ctx& c, uint32_t code) {
     if (c.rays) c.reused++;
     c.last = code;
     if (code & MEMO_KNOWN) return (code & 1u) ? 1.0f : 0.0f;
-    return c.rays ? 1.0f : (c.vis[c.base + code] ? 1.0f : 0.0f);
+    return c.rays ? 1.0f : (c.vis[c.base + code * c.stride] ? 1.0f : 0.0f);
 }
 
 // shadow test toward point light idx at its full distance (minus == false) or at
@@ -189,7 +191,7 @@ __device__ __forceinline__ uint4 key_em(uint32_t inst, uint32_t tri, float u, fl
 
 // after a replay: tests still pointing at slots of the replayed queue get their results
 __device__ __forceinline__ uint32_t resolve_code(const Ctx& c, uint32_t code) {
-    return (code & MEMO_KNOWN) ? code : (MEMO_KNOWN | (c.vis[c.base + code] ? 1u : 0u));
+    return (code & MEMO_KNOWN) ? code : (MEMO_KNOWN | (c.vis[c.base + code * c.stride] ? 1u : 0u));
 }
 __device__ __forceinline__ void memo_resolve(Ctx& c) {
     Memo* m = c.m;
@@ -234,7 +236,7 @@ __device__ __forceinline__ float plan_vis(const Ctx& c, uint32_t code) {
     if (code == MEMO_NONE) return 0.0f;   // (phase 2 only asks for tests phase 1 made)
     if (code & MEMO_KNOWN) return (code & 1u) ? 1.0f : 0.0f;
     if (code >= c.cap || !c.vis) return 0.0f;
-    return c.vis[c.base + code] ? 1.0f : 0.0f;
+    return c.vis[c.base + code * c.stride] ? 1.0f : 0.0f;
 }
 
 __device__ __forceinline__ void ctx_check(Ctx& c) {

@@ -101,14 +101,16 @@ struct RestirSettings {
     uint32_t pad;
 };
 
-// Visibility rays of a ReSTIR pass: per pixel `per_pixel` slots of 2 float4
-// (origin, tmin | direction, tmax) at rays[2 * (pixel * per_pixel + k)].  A pass
-// either records its rays into `rays` or replays their results from `vis`.
+// Visibility rays of a ReSTIR pass: `per_pixel` slots for each of the view's
+// `pixels` pixels, slot-major: slot k of pixel p is entry k * pixels + p, whose
+// ray is 2 float4 (origin, tmin | direction, tmax) at rays[2 * entry].  Slot k
+// of neighbouring pixels is written, traced and read together.  A pass either
+// records its rays into `rays` or replays their results from `vis`.
 struct RestirQueue {
     float4* rays;
     const uint8_t* vis;
     uint32_t per_pixel;
-    uint32_t pad;
+    uint32_t pixels;
 };
 // slots per pixel of the passes
 constexpr uint32_t RESTIR_INITIAL_SLOTS = 6;   // 2 visibility + 2 x 2 temporal combine
