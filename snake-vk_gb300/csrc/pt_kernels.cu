@@ -116,9 +116,8 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
             if (i < n) {
                 hit = F.hits[i].flags != 0u;
                 if (!hit) {
-                    float4* sr = F.shadow_rays + 4ull * i;
-                    sr[1].w = -1.0f;
-                    sr[3].w = -1.0f;
+                    F.shadow_rays[2 * shadow_entry(F, i, 0) + 1].w = -1.0f;
+                    F.shadow_rays[2 * shadow_entry(F, i, 1) + 1].w = -1.0f;
                     if (d == 0) {
                         uint32_t gpix, s, vi, x, y;
                         const bool train = decode_path(F, F.path_ids[cur][i], &gpix, &s, &vi, &x, &y);
@@ -154,9 +153,10 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 float4 rd4 = F.rays[cur][2ull * i + 1];
                 V3 rd = v3(rd4.x, rd4.y, rd4.z);
                 HitDev h = F.hits[i];
-                float4* sr = F.shadow_rays + 4ull * i;
-                sr[1].w = -1.0f;
-                sr[3].w = -1.0f;
+                float4* sr0 = F.shadow_rays + 2 * shadow_entry(F, i, 0);
+                float4* sr1 = F.shadow_rays + 2 * shadow_entry(F, i, 1);
+                sr0[1].w = -1.0f;
+                sr1[1].w = -1.0f;
                 Pcg rng = pcg_stream(gpix, s, d, F.seed);
                 if (d == 0) { pcg_next(rng); pcg_next(rng); }
                 const bool gbuf = d == 0 && s == 0 && !train;
@@ -211,9 +211,9 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                                                     sf.roughness, sf.metallic, sf.albedo);
                             if (maxc(c) > 0.0f) {
                                 V3 cb = cmul(beta, c);
-                                sr[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
-                                sr[1] = make_float4(S.dir_light.dir[0], S.dir_light.dir[1], S.dir_light.dir[2], T_FAR);
-                                F.shadow_contrib[2ull * i] = make_float4(cb.x, cb.y, cb.z, 0.0f);
+                                sr0[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
+                                sr0[1] = make_float4(S.dir_light.dir[0], S.dir_light.dir[1], S.dir_light.dir[2], T_FAR);
+                                F.shadow_contrib[shadow_entry(F, i, 0)] = make_float4(cb.x, cb.y, cb.z, 0.0f);
                                 sv0 = true;
                             }
                         }
@@ -221,9 +221,9 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         float ltmax;
                         if (sample_local(S, sf, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
                             V3 cb = cmul(beta, c);
-                            sr[2] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
-                            sr[3] = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
-                            F.shadow_contrib[2ull * i + 1] = make_float4(cb.x, cb.y, cb.z, 0.0f);
+                            sr1[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
+                            sr1[1] = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
+                            F.shadow_contrib[shadow_entry(F, i, 1)] = make_float4(cb.x, cb.y, cb.z, 0.0f);
                             sv1 = true;
                         }
                         bool alive = d + 1 < F.max_depth;

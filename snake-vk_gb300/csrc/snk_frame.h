@@ -43,8 +43,8 @@ struct FrameParams {
     HitDev* hits;
     float4* beta;            // per path
     float4* L;               // per path radiance
-    float4* shadow_rays;     // 2 rays per queue slot (4 float4), tmax < 0 = none
-    float4* shadow_contrib;  // 2 per queue slot
+    float4* shadow_rays;     // 2 rays per queue slot, light-major (shadow_entry), 2 float4 each, tmax < 0 = none
+    float4* shadow_contrib;  // 1 per shadow entry
     uint32_t* counters;
     unsigned long long* trav_counters;   // closest: [0] nodes [1] triangles; shadow: [2] [3]
     double2* accum;          // FP64 accumulator of view 0 (2 double2 per pixel)
@@ -60,6 +60,13 @@ struct FrameParams {
     float4* train_L;         // n_train * TRAIN_V radiance gathered at each vertex
     float4* samples;         // n_train * TRAIN_V training samples (5 float4)
 };
+
+// Shadow ray k (0: directional light, 1: local light) of queue slot i is entry
+// k * n_paths + i: the queue's directional-light rays are contiguous (one
+// direction, neighbouring origins), then its local-light rays.
+__host__ __device__ __forceinline__ size_t shadow_entry(const FrameParams& F, uint32_t i, uint32_t k) {
+    return (size_t)k * F.n_paths + i;
+}
 
 // launch helpers (defined in pt_kernels.cu / trace_kernels.cu / restir.cu)
 cudaError_t launch_generate(const FrameParams& F, int grid, cudaStream_t s);

@@ -134,8 +134,8 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
     flush_counts<COUNT>(ctr, F.trav_counters);
 }
 
-// shadow rays of segment d: entry 2*slot + k (k = 0 directional light, 1 local
-// light); tmax < 0 marks an empty entry.  The visibility goes to the w component
+// shadow rays of segment d: the queue's n directional-light entries, then its n
+// local-light entries (shadow_entry); tmax < 0 marks an empty entry.  The visibility goes to the w component
 // of the entry's contribution; k_accum_shadow adds the visible contributions in
 // entry order (the same order as the CPU oracle, so sums are bit-identical).
 template <bool COUNT, int MINB>
@@ -155,16 +155,18 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint
     for (;;) {
         unsigned act = __ballot_sync(0xFFFFFFFFu, active);
         if (__popc(~act) >= kn.refill_idle && !feed.done()) {
-            uint32_t i = feed.refill(~act, lane, work, n, kn.chunk);
-            if (i != INVALID) {
-                const float4* sr = F.shadow_rays + 2ull * i;
+            uint32_t j = feed.refill(~act, lane, work, n, kn.chunk);
+            if (j != INVALID) {
+                const uint32_t half = n >> 1;
+                const size_t i = j < half ? shadow_entry(F, j, 0) : shadow_entry(F, j - half, 1);
+                const float4* sr = F.shadow_rays + 2 * i;
                 float4 b = sr[1];
                 if (b.w < 0.0f) {
                     F.shadow_contrib[i].w = 0.0f;
                 } else {
                     float4 a = sr[0];
                     tv.init(F.S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
-                    ri = i;
+                    ri = (uint32_t)i;
                     active = true;
                 }
             }
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(256) k_accum_shadow(FrameParams F, uint32_t d)
     const uint32_t n = F.counters[CNT_QUEUE + d];
     const uint32_t* pids = F.path_ids[d & 1u];
     for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
-        float4 c0 = F.shadow_contrib[2ull * i], c1 = F.shadow_contrib[2ull * i + 1];
+        float4 c0 = F.shadow_contrib[shadow_entry(F, i, 0)], c1 = F.shadow_contrib[shadow_entry(F, i, 1)];
         if (c0.w == 0.0f && c1.w == 0.0f) continue;
         uint32_t p = pids[i];
         float4 l = F.L[p];
