@@ -69,6 +69,7 @@ def lib():
         L.snko_invert_affine.argtypes = [vp, vp, vp, vp]
         L.snko_num_local_lights.argtypes = [vp]
         L.snko_num_local_lights.restype = u32
+        L.snko_light_table.argtypes = [vp, vp, vp, vp]
         L.snko_hardware_threads.restype = u32
         L.snko_mlp_forward.argtypes = [vp, vp, u32, vp]
         L.snko_mlp_grad.argtypes = [vp, vp, vp, vp, u32, vp, C.c_int]
@@ -150,6 +151,13 @@ class OracleScene:
 
     def num_local_lights(self) -> int:
         return int(lib().snko_num_local_lights(self._h))
+
+    def light_table(self):
+        """(cdf, pmf, kind) of the path tracer's light-selection table."""
+        n = self.num_local_lights()
+        cdf, pmf, kind = np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(n, np.uint32)
+        lib().snko_light_table(self._h, cdf.ctypes.data, pmf.ctypes.data, kind.ctypes.data)
+        return cdf, pmf, kind
 
     def trace(self, rays: np.ndarray, any_hit: bool = False, nthreads: int | None = None, counters=None):
         rays = np.ascontiguousarray(rays, abi.RAY_DTYPE)

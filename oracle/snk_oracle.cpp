@@ -1559,6 +1559,15 @@ void snko_tri(const float* in, uint32_t n, float* out) {
 }
 void snko_invert_affine(const float* m, float* inv, float* nmat, float* det) { invert_affine(m, inv, nmat, det); }
 uint32_t snko_num_local_lights(void* sp) { return (uint32_t)((Scene*)sp)->lights.size(); }
+// the light-selection table: cdf[k], pmf[k] and the selection weight's record kind (0 sphere, 1 triangle)
+void snko_light_table(void* sp, float* cdf, float* pmf, uint32_t* kind) {
+    const Scene& S = *(const Scene*)sp;
+    for (size_t k = 0; k < S.lights.size(); k++) {
+        cdf[k] = S.light_cdf[k];
+        pmf[k] = S.light_pmf[k];
+        kind[k] = S.lights[k].kind;
+    }
+}
 uint32_t snko_hardware_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
 
 }  // extern "C"

@@ -230,6 +230,54 @@ def test_oracle_negative_tmin_is_zero():
         assert_hits_equal(osc.trace(r), ref, f"tmin {v}")
 
 
+def test_light_table_sphere_lights_restated():
+    """Sphere lights only: the oracle's selection table equals a numpy restatement
+    of its definition bit for bit (w = 4 pi lum(colour); q = max(1, rint(w / w_max
+    2^40)); cdf = acc / total, pmf = q / total in double rounded to float)."""
+    sc = scenes.config1(width=32, height=18)
+    pl = sc.point_lights
+    keep = pl["radius"] > 0
+    col = pl["colour"][keep].astype(np.float64)
+    w = 4.0 * np.pi * (0.2126 * col[:, 0] + 0.7152 * col[:, 1] + 0.0722 * col[:, 2])
+    q = np.where(w > 0, np.maximum(1, np.rint(w / w.max() * 2.0 ** 40)), 0).astype(np.uint64)
+    acc = np.cumsum(q, dtype=np.uint64)
+    total = float(acc[-1])
+    cdf = (acc.astype(np.float64) / total).astype(np.float32)
+    cdf[-1] = 1.0
+    pmf = (q.astype(np.float64) / total).astype(np.float32)
+    c, p, kind = O.OracleScene(sc).light_table()
+    assert (kind == 0).all() and len(c) == int(keep.sum())
+    assert np.array_equal(c.view(np.uint32), cdf.view(np.uint32))
+    assert np.array_equal(p.view(np.uint32), pmf.view(np.uint32))
+
+
+def test_light_table_properties():
+    """Sphere lights and 8,192 emissive triangles: the CDF rises to exactly 1,
+    each PMF entry is the CDF's step, a dark light is never chosen and a light
+    2^-60 as bright as the brightest still is (its integer weight is 1)."""
+    sc = scenes.config2(width=32, height=18, frames=1)
+    sc.point_lights = np.array(sc.point_lights, copy=True)
+    sc.point_lights["colour"][3] = 0.0
+    mats = np.array(sc.materials, copy=True)
+    em = np.flatnonzero((mats["flags"] & abi.MAT_EMISSIVE) != 0)
+    mats["albedo"][em[7]][:3] = np.float32(2.0 ** -60)
+    sc.materials = mats
+    osc = O.OracleScene(sc)
+    c, p, kind = osc.light_table()
+    n_sph = int((sc.point_lights["radius"] > 0).sum())
+    assert (kind[:n_sph] == 0).all() and (kind[n_sph:] == 1).all() and len(kind) == n_sph + 8192
+    assert (np.diff(c) >= 0).all() and c[-1] == 1.0 and (p >= 0).all()
+    step = np.diff(np.concatenate([[0.0], c.astype(np.float64)]))
+    assert np.abs(step - p).max() < 1e-6
+    assert abs(float(p.astype(np.float64).sum()) - 1.0) < 1e-5
+    assert p[3] == 0.0 and c[3] == c[2]
+    # the dim emitter's two triangles: instance order follows the material order of config 2
+    inst = np.flatnonzero(sc.instances["material_id"] == em[7])
+    assert len(inst) == 1
+    tri_k = n_sph + 2 * int(np.searchsorted(np.flatnonzero(np.isin(sc.instances["material_id"], em)), inst[0]))
+    assert p[tri_k] > 0.0 and p[tri_k + 1] > 0.0 and p[tri_k] < 1e-9
+
+
 def test_taa_oracle_matches_golden_restatement():
     """The oracle's TAA resolve equals the independent numpy binary32 restatement
     (tests/golden/make_taa_golden.py) bit for bit over a 3-frame sequence."""
