@@ -312,7 +312,10 @@ int snk_pt_set_materials(snk_pt_ctx* ctx, const snk_material* materials, uint32_
 int snk_pt_set_lights(snk_pt_ctx* ctx, const snk_directional_light* dir_light,
                       const snk_point_light* point_lights, uint32_t num_point_lights);
 /* BLAS builds for new meshes (GPU LBVH -> 8-wide) and the per-frame instance
- * BVH rebuild of TlasSystem::BuildTlas (TlasSystem.cpp:27-49). */
+ * BVH rebuild of TlasSystem::BuildTlas (TlasSystem.cpp:27-49).  The instance,
+ * emissive-light and light-selection tables are derived on the device from the
+ * records given to snk_pt_set_instances; tables whose inputs did not change
+ * since the last build are kept. */
 int snk_pt_build(snk_pt_ctx* ctx);
 
 /* ---- render ------------------------------------------------------------------ */
