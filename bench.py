@@ -112,9 +112,18 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.f.close()
+        with open(self.path) as f:
+            res = self.parse(f)
+        os.unlink(self.path)
+        return res
+
+    @staticmethod
+    def parse(lines) -> dict | None:
+        """Summary of nvidia-smi samples in FIELDS order (csv, noheader, nounits):
+        median SM clock, highest max clock, the throttle reasons seen active."""
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for line in open(self.path):
+        for line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 8:
                 continue
@@ -126,7 +135,6 @@ class ClockSampler:
             for n, v in zip(names, parts[4:8]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
-        os.unlink(self.path)
         if not sm:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
