@@ -498,7 +498,7 @@ class RT:
 
     def init(self, scene):
         if scene is None or not len(scene.meshes):
-            raise SnkError(abi.MODE_PATH + 4, "RT::Init: scene has no meshes")
+            raise SnkError(abi.ERR_STATE, "RT::Init: scene has no meshes")
         self.tracer.load_scene(scene)
 
     def record_render(self, views, outputs, settings: "RT.RtSettings | None" = None, mode=abi.MODE_RESTIR_DI,

@@ -56,6 +56,13 @@ def test_abi_version(built_lib):
     assert v.value == 1
 
 
+def test_status_codes_match_header():
+    hdr = open(HEADER).read()
+    for name in ("OK", "ERR_INVALID_ARG", "ERR_CUDA", "ERR_OUT_OF_MEMORY", "ERR_STATE", "ERR_LIMIT", "ERR_UNSUPPORTED"):
+        m = re.search(rf"#define\s+SNK_{name}\s+(\d+)", hdr)
+        assert m and int(m.group(1)) == getattr(abi, name), name
+
+
 def test_null_arguments_are_rejected(built_lib):
     L = snkpt.lib()
     assert L.snk_pt_create(None, None) == 1          # SNK_ERR_INVALID_ARG
