@@ -65,10 +65,10 @@ def test_status_codes_match_header():
 
 def test_null_arguments_are_rejected(built_lib):
     L = snkpt.lib()
-    assert L.snk_pt_create(None, None) == 1          # SNK_ERR_INVALID_ARG
-    assert L.snk_pt_destroy(None) == 1
-    assert L.snk_pt_render(None, None, 0, None, None) == 1
-    assert L.snk_pt_trace_rays(None, None, 0, None, 0, 0) == 1
+    assert L.snk_pt_create(None, None) == abi.ERR_INVALID_ARG
+    assert L.snk_pt_destroy(None) == abi.ERR_INVALID_ARG
+    assert L.snk_pt_render(None, None, 0, None, None) == abi.ERR_INVALID_ARG
+    assert L.snk_pt_trace_rays(None, None, 0, None, 0, 0) == abi.ERR_INVALID_ARG
 
 
 def test_create_without_gpu_fails_cleanly(built_lib):
