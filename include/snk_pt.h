@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define SNK_PT_ABI_VERSION 1u
+#define SNK_PT_ABI_VERSION 2u
 
 /* status codes */
 #define SNK_OK                 0
@@ -285,6 +285,18 @@ typedef struct snk_tuning {
     uint32_t tlas_leaf_max;         /* instances per leaf of the instance BVH, 1..4 (1) */
     uint32_t bvh_leaf_pack;         /* largest mesh-BVH subtree a full node keeps as one leaf
                                        (bvh_leaf_max..4; default bvh_leaf_max) */
+    uint32_t max_traversal_steps;   /* traversal units (node groups and primitives) one ray may take;
+                                       a ray that needs more stops and the next synchronising call
+                                       returns SNK_ERR_LIMIT (0: 65536) */
+    uint32_t stack_limit;           /* traversal stack entries per ray, 1..64; a deeper stack stops
+                                       the ray with SNK_ERR_LIMIT (0: 64) */
+    uint32_t shadow_blocks_per_sm;  /* any-hit traversal (shadow and ReSTIR visibility rays): grid =
+                                       SMs x this (0: trace_blocks_per_sm) */
+    uint32_t shadow_ray_chunk;      /* any-hit traversal: rays per work fetch (0: ray_chunk) */
+    uint32_t shadow_refill_idle;    /* any-hit traversal: refill threshold (0: refill_idle) */
+    uint32_t shadow_prim_bias;      /* any-hit traversal: primitive-step bias (0: prim_bias) */
+    uint32_t shadow_variant;        /* any-hit traversal registers: 0 as trace_variant, k + 1 variant k */
+    uint32_t reserved;              /* 0 */
 } snk_tuning;
 
 #define SNK_TREELET_PASSES_NONE 0xFFFFFFFFu
@@ -354,8 +366,10 @@ int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit*
  * width * height * spp may not exceed SNK_NOALLOC_MAX_PATHS (larger views are
  * rejected with SNK_ERR_INVALID_ARG).  Outputs must be device memory; the
  * accumulate, profile and graph flags are rejected.  The first call on a device
- * looks up the array's device address, so make it before any stream capture.
- * Calls share the array: calls whose GPU work overlaps race. */
+ * looks up the array's device address, so make it before any stream capture;
+ * the address is kept for the life of the process and does not survive a
+ * device reset (cudaDeviceReset).  The context's launch knobs (snk_pt_set_tuning)
+ * apply.  Calls share the array: calls whose GPU work overlaps race. */
 #define SNK_NOALLOC_MAX_PATHS 65536u
 int snk_pt_render_noalloc(snk_pt_ctx* ctx, const snk_view* view, const snk_render_settings* settings,
                           const snk_view_outputs* outputs);

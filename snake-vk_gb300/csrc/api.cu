@@ -534,6 +534,8 @@ SceneDev scene_dev(snk_pt_ctx* ctx) {
     S.num_tris = (uint32_t)ctx->total_tris;
     S.num_tlas_nodes = (uint32_t)ctx->tlas_nodes;
     S.num_tlas_prims = ctx->tlas_root == INVALID ? 0u : (uint32_t)ctx->tlas_prim_count;
+    S.max_steps = ctx->tune.max_traversal_steps ? ctx->tune.max_traversal_steps : MAX_TRAVERSAL_STEPS;
+    S.stack_max = ctx->tune.stack_limit ? (int)ctx->tune.stack_limit : STACK_MAX;
     return S;
 }
 
@@ -551,7 +553,7 @@ Status check_device_error(snk_pt_ctx* ctx) {
         SNK_TRY_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(unsigned), ctx->stream));
         return Status::Err(SNK_ERR_LIMIT, std::string("device traversal bound hit (error word ") + std::to_string(e) +
                                               "): bit 1 stack depth, bit 2 step limit, bit 4 bad index, bit 8 instance BVH build, "
-                                              "bit 16 tensor-core wait");
+                                              "bit 16 tensor-core wait, bit 32 its drain wait");
     }
     return Status::Ok();
 }
@@ -573,12 +575,26 @@ void** dev_slots(ViewDev& v) { return reinterpret_cast<void**>(&v.radiance); }
 int grid_of(snk_pt_ctx* ctx, int per_sm) { return ctx->num_sms * per_sm; }
 int trace_grid(snk_pt_ctx* ctx) { return grid_of(ctx, ctx->tune.trace_blocks_per_sm ? (int)ctx->tune.trace_blocks_per_sm : 16); }
 int shade_grid(snk_pt_ctx* ctx) { return grid_of(ctx, ctx->tune.shade_blocks_per_sm ? (int)ctx->tune.shade_blocks_per_sm : 8); }
+// any-hit traversal grid (shadow and visibility rays): its own knob, else the closest-hit one
+int any_grid(snk_pt_ctx* ctx) {
+    return ctx->tune.shadow_blocks_per_sm ? grid_of(ctx, (int)ctx->tune.shadow_blocks_per_sm) : trace_grid(ctx);
+}
 TraceTuning trace_tuning(snk_pt_ctx* ctx) {
     TraceTuning t;
     t.chunk = ctx->tune.ray_chunk;
     t.refill_idle = ctx->tune.refill_idle;
     t.prim_bias = ctx->tune.prim_bias;
     t.variant = ctx->tune.trace_variant;
+    return t;
+}
+// knobs of the any-hit kernels: each falls back to the closest-hit knob when 0
+TraceTuning any_tuning(snk_pt_ctx* ctx) {
+    TraceTuning t = trace_tuning(ctx);
+    const snk_tuning& k = ctx->tune;
+    if (k.shadow_ray_chunk) t.chunk = k.shadow_ray_chunk;
+    if (k.shadow_refill_idle) t.refill_idle = k.shadow_refill_idle;
+    if (k.shadow_prim_bias) t.prim_bias = k.shadow_prim_bias;
+    if (k.shadow_variant) t.variant = k.shadow_variant - 1u;
     return t;
 }
 
@@ -833,6 +849,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     F.n_paths = n_paths;
     F.n_pixels = (uint32_t)n_pixels;
     F.tune = trace_tuning(ctx);
+    F.tune_any = any_tuning(ctx);
     const bool count_nodes = (rs.flags & SNK_RENDER_COUNT_NODES) != 0;
     const bool profile = (rs.flags & SNK_RENDER_PROFILE) != 0;
     if (ctx->prof_pending) cudaStreamSynchronize(st);   // events of the previous frame are reused
@@ -908,7 +925,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         F.hits = ctx->hits.p; F.beta = ctx->beta.p; F.L = ctx->L.p;
         F.shadow_rays = ctx->srays.p; F.shadow_contrib = ctx->scontrib.p;
         if (!use_graph) cudaEventRecord(ctx->ev0, st);
-        const int g8 = shade_grid(ctx), g16 = trace_grid(ctx);
+        const int g8 = shade_grid(ctx), g16 = trace_grid(ctx), gany = any_grid(ctx);
         cudaError_t e = cudaSuccess;
         if (use_graph) {
             e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -921,7 +938,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_SHADE, [&] { return launch_shade(F, d, g8, st); });
             if (e == cudaSuccess)
                 e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
-                           [&] { return launch_trace_shadow(F, d, g16, count_nodes, st); });
+                           [&] { return launch_trace_shadow(F, d, gany, count_nodes, st); });
         }
         if (cache && e == cudaSuccess) {
             const EncodeParams ep = cache_encode_params(ctx);
@@ -1015,7 +1032,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 q2{ctx->rq_rays.p, ctx->rq_vis_b.p, K2, (uint32_t)np}, q3{ctx->rq_rays.p, ctx->rq_vis_a.p, K3, (uint32_t)np};
             const int tg = trace_grid(ctx);
             const SceneDev SD = scene_dev(ctx);
-            const TraceTuning tt = trace_tuning(ctx);
+            const TraceTuning tt = any_tuning(ctx);
+            const int ta = any_grid(ctx);
             auto pass = [&](int stage, int phase, const RestirQueue& qa, const RestirQueue& qb) {
                 return staged(ctx, profile, SNK_STAGE_RESTIR_GBUFFER + stage,
                               [&] { return launch_restir_stage(stage, phase, F, v, RV, s, qa, qb, tg, st); });
@@ -1023,7 +1041,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             auto visibility = [&](uint32_t K, uint8_t* vis, int slot) {
                 return staged(ctx, profile, SNK_STAGE_TRACE_SHADOW, [&] {
                     return launch_trace_visibility(SD, ctx->rq_rays.p, (uint32_t)(K * np), vis, ctx->rq_work.p + slot,
-                                                   tg, tt, st);
+                                                   ta, tt, st);
                 });
             };
             cudaError_t e = pass(0, 0, q1, q3);
@@ -1076,7 +1094,10 @@ int snk_pt_set_tuning(snk_pt_ctx* ctx, const snk_tuning* t) {
         t->prim_bias > 64 || t->trace_variant > 2 || 
         (t->bvh_treelet_passes > 16 && t->bvh_treelet_passes != SNK_TREELET_PASSES_NONE) ||
         (t->tlas_treelet_passes > 16 && t->tlas_treelet_passes != SNK_TREELET_PASSES_NONE) ||
-        t->bvh_leaf_max > LEAF_MAX_LIMIT || t->tlas_leaf_max > LEAF_MAX_LIMIT || t->bvh_leaf_pack > LEAF_MAX_LIMIT)
+        t->bvh_leaf_max > LEAF_MAX_LIMIT || t->tlas_leaf_max > LEAF_MAX_LIMIT || t->bvh_leaf_pack > LEAF_MAX_LIMIT ||
+        t->max_traversal_steps > MAX_TRAVERSAL_STEPS || t->stack_limit > (uint32_t)STACK_MAX ||
+        t->shadow_blocks_per_sm > 64 || t->shadow_ray_chunk > 4096 || t->shadow_refill_idle > 32 ||
+        t->shadow_prim_bias > 64 || t->shadow_variant > 3 || t->reserved != 0)
         return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: knob out of range");
     ctx->tune = *t;
     return SNK_OK;
@@ -1337,8 +1358,9 @@ int snk_pt_trace_rays(snk_pt_ctx* ctx, const snk_ray* rays, uint32_t n, snk_hit*
     }
     if (ctx->tr_work.reserve(1) || cudaMemsetAsync(ctx->tr_work.p, 0, sizeof(uint32_t), st))
         return fail(ctx, SNK_ERR_CUDA, "trace_rays: work counter");
-    cudaError_t e = launch_trace_rays(scene_dev(ctx), d_rays, n, d_hits, (flags & SNK_TRACE_ANY_HIT) != 0,
-                                      ctx->tr_work.p, trace_grid(ctx), trace_tuning(ctx), st);
+    const bool any = (flags & SNK_TRACE_ANY_HIT) != 0;
+    cudaError_t e = launch_trace_rays(scene_dev(ctx), d_rays, n, d_hits, any, ctx->tr_work.p,
+                                      any ? any_grid(ctx) : trace_grid(ctx), any ? any_tuning(ctx) : trace_tuning(ctx), st);
     if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("trace_rays: ") + cudaGetErrorString(e));
     if (memory == SNK_MEM_HOST &&
         cudaMemcpyAsync(hits, d_hits, sizeof(snk_hit) * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
@@ -1538,6 +1560,11 @@ bool ctx_view(snk_pt_ctx* ctx, CtxView* out) {
     out->scene = scene_dev(ctx);
     out->h_counters = ctx->h_counters;
     out->h_trav = ctx->h_trav;
+    out->tune = trace_tuning(ctx);
+    out->tune_any = any_tuning(ctx);
+    out->trace_grid = trace_grid(ctx);
+    out->any_grid = any_grid(ctx);
+    out->shade_grid = shade_grid(ctx);
     return true;
 }
 

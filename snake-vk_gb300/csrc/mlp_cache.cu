@@ -148,6 +148,29 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
+// Give-up protocol of the tensor-core kernels.  When a bounded wait gives up, the
+// work it waited for (MMAs writing tensor memory, bulk copies writing shared
+// memory) may still be in flight, so the CTA issues nothing more and records the
+// abandoned barrier phase; before it frees its tensor memory and exits, thread 0
+// waits for that phase once more, again with a bound (drain_abandoned).  Status
+// bits: 16 a wait gave up; 32 the second wait gave up too (the tensor memory is
+// then freed with that work still pending, as the kernel cannot stall forever).
+struct GiveUp {
+    uint32_t failed;    // a wait gave up: issue nothing more
+    uint32_t bar, parity;   // the barrier phase that was abandoned
+};
+__device__ __forceinline__ void give_up(GiveUp& g, uint32_t bar, uint32_t parity) {
+    g.failed = 1u;
+    g.bar = bar;
+    g.parity = parity;
+}
+// thread 0, before the final barrier of the CTA: drain, then report
+__device__ __forceinline__ void drain_abandoned(const GiveUp& g, unsigned* status) {
+    if (!g.failed) return;
+    const bool drained = mbar_wait(g.bar, g.parity);
+    if (status) atomicOr(status, drained ? 16u : 48u);
+}
+
 #define SNK_TC_LD16(base, r, o)                                                                        \
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "                                             \
                  "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"                   \
@@ -164,7 +187,7 @@ struct InferSmem {
     unsigned short a[128 * 64];       // this tile's activations (A operand)
     unsigned long long mbar;
     uint32_t tmem;
-    uint32_t failed;
+    GiveUp gu;
 };
 
 // ---- inference -------------------------------------------------------------------
@@ -186,7 +209,7 @@ __global__ void __launch_bounds__(INFER_THREADS) k_mlp_infer_tc(const unsigned s
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&S.mbar)));
-        S.failed = 0u;
+        S.gu.failed = 0u;
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" :: "r"(smem_u32(&S.tmem)));
@@ -231,12 +254,12 @@ __global__ void __launch_bounds__(INFER_THREADS) k_mlp_infer_tc(const unsigned s
             if (tid == 0) {
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 tc_gemm_k64(tmem, a_addr, w_addr + (uint32_t)l * 8192u, l < 4 ? 64u : 16u, mbar);
-                if (!mbar_wait(mbar, parity)) S.failed = 1u;
+                if (!mbar_wait(mbar, parity)) give_up(S.gu, mbar, parity);
             }
             parity ^= 1u;
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;");
-            ok = S.failed == 0u;
+            ok = S.gu.failed == 0u;
             if (!ok) break;
             if (l < 4) {
                 uint32_t r[64];
@@ -273,7 +296,7 @@ __global__ void __launch_bounds__(INFER_THREADS) k_mlp_infer_tc(const unsigned s
             }
         }
     }
-    if (tid == 0 && S.failed && status) atomicOr(status, 16u);   // bit 16: a tensor-core wait gave up
+    if (tid == 0) drain_abandoned(S.gu, status);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" :: "r"(tmem));
@@ -309,7 +332,7 @@ struct TrainTcSmem {
     unsigned long long mbar;             // MMA completion
     unsigned long long wbar;             // weight copies
     uint32_t tmem;
-    uint32_t failed;
+    GiveUp gu;
     float loss[8];
 };
 
@@ -385,7 +408,7 @@ __global__ void __launch_bounds__(TRAIN_TC_THREADS, 1) k_mlp_train_tc(const unsi
     const uint32_t mbar = smem_u32(&S.mbar), wbar = smem_u32(&S.wbar);
     constexpr uint32_t WF_BYTES = MLP_TC_ELEMS * 2, WB_BYTES = MLP_TCB_ELEMS * 2;
     if (tid == 0) {
-        S.failed = 0u;
+        S.gu.failed = 0u;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(mbar));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(wbar));
         asm volatile("fence.mbarrier_init.release.cluster;");
@@ -421,22 +444,22 @@ __global__ void __launch_bounds__(TRAIN_TC_THREADS, 1) k_mlp_train_tc(const unsi
     uint32_t msk[4] = {0u, 0u, 0u, 0u};   // positive masks of this thread's columns of A_1 .. A_4
     float lsum = 0.0f;
     bool ok = true;
-    if (tid == 0 && !mbar_wait(wbar, 0)) S.failed = 1u;   // the weights are in shared memory
+    if (tid == 0 && !mbar_wait(wbar, 0)) give_up(S.gu, wbar, 0u);   // the weights are in shared memory
     // runs the GEMMs `issue` queues (thread 0), then waits for them with a bound
     auto run = [&](auto issue) {
         asm volatile("fence.proxy.async.shared::cta;");
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
-        if (tid == 0 && S.failed == 0u) {
+        if (tid == 0 && S.gu.failed == 0u) {
             asm volatile("tcgen05.fence::after_thread_sync;");
             issue();
             tc_commit(mbar);
-            if (!mbar_wait(mbar, parity)) S.failed = 1u;
+            if (!mbar_wait(mbar, parity)) give_up(S.gu, mbar, parity);
         }
         parity ^= 1u;
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;");
-        return S.failed == 0u;
+        return S.gu.failed == 0u;
     };
     // forward
 #pragma unroll
@@ -531,7 +554,7 @@ __global__ void __launch_bounds__(TRAIN_TC_THREADS, 1) k_mlp_train_tc(const unsi
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xFFFFFFFFu, lsum, o);
     if (lane == 0) S.loss[warp] = lsum;
-    if (tid == 0 && S.failed && status) atomicOr(status, 16u);   // bit 16: a tensor-core wait gave up
+    if (tid == 0) drain_abandoned(S.gu, status);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (tid == 0) {

@@ -20,7 +20,14 @@
 // Set-up: host code cannot use the array's name as a device address; the first
 // call on each device looks the address up with cudaGetSymbolAddress (with that
 // device current) and caches it.  That first call should come before any stream
-// capture begins.
+// capture begins.  The cached address belongs to the device's current primary
+// context: a caller that resets the device (cudaDeviceReset) unloads the module,
+// and the address must not be used after that.
+//
+// Launch settings: the context's traversal knobs and grids (snk_pt_set_tuning,
+// snk_pt_autotune) apply here as in snk_pt_render.  The view descriptor is
+// written into the scratch header by a one-warp kernel from its by-value
+// argument, so no host memory is read by the stream after the call returns.
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -42,6 +49,14 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 constexpr int MAX_DEVICES = 64;
 std::mutex g_scratch_mu;
 unsigned char* g_scratch_addr[MAX_DEVICES] = {};
+
+// Copies the view descriptor (a kernel parameter) into the scratch header.
+__global__ void k_put_view(ViewDev* dst, ViewDev v) {
+    static_assert(sizeof(ViewDev) % 4 == 0, "view descriptor is whole words");
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&v);
+    uint32_t* out = reinterpret_cast<uint32_t*>(dst);
+    for (uint32_t i = threadIdx.x; i < sizeof(ViewDev) / 4; i += blockDim.x) out[i] = src[i];
+}
 
 // Device address of g_noalloc_scratch on `device` (which must be current).
 cudaError_t scratch_address(int device, unsigned char** out) {
@@ -131,10 +146,11 @@ extern "C" int snk_pt_render_noalloc(snk_pt_ctx* ctx, const snk_view* view, cons
 
     cudaStream_t st = cv.stream;
     const bool count_nodes = (rs.flags & SNK_RENDER_COUNT_NODES) != 0;
-    if (cudaMemcpyAsync(dview, &vd, sizeof(vd), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+    k_put_view<<<1, 32, 0, st>>>(dview, vd);
+    if (cudaGetLastError() != cudaSuccess ||
         cudaMemsetAsync(counters, 0, CNT_TOTAL * sizeof(uint32_t), st) != cudaSuccess ||
         cudaMemsetAsync(trav, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess)
-        return ctx_fail(ctx, SNK_ERR_CUDA, "render_noalloc: scratch set-up copies");
+        return ctx_fail(ctx, SNK_ERR_CUDA, "render_noalloc: scratch set-up");
 
     F.S = cv.scene;
     F.views = dview;
@@ -147,20 +163,22 @@ extern "C" int snk_pt_render_noalloc(snk_pt_ctx* ctx, const snk_view* view, cons
     F.n_pixels = (uint32_t)n_pixels;
     F.counters = counters;
     F.trav_counters = count_nodes ? trav : nullptr;
+    F.tune = cv.tune;
+    F.tune_any = cv.tune_any;
 
-    const int g8 = cv.num_sms * 8, g16 = cv.num_sms * 16;
-    e = launch_generate(F, g8, st);
+    e = launch_generate(F, cv.shade_grid, st);
     for (uint32_t d = 0; d < rs.max_depth && e == cudaSuccess; d++) {
-        e = launch_trace_closest(F, d, g16, count_nodes, st);
-        if (e == cudaSuccess) e = launch_shade(F, d, g8, st);
-        if (e == cudaSuccess) e = launch_trace_shadow(F, d, g16, count_nodes, st);
+        e = launch_trace_closest(F, d, cv.trace_grid, count_nodes, st);
+        if (e == cudaSuccess) e = launch_shade(F, d, cv.shade_grid, st);
+        if (e == cudaSuccess) e = launch_trace_shadow(F, d, cv.any_grid, count_nodes, st);
     }
-    if (e == cudaSuccess) e = launch_resolve(F, g8, st);
+    if (e == cudaSuccess) e = launch_resolve(F, cv.shade_grid, st);
     if (e != cudaSuccess)
         return ctx_fail(ctx, SNK_ERR_CUDA, (std::string("render_noalloc: launch: ") + cudaGetErrorString(e)).c_str());
     // counters for snk_pt_get_stats (pinned host buffers owned by the context)
-    cudaMemcpyAsync(cv.h_counters, counters, CNT_TOTAL * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(cv.h_trav, trav, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (cudaMemcpyAsync(cv.h_counters, counters, CNT_TOTAL * sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(cv.h_trav, trav, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return ctx_fail(ctx, SNK_ERR_CUDA, "render_noalloc: counter copies");
     ctx_note_render(ctx, SNK_MODE_PATH, rs.max_depth, n_paths, n_pixels, count_nodes);
     return SNK_OK;
 }

@@ -284,6 +284,15 @@ static_assert(sizeof(EmissiveRec) == 80, "emissive record is 80 bytes");
 
 struct DirLightDev { float dir[3]; uint32_t enabled; float colour[3]; float pad; };
 
+// Traversal bounds: the default number of traversal units (node groups and
+// primitives) a ray may take, and the capacity of its stack (STACK_SH entries in
+// shared memory, the rest in a local array).  A context may lower both
+// (snk_tuning.max_traversal_steps / stack_limit); a ray that reaches either
+// bound stops and sets a bit in the scene's error word.
+constexpr uint32_t MAX_TRAVERSAL_STEPS = 1u << 16;
+constexpr int STACK_SH = 8;
+constexpr int STACK_MAX = 64;
+
 // device pointers of the whole scene, passed by value to kernels
 struct SceneDev {
     const WideNode* blas_nodes;
@@ -312,6 +321,8 @@ struct SceneDev {
     DirLightDev dir_light;
     unsigned int* error_word;   // device status: 0 ok, else SNK_ERR_LIMIT info
     uint32_t num_blas_nodes, num_tris, num_tlas_nodes, num_tlas_prims;   // bounds checked by traversal
+    uint32_t max_steps;         // traversal units per ray (1..MAX_TRAVERSAL_STEPS)
+    int stack_max;              // stack entries per ray (1..STACK_MAX)
 };
 
 // --------------------------------------------------------------------------

@@ -48,7 +48,8 @@ struct FrameParams {
     uint32_t* counters;
     unsigned long long* trav_counters;   // closest: [0] nodes [1] triangles; shadow: [2] [3]
     double2* accum;          // FP64 accumulator of view 0 (2 double2 per pixel)
-    TraceTuning tune;
+    TraceTuning tune;        // closest-hit traversal knobs
+    TraceTuning tune_any;    // any-hit (shadow ray) traversal knobs
     // radiance cache mode: paths [0, n_render) render pixels, [n_render, n_paths) train
     uint32_t cache, n_render, n_train, frame;
     float spread_c;
@@ -145,6 +146,8 @@ struct CtxView {
     SceneDev scene;
     uint32_t* h_counters;       // pinned host copy of the frame counters (CNT_TOTAL)
     unsigned long long* h_trav; // pinned host copy of the traversal counters (4)
+    TraceTuning tune, tune_any; // the context's traversal knobs (closest hit, any hit)
+    int trace_grid, any_grid, shade_grid;   // the context's launch grids
 };
 
 }  // namespace snk

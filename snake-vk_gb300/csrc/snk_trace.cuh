@@ -27,9 +27,6 @@
 
 namespace snk {
 
-constexpr int STACK_SH = 8;           // shared-memory entries per thread
-constexpr int STACK_MAX = 64;         // total entries (shared + local spill)
-constexpr uint32_t MAX_TRAVERSAL_STEPS = 1u << 16;   // node groups popped per ray
 constexpr uint32_t PRIM_GROUP = 0x80000000u;         // stack tag of a primitive group (bases are < 2^31)
 // A child box is accepted when bits(t_enter) <= bits(t_exit) + BOX_SLACK_ULPS as
 // signed integers.  With t_enter >= tmin >= 0 this orders like the floats, and
@@ -161,16 +158,16 @@ struct TraceResult { float t, u, v; uint32_t inst, prim; bool hit; };
 struct TraceCounters { unsigned long long nodes, tris; };
 
 // Short stack: entries [0, STACK_SH) live in shared memory at sh[k * nthreads + tid],
-// deeper entries in a local array.
+// deeper entries in a local array; at most lim (<= STACK_MAX) entries.
 struct ShortStack {
     uint2* sh;
     uint2* spill;   // STACK_MAX - STACK_SH entries (a local array of the caller)
     uint32_t tid, nthreads;
-    int sp;
+    int sp, lim;
     __device__ __forceinline__ bool push(uint2 v) {
+        if (sp >= lim) return false;
         if (sp < STACK_SH) sh[sp * nthreads + tid] = v;
-        else if (sp < STACK_MAX) spill[sp - STACK_SH] = v;
-        else return false;
+        else spill[sp - STACK_SH] = v;
         sp++;
         return true;
     }
@@ -210,6 +207,7 @@ struct Traverser {
         best_t = tmax; best_u = 0.0f; best_v = 0.0f; best_inst = INVALID; best_prim = INVALID;
         level = 0; blas_sp = 0; cur_inst = 0; steps = 0; err = 0; done = false;
         st.sh = sh; st.spill = spill; st.tid = tid; st.nthreads = nthreads; st.sp = 0;
+        st.lim = S.stack_max < STACK_MAX ? S.stack_max : STACK_MAX;
         ngroup = S.tlas_root == INVALID ? make_uint2(0u, 0u) : make_uint2(S.tlas_root, (1u << (24 + (ORD ? cr.oct : 0u))) | 1u);
         tgroup = make_uint2(0u, 0u);
     }
@@ -231,7 +229,7 @@ struct Traverser {
     }
 
     __device__ __forceinline__ void node_step(const SceneDev& S, TraceCounters* ctr) {
-        if (++steps > MAX_TRAVERSAL_STEPS) { fail(ERR_STEP_LIMIT); return; }
+        if (++steps > S.max_steps) { fail(ERR_STEP_LIMIT); return; }
         // a pending primitive group is postponed onto the stack
         if (has_prim()) {
             if (!st.push(make_uint2(tgroup.x | PRIM_GROUP, tgroup.y))) { fail(ERR_STACK_OVERFLOW); return; }
@@ -250,7 +248,7 @@ struct Traverser {
     }
 
     __device__ __forceinline__ void prim_step(const SceneDev& S, TraceCounters* ctr) {
-        if (++steps > MAX_TRAVERSAL_STEPS) { fail(ERR_STEP_LIMIT); return; }
+        if (++steps > S.max_steps) { fail(ERR_STEP_LIMIT); return; }
         uint32_t k = __ffs(tgroup.y) - 1;
         tgroup.y &= tgroup.y - 1u;
         uint32_t pidx = tgroup.x + k;

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
 // entry order (the same order as the CPU oracle, so sums are bit-identical).
 template <bool COUNT, int MINB>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint32_t d) {
-    const Knobs kn(F.tune);
+    const Knobs kn(F.tune_any);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
     const uint32_t n = 2u * F.counters[CNT_QUEUE + d];
     uint32_t* work = &F.counters[CNT_WORK_SHADOW + d];
@@ -310,8 +310,8 @@ void launch_closest_variant(const FrameParams& F, uint32_t depth, int grid, cuda
 }
 template <bool COUNT>
 void launch_shadow_variant(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s) {
-    if (F.tune.variant == 1) k_trace_shadow<COUNT, 8><<<grid, TBLK, 0, s>>>(F, depth);
-    else if (F.tune.variant == 2) k_trace_shadow<COUNT, 4><<<grid, TBLK, 0, s>>>(F, depth);
+    if (F.tune_any.variant == 1) k_trace_shadow<COUNT, 8><<<grid, TBLK, 0, s>>>(F, depth);
+    else if (F.tune_any.variant == 2) k_trace_shadow<COUNT, 4><<<grid, TBLK, 0, s>>>(F, depth);
     else k_trace_shadow<COUNT, 6><<<grid, TBLK, 0, s>>>(F, depth);
 }
 

@@ -54,9 +54,14 @@ class Tuning(C.Structure):
                 ("ray_chunk", C.c_uint32), ("refill_idle", C.c_uint32), ("prim_bias", C.c_uint32),
                 ("trace_variant", C.c_uint32), ("bvh_treelet_passes", C.c_uint32), ("tlas_treelet_passes", C.c_uint32),
                 ("tlas_refit_interval", C.c_uint32), ("bvh_leaf_max", C.c_uint32), ("tlas_leaf_max", C.c_uint32),
-                ("bvh_leaf_pack", C.c_uint32)]
+                ("bvh_leaf_pack", C.c_uint32), ("max_traversal_steps", C.c_uint32), ("stack_limit", C.c_uint32),
+                ("shadow_blocks_per_sm", C.c_uint32), ("shadow_ray_chunk", C.c_uint32),
+                ("shadow_refill_idle", C.c_uint32), ("shadow_prim_bias", C.c_uint32), ("shadow_variant", C.c_uint32),
+                ("reserved", C.c_uint32)]
     KNOBS = ("trace_blocks_per_sm", "shade_blocks_per_sm", "ray_chunk", "refill_idle", "prim_bias", "trace_variant",
-             "bvh_treelet_passes", "tlas_treelet_passes", "tlas_refit_interval", "bvh_leaf_max", "tlas_leaf_max", "bvh_leaf_pack")
+             "bvh_treelet_passes", "tlas_treelet_passes", "tlas_refit_interval", "bvh_leaf_max", "tlas_leaf_max",
+             "bvh_leaf_pack", "max_traversal_steps", "stack_limit", "shadow_blocks_per_sm", "shadow_ray_chunk",
+             "shadow_refill_idle", "shadow_prim_bias", "shadow_variant")
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k in self.KNOBS}
@@ -153,6 +158,30 @@ def _is_device(a) -> bool:
     return hasattr(a, "is_cuda") and a.is_cuda
 
 
+def check_device_outputs(outputs: dict, width: int, height: int, device: int):
+    """Raises ValueError unless every given output is a contiguous torch CUDA
+    tensor on `device` with the element type of its snk_view_outputs slot and
+    room for width * height pixels (the sizes of alloc_outputs)."""
+    n = width * height
+    for k, b in outputs.items():
+        if k not in OUTPUT_SHAPES:
+            raise ValueError(f"unknown output {k!r}")
+        if b is None:
+            continue
+        if not _is_device(b):
+            raise ValueError(f"output {k!r} must be a torch CUDA tensor (device memory)")
+        if b.device.index != device:
+            raise ValueError(f"output {k!r} is on cuda:{b.device.index}, the context renders on cuda:{device}")
+        if not b.is_contiguous():
+            raise ValueError(f"output {k!r} must be contiguous")
+        import torch
+        want = (torch.float32,) if OUTPUT_DTYPES[k] == np.float32 else (torch.int32, torch.uint32)
+        if b.dtype not in want:
+            raise ValueError(f"output {k!r} must have dtype {want[0]}, not {b.dtype}")
+        if b.numel() < n * OUTPUT_SHAPES[k]:
+            raise ValueError(f"output {k!r} holds {b.numel()} elements, the view needs {n * OUTPUT_SHAPES[k]}")
+
+
 class PathTracer:
     """One library context (``snk_pt_ctx``): scene, acceleration structures, frame state."""
 
@@ -166,6 +195,7 @@ class PathTracer:
         if rc != 0:
             raise SnkError(rc, "snk_pt_create failed (no usable CUDA device?)")
         self._h = h
+        self.device = device
         self._keep = []
 
     def close(self):
@@ -243,10 +273,13 @@ class PathTracer:
 
     def render_noalloc(self, view, settings, outputs: dict):
         """Path-traced render of one small view through snk_pt_render_noalloc: no
-        device allocation; outputs must be torch CUDA tensors; at most
+        device allocation; outputs must be contiguous torch CUDA tensors on this
+        context's device with the dtype and size of alloc_outputs (checked here:
+        the library writes through the pointers as device memory); at most
         NOALLOC_MAX_PATHS = width * height * spp paths."""
         v = np.ascontiguousarray(np.asarray(view, abi.VIEW_DTYPE).reshape(1))
         st = np.ascontiguousarray(np.asarray(settings, abi.SETTINGS_DTYPE).reshape(1))
+        check_device_outputs(outputs, int(v["width"][0]), int(v["height"][0]), self.device)
         o = ViewOutputs()
         for k in OUTPUT_NAMES:
             b = outputs.get(k)

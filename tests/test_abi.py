@@ -36,9 +36,10 @@ def test_library_exports_every_declared_symbol(built_lib):
 def test_struct_layouts_match_header(tmp_path):
     prog = tmp_path / "sizes.c"
     prog.write_text('#include "snk_pt.h"\n#include <stdio.h>\n#include <stddef.h>\nint main(void){'
-                    'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(snk_instance), sizeof(snk_material),'
+                    'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(snk_instance), sizeof(snk_material),'
                     'sizeof(snk_directional_light), sizeof(snk_point_light), sizeof(snk_view), sizeof(snk_render_settings),'
-                    'sizeof(snk_ray), sizeof(snk_hit), sizeof(snk_pt_stats), sizeof(snk_view_outputs), sizeof(snk_mesh));'
+                    'sizeof(snk_ray), sizeof(snk_hit), sizeof(snk_pt_stats), sizeof(snk_view_outputs), sizeof(snk_mesh),'
+                    'sizeof(snk_tuning), offsetof(snk_tuning, max_traversal_steps), offsetof(snk_tuning, shadow_variant));'
                     'return 0;}\n')
     exe = tmp_path / "sizes"
     subprocess.check_call(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), str(prog), "-o", str(exe)])
@@ -46,14 +47,16 @@ def test_struct_layouts_match_header(tmp_path):
     expect = [abi.INSTANCE_DTYPE.itemsize, abi.MATERIAL_DTYPE.itemsize, abi.DIR_LIGHT_DTYPE.itemsize,
               abi.POINT_LIGHT_DTYPE.itemsize, abi.VIEW_DTYPE.itemsize, abi.SETTINGS_DTYPE.itemsize,
               abi.RAY_DTYPE.itemsize, abi.HIT_DTYPE.itemsize, abi.STATS_DTYPE.itemsize,
-              C.sizeof(snkpt.ViewOutputs), C.sizeof(snkpt.Mesh)]
+              C.sizeof(snkpt.ViewOutputs), C.sizeof(snkpt.Mesh), C.sizeof(snkpt.Tuning),
+              snkpt.Tuning.max_traversal_steps.offset, snkpt.Tuning.shadow_variant.offset]
     assert got == expect
 
 
 def test_abi_version(built_lib):
     v = C.c_uint32()
     assert snkpt.lib().snk_pt_abi_version(C.byref(v)) == 0
-    assert v.value == 1
+    hdr = open(HEADER).read()
+    assert v.value == int(re.search(r"#define\s+SNK_PT_ABI_VERSION\s+(\d+)u", hdr).group(1)) == 2
 
 
 def test_status_codes_match_header():

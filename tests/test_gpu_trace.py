@@ -199,6 +199,34 @@ def test_invalid_scene_is_rejected(cuda, built_lib):
         pt.set_instances(bad)
 
 
+def test_traversal_bounds_report_limit_and_recover(cuda, built_lib):
+    """The traversal's step cap and stack bound are software loop bounds the
+    context can lower: a ray that reaches one stops, the error word gets the
+    bound's bit (2 steps, 1 stack) and the next synchronising call returns
+    SNK_ERR_LIMIT naming it.  With the defaults back the same context traces
+    bit-exactly again (the error word was cleared)."""
+    sc = scenes.config1(width=64, height=36)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    rng = np.random.default_rng(5)
+    rays = np.concatenate([camera_rays(sc.views[0]), random_rays(sc, 20_000, rng)])
+    for knob, bit in (("max_traversal_steps", 2), ("stack_limit", 1)):
+        pt.set_tuning({knob: 1})
+        with pytest.raises(snkpt.SnkError) as e:
+            pt.trace_rays(rays)
+        assert e.value.code == abi.ERR_LIMIT
+        assert f"error word {bit})" in str(e.value), str(e.value)
+    pt.set_tuning({"max_traversal_steps": 1})
+    out = snkpt.alloc_outputs(64, 36, names=("radiance",))
+    with pytest.raises(snkpt.SnkError) as e:   # a frame with host outputs synchronises and reports it too
+        pt.render([sc.views[0]], abi.settings(), [out])
+    assert e.value.code == abi.ERR_LIMIT
+    pt.set_tuning({})
+    assert_hits_equal(pt.trace_rays(rays), O.OracleScene(sc).trace(rays), "after the bounds were restored")
+    with pytest.raises(snkpt.SnkError):
+        pt.set_tuning({"stack_limit": 65})
+
+
 def test_treelet_restructuring_lowers_sah_and_keeps_hits(cuda, built_lib):
     """The restructured BVH must have a lower SAH cost and fewer node visits than
     the plain LBVH while every hit stays identical (hits do not depend on the tree)."""

@@ -50,14 +50,22 @@ def test_noalloc_matches_regular_render_on_consecutive_calls(cuda, built_lib):
     pt.synchronize()
     ref = _host(ref_out)
     ref_stats = pt.stats()
-    for call in range(2):
-        out = snkpt.alloc_outputs(W, H, device=cuda)
+    outs = [snkpt.alloc_outputs(W, H, device=cuda) for _ in range(3)]
+    import torch
+    torch.cuda.synchronize()
+    free_before = None
+    for call in range(3):
+        out = outs[call]
         pt.render_noalloc(sc.views[0], st, out)
         pt.synchronize()
+        if call == 0:   # the first call may load kernels; later calls must not change free memory
+            free_before = torch.cuda.mem_get_info(cuda)[0]
         _assert_same(_host(out), ref, f"no-alloc call {call}")
         s = pt.stats()
         assert (s["rays_camera"], s["rays_extension"], s["rays_shadow"]) == \
                (ref_stats["rays_camera"], ref_stats["rays_extension"], ref_stats["rays_shadow"])
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(cuda)[0] == free_before, "device free memory changed across no-alloc calls"
 
 
 def test_noalloc_rejects_views_beyond_its_scratch(cuda, built_lib):
