@@ -411,39 +411,47 @@ def bvh_bench(snkpt, scenes, device, stream, reps=3):
     return out
 
 
-def restir_bench(snkpt, abi, scenes, device, stream, tuning, frames=16, warmup=3):
-    """ReSTIR DI on the stress scene (config 2: the 1080p sphere field + 4096
-    emissive quads, camera moving 0.05 units per frame): per frame the G-buffer
-    pass, 32 initial light candidates + 1 visibility ray with temporal reuse
-    (M cap 20), and spatial reuse over 5 neighbours in a 30-pixel radius.
-    Device-resident outputs; CUDA events on the library's stream."""
+def restir_bench(snkpt, abi, scenes, device, stream, tuning, frames=16, warmup=3, mode=None):
+    """ReSTIR on the stress scene (config 2: the 1080p sphere field + 4096
+    emissive quads, camera moving 0.05 units per frame): per frame the G-buffer,
+    32 initial light candidates + 1 visibility ray with temporal reuse (M cap 20),
+    and spatial reuse over 5 neighbours in a 30-pixel radius.  mode
+    MODE_RESTIR_DI: direct light only; MODE_RESTIR_PT: the reference's whole pass-2
+    output, direct light plus one 4-segment indirect path per pixel (roulette from
+    segment 3), the paths' first segment giving the G-buffer.  Device-resident
+    outputs; CUDA events on the library's stream."""
     import torch
+    mode = abi.MODE_RESTIR_DI if mode is None else mode
     sc = scenes.config2(frames=frames)
     pt = snkpt.PathTracer(device.index or 0, stream=stream)
     pt.load_scene(sc)
     if tuning:
         pt.set_tuning(tuning)
     out = snkpt.alloc_outputs(1920, 1080, device=device, names=("radiance", "albedo", "normal", "motion", "depth"))
+
+    def st(f, flags=0):
+        return abi.settings(mode=mode, spp=1, max_depth=4, rr_depth=3, frame_index=f, seed=1, flags=flags)
     for k in range(warmup):
-        pt.render([sc.views[0]], abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=k, seed=1), [out])
+        pt.render([sc.views[0]], st(k), [out])
         pt.stats()
     ms, rays = 0.0, 0
     per_stage = {}
     for f in range(frames):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        pt.render([sc.views[f]], abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=warmup + f, seed=1,
-                                              flags=abi.RENDER_PROFILE), [out])
+        pt.render([sc.views[f]], st(warmup + f, abi.RENDER_PROFILE), [out])
         b.record(stream)
         s = pt.stats()
         b.synchronize()
         ms += a.elapsed_time(b)
-        rays += s["rays_camera"] + s["rays_shadow"]
+        rays += s["rays_camera"] + s["rays_extension"] + s["rays_shadow"]
         for k, v in s["stage_ms"].items():
             if v > 0:
                 per_stage[k] = per_stage.get(k, 0.0) + v / frames
     del pt, out
-    return {"workload": "config 2: ReSTIR DI, 1920x1080, 4096 emissive quads + 16 sphere lights + sun, 32 "
+    what = ("ReSTIR DI" if mode == abi.MODE_RESTIR_DI else
+            "ReSTIR DI + path-traced indirect (1 path/pixel, 4 segments, roulette from 3)")
+    return {"workload": f"config 2: {what}, 1920x1080, 4096 emissive quads + 16 sphere lights + sun, 32 "
                         "candidates, temporal (M cap 20) + 5 spatial neighbours in 30 px, camera +0.05/frame",
             "frames": frames, "ms_per_frame": ms / frames, "Mrays_per_s": rays / (ms / 1e3) / 1e6,
             "rays_per_frame": rays / frames, "stage_ms_per_frame": per_stage}
@@ -652,6 +660,7 @@ def run_ours(args):
         line["taa"] = taa_bench(snkpt, dev, stream)
         line["particles"] = particle_bench(pt, abi, sc, dev)
         line["restir"] = restir_bench(snkpt, abi, scenes, dev, stream, tuning)
+        line["restir_pt"] = restir_bench(snkpt, abi, scenes, dev, stream, tuning, mode=abi.MODE_RESTIR_PT)
         line["bvh_build"] = bvh_bench(snkpt, scenes, dev, stream)
         if not args.no_batched:
             line["batched_views"] = batched_views(snkpt, abi, scenes, dev, stream, tuning)

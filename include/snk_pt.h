@@ -60,6 +60,12 @@ extern "C" {
 #define SNK_MODE_PATH        0u  /* plain unbiased wavefront path tracing with NEE */
 #define SNK_MODE_RESTIR_DI   1u  /* the reference's two-pass ReSTIR DI (RayGen.rgen:411-570) */
 #define SNK_MODE_PATH_CACHE  2u  /* path tracing with the online-trained MLP radiance cache */
+#define SNK_MODE_RESTIR_PT   3u  /* the reference's whole pass-2 output (RayGen.rgen:530-570): ReSTIR DI at
+                                    the primary vertex plus path-traced indirect light from it -- spp
+                                    unbiased paths of max_depth segments per pixel (NEE from the second
+                                    vertex on, roulette from rr_depth) in place of the biased BounceDiffuse
+                                    (:139-213); the paths' streams are keyed by seed + 0x9E3779B9 x
+                                    frame_index */
 
 /* render flags */
 #define SNK_RENDER_ACCUMULATE_F64  1u  /* add this frame's radiance into the FP64 accumulator */

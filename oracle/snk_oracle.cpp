@@ -17,6 +17,8 @@
 //   misses ..................... Core/res/shaders/RayMiss.rmiss:15-26, Shadow.rmiss:11-13
 //   shadow rays ................ Core/res/shaders/RayGen.rgen:101-121
 //   ReSTIR DI .................. Core/res/shaders/RayGen.rgen:215-528, main :530-570
+//   ReSTIR + indirect light .... main :562-569 (colour_sum = light + BounceDiffuse), the
+//                                indirect term from unbiased paths (see trace_path)
 //   motion vectors ............. Core/res/shaders/GBuffer.frag:41-43
 // Not in the reference (specified by the project):
 //   watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2(1) 2013)
@@ -897,8 +899,11 @@ static inline bool sample_continuation(const Surface& s, V3 v, V3 f0, float u_lo
     return true;
 }
 
+// indirect: the path carries only the light that reaches the primary vertex
+// indirectly (the ReSTIR + indirect mode): no emission and no NEE at the primary
+// vertex, which the ReSTIR passes shade; its random numbers are drawn all the same.
 static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uint32_t pixel_key, uint32_t sample,
-                     const Settings& st, GSample* g, Counters* ctr) {
+                     const Settings& st, GSample* g, Counters* ctr, bool indirect = false) {
     Pcg rng = pcg_stream(pixel_key, sample, 0, st.seed);
     float j1 = pcg_float(rng), j2 = pcg_float(rng);
     float jx = sample == 0 ? 0.5f : j1, jy = sample == 0 ? 0.5f : j2;
@@ -920,15 +925,16 @@ static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uin
         float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
         float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
         float u_lobe = pcg_float(rng);
+        const bool direct = !(indirect && d == 0);
         if (s.flags & MAT_EMISSIVE) {
-            if (d == 0) L = add(L, cmul(beta, s.albedo));
+            if (d == 0 && direct) L = add(L, cmul(beta, s.albedo));
             break;
         }
         V3 v = neg(rd);
         V3 f0 = f0_of(s.albedo, s.metallic);
         V3 xb = add(s.pos, mul(s.n, SURFACE_BIAS));
         // directional light (CalcDirectionalLight x ShadowTest, RayClosestHit.rchit:136)
-        if (S.dl.enabled) {
+        if (direct && S.dl.enabled) {
             V3 c = calc_directional(load3(S.dl.dir), load3(S.dl.colour), v, f0, s.n, s.roughness, s.metallic, s.albedo);
             if (maxc(c) > 0.0f) {
                 V3 cb = cmul(beta, c);
@@ -936,7 +942,7 @@ static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uin
             }
         }
         V3 c, ldir; float ltmax;
-        if (sample_local(S, s, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
+        if (direct && sample_local(S, s, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
             V3 cb = cmul(beta, c);
             if (shadow_test(S, xb, ldir, ltmax, ctr) > 0.0f) L = add(L, cb);
         }
@@ -1436,9 +1442,13 @@ int snko_render_restir(void* sp, void* statep, const View* vw, const Settings* s
     uint32_t W = vw->width, H = vw->height;
     if (W != R.W || H != R.H) return 1;
     size_t n = (size_t)W * H;
+    // SNK_MODE_RESTIR_PT: main's colour_sum = light + BounceDiffuse (RayGen.rgen:565-566),
+    // with st->spp unbiased indirect paths per pixel in place of BounceDiffuse
+    const bool with_indirect = st->mode == 3u;
     std::vector<GPix> gb(n);
     std::vector<Counters> ctr(std::max(1u, nthreads));
-    // G-buffer from primary rays through pixel centres
+    // G-buffer from primary rays through pixel centres (with the indirect paths, the
+    // camera ray of each pixel's first path is this ray: counted once, with the paths)
     parallel_for((uint32_t)n, nthreads, 256, [&](uint32_t b, uint32_t e, uint32_t t) {
         for (uint32_t i = b; i < e; i++) {
             uint32_t x = i % W, y = i / W;
@@ -1446,7 +1456,7 @@ int snko_render_restir(void* sp, void* statep, const View* vw, const Settings* s
             HitRec h;
             GSample g;
             g.hit = false;
-            ctr[t].camera++;
+            if (!with_indirect) ctr[t].camera++;
             if (trace(S, load3(vw->pos), rd, 0.0f, T_FAR, false, &h, nullptr)) {
                 g.hit = true;
                 g.s = surface_at(S, h, rd);
@@ -1473,12 +1483,31 @@ int snko_render_restir(void* sp, void* statep, const View* vw, const Settings* s
                                                     R.history_valid, x, y, pixel_base + i, &ctr[t]);
         }
     });
+    // indirect light of every pixel: the mean of st->spp paths from its primary vertex
+    // (their random streams are keyed by seed + 0x9E3779B9 x frame_index)
+    std::vector<V3> indirect;
+    if (with_indirect) {
+        indirect.assign(n, v3(0, 0, 0));
+        Settings pst = *st;
+        pst.seed = st->seed + 0x9E3779B9u * st->frame_index;
+        parallel_for((uint32_t)n, nthreads, 64, [&](uint32_t b, uint32_t e, uint32_t t) {
+            for (uint32_t i = b; i < e; i++) {
+                uint32_t x = i % W, y = i / W;
+                V3 sum = v3(0, 0, 0);
+                for (uint32_t s = 0; s < pst.spp; s++)
+                    sum = add(sum, trace_path(S, *vw, x, y, pixel_base + i, s, pst, nullptr, &ctr[t], true));
+                float inv = 1.0f / (float)pst.spp;
+                indirect[i] = v3(sum.x * inv, sum.y * inv, sum.z * inv);
+            }
+        });
+    }
     // pass 2: spatial reuse + shading
     std::vector<Reservoir> spatial(n);
     parallel_for((uint32_t)n, nthreads, 64, [&](uint32_t b, uint32_t e, uint32_t t) {
         for (uint32_t i = b; i < e; i++) {
             uint32_t x = i % W, y = i / W;
             V3 c = restir_spatial_shade(S, *vw, *st, gb.data(), R.temporal.data(), &spatial[i], x, y, pixel_base + i, &ctr[t]);
+            if (with_indirect && gb[i].valid) c = add(c, indirect[i]);
             if (out && out->radiance) {
                 float* r = &out->radiance[4 * (size_t)i];
                 r[0] = c.x; r[1] = c.y; r[2] = c.z; r[3] = 1.0f;

@@ -122,6 +122,7 @@ struct snk_pt_ctx {
     uint64_t last_paths = 0, last_pixels = 0;
 
     std::vector<RestirState> restir;
+    DBuf<float4> indirect;             // SNK_MODE_RESTIR_PT: per-pixel path-traced indirect light
     DBuf<double2> accum;
     uint32_t accum_w = 0, accum_h = 0;
     uint64_t accum_frames = 0;
@@ -776,10 +777,15 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     if (!views || !settings || !outputs || num_views == 0 || num_views > MAX_VIEWS)
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad views/settings/outputs");
     const snk_render_settings& rs = *settings;
-    if (rs.mode != SNK_MODE_PATH && rs.mode != SNK_MODE_RESTIR_DI && rs.mode != SNK_MODE_PATH_CACHE)
+    if (rs.mode != SNK_MODE_PATH && rs.mode != SNK_MODE_RESTIR_DI && rs.mode != SNK_MODE_PATH_CACHE &&
+        rs.mode != SNK_MODE_RESTIR_PT)
         return fail(ctx, SNK_ERR_UNSUPPORTED, "render: mode not supported by this entry point");
     const bool path_like = rs.mode == SNK_MODE_PATH || rs.mode == SNK_MODE_PATH_CACHE;
-    if (path_like && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
+    // ReSTIR DI at the primary vertex + path-traced indirect light (the wavefront
+    // paths start at the primary vertex and also write the ReSTIR surface records)
+    const bool restir_pt = rs.mode == SNK_MODE_RESTIR_PT;
+    const bool wavefront = path_like || restir_pt;
+    if (wavefront && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: spp must be >= 1 and 1 <= max_depth <= 16");
     if (!path_like && (rs.restir_spatial < 0 || rs.restir_spatial > 32 || rs.restir_candidates > 4096))
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: restir_spatial must be 0..32, restir_candidates <= 4096");
@@ -789,10 +795,26 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         if (outputs[v].memory > SNK_MEM_HOST) return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad memory space");
         n_pixels += (uint64_t)views[v].width * views[v].height;
     }
-    const uint32_t spp = path_like ? rs.spp : 1u;
+    const uint32_t spp = wavefront ? rs.spp : 1u;
     if (n_pixels * spp >= (1ull << 31)) return fail(ctx, SNK_ERR_INVALID_ARG, "render: too many paths");
     API_TRY(set_device(ctx));
     API_TRY(ensure_built(ctx));
+    if (!path_like) {   // per-view ReSTIR state (G-buffer records, reservoirs, history)
+        if (ctx->restir.size() < num_views) ctx->restir.resize(num_views);
+        for (uint32_t v = 0; v < num_views; v++) {
+            RestirState& R = ctx->restir[v];
+            const uint32_t w = views[v].width, h = views[v].height;
+            const size_t np = (size_t)w * h;
+            if (R.w != w || R.h != h) {
+                if (R.g_pos.reserve(np) || R.g_normal.reserve(np) || R.g_albedo.reserve(np) || R.g_misc.reserve(np) ||
+                    R.prev_normal.reserve(np) || R.res_a.reserve(3 * np) || R.res_b.reserve(3 * np) ||
+                    R.res_c.reserve(3 * np) || R.ris.reserve(2 * np) || R.memo_keys.reserve(4 * np) ||
+                    R.plan.reserve(np))
+                    return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir buffers");
+                R.w = w; R.h = h; R.history_valid = 0; R.hist = 1; R.spat = 2;
+            }
+        }
+    }
     cudaStream_t st = ctx->stream;
     const bool cache = rs.mode == SNK_MODE_PATH_CACHE;
     const uint32_t n_train = cache ? (rs.cache_train_paths ? rs.cache_train_paths : 16384u) : 0u;
@@ -833,6 +855,10 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 dst[k] = src[k];
             }
         }
+        if (restir_pt) {   // the first shading pass writes the ReSTIR surface records
+            RestirState& R = ctx->restir[v];
+            D.rs_pos = R.g_pos.p; D.rs_normal = R.g_normal.p; D.rs_albedo = R.g_albedo.p; D.rs_misc = R.g_misc.p;
+        }
         off += np;
     }
     API_TRY(upload(ctx->d_views, vd.data(), vd.size(), st));
@@ -845,7 +871,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     F.spp = spp;
     F.max_depth = rs.max_depth;
     F.rr_depth = rs.rr_depth;
-    F.seed = rs.seed;
+    // the indirect paths of the ReSTIR mode get new random streams every frame
+    F.seed = restir_pt ? rs.seed + 0x9E3779B9u * rs.frame_index : rs.seed;
     F.n_paths = n_paths;
     F.n_pixels = (uint32_t)n_pixels;
     F.tune = trace_tuning(ctx);
@@ -890,7 +917,13 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     const bool use_graph = (rs.flags & SNK_RENDER_USE_GRAPH) && path_like && !profile;
     if (!use_graph && reset_counters() != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, "counter reset");
 
-    if (path_like) {
+    if (wavefront) {
+        if (restir_pt) {
+            if (ctx->indirect.reserve(n_pixels) != cudaSuccess)
+                return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "render: indirect light buffer");
+            F.indirect = 1;
+            F.indirect_out = ctx->indirect.p;
+        }
         if (cache) {
             API_TRY(cache_ensure(ctx));
             const size_t nv = (size_t)n_train * TRAIN_V;
@@ -936,7 +969,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
                        [&] { return launch_trace_closest(F, d, g16, count_nodes, st); });
             if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_SHADE, [&] { return launch_shade(F, d, g8, st); });
-            if (e == cudaSuccess)
+            // (the indirect mode's primary vertex queues no shadow rays: ReSTIR shades it)
+            if (e == cudaSuccess && !(restir_pt && d == 0))
                 e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
                            [&] { return launch_trace_shadow(F, d, gany, count_nodes, st); });
         }
@@ -987,23 +1021,14 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 ctx->graph_launches++;
             }
         }
-        cudaEventRecord(ctx->ev1, st);
+        if (!restir_pt) cudaEventRecord(ctx->ev1, st);
         if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
-    } else {
-        if (ctx->restir.size() < num_views) ctx->restir.resize(num_views);
-        cudaEventRecord(ctx->ev0, st);
+    }
+    if (!path_like) {
+        if (!restir_pt) cudaEventRecord(ctx->ev0, st);
         for (uint32_t v = 0; v < num_views; v++) {
             RestirState& R = ctx->restir[v];
-            uint32_t w = views[v].width, h = views[v].height;
-            size_t np = (size_t)w * h;
-            if (R.w != w || R.h != h) {
-                if (R.g_pos.reserve(np) || R.g_normal.reserve(np) || R.g_albedo.reserve(np) || R.g_misc.reserve(np) ||
-                    R.prev_normal.reserve(np) || R.res_a.reserve(3 * np) || R.res_b.reserve(3 * np) ||
-                    R.res_c.reserve(3 * np) || R.ris.reserve(2 * np) || R.memo_keys.reserve(4 * np) ||
-                    R.plan.reserve(np))
-                    return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir buffers");
-                R.w = w; R.h = h; R.history_valid = 0; R.hist = 1; R.spat = 2;
-            }
+            const size_t np = (size_t)views[v].width * views[v].height;
             RestirView RV;
             RV.g_pos = R.g_pos.p; RV.g_normal = R.g_normal.p; RV.g_albedo = R.g_albedo.p; RV.g_misc = R.g_misc.p;
             RV.prev_normal = R.prev_normal.p;
@@ -1015,6 +1040,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (R.combo.reserve((RESTIR_TEMPORAL_COMBOS + 1u + (uint32_t)std::max(rs.restir_spatial, 0)) * np))
                 return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "restir buffers");
             RV.combo = R.combo.p;
+            RV.indirect = restir_pt ? ctx->indirect.p + vd[v].pixel_offset : nullptr;
             RV.history_valid = R.history_valid;
             RestirSettings s;
             s.frame_index = rs.frame_index; s.seed = rs.seed; s.candidates = rs.restir_candidates;
@@ -1044,7 +1070,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                                                    ta, tt, st);
                 });
             };
-            cudaError_t e = pass(0, 0, q1, q3);
+            // (the indirect mode's first shading pass wrote the G-buffer and the surface records)
+            cudaError_t e = restir_pt ? cudaSuccess : pass(0, 0, q1, q3);
             if (e == cudaSuccess) e = pass(1, 0, q1, q3);
             if (e == cudaSuccess) e = visibility(K1, ctx->rq_vis_a.p, 0);
             if (e == cudaSuccess) e = pass(1, 1, q1, q3);
@@ -1474,8 +1501,10 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     const uint32_t* c = ctx->h_counters;
     out->cache_queries = ctx->last_mode == SNK_MODE_PATH_CACHE ? c[CNT_CACHE_QUERIES] : 0;
     out->cache_samples = ctx->last_mode == SNK_MODE_PATH_CACHE ? ctx->last_cache_samples : 0;
-    out->shadow_tests_reused = ctx->last_mode == SNK_MODE_RESTIR_DI ? c[CNT_SHADOW_REUSED] : 0;
-    if (ctx->last_mode == SNK_MODE_PATH || ctx->last_mode == SNK_MODE_PATH_CACHE) {
+    out->shadow_tests_reused =
+        ctx->last_mode == SNK_MODE_RESTIR_DI || ctx->last_mode == SNK_MODE_RESTIR_PT ? c[CNT_SHADOW_REUSED] : 0;
+    if (ctx->last_mode == SNK_MODE_PATH || ctx->last_mode == SNK_MODE_PATH_CACHE ||
+        ctx->last_mode == SNK_MODE_RESTIR_PT) {
         out->rays_camera = ctx->last_paths;
         uint64_t ext = 0;
         for (uint32_t d = 1; d < ctx->last_depth; d++) ext += c[CNT_QUEUE + d];

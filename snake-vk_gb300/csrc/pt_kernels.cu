@@ -15,6 +15,13 @@
 //   - russian roulette from segment rr_depth with survival min(max(beta), 0.95).
 // Random numbers: PCG32 streams keyed by (pixel, sample, segment, seed); each
 // vertex draws 7 numbers, the camera segment 2 more for the pixel jitter.
+//
+// In the ReSTIR + indirect mode (F.indirect) the same paths carry only the
+// indirect light of the reference's pass 2 (RayGen.rgen:565-566): the primary
+// vertex adds no emission and does no NEE (the ReSTIR passes shade it), its
+// continuation starts the path, and every later vertex is shaded as above.  The
+// first shading pass also writes the ReSTIR surface records of sample 0, whose
+// camera ray goes through the pixel centre as the ReSTIR G-buffer's does.
 #include "snk_frame.h"
 
 namespace snk {
@@ -124,6 +131,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         if (s == 0 && !train) {
                             const ViewDev& V = F.views[vi];
                             write_gbuffer_miss(V, y * V.v.width + x);
+                            if (V.rs_pos) write_restir_miss(V, y * V.v.width + x);
                         }
                     }
                 }
@@ -162,7 +170,13 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 const bool gbuf = d == 0 && s == 0 && !train;
                 {   // a hit (misses ended in the first pass)
                     Surface sf = surface_at(S, h.inst, h.prim, h.u, h.v, rd);
-                    if (gbuf) write_gbuffer_hit(V, o, sf, h.t, motion_of(S, V.v, sf, x, y));
+                    if (gbuf) {
+                        const float2 mo = motion_of(S, V.v, sf, x, y);
+                        write_gbuffer_hit(V, o, sf, h.t, mo);
+                        if (V.rs_pos) write_restir_surface(V, o, sf, mo);
+                    }
+                    // indirect mode: ReSTIR DI shades the primary vertex (no emission, no NEE here)
+                    const bool direct = !(F.indirect && d == 0);
                     float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
                     float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
                     float u_lobe = pcg_float(rng);
@@ -197,7 +211,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         qb = make_float4(beta.x, beta.y, beta.z, 0.0f);
                         query = true;
                     } else if (sf.flags & MAT_EMISSIVE) {
-                        if (d == 0) {
+                        if (d == 0 && direct) {
                             float4 l4 = F.L[p];
                             V3 Lp = add(v3(l4.x, l4.y, l4.z), cmul(beta, sf.albedo));
                             F.L[p] = make_float4(Lp.x, Lp.y, Lp.z, 0.0f);
@@ -206,7 +220,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         V3 v = neg(rd);
                         V3 f0 = f0_of(sf.albedo, sf.metallic);
                         V3 xb = add(sf.pos, mul(sf.n, SURFACE_BIAS));
-                        if (S.dir_light.enabled) {
+                        if (direct && S.dir_light.enabled) {
                             V3 c = calc_directional(load3(S.dir_light.dir), load3(S.dir_light.colour), v, f0, sf.n,
                                                     sf.roughness, sf.metallic, sf.albedo);
                             if (maxc(c) > 0.0f) {
@@ -219,7 +233,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         }
                         V3 c, ldir;
                         float ltmax;
-                        if (sample_local(S, sf, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
+                        if (direct && sample_local(S, sf, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
                             V3 cb = cmul(beta, c);
                             sr1[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
                             sr1[1] = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
@@ -319,6 +333,10 @@ __global__ void __launch_bounds__(BLK) k_resolve(FrameParams F) {
             sum = add(sum, v3(l.x, l.y, l.z));
         }
         float4 r = make_float4(sum.x * inv, sum.y * inv, sum.z * inv, 1.0f);
+        if (F.indirect) {   // the ReSTIR final pass adds it to the pixel's direct light
+            F.indirect_out[g] = r;
+            continue;
+        }
         if (V.radiance) V.radiance[o] = r;
         if (F.accumulate && vi == 0) {
             double2 a0 = F.accum[2ull * o], a1 = F.accum[2ull * o + 1];

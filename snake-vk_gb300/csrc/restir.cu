@@ -13,6 +13,9 @@
 // dispatched by RT::RecordRenderCmdBuf (Core/src/rendering/Raytracing.cpp:250-263)
 // as two full-screen launches with a barrier between them; here: a primary-ray
 // G-buffer kernel, the initial+temporal kernel and the spatial+shading kernel.
+// In the mode that adds path-traced indirect light (main, :565-566), the path
+// tracer's first shading pass writes the G-buffer records instead of the G-buffer
+// kernel, and the final shading adds each surface pixel's indirect light.
 //
 // Deviations (the CPU oracle makes the same ones):
 //   - gold_noise / random() are replaced by PCG32 streams keyed by
@@ -809,7 +812,12 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
                 ctx_close(c);
                 continue;
             }
-            write_out(o, add(light, rad), make_float4(gn.x, gn.y, gn.z, 0.0f));
+            V3 colour = add(light, rad);
+            if (R.indirect) {   // main (:565-566): colour_sum = light + indirect (BounceDiffuse's role)
+                const float4 ind = R.indirect[o];
+                colour = add(colour, v3(ind.x, ind.y, ind.z));
+            }
+            write_out(o, colour, make_float4(gn.x, gn.y, gn.z, 0.0f));
         }
         if (!more) break;
     }

@@ -60,6 +60,12 @@ struct FrameParams {
     float4* train_beta;      // n_train * TRAIN_V (throughput, valid)
     float4* train_L;         // n_train * TRAIN_V radiance gathered at each vertex
     float4* samples;         // n_train * TRAIN_V training samples (5 float4)
+    // ReSTIR + path-traced indirect mode: the primary vertex does no NEE and adds no
+    // emission (ReSTIR DI shades it); its continuation starts the indirect paths, and
+    // the resolve writes each pixel's mean into indirect_out (global pixel order)
+    // instead of the views' radiance outputs
+    uint32_t indirect;
+    float4* indirect_out;
 };
 
 // Shadow ray k (0: directional light, 1: local light) of queue slot i is entry
@@ -97,6 +103,8 @@ struct RestirView {
     uint32_t* plan;     // per pixel: how the final shading's two tests are answered (codes, 16 bits each)
     float4* combo;      // unshadowed combine targets, slot-major (slot * pixels + pixel): the temporal
                         // pass's RESTIR_TEMPORAL_COMBOS slots, then the spatial pass's 1 + spatial
+    const float4* indirect;   // per pixel of the view: path-traced indirect light added to the
+                              // shaded surface pixels (null: direct light only)
     uint32_t history_valid;
 };
 

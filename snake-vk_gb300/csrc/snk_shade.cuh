@@ -37,6 +37,13 @@ struct ViewDev {
     uint32_t* mat_flags;
     uint32_t* inst_id;
     uint32_t* prim_id;
+    // ReSTIR surface records of the view (null unless the frame's first shading
+    // pass writes them): position (w: 1 surface, 2 emissive, 0 miss), shading
+    // normal, albedo (w: roughness), (metallic, motion.x, motion.y, 0)
+    float4* rs_pos;
+    float4* rs_normal;
+    float4* rs_albedo;
+    float4* rs_misc;
 };
 
 struct Surface {
@@ -45,6 +52,20 @@ struct Surface {
     float roughness, metallic, ao;
     uint32_t flags, inst, prim;
 };
+
+// The ReSTIR passes' record of a primary hit (RayGen.rgen:530-556 reads the same
+// quantities from the G-buffer)
+__device__ __forceinline__ void write_restir_surface(const ViewDev& V, uint32_t o, const Surface& s, float2 mo) {
+    const float kind = (s.flags & MAT_EMISSIVE) ? 2.0f : 1.0f;
+    V.rs_pos[o] = make_float4(s.pos.x, s.pos.y, s.pos.z, kind);
+    V.rs_normal[o] = make_float4(s.n.x, s.n.y, s.n.z, 0.0f);
+    V.rs_albedo[o] = make_float4(s.albedo.x, s.albedo.y, s.albedo.z, s.roughness);
+    V.rs_misc[o] = make_float4(s.metallic, mo.x, mo.y, 0.0f);
+}
+__device__ __forceinline__ void write_restir_miss(const ViewDev& V, uint32_t o) {
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    V.rs_pos[o] = z; V.rs_normal[o] = z; V.rs_albedo[o] = z; V.rs_misc[o] = z;
+}
 
 __device__ __forceinline__ Surface surface_at(const SceneDev& S, uint32_t inst, uint32_t prim, float b1, float b2,
                                               V3 ray_dir) {

@@ -534,8 +534,10 @@ class RT:
             raise SnkError(abi.ERR_STATE, "RT::Init: scene has no meshes")
         self.tracer.load_scene(scene)
 
-    def record_render(self, views, outputs, settings: "RT.RtSettings | None" = None, mode=abi.MODE_RESTIR_DI,
+    def record_render(self, views, outputs, settings: "RT.RtSettings | None" = None, mode=abi.MODE_RESTIR_PT,
                       **overrides):
+        """The pass's output: by default ReSTIR DI plus path-traced indirect light
+        (main, RayGen.rgen:530-570); mode=abi.MODE_RESTIR_DI gives the direct light alone."""
         s = settings or RT.RtSettings()
         st = abi.settings(mode=mode, frame_index=self.frame_index, restir_temporal=s.num_temporal_resamples,
                           restir_spatial=s.num_spatial_resamples, **overrides)

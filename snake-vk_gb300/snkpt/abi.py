@@ -93,7 +93,7 @@ STAGES = ("generate", "trace_closest", "shade", "trace_shadow", "resolve", "rest
           "restir_spatial", "cache_infer", "cache_samples", "cache_train", "unused")
 
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_STATE, ERR_LIMIT, ERR_UNSUPPORTED = 0, 1, 2, 3, 4, 5, 6
-MODE_PATH, MODE_RESTIR_DI, MODE_PATH_CACHE = 0, 1, 2
+MODE_PATH, MODE_RESTIR_DI, MODE_PATH_CACHE, MODE_RESTIR_PT = 0, 1, 2, 3
 RENDER_ACCUMULATE_F64, RENDER_RESET_ACCUM, RENDER_COUNT_NODES, RENDER_USE_GRAPH, RENDER_PROFILE = 1, 2, 4, 8, 16
 TRACE_ANY_HIT = 1
 MEM_DEVICE, MEM_HOST = 0, 1

@@ -270,6 +270,75 @@ def test_restir_history_of_a_larger_scene(cuda, built_lib):
     pt.synchronize()   # no device error
 
 
+@pytest.mark.parametrize("spp,max_depth", [(1, 4), (2, 6)])
+def test_restir_pt_config2_frames(cuda, built_lib, spp, max_depth):
+    """The reference's whole pass-2 output (RayGen.rgen:530-570): ReSTIR DI plus
+    path-traced indirect light, over 4 frames of the moving config-2 camera.  The
+    G-buffer is identical, radiance within 1e-4, and every ray is accounted for:
+    one camera ray per path (the first path's camera ray is the G-buffer's), the
+    paths' extension rays, and the paths' shadow rays plus ReSTIR's visibility
+    tests (traced or answered by an identical earlier test)."""
+    W, H, F = 192, 108, 4
+    sc = scenes.config2(width=W, height=H, frames=F)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    ors = O.OracleRestir(O.OracleScene(sc), W, H)
+    for f in range(F):
+        st = abi.settings(mode=abi.MODE_RESTIR_PT, spp=spp, max_depth=max_depth, rr_depth=3, frame_index=f, seed=1)
+        g = _gpu_frame(pt, [sc.views[f]], st, cuda)[0]
+        ctr = np.zeros(5, np.uint64)
+        r, _ = ors.frame(sc.views[f], st, counters=ctr)
+        _compare(g, r, f"ReSTIR + indirect frame {f}")
+        s = pt.stats()
+        assert s["rays_camera"] == W * H * spp == int(ctr[0])
+        assert s["rays_extension"] == int(ctr[1]) > 0
+        assert s["rays_shadow"] + s["shadow_tests_reused"] == int(ctr[2])
+
+
+def test_restir_pt_is_restir_di_plus_indirect(cuda, built_lib):
+    """Frame by frame, the combined mode equals the DI-only mode plus a
+    non-negative indirect term on surface pixels, and equals it exactly on
+    background and emissive pixels; with one path segment (no continuation) the
+    indirect term is zero and the two modes agree bit for bit."""
+    W, H, F = 160, 90, 3
+    sc = scenes.config2(width=W, height=H, frames=F)
+    di, ptm, one = (snkpt.PathTracer(0) for _ in range(3))
+    for p in (di, ptm, one):
+        p.load_scene(sc)
+    for f in range(F):
+        a = _gpu_frame(di, [sc.views[f]], abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=f, seed=3), cuda)[0]
+        b = _gpu_frame(ptm, [sc.views[f]], abi.settings(mode=abi.MODE_RESTIR_PT, frame_index=f, seed=3), cuda)[0]
+        c = _gpu_frame(one, [sc.views[f]], abi.settings(mode=abi.MODE_RESTIR_PT, max_depth=1, frame_index=f, seed=3),
+                       cuda)[0]
+        for k in GBUF:
+            assert np.array_equal(a[k], b[k]) and np.array_equal(a[k], c[k]), k
+        assert np.array_equal(a["radiance"], c["radiance"]), f"frame {f}: depth-1 combined mode differs from DI"
+        surf = (a["inst_id"] != abi.INVALID_INDEX) & ((a["mat_flags"] & abi.MAT_EMISSIVE) == 0)
+        ind = b["radiance"][:, :3].astype(np.float64) - a["radiance"][:, :3]
+        assert np.array_equal(b["radiance"][~surf], a["radiance"][~surf])
+        assert (ind[surf] >= -1e-5 * np.abs(a["radiance"][surf, :3]) - 1e-7).all()
+        assert ind[surf].mean() > 1e-3 * a["radiance"][surf, :3].mean()
+
+
+def test_restir_pt_two_views_per_call(cuda, built_lib):
+    """Two views in one call: the indirect paths are batched over both views (keyed
+    by global pixel), the ReSTIR passes run per view."""
+    F = 2
+    a = scenes.config2(width=128, height=72, frames=F)
+    b = scenes.config2(width=80, height=45, frames=F)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(a)
+    osc = O.OracleScene(a)
+    ra, rb = O.OracleRestir(osc, 128, 72), O.OracleRestir(osc, 80, 45)
+    for f in range(F):
+        st = abi.settings(mode=abi.MODE_RESTIR_PT, spp=1, max_depth=4, frame_index=f, seed=2)
+        ga, gb = _gpu_frame(pt, [a.views[f], b.views[f]], st, cuda)
+        oa, _ = ra.frame(a.views[f], st, pixel_base=0)
+        ob, _ = rb.frame(b.views[f], st, pixel_base=128 * 72)
+        _compare(ga, oa, f"view 0 frame {f}")
+        _compare(gb, ob, f"view 1 frame {f}")
+
+
 def test_launch_knobs_do_not_change_results(cuda, built_lib):
     """Every autotuner candidate must render the same bits (the knobs only move work)."""
     sc = scenes.config1(width=320, height=180)
@@ -278,7 +347,9 @@ def test_launch_knobs_do_not_change_results(cuda, built_lib):
     pt.load_scene(sc)
     base = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
     for knobs in [dict(trace_blocks_per_sm=4, ray_chunk=32, refill_idle=1, prim_bias=2, trace_variant=1),
-                  dict(trace_blocks_per_sm=32, ray_chunk=256, refill_idle=16, prim_bias=8, shade_blocks_per_sm=4)]:
+                  dict(trace_blocks_per_sm=32, ray_chunk=256, refill_idle=16, prim_bias=8, shade_blocks_per_sm=4),
+                  dict(shadow_blocks_per_sm=8, shadow_ray_chunk=128, shadow_refill_idle=8, shadow_prim_bias=2,
+                       shadow_variant=3)]:
         pt.set_tuning(knobs)
         g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
         for k in g:

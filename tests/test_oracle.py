@@ -196,6 +196,41 @@ def test_oracle_restir_frames():
     assert ms[0] >= 32 and ms[2] > ms[0]
 
 
+def test_oracle_restir_pt_is_di_plus_indirect_paths():
+    """The oracle's combined mode: on surface pixels the DI-only frame plus the mean
+    of the pixel's indirect paths; the indirect paths of frame 0 are the plain path
+    tracer's paths minus what their primary vertex gathers (emission, NEE), so a
+    path frame with that vertex's light removed restates them."""
+    W, H = 48, 27
+    sc = scenes.config2(width=W, height=H, frames=2)
+    osc = O.OracleScene(sc)
+    a, b, c = (O.OracleRestir(osc, W, H) for _ in range(3))
+    for f in range(2):
+        di, _ = a.frame(sc.views[f], abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=f, seed=5))
+        ctr = np.zeros(5, np.uint64)
+        pt, _ = b.frame(sc.views[f], abi.settings(mode=abi.MODE_RESTIR_PT, spp=2, max_depth=4, frame_index=f, seed=5),
+                        counters=ctr)
+        one, _ = c.frame(sc.views[f], abi.settings(mode=abi.MODE_RESTIR_PT, max_depth=1, frame_index=f, seed=5))
+        assert np.array_equal(one["radiance"], di["radiance"])
+        surf = (di["inst_id"] != abi.INVALID_INDEX) & ((di["mat_flags"] & abi.MAT_EMISSIVE) == 0)
+        assert np.array_equal(pt["radiance"][~surf], di["radiance"][~surf])
+        assert (pt["radiance"][surf, :3] >= di["radiance"][surf, :3]).all()
+        assert (pt["radiance"][surf, :3] > di["radiance"][surf, :3]).any()
+        assert int(ctr[0]) == W * H * 2   # one camera ray per path, none extra for the G-buffer
+    # frame 0: seed + 0 x 0x9E3779B9 = seed, the plain tracer's own streams; a path
+    # of depth 1 gathers only primary-vertex light, so (depth 4) - (depth 1) is the indirect part
+    st4 = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=5)
+    st1 = abi.settings(spp=1, max_depth=1, rr_depth=3, seed=5)
+    p4 = osc.render_path(sc.views[0], st4)["radiance"][:, :3].astype(np.float64)
+    p1 = osc.render_path(sc.views[0], st1)["radiance"][:, :3].astype(np.float64)
+    d = O.OracleRestir(osc, W, H)
+    di0, _ = O.OracleRestir(osc, W, H).frame(sc.views[0], abi.settings(mode=abi.MODE_RESTIR_DI, seed=5))
+    pt0, _ = d.frame(sc.views[0], abi.settings(mode=abi.MODE_RESTIR_PT, spp=1, max_depth=4, rr_depth=3, seed=5))
+    surf = (di0["inst_id"] != abi.INVALID_INDEX) & ((di0["mat_flags"] & abi.MAT_EMISSIVE) == 0)
+    ind = pt0["radiance"][surf, :3].astype(np.float64) - di0["radiance"][surf, :3]
+    assert np.allclose(ind, (p4 - p1)[surf], rtol=1e-4, atol=1e-5)
+
+
 def test_scene_configs():
     c0 = scenes.config0()
     assert c0.num_instanced_triangles == 2048 + 10 + 60 + 2
