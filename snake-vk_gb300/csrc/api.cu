@@ -782,10 +782,14 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         return fail(ctx, SNK_ERR_UNSUPPORTED, "render: mode not supported by this entry point");
     const bool path_like = rs.mode == SNK_MODE_PATH || rs.mode == SNK_MODE_PATH_CACHE;
     // ReSTIR DI at the primary vertex + path-traced indirect light (the wavefront
-    // paths start at the primary vertex and also write the ReSTIR surface records)
+    // paths start at the primary vertex and also write the ReSTIR surface records).
+    // ReSTIR DI alone runs the same wavefront for one segment of one path per pixel:
+    // the persistent traversal traces the primary rays and the first shading pass
+    // writes the G-buffer and the surface records.
     const bool restir_pt = rs.mode == SNK_MODE_RESTIR_PT;
-    const bool wavefront = path_like || restir_pt;
-    if (wavefront && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
+    const bool restir_di = rs.mode == SNK_MODE_RESTIR_DI;
+    const uint32_t max_depth = restir_di ? 1u : rs.max_depth;
+    if (!restir_di && (rs.spp == 0 || rs.max_depth == 0 || rs.max_depth > MAX_DEPTH))
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: spp must be >= 1 and 1 <= max_depth <= 16");
     if (!path_like && (rs.restir_spatial < 0 || rs.restir_spatial > 32 || rs.restir_candidates > 4096))
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: restir_spatial must be 0..32, restir_candidates <= 4096");
@@ -795,7 +799,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         if (outputs[v].memory > SNK_MEM_HOST) return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad memory space");
         n_pixels += (uint64_t)views[v].width * views[v].height;
     }
-    const uint32_t spp = wavefront ? rs.spp : 1u;
+    const uint32_t spp = restir_di ? 1u : rs.spp;
     if (n_pixels * spp >= (1ull << 31)) return fail(ctx, SNK_ERR_INVALID_ARG, "render: too many paths");
     API_TRY(set_device(ctx));
     API_TRY(ensure_built(ctx));
@@ -855,7 +859,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 dst[k] = src[k];
             }
         }
-        if (restir_pt) {   // the first shading pass writes the ReSTIR surface records
+        if (!path_like) {   // the first shading pass writes the ReSTIR surface records
             RestirState& R = ctx->restir[v];
             D.rs_pos = R.g_pos.p; D.rs_normal = R.g_normal.p; D.rs_albedo = R.g_albedo.p; D.rs_misc = R.g_misc.p;
         }
@@ -869,7 +873,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     F.views = ctx->d_views.p;
     F.nviews = num_views;
     F.spp = spp;
-    F.max_depth = rs.max_depth;
+    F.max_depth = max_depth;
     F.rr_depth = rs.rr_depth;
     // the indirect paths of the ReSTIR mode get new random streams every frame
     F.seed = restir_pt ? rs.seed + 0x9E3779B9u * rs.frame_index : rs.seed;
@@ -917,11 +921,11 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     const bool use_graph = (rs.flags & SNK_RENDER_USE_GRAPH) && path_like && !profile;
     if (!use_graph && reset_counters() != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, "counter reset");
 
-    if (wavefront) {
+    {
+        if (!path_like) F.indirect = 1;   // ReSTIR shades the primary vertex
         if (restir_pt) {
             if (ctx->indirect.reserve(n_pixels) != cudaSuccess)
                 return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "render: indirect light buffer");
-            F.indirect = 1;
             F.indirect_out = ctx->indirect.p;
         }
         if (cache) {
@@ -965,12 +969,12 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (e == cudaSuccess) e = reset_counters();
         }
         if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_GENERATE, [&] { return launch_generate(F, g8, st); });
-        for (uint32_t d = 0; d < rs.max_depth && e == cudaSuccess; d++) {
+        for (uint32_t d = 0; d < max_depth && e == cudaSuccess; d++) {
             e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
                        [&] { return launch_trace_closest(F, d, g16, count_nodes, st); });
             if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_SHADE, [&] { return launch_shade(F, d, g8, st); });
-            // (the indirect mode's primary vertex queues no shadow rays: ReSTIR shades it)
-            if (e == cudaSuccess && !(restir_pt && d == 0))
+            // (in the ReSTIR modes the primary vertex queues no shadow rays: ReSTIR shades it)
+            if (e == cudaSuccess && !(F.indirect && d == 0))
                 e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
                            [&] { return launch_trace_shadow(F, d, gany, count_nodes, st); });
         }
@@ -982,7 +986,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
             });
         }
-        if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_RESOLVE, [&] { return launch_resolve(F, g8, st); });
+        if (e == cudaSuccess && !restir_di)
+            e = staged(ctx, profile, SNK_STAGE_RESOLVE, [&] { return launch_resolve(F, g8, st); });
         if (cache && e == cudaSuccess) {
             e = staged(ctx, profile, SNK_STAGE_CACHE_SAMPLES, [&] { return launch_make_samples(F, g8, st); });
             const EncodeParams ep = cache_encode_params(ctx);
@@ -1021,11 +1026,10 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                 ctx->graph_launches++;
             }
         }
-        if (!restir_pt) cudaEventRecord(ctx->ev1, st);
+        if (path_like) cudaEventRecord(ctx->ev1, st);
         if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
     }
     if (!path_like) {
-        if (!restir_pt) cudaEventRecord(ctx->ev0, st);
         for (uint32_t v = 0; v < num_views; v++) {
             RestirState& R = ctx->restir[v];
             const size_t np = (size_t)views[v].width * views[v].height;
@@ -1070,9 +1074,8 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                                                    ta, tt, st);
                 });
             };
-            // (the indirect mode's first shading pass wrote the G-buffer and the surface records)
-            cudaError_t e = restir_pt ? cudaSuccess : pass(0, 0, q1, q3);
-            if (e == cudaSuccess) e = pass(1, 0, q1, q3);
+            // (the first shading pass wrote the G-buffer and the surface records)
+            cudaError_t e = pass(1, 0, q1, q3);
             if (e == cudaSuccess) e = visibility(K1, ctx->rq_vis_a.p, 0);
             if (e == cudaSuccess) e = pass(1, 1, q1, q3);
             if (e == cudaSuccess) e = pass(2, 0, q2, q3);
@@ -1091,7 +1094,7 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
     cudaMemcpyAsync(ctx->h_trav, ctx->trav.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
     ctx->counters_pending = true;
     ctx->last_mode = rs.mode;
-    ctx->last_depth = rs.max_depth;
+    ctx->last_depth = max_depth;
     ctx->last_paths = n_paths;
     ctx->last_pixels = n_pixels;
     ctx->last_count_nodes = count_nodes;

@@ -11,11 +11,13 @@
 //   ComputeAndWriteSpatialReservoirReuse :470-506
 //   CalculateRadianceFromReservoirs .... :508-528, main :530-570
 // dispatched by RT::RecordRenderCmdBuf (Core/src/rendering/Raytracing.cpp:250-263)
-// as two full-screen launches with a barrier between them; here: a primary-ray
-// G-buffer kernel, the initial+temporal kernel and the spatial+shading kernel.
-// In the mode that adds path-traced indirect light (main, :565-566), the path
-// tracer's first shading pass writes the G-buffer records instead of the G-buffer
-// kernel, and the final shading adds each surface pixel's indirect light.
+// as two full-screen launches with a barrier between them; here: the
+// initial+temporal kernel and the spatial+shading kernel.  The G-buffer (the reference's raster G-buffer pass, read at :534-555) comes
+// from the wavefront: camera rays through pixel centres traced by the persistent
+// closest-hit kernel, whose first shading pass writes the G-buffer outputs and the
+// surface records these passes read.  In the mode that adds path-traced indirect
+// light (main, :565-566) the same paths continue from the primary vertex, and the
+// final shading adds each surface pixel's indirect light.
 //
 // Deviations (the CPU oracle makes the same ones):
 //   - gold_noise / random() are replaced by PCG32 streams keyed by
@@ -247,10 +249,6 @@ __device__ __forceinline__ void ctx_check(Ctx& c) {
     c.overflow = false;
 }
 
-__device__ __noinline__ bool trace_primary(const SceneDev& S, V3 o, V3 d, TraceResult& r, uint2* sh) {
-    return trace_scene<false, false>(S, o, d, 0.0f, T_FAR, r, sh, threadIdx.x, RBLK, nullptr);
-}
-
 struct Shade { V3 ro, n, albedo, v, f0, biased; float rough, metal; };
 
 __device__ __forceinline__ bool update_pl(Reservoir& r, uint32_t idx, float w, Pcg& rng) {
@@ -435,50 +433,6 @@ __device__ __forceinline__ Shade shade_of(const ViewParams& vw, V3 pos, V3 n, V3
 __device__ __forceinline__ void flush_rays(uint32_t n, uint32_t* ctr) {
     for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xFFFFFFFFu, n, o);
     if ((threadIdx.x & 31u) == 0 && n) atomicAdd(ctr, n);
-}
-
-// primary rays through pixel centres -> G-buffer outputs + ReSTIR surface data
-__global__ void __launch_bounds__(RBLK) k_restir_gbuffer(FrameParams F, uint32_t vi, RestirView R) {
-    __shared__ uint2 sh[STACK_SH * RBLK];
-    const ViewDev& V = F.views[vi];
-    const uint32_t W = V.v.width, H = V.v.height, n = W * H;
-    for (uint32_t base = blockIdx.x * RBLK; base < n; base += gridDim.x * RBLK) {
-        uint32_t o = base + threadIdx.x;
-        if (o >= n) continue;
-        uint32_t x = o % W, y = o / W;
-        V3 rd = camera_dir(V.v, x, y, 0.5f, 0.5f);
-        TraceResult r;
-        if (trace_primary(F.S, load3(V.v.pos), rd, r, sh)) {
-            Surface s = surface_at(F.S, r.inst, r.prim, r.u, r.v, rd);
-            float2 mo = motion_of(F.S, V.v, s, x, y);
-            if (V.albedo) V.albedo[o] = make_float4(s.albedo.x, s.albedo.y, s.albedo.z, 1.0f);
-            if (V.normal) V.normal[o] = make_float4(s.n.x, s.n.y, s.n.z, 0.0f);
-            if (V.position) V.position[o] = make_float4(s.pos.x, s.pos.y, s.pos.z, 1.0f);
-            if (V.rma) V.rma[o] = make_float4(s.roughness, s.metallic, s.ao, 1.0f);
-            if (V.motion) V.motion[o] = mo;
-            if (V.depth) V.depth[o] = r.t;
-            if (V.mat_flags) V.mat_flags[o] = s.flags;
-            if (V.inst_id) V.inst_id[o] = s.inst;
-            if (V.prim_id) V.prim_id[o] = s.prim;
-            float kind = (s.flags & MAT_EMISSIVE) ? 2.0f : 1.0f;
-            R.g_pos[o] = make_float4(s.pos.x, s.pos.y, s.pos.z, kind);
-            R.g_normal[o] = make_float4(s.n.x, s.n.y, s.n.z, 0.0f);
-            R.g_albedo[o] = make_float4(s.albedo.x, s.albedo.y, s.albedo.z, s.roughness);
-            R.g_misc[o] = make_float4(s.metallic, mo.x, mo.y, 0.0f);
-        } else {
-            float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (V.albedo) V.albedo[o] = z;
-            if (V.normal) V.normal[o] = z;
-            if (V.position) V.position[o] = z;
-            if (V.rma) V.rma[o] = z;
-            if (V.motion) V.motion[o] = make_float2(0.0f, 0.0f);
-            if (V.depth) V.depth[o] = -1.0f;
-            if (V.mat_flags) V.mat_flags[o] = 0u;
-            if (V.inst_id) V.inst_id[o] = INVALID;
-            if (V.prim_id) V.prim_id[o] = INVALID;
-            R.g_pos[o] = z; R.g_normal[o] = z; R.g_albedo[o] = z; R.g_misc[o] = z;
-        }
-    }
 }
 
 // WriteInitialReservoirs: initial RIS + temporal reuse
@@ -830,9 +784,9 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
 cudaError_t launch_restir_stage(int stage, int phase, const FrameParams& F, uint32_t vi, const RestirView& R,
                                 const RestirSettings& rs, const RestirQueue& q, const RestirQueue& qs, int grid,
                                 cudaStream_t s) {
-    if (stage == 0) k_restir_gbuffer<<<grid, RBLK, 0, s>>>(F, vi, R);
-    else if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, phase);
-    else k_restir_spatial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs, phase);
+    if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, phase);
+    else if (stage == 2) k_restir_spatial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs, phase);
+    else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 

@@ -135,7 +135,7 @@ __host__ __device__ constexpr uint32_t restir_spatial_slots(int spatial) {
 }
 constexpr uint32_t RESTIR_SHADE_SLOTS = 2;
 
-// stage 0: primary G-buffer
+// (the G-buffer and surface records come from the wavefront's first shading pass)
 // stage 1: initial RIS + temporal reuse: phase 0 records q's rays, phase 1 replays them
 // stage 2: spatial reuse + shading: phase 0 records q's rays; phase 1 replays q,
 //          writes the spatial reservoirs and records qs's (final shading) rays;
