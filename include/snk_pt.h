@@ -286,7 +286,7 @@ typedef struct snk_tuning {
                                        TlasSystem::BuildTlas, TlasSystem.cpp:16-20); k >= 1:
                                        refit it (same topology, new boxes) when only transforms
                                        or materials changed, with a full rebuild every k-th
-                                       update (instance BVHs of up to 1024 instances) */
+                                       update (any number of instances) */
     uint32_t bvh_leaf_max;          /* primitives per leaf of later mesh BVH builds, 1..4 (1) */
     uint32_t tlas_leaf_max;         /* instances per leaf of the instance BVH, 1..4 (1) */
     uint32_t bvh_leaf_pack;         /* largest mesh-BVH subtree a full node keeps as one leaf

@@ -95,7 +95,8 @@ struct snk_pt_ctx {
     DBuf<uint32_t> rq_work;                            // work counters of the three visibility traces
     UploadMemo memo[7];                // raw instances, emissive firsts, emissive list, -, -, -, BVH list
     DBuf<SmallBuildOut> d_small_out;   // result record of the single-launch instance BVH build
-    bool tlas_small = false;
+    bool tlas_small = false;           // built by the single-launch builder (<= 1024 instances)
+    bool tlas_refittable = false;      // the last build left the record, depths and order a refit needs
     // instance BVH refit state: exact node boxes and depths, primitive order and
     // the mesh of every listed instance at the last full build
     DBuf<float4> d_tlas_box;
@@ -419,14 +420,12 @@ Status build_instances(snk_pt_ctx* ctx) {
         std::vector<uint32_t> meshes_now(n);
         for (uint32_t k = 0; k < n; k++) meshes_now[k] = ctx->instances[list[k]].mesh_id;
         const uint32_t interval = ctx->tune.tlas_refit_interval;
-        const bool refit = interval > 0 && ctx->tlas_small && prev_root != INVALID &&
-                           n <= (uint32_t)SMALL_BUILD_MAX && prev_prims == n && meshes_now == ctx->tlas_meshes &&
-                           ctx->tlas_updates_since_build + 1 < interval;
+        const bool refit = interval > 0 && ctx->tlas_refittable && prev_root != INVALID && prev_prims == n &&
+                           meshes_now == ctx->tlas_meshes && ctx->tlas_updates_since_build + 1 < interval;
         if (refit) {
             // same instances on the same meshes: new boxes into the existing tree
-            SNK_TRY(refit_wide_bvh_small(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
-                                         ctx->d_tlas_order.p, ctx->d_small_out.p, ctx->d_tlas_box.p,
-                                         ctx->d_tlas_depth.p, ctx->d_err.p, st));
+            SNK_TRY(refit_wide_bvh(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u, ctx->d_tlas_order.p,
+                                   ctx->d_small_out.p, ctx->d_tlas_box.p, ctx->d_tlas_depth.p, ctx->d_err.p, st));
             ctx->tlas_updates_since_build++;
             ctx->tlas_refits++;
             ctx->tlas_root = prev_root;   // the primitive map and counts are unchanged
@@ -434,13 +433,17 @@ Status build_instances(snk_pt_ctx* ctx) {
             ctx->tlas_prim_count = n;
             return Status::Ok();
         }
+        // the refit state of either builder: build record, node depths, primitive order
+        SNK_TRY_CUDA(ctx->d_small_out.reserve(1));
+        SNK_TRY_CUDA(ctx->d_tlas_box.reserve(2ull * (n + 1)));
+        SNK_TRY_CUDA(ctx->d_tlas_depth.reserve(n + 1));
+        SNK_TRY_CUDA(ctx->d_tlas_order.reserve(n));
+        ctx->tlas_meshes = meshes_now;
+        ctx->tlas_updates_since_build = 0;
+        ctx->tlas_refittable = true;
         if (n <= (uint32_t)SMALL_BUILD_MAX) {
             // one launch, no host round trip; the node count stays on the device
             // (traversal bounds its node indices by the capacity, n + 1)
-            SNK_TRY_CUDA(ctx->d_small_out.reserve(1));
-            SNK_TRY_CUDA(ctx->d_tlas_box.reserve(2ull * (n + 1)));
-            SNK_TRY_CUDA(ctx->d_tlas_depth.reserve(n + 1));
-            SNK_TRY_CUDA(ctx->d_tlas_order.reserve(n));
             SNK_TRY(build_wide_bvh_small(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
                                          ctx->d_tlas_order.p, passes, ctx->d_small_out.p, ctx->d_err.p,
                                          ctx->d_tlas_box.p, ctx->d_tlas_depth.p, st,
@@ -448,8 +451,6 @@ Status build_instances(snk_pt_ctx* ctx) {
             SNK_TRY(launch_map_prims(ctx->d_tlas_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
             ctx->tlas_nodes = n + 1;
             ctx->tlas_small = true;
-            ctx->tlas_meshes = meshes_now;
-            ctx->tlas_updates_since_build = 0;
             ctx->tlas_builds++;
             ctx->tlas_root = 0;
             ctx->tlas_prim_count = n;
@@ -457,13 +458,14 @@ Status build_instances(snk_pt_ctx* ctx) {
         } else {
             // multi-launch build, also without a host round trip (node count bounded by n + 1)
             SNK_TRY(build_wide_bvh_device(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
-                                          ctx->d_prim_order.p, ctx->d_err.p, st, passes,
-                                          leaf_size(ctx->tune.tlas_leaf_max, 1), leaf_size(ctx->tune.tlas_leaf_max, 1)));
+                                          ctx->d_tlas_order.p, ctx->d_err.p, st, passes,
+                                          leaf_size(ctx->tune.tlas_leaf_max, 1), leaf_size(ctx->tune.tlas_leaf_max, 1),
+                                          ctx->d_small_out.p, ctx->d_tlas_depth.p));
             ctx->tlas_nodes = n + 1;
             ctx->tlas_small = false;
             ctx->tlas_builds++;
         }
-        SNK_TRY(launch_map_prims(ctx->d_prim_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
+        SNK_TRY(launch_map_prims(ctx->d_tlas_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
         ctx->tlas_root = 0;
         ctx->tlas_prim_count = n;
     }
@@ -1534,7 +1536,7 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
         out->stage_launches[k] = ctx->stage_launches[k];
     }
     uint64_t tlas_nodes = ctx->tlas_nodes;
-    if (ctx->tlas_small && ctx->tlas_root != INVALID && ctx->d_small_out.p) {
+    if (ctx->tlas_refittable && ctx->tlas_root != INVALID && ctx->d_small_out.p) {
         SmallBuildOut r{};
         if (cudaMemcpyAsync(&r, ctx->d_small_out.p, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
             cudaStreamSynchronize(ctx->stream) == cudaSuccess)

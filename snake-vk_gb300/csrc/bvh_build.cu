@@ -8,7 +8,8 @@
 // Pipeline (all on the device, one stream):
 //   1. centroid bounds (block reduction + order-preserving atomics)
 //   2. 63-bit Morton codes of the centroids (21 bits per axis)
-//   3. radix sort of (code, primitive) pairs (CUB DeviceRadixSort)
+//   3. radix sort of (code, primitive) pairs (project LSD radix sort below: one
+//      CTA for the per-frame instance sets, three kernels per digit beyond)
 //   4. binary radix tree (Karras, HPG 2012): one thread per internal node
 //   5. bottom-up boxes and leaf counts (atomic arrival flags)
 //   5b. treelet restructuring (Karras & Aila, HPG 2013): bottom-up over the binary
@@ -36,7 +37,6 @@
 // per-frame instance BVH of up to 1024 instances is built by one single-CTA
 // launch instead (k_build_small: clustering in shared memory, then treelet passes
 // and the same collapse), so that a frame's rebuild costs no host round trip.
-#include <cub/device/device_radix_sort.cuh>
 
 #include "snk_host.h"
 
@@ -148,6 +148,180 @@ __device__ void karras_node(int i, const unsigned long long* __restrict__ keys, 
     children[i] = make_int2(left, right);
     parent[left] = i;
     parent[right] = i;
+}
+
+// ---- radix sort of (63-bit Morton code, primitive) pairs ------------------------------
+// LSD radix sort with 8-bit digits.  Every pass is stable: the elements of one
+// digit keep their current order.  A CTA ranks a chunk of 1024 consecutive
+// elements at a time: lanes holding the same digit find each other with
+// __match_any_sync (their order within the warp is their lane order), every warp
+// counts its digits in shared memory, and an exclusive scan of those counts over
+// the warps gives each warp its start within the digit.  Up to SORT_SMALL_MAX
+// elements (every per-frame instance BVH in practice) one CTA runs all passes in
+// one launch and skips the passes whose digit is the same for every key; larger
+// sets (mesh BVHs, at load time) take three launches per pass (per-tile digit
+// counts, their exclusive scan in digit-major order, the stable scatter).  The
+// result is always back in the first buffer pair.
+constexpr int SORT_THREADS = 1024;
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+constexpr int SORT_RADIX = 256;
+constexpr int SORT_PASSES = 8;                      // 64 bits (the codes use 63)
+constexpr uint32_t SORT_SMALL_MAX = 1u << 16;
+constexpr uint32_t SORT_TILE = 4u * SORT_THREADS;  // elements per CTA and pass (multi-CTA sort)
+
+struct SortSmem {
+    uint32_t wcnt[SORT_WARPS][SORT_RADIX];   // per-warp digit counts, then their exclusive scan
+    uint32_t base[SORT_RADIX];               // next output position of each digit
+    uint32_t total[SORT_RADIX];              // the current chunk's count of each digit
+    uint32_t warp_sum[SORT_RADIX / 32];
+};
+
+__device__ __forceinline__ uint32_t sort_digit(unsigned long long k, int shift) {
+    return (uint32_t)(k >> shift) & (SORT_RADIX - 1u);
+}
+
+// threads 0..255: base[d] = sum of in[0..d) (in may alias base)
+__device__ __forceinline__ void scan_radix(SortSmem& S, const uint32_t* in) {
+    const int t = threadIdx.x, lane = t & 31;
+    uint32_t v = 0, incl = 0;
+    if (t < SORT_RADIX) {
+        v = in[t];
+        incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) S.warp_sum[t >> 5] = incl;
+    }
+    __syncthreads();
+    if (t < SORT_RADIX) {
+        uint32_t off = 0;
+        for (int w = 0; w < (t >> 5); w++) off += S.warp_sum[w];
+        S.base[t] = off + incl - v;
+    }
+    __syncthreads();
+}
+
+// Output position of this thread's element (valid, digit d) in a chunk of one
+// element per thread, in thread order; then base advances past the chunk.
+__device__ __forceinline__ uint32_t rank_chunk(SortSmem& S, bool valid, uint32_t d) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (int i = t; i < SORT_WARPS * SORT_RADIX; i += SORT_THREADS) (&S.wcnt[0][0])[i] = 0u;
+    __syncthreads();
+    const uint32_t key = valid ? d : (uint32_t)(SORT_RADIX + lane);   // lanes without an element match nobody
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+    const uint32_t before = (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    if (valid && before == 0u) S.wcnt[warp][d] = (uint32_t)__popc(peers);
+    __syncthreads();
+    if (t < SORT_RADIX) {
+        uint32_t run = 0;
+        for (int w = 0; w < SORT_WARPS; w++) {
+            const uint32_t c = S.wcnt[w][t];
+            S.wcnt[w][t] = run;
+            run += c;
+        }
+        S.total[t] = run;
+    }
+    __syncthreads();
+    const uint32_t pos = valid ? S.base[d] + S.wcnt[warp][d] + before : 0u;
+    __syncthreads();
+    if (t < SORT_RADIX) S.base[t] += S.total[t];
+    return pos;   // (the next chunk's first barrier orders the base update)
+}
+
+__global__ void __launch_bounds__(SORT_THREADS, 1) k_sort_small(unsigned long long* keys, uint32_t* vals,
+                                                              unsigned long long* keys_alt, uint32_t* vals_alt,
+                                                              uint32_t n) {
+    __shared__ SortSmem S;
+    __shared__ uint32_t hist[SORT_RADIX];
+    __shared__ int skip;
+    const int t = threadIdx.x;
+    unsigned long long* sk = keys;
+    uint32_t* sv = vals;
+    unsigned long long* dk = keys_alt;
+    uint32_t* dv = vals_alt;
+    for (int pass = 0; pass < SORT_PASSES; pass++) {
+        const int shift = 8 * pass;
+        if (t < SORT_RADIX) hist[t] = 0u;
+        __syncthreads();
+        for (uint32_t i = t; i < n; i += SORT_THREADS) atomicAdd(&hist[sort_digit(sk[i], shift)], 1u);
+        __syncthreads();
+        if (t == 0) skip = hist[sort_digit(sk[0], shift)] == n;   // every key has this digit
+        scan_radix(S, hist);
+        if (skip) continue;
+        for (uint32_t c = 0; c < n; c += SORT_THREADS) {
+            const uint32_t i = c + (uint32_t)t;
+            const bool valid = i < n;
+            const unsigned long long k = valid ? sk[i] : 0ull;
+            const uint32_t v = valid ? sv[i] : 0u;
+            const uint32_t pos = rank_chunk(S, valid, sort_digit(k, shift));
+            if (valid) { dk[pos] = k; dv[pos] = v; }
+        }
+        __syncthreads();
+        unsigned long long* tk = sk; sk = dk; dk = tk;
+        uint32_t* tv = sv; sv = dv; dv = tv;
+    }
+    if (sk != keys) {   // an odd number of passes ran: the result goes back to the first pair
+        for (uint32_t i = t; i < n; i += SORT_THREADS) { keys[i] = sk[i]; vals[i] = sv[i]; }
+    }
+}
+
+// multi-CTA pass, step 1: digit counts of each tile, digit-major (hist[d * tiles + tile])
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_hist(const unsigned long long* __restrict__ keys, uint32_t n,
+                                                            int shift, uint32_t* hist, uint32_t tiles) {
+    __shared__ uint32_t h[SORT_RADIX];
+    const int t = threadIdx.x;
+    if (t < SORT_RADIX) h[t] = 0u;
+    __syncthreads();
+    const uint32_t b0 = blockIdx.x * SORT_TILE, b1 = min(b0 + SORT_TILE, n);
+    for (uint32_t i = b0 + t; i < b1; i += SORT_THREADS) atomicAdd(&h[sort_digit(keys[i], shift)], 1u);
+    __syncthreads();
+    if (t < SORT_RADIX) hist[(size_t)t * tiles + blockIdx.x] = h[t];
+}
+
+// step 2: exclusive scan of the m = 256 x tiles counts in place (one CTA; each
+// thread scans a contiguous run, the runs' totals are scanned across the block)
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_scan(uint32_t* hist, uint32_t m) {
+    __shared__ uint32_t warp_tot[SORT_WARPS];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t per = (m + SORT_THREADS - 1) / SORT_THREADS;
+    const uint32_t b0 = min((uint32_t)t * per, m), b1 = min(b0 + per, m);
+    uint32_t sum = 0;
+    for (uint32_t i = b0; i < b1; i++) sum += hist[i];
+    uint32_t incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    uint32_t off = 0;
+    for (int w = 0; w < warp; w++) off += warp_tot[w];
+    uint32_t run = off + incl - sum;
+    for (uint32_t i = b0; i < b1; i++) {
+        const uint32_t c = hist[i];
+        hist[i] = run;
+        run += c;
+    }
+}
+
+// step 3: stable scatter of each tile from its digits' scanned starts
+__global__ void __launch_bounds__(SORT_THREADS, 1) k_sort_scatter(const unsigned long long* __restrict__ sk,
+                                                                const uint32_t* __restrict__ sv, uint32_t n, int shift,
+                                                                const uint32_t* __restrict__ hist, uint32_t tiles,
+                                                                unsigned long long* dk, uint32_t* dv) {
+    __shared__ SortSmem S;
+    const int t = threadIdx.x;
+    if (t < SORT_RADIX) S.base[t] = hist[(size_t)t * tiles + blockIdx.x];
+    const uint32_t b0 = blockIdx.x * SORT_TILE, b1 = min(b0 + SORT_TILE, n);
+    for (uint32_t c = b0; c < b1; c += SORT_THREADS) {
+        const uint32_t i = c + (uint32_t)t;
+        const bool valid = i < b1;
+        const unsigned long long k = valid ? sk[i] : 0ull;
+        const uint32_t v = valid ? sv[i] : 0u;
+        const uint32_t pos = rank_chunk(S, valid, sort_digit(k, shift));
+        if (valid) { dk[pos] = k; dv[pos] = v; }
+    }
 }
 
 __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int2* children, int* parent) {
@@ -1118,26 +1292,36 @@ __global__ void k_collapse_init(uint2* tasks_a, uint32_t* counters, uint32_t* le
     }
 }
 
+// the depth of the wide node a task writes (for a later refit), by lane 0 of its warp
+__device__ __forceinline__ void note_depth(uint32_t* wide_depth, uint2 task, uint32_t node_base, int n, int level) {
+    const uint32_t local = task.y - node_base;
+    if (wide_depth && (threadIdx.x & 31) == 0 && local <= (uint32_t)n) wide_depth[local] = (uint32_t)level;
+}
+
 __global__ void __launch_bounds__(32 * LEVEL_WARPS) k_collapse_level(
     int level, uint2* tasks_a, uint2* tasks_b, uint32_t* level_tasks, uint32_t* counters, int n, const int2* children,
     const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count, const uint32_t* sorted, WideNode* nodes,
-    uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack) {
+    uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack,
+    uint32_t* wide_depth) {
     __shared__ WideNode stage[LEVEL_WARPS];
     const uint32_t nin = min(level_tasks[level], (uint32_t)n);   // the task arrays hold n entries
     if (nin == 0 || counters[4] != 0u) return;
     const uint2* tin = (level & 1) ? tasks_b : tasks_a;
     uint2* tout = (level & 1) ? tasks_a : tasks_b;
     const uint32_t w = threadIdx.x >> 5;
-    for (uint32_t t = blockIdx.x * LEVEL_WARPS + w; t < nin; t += gridDim.x * LEVEL_WARPS)
-        collapse_task_warp(tin[t], counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi, leaf_count,
+    for (uint32_t t = blockIdx.x * LEVEL_WARPS + w; t < nin; t += gridDim.x * LEVEL_WARPS) {
+        const uint2 task = tin[t];
+        note_depth(wide_depth, task, node_base, n, level);
+        collapse_task_warp(task, counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi, leaf_count,
                            sorted, nodes, &stage[w], node_base, prim_base, prim_order, leaf_max, leaf_pack);
+    }
 }
 
 __global__ void __launch_bounds__(1024) k_collapse_finish(
     int first_level, uint2* tasks_a, uint2* tasks_b, uint32_t* level_tasks, uint32_t* counters, int n,
     const int2* children, const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count,
     const uint32_t* sorted, WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
-    uint32_t leaf_max, uint32_t leaf_pack, unsigned* err_word) {
+    uint32_t leaf_max, uint32_t leaf_pack, unsigned* err_word, uint32_t* wide_depth, SmallBuildOut* out) {
     __shared__ WideNode stage[32];
     const uint32_t w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int level = first_level;
@@ -1146,21 +1330,37 @@ __global__ void __launch_bounds__(1024) k_collapse_finish(
         if (nin == 0 || counters[4] != 0u) break;
         const uint2* tin = (level & 1) ? tasks_b : tasks_a;
         uint2* tout = (level & 1) ? tasks_a : tasks_b;
-        for (uint32_t t = w; t < nin; t += nw)
-            collapse_task_warp(tin[t], counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi,
+        for (uint32_t t = w; t < nin; t += nw) {
+            const uint2 task = tin[t];
+            note_depth(wide_depth, task, node_base, n, level);
+            collapse_task_warp(task, counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi,
                                leaf_count, sorted, nodes, &stage[w], node_base, prim_base, prim_order, leaf_max,
                                leaf_pack);
+        }
         __syncthreads();   // this level's child tasks and their count are complete
     }
     if (threadIdx.x == 0) {
         const bool unfinished = level >= COLLAPSE_MAX_LEVELS && level_tasks[COLLAPSE_MAX_LEVELS] != 0u;
-        if ((counters[4] != 0u || unfinished || counters[3] != (uint32_t)n) && err_word) atomicOr(err_word, 8u);
+        const bool bad = counters[4] != 0u || unfinished || counters[3] != (uint32_t)n;
+        if (bad && err_word) atomicOr(err_word, 8u);
+        if (out) {   // the record a refit reads: node count and deepest level
+            uint32_t deepest = 0;
+            for (int l = 0; l < COLLAPSE_MAX_LEVELS; l++)
+                if (level_tasks[l] != 0u) deepest = (uint32_t)l;
+            out->num_nodes = counters[2];
+            out->prims = counters[3];
+            out->error = bad ? 8u : 0u;
+            out->max_depth = deepest;
+            out->sah = 0.0;
+        }
     }
 }
 
-// Refit of a wide BVH made by k_build_small, for moved primitives: the topology
-// (child and primitive slots) stays, every node's exact box and quantised child
-// planes are recomputed, deepest level first (one block, a barrier per level).
+// Refit of a per-frame wide BVH (made by k_build_small or by the device-driven
+// multi-launch build) for moved primitives: the topology (child and primitive
+// slots) stays, every node's exact box and quantised child planes are
+// recomputed, deepest level first (one block, a barrier per level; the tree of
+// n primitives has at most n + 1 nodes, each visited once per refit).
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
 k_refit_small(WideNode* nodes, uint32_t node_base, uint32_t prim_base, const SmallBuildOut* info,
               float4* wide_box, const uint32_t* wide_depth, const uint32_t* prim_order,
@@ -1287,6 +1487,30 @@ inline unsigned grid_for(uint32_t n) { return (n + BLK - 1) / BLK; }
 }  // namespace
 
 namespace {
+// sorts (sc.keys, sc.vals) by key, stably (sc.keys_alt / sc.vals_alt: scratch)
+Status sort_pairs(BuildScratch& sc, uint32_t n, cudaStream_t st) {
+    if (n <= SORT_SMALL_MAX) {
+        k_sort_small<<<1, SORT_THREADS, 0, st>>>(sc.keys.p, sc.vals.p, sc.keys_alt.p, sc.vals_alt.p, n);
+        SNK_TRY_CUDA(cudaGetLastError());
+        return Status::Ok();
+    }
+    const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    SNK_TRY_CUDA(sc.sort_hist.reserve((size_t)SORT_RADIX * tiles));
+    unsigned long long *sk = sc.keys.p, *dk = sc.keys_alt.p;
+    uint32_t *sv = sc.vals.p, *dv = sc.vals_alt.p;
+    for (int pass = 0; pass < SORT_PASSES; pass++) {   // an even number: the result ends in sc.keys / sc.vals
+        const int shift = 8 * pass;
+        k_sort_hist<<<tiles, SORT_THREADS, 0, st>>>(sk, n, shift, sc.sort_hist.p, tiles);
+        k_sort_scan<<<1, SORT_THREADS, 0, st>>>(sc.sort_hist.p, (uint32_t)SORT_RADIX * tiles);
+        k_sort_scatter<<<tiles, SORT_THREADS, 0, st>>>(sk, sv, n, shift, sc.sort_hist.p, tiles, dk, dv);
+        SNK_TRY_CUDA(cudaGetLastError());
+        std::swap(sk, dk);
+        std::swap(sv, dv);
+    }
+    static_assert(SORT_PASSES % 2 == 0, "the multi-CTA sort ends in the first buffer pair");
+    return Status::Ok();
+}
+
 // the binary tree of build_wide_bvh and build_wide_bvh_device (Morton codes, radix
 // sort, Karras hierarchy, bottom-up boxes, treelet passes); *sorted_out receives
 // the primitive of each sorted position
@@ -1319,14 +1543,9 @@ Status build_binary_tree(BuildScratch& sc, const float4* prim_lo, const float4* 
     k_morton<<<g, BLK, 0, st>>>(prim_lo, prim_hi, n, sc.cbounds.p, sc.keys.p, sc.vals.p);
     SNK_TRY_CUDA(cudaGetLastError());
 
-    cub::DoubleBuffer<unsigned long long> dk(sc.keys.p, sc.keys_alt.p);
-    cub::DoubleBuffer<uint32_t> dv(sc.vals.p, sc.vals_alt.p);
-    size_t tmp_bytes = 0;
-    SNK_TRY_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, dk, dv, (int)n, 0, 63, st));
-    SNK_TRY_CUDA(sc.cub_tmp.reserve(tmp_bytes));
-    SNK_TRY_CUDA(cub::DeviceRadixSort::SortPairs(sc.cub_tmp.p, tmp_bytes, dk, dv, (int)n, 0, 63, st));
-    const unsigned long long* keys = dk.Current();
-    const uint32_t* sorted = dv.Current();
+    SNK_TRY(sort_pairs(sc, n, st));
+    const unsigned long long* keys = sc.keys.p;
+    const uint32_t* sorted = sc.vals.p;
     *sorted_out = sorted;
 
     SNK_TRY_CUDA(cudaMemsetAsync(sc.flags.p, 0, sizeof(int) * n, st));
@@ -1399,7 +1618,7 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
 Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n,
                              WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
                              unsigned* err_word, cudaStream_t st, int treelet_passes, uint32_t leaf_max,
-                             uint32_t leaf_pack) {
+                             uint32_t leaf_pack, SmallBuildOut* out, uint32_t* wide_depth) {
     const uint32_t* sorted = nullptr;
     SNK_TRY(build_binary_tree(sc, prim_lo, prim_hi, n, st, treelet_passes, leaf_max, leaf_pack, &sorted));
     SNK_TRY_CUDA(sc.level_tasks.reserve(COLLAPSE_MAX_LEVELS + 1));
@@ -1416,11 +1635,11 @@ Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const floa
         k_collapse_level<<<grid, 32 * LEVEL_WARPS, 0, st>>>(level, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
                                                             sc.counters.p, (int)n, sc.children.p, sc.node_lo.p,
                                                             sc.node_hi.p, sc.leaf_count.p, sorted, nodes, node_base,
-                                                            prim_base, prim_order, leaf_max, leaf_pack);
+                                                            prim_base, prim_order, leaf_max, leaf_pack, wide_depth);
     k_collapse_finish<<<1, 1024, 0, st>>>(fast, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
                                           sc.counters.p, (int)n, sc.children.p, sc.node_lo.p, sc.node_hi.p,
                                           sc.leaf_count.p, sorted, nodes, node_base, prim_base, prim_order, leaf_max,
-                                          leaf_pack, err_word);
+                                          leaf_pack, err_word, wide_depth, out);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }
@@ -1440,11 +1659,10 @@ Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32
     return Status::Ok();
 }
 
-Status refit_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
-                            uint32_t node_base, uint32_t prim_base, const uint32_t* prim_order,
-                            const SmallBuildOut* info, float4* wide_box, const uint32_t* wide_depth, unsigned* err_word,
-                            cudaStream_t st) {
-    if (n == 0 || n > (uint32_t)SMALL_BUILD_MAX) return Status::Err(1, "refit_wide_bvh_small: bad primitive count");
+Status refit_wide_bvh(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes, uint32_t node_base,
+                      uint32_t prim_base, const uint32_t* prim_order, const SmallBuildOut* info, float4* wide_box,
+                      const uint32_t* wide_depth, unsigned* err_word, cudaStream_t st) {
+    if (n == 0 || n > (1u << 30)) return Status::Err(1, "refit_wide_bvh: bad primitive count");
     k_refit_small<<<1, SMALL_THREADS, 0, st>>>(nodes, node_base, prim_base, info, wide_box, wide_depth, prim_order,
                                                prim_lo, prim_hi, (int)n, err_word);
     SNK_TRY_CUDA(cudaGetLastError());

@@ -16,9 +16,6 @@
 // of summation, so the parallel scan and the oracle's sequential loop agree
 // bit for bit.  This unit is compiled without contraction (--fmad=false): the
 // float and double expressions round exactly as the oracle's.
-#include <cub/device/device_scan.cuh>
-#include <thrust/iterator/counting_iterator.h>
-#include <thrust/iterator/transform_iterator.h>
 
 #include <algorithm>
 #include <cmath>
@@ -168,6 +165,67 @@ struct QuantisedWeight {
     }
 };
 
+// Inclusive prefix sums of the quantised weights.  The sums are exact integers,
+// so any order of summation gives the same bits: k_scan_tiles sums each tile of
+// `tile` weights, k_scan_apply scans each tile (a contiguous run per thread, then
+// the runs' totals across the block) starting from the sum of the tiles before it.
+constexpr int SCAN_THREADS = 1024;
+
+// inclusive scan of one value per thread across the block; *block_total = the sum
+__device__ __forceinline__ unsigned long long block_scan_incl(unsigned long long v, unsigned long long* warp_tot,
+                                                              unsigned long long* block_total) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned long long incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    unsigned long long off = 0ull, all = 0ull;
+    for (int w = 0; w < SCAN_THREADS / 32; w++) {
+        if (w < warp) off += warp_tot[w];
+        all += warp_tot[w];
+    }
+    *block_total = all;
+    return off + incl;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(QuantisedWeight q, uint32_t n, uint32_t tile,
+                                                             unsigned long long* tile_sums) {
+    __shared__ unsigned long long warp_tot[SCAN_THREADS / 32];
+    const uint32_t b0 = blockIdx.x * tile, b1 = min(b0 + tile, n);
+    unsigned long long s = 0ull;
+    for (uint32_t k = b0 + threadIdx.x; k < b1; k += SCAN_THREADS) s += q(k);
+    unsigned long long total;
+    block_scan_incl(s, warp_tot, &total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(QuantisedWeight q, uint32_t n, uint32_t tile,
+                                                             const unsigned long long* __restrict__ tile_sums,
+                                                             unsigned long long* acc) {
+    __shared__ unsigned long long warp_tot[SCAN_THREADS / 32];
+    __shared__ unsigned long long before;
+    if (threadIdx.x == 0) {
+        unsigned long long b = 0ull;
+        for (uint32_t j = 0; j < blockIdx.x; j++) b += tile_sums[j];
+        before = b;
+    }
+    const uint32_t b0 = blockIdx.x * tile, b1 = min(b0 + tile, n);
+    const uint32_t per = (tile + SCAN_THREADS - 1) / SCAN_THREADS;
+    const uint32_t r0 = min(b0 + threadIdx.x * per, b1), r1 = min(r0 + per, b1);
+    unsigned long long s = 0ull;
+    for (uint32_t k = r0; k < r1; k++) s += q(k);
+    unsigned long long total;
+    const unsigned long long incl = block_scan_incl(s, warp_tot, &total);   // (its barrier orders `before`)
+    unsigned long long run = before + incl - s;
+    for (uint32_t k = r0; k < r1; k++) {
+        run += q(k);
+        acc[k] = run;
+    }
+}
+
 __global__ void k_light_cdf(const unsigned long long* __restrict__ acc, uint32_t n, float* __restrict__ cdf,
                             float* __restrict__ pmf) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -216,16 +274,19 @@ Status launch_emissive_lights(const snk_instance* raw, const uint32_t* em_list, 
 
 Status launch_light_cdf(const double* w, uint32_t n, LightCdfScratch& sc, float* cdf, float* pmf, cudaStream_t st) {
     if (n == 0) return Status::Ok();
+    // tiles of at least 16 weights per thread, at most 1024 tiles
+    const uint32_t per_tile = std::max<uint32_t>(16u * SCAN_THREADS, (uint32_t)((n + 1023ull) / 1024ull));
+    const uint32_t tile = (per_tile + SCAN_THREADS - 1) / SCAN_THREADS * SCAN_THREADS;
+    const uint32_t tiles = (n + tile - 1) / tile;
     SNK_TRY_CUDA(sc.acc.reserve(n));
     SNK_TRY_CUDA(sc.wmax.reserve(1));
-    const auto q = thrust::make_transform_iterator(thrust::counting_iterator<uint32_t>(0u), QuantisedWeight{w, sc.wmax.p});
-    size_t tmp = 0;
-    SNK_TRY_CUDA(cub::DeviceScan::InclusiveSum(nullptr, tmp, q, sc.acc.p, (int)n, st));
-    SNK_TRY_CUDA(sc.tmp.reserve(tmp));
+    SNK_TRY_CUDA(sc.tile_sums.reserve(tiles));
+    const QuantisedWeight q{w, sc.wmax.p};
     SNK_TRY_CUDA(cudaMemsetAsync(sc.wmax.p, 0, sizeof(unsigned long long), st));
     k_weight_max<<<std::min<uint32_t>(blocks_for(n, 256), 1024), 256, 0, st>>>(w, n, sc.wmax.p);
+    k_scan_tiles<<<tiles, SCAN_THREADS, 0, st>>>(q, n, tile, sc.tile_sums.p);
+    k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(q, n, tile, sc.tile_sums.p, sc.acc.p);
     SNK_TRY_CUDA(cudaGetLastError());
-    SNK_TRY_CUDA(cub::DeviceScan::InclusiveSum(sc.tmp.p, tmp, q, sc.acc.p, (int)n, st));
     k_light_cdf<<<blocks_for(n, 256), 256, 0, st>>>(sc.acc.p, n, cdf, pmf);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();

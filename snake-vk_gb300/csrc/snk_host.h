@@ -75,7 +75,7 @@ struct BuildScratch {
     DBuf<uint2> tasks_a, tasks_b;
     DBuf<uint32_t> counters;      // [0] tasks in, [1] tasks out, [2] wide nodes, [3] prims
     DBuf<unsigned> cbounds;       // centroid bounds, order-preserving encoded
-    DBuf<unsigned char> cub_tmp;
+    DBuf<uint32_t> sort_hist;     // per-tile digit counts of the multi-CTA radix sort
     DBuf<double> sah;             // SAH accumulator
     DBuf<uint32_t> level_tasks;   // task count per wide level (device-driven collapse)
     size_t cap = 0;
@@ -95,14 +95,16 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t stream,
                       BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack);
 
+struct SmallBuildOut;
 // The same tree without host round trips (for per-frame rebuilds): the collapse
 // runs level by level on the device, nothing is read back, and a build error
-// (never seen for a correct tree) sets bit 8 of *err_word.  The node count is
-// not reported; at most n + 1 nodes are written.
+// (never seen for a correct tree) sets bit 8 of *err_word.  At most n + 1 nodes
+// are written.  With out and wide_depth (n + 1 entries) given, the device keeps
+// the node count, the deepest level and every node's depth for a later refit.
 Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n,
                              WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
                              unsigned* err_word, cudaStream_t stream, int treelet_passes, uint32_t leaf_max,
-                             uint32_t leaf_pack);
+                             uint32_t leaf_pack, SmallBuildOut* out = nullptr, uint32_t* wide_depth = nullptr);
 
 // Single-launch build for n <= SMALL_BUILD_MAX primitives (one CTA, shared
 // memory, no host synchronisation); same algorithm and output layout as
@@ -120,12 +122,13 @@ Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32
                             uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
                             SmallBuildOut* out, unsigned* err_word, float4* wide_box, uint32_t* wide_depth,
                             cudaStream_t stream, uint32_t leaf_max);
-// Refit of a tree made by build_wide_bvh_small for the same n primitives in new
-// boxes (prim_order as that build wrote it; everything stays on the device).
-Status refit_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
-                            uint32_t node_base, uint32_t prim_base, const uint32_t* prim_order,
-                            const SmallBuildOut* info, float4* wide_box, const uint32_t* wide_depth,
-                            unsigned* err_word, cudaStream_t stream);
+// Refit of a tree made by build_wide_bvh_small or build_wide_bvh_device (with its
+// record and depths) for the same n primitives in new boxes (prim_order as that
+// build wrote it; wide_box: 2 x (n + 1) float4 of scratch that receives every
+// node's exact box; everything stays on the device).
+Status refit_wide_bvh(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes, uint32_t node_base,
+                      uint32_t prim_base, const uint32_t* prim_order, const SmallBuildOut* info, float4* wide_box,
+                      const uint32_t* wide_depth, unsigned* err_word, cudaStream_t stream);
 
 // Per-triangle padded boxes of one mesh (object space).
 Status launch_triangle_boxes(const float* positions, const uint32_t* indices, uint32_t vertex_offset,
@@ -138,8 +141,7 @@ Status launch_instance_boxes(const uint32_t* inst_list, uint32_t n, const InstSh
                              float4* lo, float4* hi, cudaStream_t s);
 // ---- per-frame scene tables (scene_tables.cu) ---------------------------------
 struct LightCdfScratch {
-    DBuf<unsigned long long> acc, wmax;
-    DBuf<unsigned char> tmp;
+    DBuf<unsigned long long> acc, wmax, tile_sums;
 };
 // traversal and shading records of n instances from their raw records
 Status launch_instance_records(const snk_instance* raw, uint32_t n, const MeshInfo* meshes, InstTrace* it,

@@ -251,10 +251,13 @@ def test_treelet_restructuring_lowers_sah_and_keeps_hits(cuda, built_lib):
     assert_hits_equal(full[1], O.OracleScene(sc).trace(rays), "restructured BVH vs oracle")
 
 
-def test_instance_bvh_refit_keeps_hits(cuda, built_lib):
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_instance_bvh_refit_keeps_hits(cuda, built_lib, cfg):
     """Refitting the instance BVH (tlas_refit_interval) while instances move must
-    give the same hits as rebuilding it every update, and as the oracle."""
-    sc = scenes.config1(width=320, height=180)
+    give the same hits as rebuilding it every update, and as the oracle: config 1's
+    201 instances (single-launch builder) and config 2's 4,297 (multi-launch
+    builder)."""
+    sc = scenes.config1(width=320, height=180) if cfg == 1 else scenes.config2(width=320, height=180, frames=1)
     rng = np.random.default_rng(21)
     rays = np.concatenate([camera_rays(sc.views[0]), random_rays(sc, 100_000, rng)])
     refit = snkpt.PathTracer(0)
@@ -266,7 +269,7 @@ def test_instance_bvh_refit_keeps_hits(cuda, built_lib):
     for f in range(5):
         prev = inst["transform"].copy()
         move = rng.normal(0.0, 2.0 + 4.0 * f, (len(inst), 3)).astype(np.float32)
-        move[-1] = 0.0                                      # the ground stays
+        move[inst["mesh_id"] == 1] = 0.0                    # the ground stays
         t = inst["transform"].reshape(-1, 3, 4)
         t[:, :, 3] += move
         inst["transform"] = t.reshape(inst["transform"].shape)
