@@ -261,9 +261,12 @@ typedef struct snk_pt_stats {
     uint64_t stage_launches[12]; /* kernel launches per stage of the last render */
     uint64_t cache_queries;      /* paths terminated into the radiance cache */
     uint64_t cache_samples;      /* training samples of the last frame */
-    uint64_t shadow_tests_reused; /* SNK_MODE_RESTIR_DI: visibility tests answered by an identical
+    uint64_t shadow_tests_reused; /* ReSTIR modes: visibility tests answered by an identical
                                      earlier test of the same pixel and frame (not traced; they are
                                      not counted in rays_shadow) */
+    uint64_t graph_launches;     /* SNK_RENDER_USE_GRAPH frames launched as a CUDA graph since create */
+    uint64_t graph_captures;     /* of those, frames captured anew (the others replayed the last
+                                    capture: same views, sizes, settings and scene buffers) */
 } snk_pt_stats;
 
 /* Launch knobs of the wavefront (0 = default).  The reference has no equivalent:

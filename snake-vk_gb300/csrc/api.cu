@@ -148,7 +148,10 @@ struct snk_pt_ctx {
 
     snk_tuning tune{};   // launch knobs (zero = defaults)
     cudaGraphExec_t graph_exec = nullptr;   // replayed frame (SNK_RENDER_USE_GRAPH)
-    uint64_t graph_launches = 0;
+    std::vector<unsigned char> graph_key;   // what the captured launches bake in
+    uint64_t graph_launches = 0, graph_captures = 0;
+    uint64_t graph_stage_launches[SNK_NUM_STAGES] = {0};   // kernel launches per stage of the captured frame
+    DBuf<uint32_t> d_dyn;                   // per-frame seed, frame index, accumulate flag
 
     // MLP radiance cache
     MlpState mlp;
@@ -904,9 +907,9 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             ctx->accum_frames = 0;
         }
         F.accumulate = 1;
-        F.accum = ctx->accum.p;
         ctx->accum_frames++;
     }
+    F.accum = ctx->accum.p;   // (read only when accumulating)
 
     if (ctx->counters.reserve(CNT_TOTAL) != cudaSuccess || ctx->trav.reserve(4) != cudaSuccess)
         return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "counters");
@@ -918,8 +921,11 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         return r;
     };
     // CUDA-graph replay (path modes): the frame's memsets and kernels are captured
-    // once and replayed; a new capture with different parameters updates the
-    // instantiated graph in place (cudaGraphExecUpdate) when the topology matches
+    // once and replayed as long as nothing they bake in changes (the per-frame seed,
+    // frame index and accumulate flag are read from device memory, the views'
+    // poses and outputs from the uploaded view table); otherwise the frame is
+    // captured again and the instantiated graph updated in place
+    // (cudaGraphExecUpdate) when the topology matches
     const bool use_graph = (rs.flags & SNK_RENDER_USE_GRAPH) && path_like && !profile;
     if (!use_graph && reset_counters() != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, "counter reset");
 
@@ -963,13 +969,39 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         F.path_ids[0] = ctx->pid0.p; F.path_ids[1] = ctx->pid1.p;
         F.hits = ctx->hits.p; F.beta = ctx->beta.p; F.L = ctx->L.p;
         F.shadow_rays = ctx->srays.p; F.shadow_contrib = ctx->scontrib.p;
-        if (!use_graph) cudaEventRecord(ctx->ev0, st);
+        const uint32_t dyn[4] = {F.seed, F.frame, F.accumulate, 0u};
+        if (ctx->d_dyn.reserve(4) != cudaSuccess ||
+            cudaMemcpyAsync(ctx->d_dyn.p, dyn, sizeof(dyn), cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return fail(ctx, SNK_ERR_CUDA, "render: frame values upload");
+        F.dyn = ctx->d_dyn.p;
         const int g8 = shade_grid(ctx), g16 = trace_grid(ctx), gany = any_grid(ctx);
+        const uint32_t train_steps = rs.cache_train_steps ? rs.cache_train_steps : 4u;
+        const float train_lr = rs.cache_lr > 0.0f ? rs.cache_lr : (rs.cache_lr < 0.0f ? 0.0f : 1e-2f);
+        if (cache) ctx->last_cache_samples = (uint64_t)n_train * TRAIN_V;
+        bool replay = false;
+        if (use_graph) {   // the key: the frame parameters without the per-frame values, grids, training steps
+            FrameParams K = F;
+            K.seed = 0; K.frame = 0; K.accumulate = 0;
+            const EncodeParams ep = cache ? cache_encode_params(ctx) : EncodeParams{};
+            const int grids[3] = {g8, g16, gany};
+            // (the Adam steps bake their bias corrections in: a cache frame is captured every time)
+            const uint32_t adam_step = cache ? ctx->mlp.step : 0u;
+            std::vector<unsigned char> key(sizeof(K) + sizeof(ep) + sizeof(grids) + 3 * sizeof(uint32_t) + sizeof(float));
+            unsigned char* kp = key.data();
+            auto put = [&](const void* x, size_t b) { std::memcpy(kp, x, b); kp += b; };
+            put(&K, sizeof(K)); put(&ep, sizeof(ep)); put(grids, sizeof(grids));
+            put(&max_depth, sizeof(max_depth)); put(&train_steps, sizeof(train_steps)); put(&train_lr, sizeof(train_lr));
+            put(&adam_step, sizeof(adam_step));
+            replay = ctx->graph_exec && key == ctx->graph_key;
+            if (!replay) ctx->graph_key.swap(key);
+        }
+        if (!use_graph) cudaEventRecord(ctx->ev0, st);
         cudaError_t e = cudaSuccess;
-        if (use_graph) {
+        if (use_graph && !replay) {
             e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) e = reset_counters();
         }
+        if (!replay) {
         if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_GENERATE, [&] { return launch_generate(F, g8, st); });
         for (uint32_t d = 0; d < max_depth && e == cudaSuccess; d++) {
             e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
@@ -1006,9 +1038,13 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
                     return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
                 });
             }
-            ctx->last_cache_samples = total;
         }
-        if (use_graph) {
+        }   // (!replay)
+        // a replayed frame runs the launches its capture counted
+        if (replay) std::memcpy(ctx->stage_launches, ctx->graph_stage_launches, sizeof(ctx->stage_launches));
+        else if (use_graph) std::memcpy(ctx->graph_stage_launches, ctx->stage_launches, sizeof(ctx->stage_launches));
+        if (use_graph && !replay) {
+            ctx->graph_captures++;
             cudaGraph_t graph = nullptr;
             cudaError_t ec = cudaStreamEndCapture(st, &graph);
             if (e == cudaSuccess) e = ec;
@@ -1022,11 +1058,12 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             }
             if (e == cudaSuccess && !ctx->graph_exec) e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
             if (graph) cudaGraphDestroy(graph);
-            if (e == cudaSuccess) {
-                cudaEventRecord(ctx->ev0, st);
-                e = cudaGraphLaunch(ctx->graph_exec, st);
-                ctx->graph_launches++;
-            }
+            if (e != cudaSuccess) ctx->graph_key.clear();
+        }
+        if (use_graph && e == cudaSuccess) {
+            cudaEventRecord(ctx->ev0, st);
+            e = cudaGraphLaunch(ctx->graph_exec, st);
+            ctx->graph_launches++;
         }
         if (path_like) cudaEventRecord(ctx->ev1, st);
         if (e != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
@@ -1551,6 +1588,8 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     if (ctx->d_err.p) cudaMemcpy(&e, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost);
     out->device_error = e;
     out->instance_bvh_refits = (uint32_t)ctx->tlas_refits;
+    out->graph_launches = ctx->graph_launches;
+    out->graph_captures = ctx->graph_captures;
     return SNK_OK;
 }
 

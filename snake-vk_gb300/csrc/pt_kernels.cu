@@ -41,7 +41,7 @@ __device__ __forceinline__ bool decode_path(const FrameParams& F, uint32_t p, ui
         *s = p - *gpix * F.spp;
     } else {
         const uint32_t tid = p - F.n_render;
-        *gpix = (uint32_t)(splitmix64(((uint64_t)F.frame << 32) | tid) % (uint64_t)F.n_pixels);
+        *gpix = (uint32_t)(splitmix64(((uint64_t)frame_index(F) << 32) | tid) % (uint64_t)F.n_pixels);
         *s = 0x40000000u | tid;
     }
     *vi = find_view(F.views, F.nviews, *gpix);
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(BLK) k_generate(FrameParams F) {
         uint32_t gpix, s, vi, x, y;
         decode_path(F, p, &gpix, &s, &vi, &x, &y);
         const ViewDev& V = F.views[vi];
-        Pcg rng = pcg_stream(gpix, s, 0u, F.seed);
+        Pcg rng = pcg_stream(gpix, s, 0u, frame_seed(F));
         float j1 = pcg_float(rng), j2 = pcg_float(rng);
         float jx = s == 0 ? 0.5f : j1, jy = s == 0 ? 0.5f : j2;
         V3 d = camera_dir(V.v, x, y, jx, jy);
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 float4* sr1 = F.shadow_rays + 2 * shadow_entry(F, i, 1);
                 sr0[1].w = -1.0f;
                 sr1[1].w = -1.0f;
-                Pcg rng = pcg_stream(gpix, s, d, F.seed);
+                Pcg rng = pcg_stream(gpix, s, d, frame_seed(F));
                 if (d == 0) { pcg_next(rng); pcg_next(rng); }
                 const bool gbuf = d == 0 && s == 0 && !train;
                 {   // a hit (misses ended in the first pass)
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(BLK) k_resolve(FrameParams F) {
             continue;
         }
         if (V.radiance) V.radiance[o] = r;
-        if (F.accumulate && vi == 0) {
+        if (vi == 0 && frame_accumulate(F)) {
             double2 a0 = F.accum[2ull * o], a1 = F.accum[2ull * o + 1];
             a0.x += (double)r.x; a0.y += (double)r.y; a1.x += (double)r.z; a1.y += 1.0;
             F.accum[2ull * o] = a0;

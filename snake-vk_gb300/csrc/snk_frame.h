@@ -66,7 +66,17 @@ struct FrameParams {
     // instead of the views' radiance outputs
     uint32_t indirect;
     float4* indirect_out;
+    // per-frame values in device memory (seed, frame, accumulate), read by the kernels
+    // instead of the fields above when set, so that a captured frame replays for new
+    // values of them
+    const uint32_t* dyn;
 };
+
+__device__ __forceinline__ uint32_t frame_seed(const FrameParams& F) { return F.dyn ? __ldg(F.dyn) : F.seed; }
+__device__ __forceinline__ uint32_t frame_index(const FrameParams& F) { return F.dyn ? __ldg(F.dyn + 1) : F.frame; }
+__device__ __forceinline__ uint32_t frame_accumulate(const FrameParams& F) {
+    return F.dyn ? __ldg(F.dyn + 2) : F.accumulate;
+}
 
 // Shadow ray k (0: directional light, 1: local light) of queue slot i is entry
 // k * n_paths + i: the queue's directional-light rays are contiguous (one

@@ -86,9 +86,9 @@ STATS_DTYPE = np.dtype([
     ("triangles", "<u8"), ("instances", "<u8"), ("blas_sah_cost", "<f8"),
     ("last_render_ms", "<f8"), ("device_error", "<u4"), ("instance_bvh_refits", "<u4"),
     ("stage_ms", "<f8", (12,)), ("stage_launches", "<u8", (12,)), ("cache_queries", "<u8"),
-    ("cache_samples", "<u8"), ("shadow_tests_reused", "<u8"),
+    ("cache_samples", "<u8"), ("shadow_tests_reused", "<u8"), ("graph_launches", "<u8"), ("graph_captures", "<u8"),
 ])
-assert STATS_DTYPE.itemsize == 320
+assert STATS_DTYPE.itemsize == 336
 STAGES = ("generate", "trace_closest", "shade", "trace_shadow", "resolve", "restir_gbuffer", "restir_initial",
           "restir_spatial", "cache_infer", "cache_samples", "cache_train", "unused")
 

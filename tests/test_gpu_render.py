@@ -377,6 +377,24 @@ def test_graph_replay_matches_stream_launches(cuda, built_lib):
         for g, b in zip(got, base):
             for k in b:
                 assert np.array_equal(g[k], b[k]), (f, k)
+    # new seeds, frame indices, camera poses and output buffers replay the one capture
+    s = pt.stats()
+    assert (s["graph_launches"], s["graph_captures"]) == (3, 1)
+    moved = [v.copy() for v in sc.views]
+    for v in moved:
+        v["pos"] += np.float32(0.5)
+    st = abi.settings(spp=1, max_depth=6, rr_depth=3, seed=99, frame_index=7)
+    base = _gpu_frame(pt, moved, st, cuda)
+    st["flags"] = abi.RENDER_USE_GRAPH
+    got = _gpu_frame(pt, moved, st, cuda)
+    for g, b in zip(got, base):
+        for k in b:
+            assert np.array_equal(g[k], b[k]), ("moved views", k)
+    assert pt.stats()["graph_captures"] == 1
+    # a different depth is a different frame: captured again
+    st = abi.settings(spp=1, max_depth=3, rr_depth=3, seed=5, flags=abi.RENDER_USE_GRAPH)
+    _gpu_frame(pt, sc.views, st, cuda)
+    assert pt.stats()["graph_captures"] == 2
     # cache mode: training kernels (Adam step counters) are captured each frame
     weights = []
     for flags in (0, abi.RENDER_USE_GRAPH):
