@@ -45,7 +45,7 @@ METRIC = "Mrays/s at 1080p"
 UNIT = "Mrays/s"
 WORKLOAD = ("config 1: 200 icosphere-3 instances (1280 tris) + 256x256 ground (131072 tris), 1 directional + "
             "16 sphere lights, 1920x1080, 1 spp, max depth 4, russian roulette from 3, plain wavefront path tracing")
-PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "trace_closest_config1.txt")
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "trace_traversal_config1.txt")
 
 
 def dist_info():
@@ -150,11 +150,12 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    """DRAM bytes of the traversal launches of one frame (closest hits and shadow
+    rays, read + write) from the committed ncu summary of this build."""
     if not os.path.exists(PROFILE_SUMMARY):
         return None
     for line in open(PROFILE_SUMMARY):
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith("dram_bytes_per_frame:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -585,24 +586,30 @@ def run_ours(args):
     total_ms, rays_all = over_ranks(total_ms, rays, ws, dev)
     value = rays_all / (total_ms / 1e3) / 1e6
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel: the traversal core.  Its closest-hit and
+    # shadow launches overlap (the shadow rays of segment d run beside the closest
+    # hits of segment d + 1 on a second stream), so the unit is the frame's
+    # traversal: the algorithmic bytes of all its closest-hit and shadow rays over
+    # the time during which a traversal launch runs (the union of their spans,
+    # stage "trace_any", from CUDA events on the streams the kernels run on)
     peak, peak_kind = measured_peaks()
-    dom = max(("trace_closest", "trace_shadow"), key=lambda n: stage_ms[n])
-    if dom == "trace_closest":
-        nrays, nodes, tris, io = rays_closest, cnt["node_visits"], cnt["triangle_tests"], 32 + 24
-        crays = cnt["rays_camera"] + cnt["rays_extension"]
-    else:
-        nrays, nodes, tris, io = rays_shadow, cnt["shadow_node_visits"], cnt["shadow_triangle_tests"], 32 + 16
-        crays = cnt["rays_shadow"]
-    b_ray = io + 80.0 * nodes / max(crays, 1) + 48.0 * tris / max(crays, 1)
-    bytes_per_launch = b_ray * nrays / max(stage_n[dom], 1)
-    avg_launch_s = stage_ms[dom] / max(stage_n[dom], 1) / 1e3
-    achieved = bytes_per_launch / avg_launch_s / 1e9
-    traffic = profile_traffic() if dom == "trace_closest" else None
-    roofline = {"bound": "hbm", "kernel": f"k_trace_{dom.split('_')[1]}", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                "traffic": traffic, "bytes_per_ray": b_ray,
-                "nodes_per_ray": nodes / max(crays, 1), "tris_per_ray": tris / max(crays, 1),
+    c_rays = cnt["rays_camera"] + cnt["rays_extension"]
+    s_rays = cnt["rays_shadow"]
+    b_closest = 32 + 24 + 80.0 * cnt["node_visits"] / max(c_rays, 1) + 48.0 * cnt["triangle_tests"] / max(c_rays, 1)
+    b_shadow = 32 + 16 + 80.0 * cnt["shadow_node_visits"] / max(s_rays, 1) + \
+        48.0 * cnt["shadow_triangle_tests"] / max(s_rays, 1)
+    trav_bytes = b_closest * rays_closest + b_shadow * rays_shadow   # over the timed frames
+    trav_s = stage_ms["trace_any"] / 1e3
+    achieved = trav_bytes / trav_s / 1e9
+    traffic = profile_traffic()
+    roofline = {"bound": "hbm", "kernel": "k_trace_closest + k_trace_shadow (one traversal core, overlapped)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": traffic, "traffic_source": os.path.relpath(PROFILE_SUMMARY, ROOT) if traffic else None,
+                "bytes_per_closest_ray": b_closest, "bytes_per_shadow_ray": b_shadow,
+                "traversal_ms_per_frame": stage_ms["trace_any"] / args.steps,
+                "algorithmic_bytes_per_frame": trav_bytes / args.steps,
+                "nodes_per_ray": cnt["node_visits"] / max(c_rays, 1), "tris_per_ray": cnt["triangle_tests"] / max(c_rays, 1),
+                "shadow_nodes_per_ray": cnt["shadow_node_visits"] / max(s_rays, 1),
                 "stage_ms_per_frame": {k: v / args.steps for k, v in stage_ms.items() if v > 0}}
 
     # end to end through the C ABI with host buffers

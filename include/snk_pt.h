@@ -80,12 +80,15 @@ extern "C" {
 #define SNK_STAGE_SHADE           2
 #define SNK_STAGE_TRACE_SHADOW    3
 #define SNK_STAGE_RESOLVE         4
-#define SNK_STAGE_RESTIR_GBUFFER  5
+#define SNK_STAGE_RESTIR_GBUFFER  5  /* (no longer used: the ReSTIR G-buffer is the wavefront's first segment) */
 #define SNK_STAGE_RESTIR_INITIAL  6
 #define SNK_STAGE_RESTIR_SPATIAL  7
 #define SNK_STAGE_CACHE_INFER     8
 #define SNK_STAGE_CACHE_SAMPLES   9
 #define SNK_STAGE_CACHE_TRAIN    10
+#define SNK_STAGE_TRACE_ANY      11  /* stage_ms only: time during which a path-tracing traversal kernel
+                                        runs (the union of the closest-hit and shadow launches' spans,
+                                        which overlap on two streams) */
 #define SNK_NUM_STAGES           12
 
 /* trace flags */

@@ -5,6 +5,7 @@
 // RT::Init / RT::RecordRenderCmdBuf (Core/src/rendering/Raytracing.cpp:227-278)
 // and the scene buffer systems that fill its descriptor table
 // (Core/src/rendering/Raytracing.cpp:72-145).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -143,6 +144,9 @@ struct snk_pt_ctx {
     size_t prof_used = 0;
     bool prof_pending = false;
     bool prof_chain = false;   // the last recorded event ended a stage and nothing was enqueued since
+    cudaStream_t prof_stream = nullptr;   // the stream of that event
+    cudaStream_t side = nullptr;          // second wavefront stream (shadow rays)
+    cudaEvent_t ev_fork[MAX_DEPTH] = {}, ev_join[MAX_DEPTH] = {};
     double stage_ms[SNK_NUM_STAGES] = {0};
     uint64_t stage_launches[SNK_NUM_STAGES] = {0};
 
@@ -604,14 +608,15 @@ TraceTuning any_tuning(snk_pt_ctx* ctx) {
     return t;
 }
 
-// Runs one kernel launch; with profiling on, brackets it with an event pair.
+// Runs one stage's launches; when profiling, CUDA events bracket them on the stream
+// they are issued to (the context's stream unless given).  Stages enqueued back to
+// back on one stream share the event between them (the end of one is the start of
+// the next), so a profiled frame records about one event per stage boundary.
 template <class Fn>
-// Runs one stage's launches; when profiling, CUDA events bracket them.  Stages
-// enqueued back to back share the event between them (the end of one is the
-// start of the next), so a profiled frame records one event per stage boundary.
-cudaError_t staged(snk_pt_ctx* ctx, bool profile, int stage, Fn&& fn) {
+cudaError_t staged(snk_pt_ctx* ctx, bool profile, int stage, Fn&& fn, cudaStream_t stream = nullptr) {
     ctx->stage_launches[stage]++;
     if (!profile) return fn();
+    if (!stream) stream = ctx->stream;
     if (ctx->prof_used + 2 > ctx->prof_ev.size()) {
         for (int k = 0; k < 16; k++) {
             cudaEvent_t e;
@@ -621,18 +626,31 @@ cudaError_t staged(snk_pt_ctx* ctx, bool profile, int stage, Fn&& fn) {
         }
     }
     uint32_t b;
-    if (ctx->prof_chain && ctx->prof_used > 0) {
+    if (ctx->prof_chain && ctx->prof_used > 0 && ctx->prof_stream == stream) {
         b = (uint32_t)(ctx->prof_used - 1);
     } else {
         b = (uint32_t)ctx->prof_used++;
-        cudaEventRecord(ctx->prof_ev[b], ctx->stream);
+        cudaEventRecord(ctx->prof_ev[b], stream);
     }
     cudaError_t r = fn();
     const uint32_t e = (uint32_t)ctx->prof_used++;
-    cudaEventRecord(ctx->prof_ev[e], ctx->stream);
+    cudaEventRecord(ctx->prof_ev[e], stream);
     ctx->prof_iv.push_back({b, e, stage});
     ctx->prof_chain = true;
+    ctx->prof_stream = stream;
     return r;
+}
+
+// The second stream of the wavefront (shadow rays of segment d traced while the
+// closest hits of segment d + 1 are) and its fork / join events, made on first use.
+cudaError_t ensure_side_stream(snk_pt_ctx* ctx) {
+    if (ctx->side) return cudaSuccess;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    for (uint32_t d = 0; d < MAX_DEPTH && e == cudaSuccess; d++) {
+        e = cudaEventCreateWithFlags(&ctx->ev_fork[d], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join[d], cudaEventDisableTiming);
+    }
+    return e;
 }
 
 }  // namespace
@@ -687,6 +705,12 @@ int snk_pt_destroy(snk_pt_ctx* ctx) {
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    for (uint32_t d = 0; d < MAX_DEPTH; d++) {
+        if (ctx->ev_fork[d]) cudaEventDestroy(ctx->ev_fork[d]);
+        if (ctx->ev_join[d]) cudaEventDestroy(ctx->ev_join[d]);
+    }
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     cudaStream_t s = ctx->own_stream ? ctx->stream : nullptr;
     delete ctx;
     if (s) cudaStreamDestroy(s);
@@ -1002,15 +1026,37 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
             if (e == cudaSuccess) e = reset_counters();
         }
         if (!replay) {
+        // Segment d: closest hits, shading, then its shadow rays.  The shadow rays of
+        // segment d and the closest hits of segment d + 1 are independent (they read
+        // the queues shade(d) wrote and write different outputs), so they run
+        // concurrently on two streams; shade(d + 1), which reuses segment d's shadow
+        // slots, waits for both.  The kernels that end a launch early overlap the
+        // other's tail instead of leaving SMs idle.
+        if (e == cudaSuccess) e = ensure_side_stream(ctx);
+        cudaStream_t side = ctx->side;
         if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_GENERATE, [&] { return launch_generate(F, g8, st); });
-        for (uint32_t d = 0; d < max_depth && e == cudaSuccess; d++) {
+        if (e == cudaSuccess)
             e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
-                       [&] { return launch_trace_closest(F, d, g16, count_nodes, st); });
-            if (e == cudaSuccess) e = staged(ctx, profile, SNK_STAGE_SHADE, [&] { return launch_shade(F, d, g8, st); });
+                       [&] { return launch_trace_closest(F, 0, g16, count_nodes, st); });
+        for (uint32_t d = 0; d < max_depth && e == cudaSuccess; d++) {
+            e = staged(ctx, profile, SNK_STAGE_SHADE, [&] { return launch_shade(F, d, g8, st); });
             // (in the ReSTIR modes the primary vertex queues no shadow rays: ReSTIR shades it)
-            if (e == cudaSuccess && !(F.indirect && d == 0))
-                e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
-                           [&] { return launch_trace_shadow(F, d, gany, count_nodes, st); });
+            const bool shadows = !(F.indirect && d == 0);
+            if (e == cudaSuccess && shadows) {
+                e = cudaEventRecord(ctx->ev_fork[d], st);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ctx->ev_fork[d], 0);
+                if (e == cudaSuccess)
+                    e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
+                               [&] { return launch_trace_shadow(F, d, gany, count_nodes, side); }, side);
+                if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join[d], side);
+            }
+            if (e == cudaSuccess && d + 1 < max_depth)
+                e = staged(ctx, profile, SNK_STAGE_TRACE_CLOSEST,
+                           [&] { return launch_trace_closest(F, d + 1, g16, count_nodes, st); });
+            if (e == cudaSuccess && shadows) {
+                e = cudaStreamWaitEvent(st, ctx->ev_join[d], 0);
+                ctx->prof_chain = false;   // the next stage starts after the wait, not at the last event
+            }
         }
         if (cache && e == cudaSuccess) {
             const EncodeParams ep = cache_encode_params(ctx);
@@ -1561,11 +1607,34 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     out->shadow_triangle_tests = ctx->last_count_nodes ? ctx->h_trav[3] : 0;
     if (ctx->prof_pending) {
         for (int k = 0; k < SNK_NUM_STAGES; k++) ctx->stage_ms[k] = 0.0;
+        // traversal intervals (closest hits and shadow rays overlap on two streams),
+        // as times from the frame's first event, for the union of their spans
+        std::vector<std::pair<float, float>> trav;
         for (const auto& iv : ctx->prof_iv) {
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, ctx->prof_ev[iv.begin], ctx->prof_ev[iv.end]);
             ctx->stage_ms[iv.stage] += ms;
+            if (iv.stage == SNK_STAGE_TRACE_CLOSEST || iv.stage == SNK_STAGE_TRACE_SHADOW) {
+                float t0 = 0.0f, t1 = 0.0f;
+                cudaEventElapsedTime(&t0, ctx->prof_ev[0], ctx->prof_ev[iv.begin]);
+                cudaEventElapsedTime(&t1, ctx->prof_ev[0], ctx->prof_ev[iv.end]);
+                trav.emplace_back(t0, t1);
+            }
         }
+        std::sort(trav.begin(), trav.end());
+        double uni = 0.0;
+        float cur0 = 0.0f, cur1 = -1.0f;
+        for (const auto& t : trav) {
+            if (t.first > cur1) {
+                if (cur1 > cur0) uni += cur1 - cur0;
+                cur0 = t.first;
+                cur1 = t.second;
+            } else if (t.second > cur1) {
+                cur1 = t.second;
+            }
+        }
+        if (cur1 > cur0) uni += cur1 - cur0;
+        ctx->stage_ms[SNK_STAGE_TRACE_ANY] = uni;
         ctx->prof_pending = false;
     }
     for (int k = 0; k < SNK_NUM_STAGES; k++) {

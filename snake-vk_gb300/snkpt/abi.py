@@ -90,7 +90,7 @@ STATS_DTYPE = np.dtype([
 ])
 assert STATS_DTYPE.itemsize == 336
 STAGES = ("generate", "trace_closest", "shade", "trace_shadow", "resolve", "restir_gbuffer", "restir_initial",
-          "restir_spatial", "cache_infer", "cache_samples", "cache_train", "unused")
+          "restir_spatial", "cache_infer", "cache_samples", "cache_train", "trace_any")
 
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_STATE, ERR_LIMIT, ERR_UNSUPPORTED = 0, 1, 2, 3, 4, 5, 6
 MODE_PATH, MODE_RESTIR_DI, MODE_PATH_CACHE, MODE_RESTIR_PT = 0, 1, 2, 3

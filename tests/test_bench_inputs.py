@@ -1,5 +1,5 @@
 """Inputs of the benchmark line: the measured HBM peak (roofline denominator) and
-the dominant kernel's DRAM bytes per launch from its committed ncu summary
+the traversal kernels' DRAM bytes per frame from their committed ncu summary
 (roofline.traffic), so that neither silently becomes a fallback or null; and the
 summary of the clock samples taken during the timed region."""
 import json
@@ -21,12 +21,13 @@ def test_roofline_peak_is_the_measured_one():
         assert kind == "fallback"
 
 
-def test_profile_summary_gives_dram_bytes_per_launch():
+def test_profile_summary_gives_dram_bytes_per_frame():
     t = bench.profile_traffic()
     assert t is not None and 1e6 < t < 1e10
-    # the summary names the kernel the bench reports and the command that made it
+    # the summary names the kernels the bench reports and the command that made it
     text = open(bench.PROFILE_SUMMARY).read()
-    assert "k_trace_closest" in text and "ncu " in text and "--clock-control none" in text
+    assert "k_trace_closest" in text and "k_trace_shadow" in text and "ncu " in text
+    assert "--clock-control none" in text
 
 
 def test_clock_samples_summary():
