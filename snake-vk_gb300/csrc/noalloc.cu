@@ -108,12 +108,13 @@ extern "C" int snk_pt_render_noalloc(snk_pt_ctx* ctx, const snk_view* view, cons
     if (e != cudaSuccess)
         return ctx_fail(ctx, SNK_ERR_CUDA, (std::string("render_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
 
-    // header: counters (256 B), traversal counters (32 B), the view descriptor
+    // header: counters (at 0), traversal counters (32 B at 512), the view descriptor (at 1024)
     const size_t P = NOALLOC_MAX_PATHS;
+    static_assert(CNT_TOTAL * sizeof(uint32_t) <= 512, "frame counters fit the header");
     uint32_t* counters = reinterpret_cast<uint32_t*>(base);
-    unsigned long long* trav = reinterpret_cast<unsigned long long*>(base + 256);
-    ViewDev* dview = reinterpret_cast<ViewDev*>(base + 512);
-    static_assert(512 + sizeof(ViewDev) <= NOALLOC_HEADER, "view descriptor fits the header");
+    unsigned long long* trav = reinterpret_cast<unsigned long long*>(base + 512);
+    ViewDev* dview = reinterpret_cast<ViewDev*>(base + 1024);
+    static_assert(1024 + sizeof(ViewDev) <= NOALLOC_HEADER, "view descriptor fits the header");
     unsigned char* q = base + NOALLOC_HEADER;
     auto take = [&](size_t bytes) { unsigned char* r = q; q += bytes; return r; };
 

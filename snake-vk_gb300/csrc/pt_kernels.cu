@@ -122,9 +122,9 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
             bool hit = false;
             if (i < n) {
                 hit = F.hits[i].flags != 0u;
-                if (!hit) {
-                    F.shadow_rays[2 * shadow_entry(F, i, 0) + 1].w = -1.0f;
-                    F.shadow_rays[2 * shadow_entry(F, i, 1) + 1].w = -1.0f;
+                if (!hit) {   // no shadow rays: zero contributions
+                    F.shadow_contrib[shadow_entry(F, i, 0)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    F.shadow_contrib[shadow_entry(F, i, 1)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (d == 0) {
                         uint32_t gpix, s, vi, x, y;
                         const bool train = decode_path(F, F.path_ids[cur][i], &gpix, &s, &vi, &x, &y);
@@ -151,6 +151,10 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
             bool cont = false, sv0 = false, sv1 = false, query = false;
             uint32_t p = 0;
             float4 nr0 = make_float4(0, 0, 0, 0), nr1 = make_float4(0, 0, 0, 0);
+            // shadow rays: their origin and the local-light ray's direction + tmax (the
+            // directional-light ray's direction is the light's); contributions are
+            // written where the rays are made
+            float4 so = make_float4(0, 0, 0, 0), sd1 = so;
             float4 q0, q1, q2, q3, qb;
             if (have) {
                 p = F.path_ids[cur][i];
@@ -161,10 +165,6 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 float4 rd4 = F.rays[cur][2ull * i + 1];
                 V3 rd = v3(rd4.x, rd4.y, rd4.z);
                 HitDev h = F.hits[i];
-                float4* sr0 = F.shadow_rays + 2 * shadow_entry(F, i, 0);
-                float4* sr1 = F.shadow_rays + 2 * shadow_entry(F, i, 1);
-                sr0[1].w = -1.0f;
-                sr1[1].w = -1.0f;
                 Pcg rng = pcg_stream(gpix, s, d, frame_seed(F));
                 if (d == 0) { pcg_next(rng); pcg_next(rng); }
                 const bool gbuf = d == 0 && s == 0 && !train;
@@ -225,8 +225,6 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                                                     sf.roughness, sf.metallic, sf.albedo);
                             if (maxc(c) > 0.0f) {
                                 V3 cb = cmul(beta, c);
-                                sr0[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
-                                sr0[1] = make_float4(S.dir_light.dir[0], S.dir_light.dir[1], S.dir_light.dir[2], T_FAR);
                                 F.shadow_contrib[shadow_entry(F, i, 0)] = make_float4(cb.x, cb.y, cb.z, 0.0f);
                                 sv0 = true;
                             }
@@ -235,11 +233,11 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         float ltmax;
                         if (direct && sample_local(S, sf, v, f0, xb, u_sel, u1, u2, &c, &ldir, &ltmax)) {
                             V3 cb = cmul(beta, c);
-                            sr1[0] = make_float4(xb.x, xb.y, xb.z, SHADOW_TMIN);
-                            sr1[1] = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
+                            sd1 = make_float4(ldir.x, ldir.y, ldir.z, ltmax);
                             F.shadow_contrib[shadow_entry(F, i, 1)] = make_float4(cb.x, cb.y, cb.z, 0.0f);
                             sv1 = true;
                         }
+                        so = make_float4(xb.x, xb.y, xb.z, 0.0f);
                         bool alive = d + 1 < F.max_depth;
                         if (alive && d + 1 >= F.rr_depth) {
                             float ps = fmin_(maxc(beta), 0.95f);
@@ -261,21 +259,42 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                     }
                 }
             }
-            // warp-ballot compaction of the continuing paths into the next queue
+            if (have) {   // zero contribution: no shadow ray of that kind
+                const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (!sv0) F.shadow_contrib[shadow_entry(F, i, 0)] = z;
+                if (!sv1) F.shadow_contrib[shadow_entry(F, i, 1)] = z;
+            }
+            // warp-ballot compaction of the continuing paths into the next queue and of
+            // the shadow rays into their kinds' parts of the shadow queue
             const unsigned full = 0xFFFFFFFFu;
-            unsigned m = __ballot_sync(full, cont);
-            unsigned sm = __popc(__ballot_sync(full, sv0)) + __popc(__ballot_sync(full, sv1));
-            uint32_t slot_base = 0;
+            const unsigned m = __ballot_sync(full, cont);
+            const unsigned m0 = __ballot_sync(full, sv0), m1 = __ballot_sync(full, sv1);
+            const unsigned lt = (1u << lane) - 1u;
+            uint32_t slot_base = 0, b0 = 0, b1 = 0;
             if (lane == 0) {
                 if (m) slot_base = atomicAdd(&F.counters[CNT_QUEUE + d + 1], (uint32_t)__popc(m));
-                if (sm) atomicAdd(&F.counters[CNT_SHADOW_RAYS], sm);
+                if (m0) b0 = atomicAdd(&F.counters[CNT_SHADOW_Q + 2 * d], (uint32_t)__popc(m0));
+                if (m1) b1 = atomicAdd(&F.counters[CNT_SHADOW_Q + 2 * d + 1], (uint32_t)__popc(m1));
+                if (m0 | m1) atomicAdd(&F.counters[CNT_SHADOW_RAYS], (uint32_t)(__popc(m0) + __popc(m1)));
             }
             slot_base = __shfl_sync(full, slot_base, 0);
+            b0 = __shfl_sync(full, b0, 0);
+            b1 = __shfl_sync(full, b1, 0);
             if (cont) {
-                uint32_t j = slot_base + __popc(m & ((1u << lane) - 1u));
+                uint32_t j = slot_base + __popc(m & lt);
                 F.rays[nxt][2ull * j] = nr0;
                 F.rays[nxt][2ull * j + 1] = nr1;
                 F.path_ids[nxt][j] = p;
+            }
+            if (sv0) {   // (the origin's w carries the bits of the contribution entry)
+                const size_t e = b0 + (uint32_t)__popc(m0 & lt);
+                F.shadow_rays[2 * e] = make_float4(so.x, so.y, so.z, __uint_as_float((uint32_t)shadow_entry(F, i, 0)));
+                F.shadow_rays[2 * e + 1] = make_float4(S.dir_light.dir[0], S.dir_light.dir[1], S.dir_light.dir[2], T_FAR);
+            }
+            if (sv1) {
+                const size_t e = (size_t)F.n_paths + b1 + (uint32_t)__popc(m1 & lt);
+                F.shadow_rays[2 * e] = make_float4(so.x, so.y, so.z, __uint_as_float((uint32_t)shadow_entry(F, i, 1)));
+                F.shadow_rays[2 * e + 1] = sd1;
             }
             if (F.cache) {
                 const unsigned qm = __ballot_sync(full, query);

@@ -16,7 +16,8 @@ constexpr uint32_t CNT_WORK_SHADOW = 32;  // [d]: work fetch of the shadow pass 
 constexpr uint32_t CNT_SHADOW_RAYS = 48;  // valid shadow rays
 constexpr uint32_t CNT_CACHE_QUERIES = 49; // paths terminated into the radiance cache
 constexpr uint32_t CNT_SHADOW_REUSED = 50;  // ReSTIR visibility tests answered by an identical earlier test
-constexpr uint32_t CNT_TOTAL = 64;
+constexpr uint32_t CNT_SHADOW_Q = 64;     // [2d + k]: shadow rays of light kind k queued by segment d
+constexpr uint32_t CNT_TOTAL = 96;
 constexpr uint32_t TRAIN_V = 4;           // recorded vertices per cache training path
 
 struct HitDev { float t; uint32_t inst, prim; float u, v; uint32_t flags; };
@@ -43,8 +44,10 @@ struct FrameParams {
     HitDev* hits;
     float4* beta;            // per path
     float4* L;               // per path radiance
-    float4* shadow_rays;     // 2 rays per queue slot, light-major (shadow_entry), 2 float4 each, tmax < 0 = none
-    float4* shadow_contrib;  // 1 per shadow entry
+    float4* shadow_rays;     // compacted shadow-ray queue of a segment, 2 float4 per ray: (origin, bits of its
+                             // contribution entry), (direction, tmax); directional-light rays from 0,
+                             // local-light rays from n_paths (counts in CNT_SHADOW_Q)
+    float4* shadow_contrib;  // 1 per shadow entry (shadow_entry): contribution, w = visibility (0: none)
     uint32_t* counters;
     unsigned long long* trav_counters;   // closest: [0] nodes [1] triangles; shadow: [2] [3]
     double2* accum;          // FP64 accumulator of view 0 (2 double2 per pixel)
@@ -78,9 +81,11 @@ __device__ __forceinline__ uint32_t frame_accumulate(const FrameParams& F) {
     return F.dyn ? __ldg(F.dyn + 2) : F.accumulate;
 }
 
-// Shadow ray k (0: directional light, 1: local light) of queue slot i is entry
-// k * n_paths + i: the queue's directional-light rays are contiguous (one
-// direction, neighbouring origins), then its local-light rays.
+// The contribution of shadow ray k (0: directional light, 1: local light) of queue
+// slot i is entry k * n_paths + i.  The rays themselves are compacted: each kind's
+// rays that carry a contribution are appended to that kind's part of the queue,
+// so the traversal kernel takes only real rays, the directional-light rays
+// together (one direction, neighbouring origins), then the local-light rays.
 __host__ __device__ __forceinline__ size_t shadow_entry(const FrameParams& F, uint32_t i, uint32_t k) {
     return (size_t)k * F.n_paths + i;
 }

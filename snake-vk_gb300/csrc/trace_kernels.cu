@@ -134,15 +134,16 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
     flush_counts<COUNT>(ctr, F.trav_counters);
 }
 
-// shadow rays of segment d: the queue's n directional-light entries, then its n
-// local-light entries (shadow_entry); tmax < 0 marks an empty entry.  The visibility goes to the w component
-// of the entry's contribution; k_accum_shadow adds the visible contributions in
-// entry order (the same order as the CPU oracle, so sums are bit-identical).
+// shadow rays of segment d: the compacted queue's n0 directional-light rays, then
+// its n1 local-light rays (from n_paths on).  A ray's origin w holds its
+// contribution entry (shadow_entry); the visibility goes to that contribution's w
+// component, and k_accum_shadow adds the visible contributions in entry order
+// (the same order as the CPU oracle, so sums are bit-identical).
 template <bool COUNT, int MINB>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint32_t d) {
     const Knobs kn(F.tune_any);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
-    const uint32_t n = 2u * F.counters[CNT_QUEUE + d];
+    const uint32_t n0 = F.counters[CNT_SHADOW_Q + 2 * d], n = n0 + F.counters[CNT_SHADOW_Q + 2 * d + 1];
     uint32_t* work = &F.counters[CNT_WORK_SHADOW + d];
     const uint32_t lane = threadIdx.x & 31u;
     TraceCounters ctr{0ull, 0ull};
@@ -157,18 +158,12 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint
         if (__popc(~act) >= kn.refill_idle && !feed.done()) {
             uint32_t j = feed.refill(~act, lane, work, n, kn.chunk);
             if (j != INVALID) {
-                const uint32_t half = n >> 1;
-                const size_t i = j < half ? shadow_entry(F, j, 0) : shadow_entry(F, j - half, 1);
-                const float4* sr = F.shadow_rays + 2 * i;
-                float4 b = sr[1];
-                if (b.w < 0.0f) {
-                    F.shadow_contrib[i].w = 0.0f;
-                } else {
-                    float4 a = sr[0];
-                    tv.init(F.S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
-                    ri = (uint32_t)i;
-                    active = true;
-                }
+                const size_t e = j < n0 ? (size_t)j : (size_t)F.n_paths + (j - n0);
+                const float4* sr = F.shadow_rays + 2 * e;
+                const float4 a = __ldg(sr), b = __ldg(sr + 1);
+                tv.init(F.S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), SHADOW_TMIN, b.w, sh_stack, spill, threadIdx.x, TBLK);
+                ri = __float_as_uint(a.w);
+                active = true;
             }
             act = __ballot_sync(0xFFFFFFFFu, active);
         }
