@@ -99,7 +99,8 @@ cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid,
 cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s);
 cudaError_t launch_trace_rays(const SceneDev& S, const float4* rays, uint32_t n, HitDev* hits, bool any,
                               uint32_t* work_counter, int grid, const TraceTuning& tune, cudaStream_t s);
-// vis[i] = 1 when segment i (origin, tmin | direction, tmax; tmax < 0: empty) is unoccluded
+// vis[i] = 1 when segment i (origin, tmin | direction, tmax) is unoccluded, 0 when it
+// is not; an empty entry (tmax < 0) is skipped and its vis[i] left as it was
 cudaError_t launch_trace_visibility(const SceneDev& S, const float4* rays, uint32_t n, uint8_t* vis,
                                     uint32_t* work_counter, int grid, const TraceTuning& tune, cudaStream_t s);
 

@@ -203,8 +203,40 @@ __global__ void __launch_bounds__(256) k_accum_shadow(FrameParams F, uint32_t d)
     }
 }
 
+// Ray feed over a queue with empty entries (tmax < 0): the warp takes 32 entries
+// at a time from the work counter, keeps the real ones in a per-warp ring in
+// shared memory and hands only those to its idle lanes, so an empty entry costs
+// one 4-byte load instead of a lane's turn.
+struct FilteredFeed {
+    RayFeed raw;
+    uint32_t head, cnt;   // the ring's pending entries (warp-uniform)
+    __device__ __forceinline__ void init() { raw.init(); head = 0; cnt = 0; }
+    __device__ __forceinline__ uint32_t refill(unsigned idle, uint32_t lane, uint32_t* work, uint32_t n, uint32_t chunk,
+                                               const float4* rays, uint32_t* ring) {
+        const uint32_t nidle = (uint32_t)__popc(idle), lt = (1u << lane) - 1u;
+        while (cnt < nidle && !raw.done()) {   // (cnt < 32 here, so the ring of 64 never overflows)
+            const uint32_t e = raw.refill(0xFFFFFFFFu, lane, work, n, chunk);
+            const bool real = e != INVALID && __ldg(reinterpret_cast<const float*>(rays + 2ull * e + 1) + 3) >= 0.0f;
+            const unsigned rm = __ballot_sync(0xFFFFFFFFu, real);
+            if (real) ring[(head + cnt + (uint32_t)__popc(rm & lt)) & 63u] = e;
+            cnt += (uint32_t)__popc(rm);
+            __syncwarp();
+        }
+        uint32_t mine = INVALID;
+        const uint32_t r = (uint32_t)__popc(idle & lt);
+        if (((idle >> lane) & 1u) && r < cnt) mine = ring[(head + r) & 63u];
+        const uint32_t take = nidle < cnt ? nidle : cnt;
+        head = (head + take) & 63u;
+        cnt -= take;
+        __syncwarp();
+        return mine;
+    }
+    __device__ __forceinline__ bool done() const { return raw.done() && cnt == 0; }
+};
+
 // visibility of a queue of segments: vis[i] = 1 when nothing is hit in (tmin, tmax),
-// 0 when something is; entries with tmax < 0 are empty (vis 1, no traversal).
+// 0 when something is; entries with tmax < 0 are empty (skipped, vis[i] not written:
+// the passes never read the result of a slot they did not record).
 // The ReSTIR passes queue their visibility rays here instead of tracing inline.
 template <int MINB>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_visibility(SceneDev S, const float4* __restrict__ rays,
@@ -212,27 +244,23 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_visibility(SceneDev S, con
                                                                  TraceTuning tune) {
     const Knobs kn(tune);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
+    __shared__ uint32_t ring[TBLK / 32][64];
     const uint32_t lane = threadIdx.x & 31u;
     Traverser<true, false> tv;
     uint2 spill[STACK_MAX - STACK_SH];
-    RayFeed feed;
+    FilteredFeed feed;
     feed.init();
     bool active = false;
     uint32_t ri = 0;
     for (;;) {
         unsigned act = __ballot_sync(0xFFFFFFFFu, active);
         if (__popc(~act) >= kn.refill_idle && !feed.done()) {
-            uint32_t i = feed.refill(~act, lane, work, n, kn.chunk);
+            uint32_t i = feed.refill(~act, lane, work, n, kn.chunk, rays, ring[threadIdx.x >> 5]);
             if (i != INVALID) {
-                float4 b = __ldg(rays + 2ull * i + 1);
-                if (b.w < 0.0f) {
-                    vis[i] = 1u;
-                } else {
-                    float4 a = __ldg(rays + 2ull * i);
-                    tv.init(S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
-                    ri = i;
-                    active = true;
-                }
+                const float4 a = __ldg(rays + 2ull * i), b = __ldg(rays + 2ull * i + 1);
+                tv.init(S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, sh_stack, spill, threadIdx.x, TBLK);
+                ri = i;
+                active = true;
             }
             act = __ballot_sync(0xFFFFFFFFu, active);
         }
