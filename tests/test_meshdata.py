@@ -53,6 +53,51 @@ def test_writer_round_trip(built_lib):
         assert np.array_equal(m.positions, pos[sub["base_vertex"][k]:sub["base_vertex"][k] + nv[k]])
 
 
+REF_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_serializer.meshdata")
+
+
+def reference_writer_content():
+    """The mesh oracle/ref_serializer/meshdata_writer.cpp serializes (same formulas)."""
+    i = np.arange(11, dtype=np.float32)
+    pos = np.stack([i * np.float32(0.5) - np.float32(2.0), i * i * np.float32(0.125), np.float32(3.0) - i * np.float32(0.25)], 1)
+    nrm = np.stack([np.zeros(11, np.float32), np.where(np.arange(11) % 2 == 1, 1.0, -1.0).astype(np.float32),
+                    np.zeros(11, np.float32)], 1)
+    tan = np.stack([np.ones(11, np.float32), np.zeros(11, np.float32), i * np.float32(0.0625)], 1)
+    uv = np.stack([i * np.float32(0.1), np.float32(1.0) - i * np.float32(0.1)], 1)
+    idx = np.concatenate([(np.arange(9) * 2 + 1) % 5, (np.arange(12) * 5 + 2) % 6]).astype(np.uint32)
+    sub = np.zeros(2, MD.SUBMESH_DTYPE)
+    sub[0] = (9, 5, 0, 0, 1)
+    sub[1] = (12, 6, 5, 9, 0)
+    return dict(uuid=0x5EED0A55E7000001, name="reference_serializer", submeshes=sub, positions=pos, normals=nrm,
+                tangents=tan, tex_coords=uv, indices=idx, materials=[0x0A0A000000000011, 0x0B0B000000000022],
+                textures=[0x0C0C000000000033])
+
+
+def test_asset_written_by_the_reference_serializer(built_lib, tmp_path):
+    """A .meshdata written by the reference's own ByteSerializer (compiled from
+    Core/headers/util/ByteSerializer.h, driven as AssetLoader::SerializeMeshDataBinary
+    drives it): the library's reader and the oracle's restatement both read back
+    every field of what was written.  Where the reference's sources are present the
+    committed file is also regenerated and must be byte-identical."""
+    import build_ref
+    data = open(REF_GOLDEN, "rb").read()
+    fresh = str(tmp_path / "fresh.meshdata")
+    if build_ref.write_meshdata(fresh):
+        assert open(fresh, "rb").read() == data
+    want = reference_writer_content()
+    md = MD.load(data)
+    ref = R.parse(data)
+    same_as_reference(md, ref)
+    assert md.uuid == want["uuid"] and md.name == want["name"]
+    assert np.array_equal(md.submeshes, want["submeshes"])
+    for k in ("positions", "normals", "tangents", "tex_coords", "indices"):
+        assert np.array_equal(getattr(md, k), want[k]), k
+    assert list(md.materials) == want["materials"] and list(md.textures) == want["textures"]
+    a, b = md.meshes()   # one snk_mesh per submesh, indices local to it
+    assert a.indices.shape == (3, 3) and b.indices.shape == (4, 3)
+    assert np.array_equal(b.positions, want["positions"][5:11])
+
+
 def test_truncated_files_are_rejected(built_lib):
     data = open(GOLDEN, "rb").read()
     for cut in range(len(data)):
