@@ -409,6 +409,40 @@ int snk_pt_cache_infer(snk_pt_ctx* ctx, const float* records, uint32_t n, float*
 int snk_pt_cache_train(snk_pt_ctx* ctx, const float* samples, uint32_t n, float lr, float* grad, float* loss,
                        uint32_t memory);
 
+/* Quality guard of the radiance cache: frames over a relMSE budget fall back to
+ * plain path tracing.  With a guard set, every check_every-th SNK_MODE_PATH_CACHE
+ * frame (from the second on) is preceded by a probe: view 0 at 1/probe_scale
+ * resolution, probe_spp samples per pixel, rendered with the cache (no training
+ * step) and plainly; their relMSE over block x block pixel means
+ * (snk_cache_guard_relmse) above relmse_budget makes the following cache frames
+ * render plainly -- no path ends in the cache, so the image is the plain tracer's
+ * bit for bit, while the frame's training paths keep training the network -- until
+ * a later probe passes.  The probe synchronises.  32 bytes. */
+typedef struct snk_cache_guard {
+    float    relmse_budget;   /* (0.05) */
+    uint32_t check_every;     /* cache frames per probe; 0 turns the guard off */
+    uint32_t probe_scale;     /* probe resolution divisor (4) */
+    uint32_t probe_spp;       /* (16) */
+    uint32_t block;           /* pixel block side of the relMSE (4) */
+    uint32_t pad[3];
+} snk_cache_guard;
+typedef struct snk_cache_guard_state {
+    uint64_t frames;          /* cache frames rendered since the guard was set */
+    uint64_t probes;
+    uint64_t fallback_frames; /* of the frames, those rendered plainly */
+    double   last_probe_relmse;  /* -1 before the first probe */
+    uint32_t fallback;        /* 1 while the last probe was over budget */
+    uint32_t pad;
+} snk_cache_guard_state;
+/* sets (or, with NULL / check_every 0, removes) the guard; resets its state */
+int snk_pt_cache_set_guard(snk_pt_ctx* ctx, const snk_cache_guard* guard);
+int snk_pt_cache_get_guard_state(const snk_pt_ctx* ctx, snk_cache_guard_state* state);
+/* the guard's error measure of two RGBA32F host images of width x height:
+ * mean over the block x block pixel means and 3 channels of (c - p)^2 / (p^2 + 0.01)
+ * (block clamped to [1, min(width, height)]; pixels past the last whole block are left out) */
+int snk_cache_guard_relmse(const float* cached, const float* plain, uint32_t width, uint32_t height, uint32_t block,
+                           double* relmse);
+
 /* FP64 converged-image accumulator of view 0: copies the running mean (samples
  * accumulated so far) as float4 into out (memory space as given). */
 int snk_pt_read_accumulator(snk_pt_ctx* ctx, float* out, uint32_t memory, uint64_t* num_frames);

@@ -168,6 +168,11 @@ struct snk_pt_ctx {
     DBuf<float2> c_spread;
     DBuf<float4> c_qrec, c_qbeta, c_trec, c_tbeta, c_tL, c_samples;
     uint64_t last_cache_samples = 0;
+    // quality guard of the cache (snk_pt_cache_set_guard; check_every 0: off)
+    snk_cache_guard guard{};
+    uint64_t guard_frames = 0, guard_probes = 0, guard_fallback_frames = 0;
+    double guard_last = -1.0;
+    bool guard_fallback = false;
 };
 
 namespace {
@@ -800,11 +805,107 @@ int snk_pt_build(snk_pt_ctx* ctx) {
     return SNK_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Error measure of the radiance-cache guard: the relative MSE, over block x block
+// pixel means and the 3 channels, of the cached probe against the plain one:
+// mean((c - p)^2 / (p^2 + 0.01)).  Block means divide the probes' own noise by the
+// block area, so what remains is mostly the cache's bias.
+double guard_relmse(const float* cached, const float* plain, uint32_t w, uint32_t h, uint32_t block) {
+    const uint32_t b = std::max(1u, std::min(block, std::min(w, h)));
+    const uint32_t bw = w / b, bh = h / b;
+    double sum = 0.0;
+    for (uint32_t by = 0; by < bh; by++)
+        for (uint32_t bx = 0; bx < bw; bx++)
+            for (int c = 0; c < 3; c++) {
+                double mc = 0.0, mp = 0.0;
+                for (uint32_t y = by * b; y < (by + 1) * b; y++)
+                    for (uint32_t x = bx * b; x < (bx + 1) * b; x++) {
+                        mc += cached[4 * ((size_t)y * w + x) + c];
+                        mp += plain[4 * ((size_t)y * w + x) + c];
+                    }
+                mc /= (double)b * b;
+                mp /= (double)b * b;
+                sum += (mc - mp) * (mc - mp) / (mp * mp + 0.01);
+            }
+    return bw && bh ? sum / ((double)bw * bh * 3.0) : 0.0;
+}
+
+int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, const snk_render_settings* settings,
+                const snk_view_outputs* outputs);
+
+// The guard's probe of a cache frame: view 0 at 1/probe_scale resolution rendered
+// with probe_spp samples per pixel twice, in cache mode without a training step
+// (cache_lr < 0) and plainly (the unbiased estimator the cache stands in for),
+// both with the frame's depth, roulette and frame index and seed + 0x5EED.
+int guard_probe(snk_pt_ctx* ctx, const snk_view& view, const snk_render_settings& rs, double* relmse) {
+    const snk_cache_guard& g = ctx->guard;
+    snk_view pv = view;
+    pv.width = std::max(1u, view.width / std::max(1u, g.probe_scale));
+    pv.height = std::max(1u, view.height / std::max(1u, g.probe_scale));
+    const size_t np = (size_t)pv.width * pv.height;
+    std::vector<float> cached(4 * np), plain(4 * np);
+    snk_render_settings ps = rs;
+    ps.spp = std::max(1u, g.probe_spp);
+    ps.seed = rs.seed + 0x5EEDu;
+    ps.flags = 0;
+    ps.cache_lr = -1.0f;
+    snk_view_outputs o;
+    std::memset(&o, 0, sizeof(o));
+    o.memory = SNK_MEM_HOST;
+    o.radiance = cached.data();
+    int rc = render_impl(ctx, &pv, 1, &ps, &o);
+    if (rc) return rc;
+    ps.mode = SNK_MODE_PATH;
+    o.radiance = plain.data();
+    rc = render_impl(ctx, &pv, 1, &ps, &o);
+    if (rc) return rc;
+    *relmse = guard_relmse(cached.data(), plain.data(), pv.width, pv.height, g.block);
+    return SNK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// RT::RecordRenderCmdBuf (Raytracing.cpp:227-267), with the radiance cache's
+// quality guard around cache-mode frames (snk_pt_cache_set_guard): every
+// check_every-th guarded frame is preceded by a probe; while the last probe was
+// over budget, frames render with an infinite spread threshold (no path ends in
+// the cache, so the image is the plain tracer's bit for bit) and keep training
+// the network, which returns to service at the next passing probe.
 int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, const snk_render_settings* settings,
                   const snk_view_outputs* outputs) {
     if (!ctx) return SNK_ERR_INVALID_ARG;
     if (!views || !settings || !outputs || num_views == 0 || num_views > MAX_VIEWS)
         return fail(ctx, SNK_ERR_INVALID_ARG, "render: bad views/settings/outputs");
+    if (settings->mode != SNK_MODE_PATH_CACHE || ctx->guard.check_every == 0)
+        return render_impl(ctx, views, num_views, settings, outputs);
+    if (ctx->guard_frames > 0 && ctx->guard_frames % ctx->guard.check_every == 0) {
+        double e = 0.0;
+        const int rc = guard_probe(ctx, views[0], *settings, &e);
+        if (rc) return rc;
+        ctx->guard_last = e;
+        ctx->guard_probes++;
+        ctx->guard_fallback = e > (double)ctx->guard.relmse_budget;
+    }
+    ctx->guard_frames++;
+    snk_render_settings rs = *settings;
+    if (ctx->guard_fallback) {
+        rs.cache_spread = 1e30f;
+        ctx->guard_fallback_frames++;
+    }
+    return render_impl(ctx, views, num_views, &rs, outputs);
+}
+
+}  // extern "C"
+
+namespace {
+
+int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, const snk_render_settings* settings,
+                const snk_view_outputs* outputs) {
     const snk_render_settings& rs = *settings;
     if (rs.mode != SNK_MODE_PATH && rs.mode != SNK_MODE_RESTIR_DI && rs.mode != SNK_MODE_PATH_CACHE &&
         rs.mode != SNK_MODE_RESTIR_PT)
@@ -1200,6 +1301,44 @@ int snk_pt_render(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, co
         }
     }
     if (any_host) API_TRY(check_device_error(ctx));
+    return SNK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int snk_pt_cache_set_guard(snk_pt_ctx* ctx, const snk_cache_guard* g) {
+    if (!ctx) return SNK_ERR_INVALID_ARG;
+    if (!g || g->check_every == 0) {
+        std::memset(&ctx->guard, 0, sizeof(ctx->guard));
+    } else {
+        if (!(g->relmse_budget > 0.0f) || g->probe_spp > 4096 || g->probe_scale > 64 || g->block > 64)
+            return fail(ctx, SNK_ERR_INVALID_ARG, "cache_set_guard: budget must be > 0, probe_spp <= 4096, "
+                                                  "probe_scale <= 64, block <= 64");
+        ctx->guard = *g;
+    }
+    ctx->guard_frames = ctx->guard_probes = ctx->guard_fallback_frames = 0;
+    ctx->guard_last = -1.0;
+    ctx->guard_fallback = false;
+    return SNK_OK;
+}
+
+int snk_pt_cache_get_guard_state(const snk_pt_ctx* ctx, snk_cache_guard_state* s) {
+    if (!ctx || !s) return SNK_ERR_INVALID_ARG;
+    std::memset(s, 0, sizeof(*s));
+    s->frames = ctx->guard_frames;
+    s->probes = ctx->guard_probes;
+    s->fallback_frames = ctx->guard_fallback_frames;
+    s->last_probe_relmse = ctx->guard_last;
+    s->fallback = ctx->guard_fallback ? 1u : 0u;
+    return SNK_OK;
+}
+
+int snk_cache_guard_relmse(const float* cached, const float* plain, uint32_t width, uint32_t height, uint32_t block,
+                           double* relmse) {
+    if (!cached || !plain || !relmse || width == 0 || height == 0) return SNK_ERR_INVALID_ARG;
+    *relmse = guard_relmse(cached, plain, width, height, block);
     return SNK_OK;
 }
 

@@ -30,6 +30,7 @@ EXPORTS = [
     "snk_taa_create", "snk_taa_destroy", "snk_taa_reset", "snk_taa_resolve", "snk_taa_get_last_error",
     "snk_meshdata_load", "snk_meshdata_get_info", "snk_meshdata_submesh", "snk_meshdata_free",
     "snk_pt_contact_rays", "snk_pt_particle_probe", "snk_pt_particle_constrain",
+    "snk_pt_cache_set_guard", "snk_pt_cache_get_guard_state", "snk_cache_guard_relmse",
 ]
 
 
@@ -72,6 +73,17 @@ class Tuning(C.Structure):
         for k in cls.KNOBS:
             setattr(t, k, int(d.get(k, 0)))
         return t
+
+
+class CacheGuard(C.Structure):
+    """snk_cache_guard: the radiance cache's quality guard (check_every 0: off)."""
+    _fields_ = [("relmse_budget", C.c_float), ("check_every", C.c_uint32), ("probe_scale", C.c_uint32),
+                ("probe_spp", C.c_uint32), ("block", C.c_uint32), ("pad", C.c_uint32 * 3)]
+
+
+class CacheGuardState(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("probes", C.c_uint64), ("fallback_frames", C.c_uint64),
+                ("last_probe_relmse", C.c_double), ("fallback", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class ViewOutputs(C.Structure):
@@ -142,6 +154,9 @@ def lib():
         L.snk_pt_contact_rays.argtypes = [vp, vp, u32, C.c_float, vp, u32]
         L.snk_pt_particle_probe.argtypes = [vp, vp, u32, C.c_float, vp, vp, u32]
         L.snk_pt_particle_constrain.argtypes = [vp, vp, vp, u32, C.c_float, vp, u32]
+        L.snk_pt_cache_set_guard.argtypes = [vp, C.POINTER(CacheGuard)]
+        L.snk_pt_cache_get_guard_state.argtypes = [vp, C.POINTER(CacheGuardState)]
+        L.snk_cache_guard_relmse.argtypes = [vp, vp, u32, u32, u32, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -330,6 +345,20 @@ class PathTracer:
         self._check(lib().snk_pt_cache_train(self._h, s.ctypes.data, s.shape[0], lr,
                                              None if grad is None else grad.ctypes.data, C.byref(loss), abi.MEM_HOST))
         return loss.value, grad
+
+    def set_cache_guard(self, relmse_budget: float = 0.05, check_every: int = 10, probe_scale: int = 4,
+                        probe_spp: int = 16, block: int = 4):
+        """Quality guard of the cache (snk_pt_cache_set_guard); check_every=0 removes it."""
+        g = CacheGuard()
+        g.relmse_budget, g.check_every, g.probe_scale = relmse_budget, check_every, probe_scale
+        g.probe_spp, g.block = probe_spp, block
+        self._check(lib().snk_pt_cache_set_guard(self._h, C.byref(g)))
+
+    def cache_guard_state(self) -> dict:
+        s = CacheGuardState()
+        self._check(lib().snk_pt_cache_get_guard_state(self._h, C.byref(s)))
+        return {"frames": s.frames, "probes": s.probes, "fallback_frames": s.fallback_frames,
+                "last_probe_relmse": s.last_probe_relmse, "fallback": bool(s.fallback)}
 
     # ---- launch knobs ------------------------------------------------------------
     def set_tuning(self, tuning: "Tuning | dict"):

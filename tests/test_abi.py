@@ -18,7 +18,7 @@ HEADER = os.path.join(ROOT, "include", "snk_pt.h")
 
 def declared_functions():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^int\s+(snk_(?:pt|taa|meshdata)_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^int\s+(snk_(?:pt|taa|meshdata|cache)_\w+)\s*\(", src, re.M)))
 
 
 def test_header_declares_entry_points():

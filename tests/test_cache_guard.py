@@ -1,79 +1,69 @@
-"""Host logic of the MLP-cache quality guard (snkpt.cache_guard) with a stand-in
-tracer: when it probes, what it renders for a probe, when it falls back to plain
-path tracing and when it returns to the cache.  No GPU: the stand-in fills host
-buffers with an image whose cache-mode version carries a chosen bias."""
+"""CPU tests of the MLP-cache quality guard: the library's error measure
+(snk_cache_guard_relmse, host code) against its numpy statement, and the Python
+face of the guard (what it asks the library to set, how it reports the library's
+guard state) with a stand-in tracer.  The guard's probes and fallback run on the
+GPU (tests/test_gpu_cache.py)."""
 import numpy as np
+import pytest
 
+import snkpt
 from snkpt import abi, scenes
-from snkpt.cache_guard import RadianceCacheGuard, block_means, rel_mse
+from snkpt.cache_guard import RadianceCacheGuard, block_means, rel_mse, relmse_library
+
+
+@pytest.mark.parametrize("w,h,block", [(64, 32, 4), (37, 21, 4), (16, 9, 1), (8, 4, 16), (50, 30, 7)])
+def test_library_measure_matches_numpy_statement(built_lib, w, h, block):
+    rng = np.random.default_rng(w * 100 + h)
+    plain = rng.uniform(0.0, 2.0, (w * h, 4)).astype(np.float32)
+    cached = (plain * rng.uniform(0.7, 1.4, (w * h, 4))).astype(np.float32)
+    b = min(block, w, h)
+    want = rel_mse(block_means(cached, w, h, b), block_means(plain, w, h, b))
+    got = relmse_library(cached, plain, w, h, block)
+    assert abs(got - want) <= 1e-12 * max(1.0, want), (got, want)
+    assert relmse_library(plain, plain, w, h, block) == 0.0
+
+
+def test_library_measure_rejects_bad_arguments(built_lib):
+    with pytest.raises(snkpt.SnkError):
+        relmse_library(np.zeros((4, 4)), np.zeros((4, 4)), 0, 4, 1)
 
 
 class FakeTracer:
+    """Keeps the guard settings and a guard state the test scripts."""
+
     def __init__(self):
-        self.bias = 0.0
-        self.calls = []   # (width, height, mode, spp, cache_spread, cache_lr)
+        self.guard = None
+        self.state = {"frames": 0, "probes": 0, "fallback_frames": 0, "last_probe_relmse": -1.0, "fallback": False}
+        self.script = []     # per render: (probe relMSE or None, fallback after it)
+        self.rendered = []
+
+    def set_cache_guard(self, **kw):
+        self.guard = kw
+
+    def cache_guard_state(self):
+        return dict(self.state)
 
     def render(self, views, settings, outputs):
-        v, st, out = views[0], settings.reshape(-1)[0] if settings.ndim else settings, outputs[0]
-        w, h = int(v["width"]), int(v["height"])
-        self.calls.append((w, h, int(st["mode"]), int(st["spp"]), float(st["cache_spread"]), float(st["cache_lr"])))
-        y, x = np.mgrid[0:h, 0:w]
-        img = (0.2 + 0.5 * (x / max(w - 1, 1)) + 0.3 * (y / max(h - 1, 1))).reshape(-1)
-        cached = int(st["mode"]) == abi.MODE_PATH_CACHE and float(st["cache_spread"]) < 1e29
-        scale = 1.0 + (self.bias if cached else 0.0)
-        out["radiance"][:, :3] = (img * scale)[:, None]
-        out["radiance"][:, 3] = 1.0
-
-    def synchronize(self):
-        pass
+        self.rendered.append(int(np.asarray(settings).reshape(-1)[0]["mode"]))
+        probe, fallback = self.script.pop(0)
+        if probe is not None:
+            self.state["probes"] += 1
+            self.state["last_probe_relmse"] = probe
+            self.state["fallback"] = fallback
+        self.state["frames"] += 1
+        if self.state["fallback"]:
+            self.state["fallback_frames"] += 1
 
 
-def _setup(budget=0.05, every=2, scale=4, spp=8):
-    view = scenes.config1(width=64, height=32).views[0]
+def test_python_guard_sets_the_library_guard_and_reports_its_state():
     t = FakeTracer()
-    g = RadianceCacheGuard(t, relmse_budget=budget, check_every=every, probe_scale=scale, probe_spp=spp)
-    out = {"radiance": np.zeros((64 * 32, 4), np.float32)}
-    st = abi.settings(mode=abi.MODE_PATH_CACHE, spp=1, max_depth=4, seed=7, frame_index=0)
-    return view, t, g, out, st
-
-
-def test_probe_schedule_and_probe_renders():
-    view, t, g, out, st = _setup()
-    modes = []
-    for f in range(5):
-        st["frame_index"] = f
-        r = g.render(view, st, out)
-        modes.append((r["mode"], r["probe_relmse"] is not None))
-    # probes on frames 2 and 4 (not on the first frame), every frame in cache mode
-    assert modes == [("cache", False), ("cache", False), ("cache", True), ("cache", False), ("cache", True)]
-    probes = [c for c in t.calls if c[0] == 16]
-    assert len(probes) == 4                                            # two renders per probe
-    assert {c[3] for c in probes} == {8}                               # probe_spp
-    assert sorted(c[2] for c in probes) == [abi.MODE_PATH, abi.MODE_PATH, abi.MODE_PATH_CACHE, abi.MODE_PATH_CACHE]
-    assert all(c[5] < 0 for c in probes if c[2] == abi.MODE_PATH_CACHE)   # no training step in a probe
-    frames = [c for c in t.calls if c[0] == 64]
-    assert len(frames) == 5 and all(c[2] == abi.MODE_PATH_CACHE and c[4] < 1e29 for c in frames)
-
-
-def test_fallback_and_recovery():
-    view, t, g, out, st = _setup(budget=0.05, every=1)
-    g.render(view, st, out)
-    t.bias = 0.5                                      # relMSE of a 50 % bias is ~0.2 > budget
-    r = g.render(view, st, out)
-    assert r["mode"] == "plain" and r["probe_relmse"] > 0.05
-    assert t.calls[-1][2] == abi.MODE_PATH_CACHE and t.calls[-1][4] >= 1e29   # plain image, training goes on
-    np.testing.assert_array_equal(out["radiance"][:, 0], out["radiance"][:, 1])
-    t.bias = 0.01                                     # the cache has recovered
-    r = g.render(view, st, out)
-    assert r["mode"] == "cache" and r["probe_relmse"] < 0.05
-    assert [h[2] for h in g.history] == [True, False]
-
-
-def test_rel_mse_of_block_means():
-    w, h = 8, 4
-    ref = np.ones((w * h, 4))
-    x = ref.copy()
-    x[:, :3] *= 1.1
-    assert abs(rel_mse(x, ref) - 0.01 / 1.01) < 1e-12
-    b = block_means(np.arange(w * h * 4, dtype=np.float64).reshape(-1, 4), w, h, 2)
-    assert b.shape == ((w // 2) * (h // 2), 3)
+    g = RadianceCacheGuard(t, relmse_budget=0.02, check_every=3, probe_scale=2, probe_spp=8, block=5)
+    assert t.guard == dict(relmse_budget=0.02, check_every=3, probe_scale=2, probe_spp=8, block=5)
+    view = scenes.config1(width=16, height=8).views[0]
+    st = abi.settings(mode=abi.MODE_PATH, spp=1)
+    t.script = [(None, False), (0.5, True), (None, True), (0.01, False)]
+    res = [g.render(view, st, {}) for _ in range(4)]
+    assert [r["mode"] for r in res] == ["cache", "plain", "plain", "cache"]
+    assert [r["probe_relmse"] for r in res] == [None, 0.5, None, 0.01]
+    assert g.history == [(1, 0.5, True), (3, 0.01, False)]
+    assert t.rendered == [abi.MODE_PATH_CACHE] * 4   # every guarded frame is a cache frame
