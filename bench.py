@@ -181,8 +181,8 @@ def cache_vs_plain(pt_mod, abi, scenes, device, frames=120, check=(60,), ref_spp
     converged render, MLP cache vs plain, on the config-4 scene at 1080p.
 
     The cache trains online along the 120-frame seeded spline (one cache frame per
-    spline frame).  At each checked frame: reference = FP64 mean of ref_spp plain
-    1-spp frames (depth 8); relMSE(x) = mean (x - ref)^2 / (ref^2 + 0.01); the
+    spline frame).  At each checked frame: reference = FP64 accumulation of ref_spp
+    plain samples per pixel (depth 8, frames of 16 spp); relMSE(x) = mean (x - ref)^2 / (ref^2 + 0.01); the
     plain tracer's relMSE is measured for the mean of k 1-spp frames, k = 1..64,
     and the k matching the cache's 1-spp relMSE is interpolated in log-log.
     Frame times: CUDA events around each render call on the library's stream."""
@@ -217,9 +217,9 @@ def cache_vs_plain(pt_mod, abi, scenes, device, frames=120, check=(60,), ref_spp
         if f not in check:
             continue
         x_cache = out["radiance"].cpu().numpy().astype(np.float64)
-        for k in range(ref_spp):   # converged reference of this frame
+        for k in range(ref_spp // 16):   # converged reference of this frame: 16 spp per call
             flags = abi.RENDER_ACCUMULATE_F64 | (abi.RENDER_RESET_ACCUM if k == 0 else 0)
-            pt.render([v], abi.settings(spp=1, max_depth=8, seed=500_000 + k, flags=flags), [{}])
+            pt.render([v], abi.settings(spp=16, max_depth=8, seed=500_000 + k, flags=flags), [{}])
         ref, _ = pt.read_accumulator(W, H)
         ref = ref.astype(np.float64)
         acc = np.zeros((W * H, 4))
@@ -250,7 +250,8 @@ def cache_vs_plain(pt_mod, abi, scenes, device, frames=120, check=(60,), ref_spp
             "value": ratio, "higher_is_better": False, "cache_ms_per_frame": t_cache,
             "workload": "config 4: 64 value-noise terrain tiles + 200 icospheres, 1920x1080, 1 spp, depth 6, "
                         "cache MLP 64-4x64-3 BF16, 65536 samples/frame, Adam 1e-2, spread threshold 0.01",
-            "reference": f"FP64 mean of {ref_spp} plain 1-spp frames (depth 8)", "checked_frames": list(check),
+            "reference": f"FP64 accumulation of {ref_spp} plain samples per pixel (depth 8; {ref_spp // 16} frames "
+                         f"of 16 spp)", "checked_frames": list(check),
             "frames": frames, "checks": results}
 
 
@@ -705,7 +706,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 8-view batched (config 3) measurement")
-    ap.add_argument("--cache-eval", default="quick", choices=["off", "quick", "full"],
+    ap.add_argument("--cache-eval", default="full", choices=["off", "quick", "full"],
                     help="MLP cache vs plain at equal relMSE: quick = one checked frame, full = every 10th frame")
     args = ap.parse_args()
     if args.warmup < 3:
