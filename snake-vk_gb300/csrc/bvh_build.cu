@@ -8,8 +8,9 @@
 // Pipeline (all on the device, one stream):
 //   1. centroid bounds (block reduction + order-preserving atomics)
 //   2. 63-bit Morton codes of the centroids (21 bits per axis)
-//   3. radix sort of (code, primitive) pairs (project LSD radix sort below: one
-//      CTA for the per-frame instance sets, three kernels per digit beyond)
+//   3. sort of (code, primitive) pairs (project kernels below: a bitonic network
+//      in one CTA's shared memory up to 8192 pairs, an LSD radix sort in one CTA
+//      up to 65,536, three kernels per radix digit beyond)
 //   4. binary radix tree (Karras, HPG 2012): one thread per internal node
 //   5. bottom-up boxes and leaf counts (atomic arrival flags)
 //   5b. treelet restructuring (Karras & Aila, HPG 2013): bottom-up over the binary
@@ -157,7 +158,7 @@ __device__ void karras_node(int i, const unsigned long long* __restrict__ keys, 
 // __match_any_sync (their order within the warp is their lane order), every warp
 // counts its digits in shared memory, and an exclusive scan of those counts over
 // the warps gives each warp its start within the digit.  Up to SORT_SMALL_MAX
-// elements (every per-frame instance BVH in practice) one CTA runs all passes in
+// elements (sets above the bitonic sort's 8192) one CTA runs all passes in
 // one launch and skips the passes whose digit is the same for every key; larger
 // sets (mesh BVHs, at load time) take three launches per pass (per-tile digit
 // counts, their exclusive scan in digit-major order, the stable scatter).  The
@@ -263,6 +264,47 @@ __global__ void __launch_bounds__(SORT_THREADS, 1) k_sort_small(unsigned long lo
     }
     if (sk != keys) {   // an odd number of passes ran: the result goes back to the first pair
         for (uint32_t i = t; i < n; i += SORT_THREADS) { keys[i] = sk[i]; vals[i] = sv[i]; }
+    }
+}
+
+// Up to SORT_BITONIC_MAX pairs (the per-frame instance sets) one CTA sorts in shared
+// memory with a bitonic network: 91 barrier-separated compare-exchange stages for
+// 8192 entries instead of 8 radix passes over global memory.  The network is not
+// stable by itself, so it orders by (key, value): the values are the primitives'
+// indices 0..n-1 in their input order, which makes the result the stable order.
+// Entries past n are padded with the largest pair.
+constexpr uint32_t SORT_BITONIC_MAX = 8192;
+
+__global__ void __launch_bounds__(SORT_THREADS, 1) k_sort_bitonic(unsigned long long* keys, uint32_t* vals,
+                                                                uint32_t n) {
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    uint32_t N = 2;
+    while (N < n) N <<= 1;
+    unsigned long long* sk = reinterpret_cast<unsigned long long*>(sort_smem);
+    uint32_t* sv = reinterpret_cast<uint32_t*>(sk + N);
+    for (uint32_t i = threadIdx.x; i < N; i += SORT_THREADS) {
+        sk[i] = i < n ? keys[i] : ~0ull;
+        sv[i] = i < n ? vals[i] : ~0u;
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < N / 2; i += SORT_THREADS) {
+                const uint32_t lo = ((i & ~(j - 1u)) << 1) | (i & (j - 1u)), hi = lo + j;
+                const unsigned long long ka = sk[lo], kb = sk[hi];
+                const uint32_t va = sv[lo], vb = sv[hi];
+                const bool a_greater = ka > kb || (ka == kb && va > vb);
+                if (a_greater == ((lo & k) == 0u)) {   // ascending blocks put the smaller first
+                    sk[lo] = kb; sk[hi] = ka;
+                    sv[lo] = vb; sv[hi] = va;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += SORT_THREADS) {
+        keys[i] = sk[i];
+        vals[i] = sv[i];
     }
 }
 
@@ -1489,6 +1531,15 @@ inline unsigned grid_for(uint32_t n) { return (n + BLK - 1) / BLK; }
 namespace {
 // sorts (sc.keys, sc.vals) by key, stably (sc.keys_alt / sc.vals_alt: scratch)
 Status sort_pairs(BuildScratch& sc, uint32_t n, cudaStream_t st) {
+    if (n <= SORT_BITONIC_MAX) {
+        uint32_t N = 2;
+        while (N < n) N <<= 1;
+        const int bytes = (int)(N * (sizeof(unsigned long long) + sizeof(uint32_t)));
+        SNK_TRY_CUDA(cudaFuncSetAttribute(k_sort_bitonic, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        k_sort_bitonic<<<1, SORT_THREADS, bytes, st>>>(sc.keys.p, sc.vals.p, n);
+        SNK_TRY_CUDA(cudaGetLastError());
+        return Status::Ok();
+    }
     if (n <= SORT_SMALL_MAX) {
         k_sort_small<<<1, SORT_THREADS, 0, st>>>(sc.keys.p, sc.vals.p, sc.keys_alt.p, sc.vals_alt.p, n);
         SNK_TRY_CUDA(cudaGetLastError());

@@ -339,6 +339,27 @@ def test_restir_pt_two_views_per_call(cuda, built_lib):
         _compare(gb, ob, f"view 1 frame {f}")
 
 
+@pytest.mark.parametrize("mode", [abi.MODE_RESTIR_DI, abi.MODE_RESTIR_PT])
+def test_restir_full_size_config2(cuda, built_lib, mode):
+    """Config 2 at its own size, 1920x1080 with 4096 emissive quads: two frames of
+    the moving camera (the second reuses the first's reservoirs), every pixel
+    against a full-frame oracle run (the reservoir passes read neighbours, so the
+    oracle renders whole frames); G-buffer identical, radiance within 1e-4."""
+    W, H, F = 1920, 1080, 2
+    sc = scenes.config2(width=W, height=H, frames=F)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    ors = O.OracleRestir(O.OracleScene(sc), W, H)
+    for f in range(F):
+        st = abi.settings(mode=mode, spp=1, max_depth=4, rr_depth=3, frame_index=f, seed=1)
+        g = _gpu_frame(pt, [sc.views[f]], st, cuda)[0]
+        ctr = np.zeros(5, np.uint64)
+        r, _ = ors.frame(sc.views[f], st, counters=ctr)
+        _compare(g, r, f"1080p mode {mode} frame {f}")
+        s = pt.stats()
+        assert s["rays_shadow"] + s["shadow_tests_reused"] == int(ctr[2])
+
+
 def test_launch_knobs_do_not_change_results(cuda, built_lib):
     """Every autotuner candidate must render the same bits (the knobs only move work)."""
     sc = scenes.config1(width=320, height=180)
