@@ -165,6 +165,12 @@ struct QuantisedWeight {
     }
 };
 
+// the quantised weight of every light, once, over the whole grid (the double
+// division is slow on this GPU, so the scan reads these instead of recomputing them)
+__global__ void k_quantise(QuantisedWeight qw, uint32_t n, unsigned long long* q) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) q[k] = qw(k);
+}
+
 // Inclusive prefix sums of the quantised weights.  The sums are exact integers,
 // so any order of summation gives the same bits: k_scan_tiles sums each tile of
 // `tile` weights, k_scan_apply scans each tile (a contiguous run per thread, then
@@ -191,18 +197,19 @@ __device__ __forceinline__ unsigned long long block_scan_incl(unsigned long long
     return off + incl;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(QuantisedWeight q, uint32_t n, uint32_t tile,
-                                                             unsigned long long* tile_sums) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const unsigned long long* __restrict__ q, uint32_t n,
+                                                             uint32_t tile, unsigned long long* tile_sums) {
     __shared__ unsigned long long warp_tot[SCAN_THREADS / 32];
     const uint32_t b0 = blockIdx.x * tile, b1 = min(b0 + tile, n);
     unsigned long long s = 0ull;
-    for (uint32_t k = b0 + threadIdx.x; k < b1; k += SCAN_THREADS) s += q(k);
+    for (uint32_t k = b0 + threadIdx.x; k < b1; k += SCAN_THREADS) s += q[k];
     unsigned long long total;
     block_scan_incl(s, warp_tot, &total);
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(QuantisedWeight q, uint32_t n, uint32_t tile,
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const unsigned long long* __restrict__ q, uint32_t n,
+                                                             uint32_t tile,
                                                              const unsigned long long* __restrict__ tile_sums,
                                                              unsigned long long* acc) {
     __shared__ unsigned long long warp_tot[SCAN_THREADS / 32];
@@ -216,12 +223,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(QuantisedWeight q, 
     const uint32_t per = (tile + SCAN_THREADS - 1) / SCAN_THREADS;
     const uint32_t r0 = min(b0 + threadIdx.x * per, b1), r1 = min(r0 + per, b1);
     unsigned long long s = 0ull;
-    for (uint32_t k = r0; k < r1; k++) s += q(k);
+    for (uint32_t k = r0; k < r1; k++) s += q[k];
     unsigned long long total;
     const unsigned long long incl = block_scan_incl(s, warp_tot, &total);   // (its barrier orders `before`)
     unsigned long long run = before + incl - s;
     for (uint32_t k = r0; k < r1; k++) {
-        run += q(k);
+        run += q[k];
         acc[k] = run;
     }
 }
@@ -274,18 +281,21 @@ Status launch_emissive_lights(const snk_instance* raw, const uint32_t* em_list, 
 
 Status launch_light_cdf(const double* w, uint32_t n, LightCdfScratch& sc, float* cdf, float* pmf, cudaStream_t st) {
     if (n == 0) return Status::Ok();
-    // tiles of at least 16 weights per thread, at most 1024 tiles
-    const uint32_t per_tile = std::max<uint32_t>(16u * SCAN_THREADS, (uint32_t)((n + 1023ull) / 1024ull));
-    const uint32_t tile = (per_tile + SCAN_THREADS - 1) / SCAN_THREADS * SCAN_THREADS;
+    // tiles of one weight per thread, or more when that would make over 1024 tiles
+    const uint32_t per_thread = std::max<uint32_t>(1u, (uint32_t)((n + 1024ull * SCAN_THREADS - 1) /
+                                                                  (1024ull * SCAN_THREADS)));
+    const uint32_t tile = per_thread * SCAN_THREADS;
     const uint32_t tiles = (n + tile - 1) / tile;
     SNK_TRY_CUDA(sc.acc.reserve(n));
+    SNK_TRY_CUDA(sc.q.reserve(n));
     SNK_TRY_CUDA(sc.wmax.reserve(1));
     SNK_TRY_CUDA(sc.tile_sums.reserve(tiles));
-    const QuantisedWeight q{w, sc.wmax.p};
+    const QuantisedWeight qw{w, sc.wmax.p};
     SNK_TRY_CUDA(cudaMemsetAsync(sc.wmax.p, 0, sizeof(unsigned long long), st));
     k_weight_max<<<std::min<uint32_t>(blocks_for(n, 256), 1024), 256, 0, st>>>(w, n, sc.wmax.p);
-    k_scan_tiles<<<tiles, SCAN_THREADS, 0, st>>>(q, n, tile, sc.tile_sums.p);
-    k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(q, n, tile, sc.tile_sums.p, sc.acc.p);
+    k_quantise<<<std::min<uint32_t>(blocks_for(n, 256), 4096), 256, 0, st>>>(qw, n, sc.q.p);
+    k_scan_tiles<<<tiles, SCAN_THREADS, 0, st>>>(sc.q.p, n, tile, sc.tile_sums.p);
+    k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(sc.q.p, n, tile, sc.tile_sums.p, sc.acc.p);
     SNK_TRY_CUDA(cudaGetLastError());
     k_light_cdf<<<blocks_for(n, 256), 256, 0, st>>>(sc.acc.p, n, cdf, pmf);
     SNK_TRY_CUDA(cudaGetLastError());

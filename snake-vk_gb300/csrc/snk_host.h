@@ -141,7 +141,7 @@ Status launch_instance_boxes(const uint32_t* inst_list, uint32_t n, const InstSh
                              float4* lo, float4* hi, cudaStream_t s);
 // ---- per-frame scene tables (scene_tables.cu) ---------------------------------
 struct LightCdfScratch {
-    DBuf<unsigned long long> acc, wmax, tile_sums;
+    DBuf<unsigned long long> acc, wmax, tile_sums, q;   // prefix sums, max weight, tile sums, quantised weights
 };
 // traversal and shading records of n instances from their raw records
 Status launch_instance_records(const snk_instance* raw, uint32_t n, const MeshInfo* meshes, InstTrace* it,
