@@ -74,6 +74,8 @@ struct snk_pt_ctx {
     uint32_t tlas_root = INVALID;
     uint64_t blas_nodes = 0, tlas_nodes = 0, total_tris = 0, tlas_prim_count = 0;
     double blas_sah = 0.0;
+    bool blas_leaf_single = true;      // the mesh BVHs were built with one primitive per leaf
+    bool tlas_leaf_single = true;      // the instance BVH was built with one instance per leaf
     DBuf<InstTrace> d_inst_trace;
     DBuf<InstShade> d_inst_shade;
     DBuf<MaterialDev> d_mats;
@@ -272,7 +274,8 @@ Status build_meshes(snk_pt_ctx* ctx) {
         SNK_TRY(build_wide_bvh(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, mi.num_triangles, ctx->d_blas.p,
                                node_base, prim_base, ctx->d_prim_order.p, st, &br,
                                treelet_passes(ctx->tune.bvh_treelet_passes, 3), leaf_size(ctx->tune.bvh_leaf_max, 1),
-                               std::max(leaf_size(ctx->tune.bvh_leaf_pack, 1), leaf_size(ctx->tune.bvh_leaf_max, 1))));
+                               std::max(leaf_size(ctx->tune.bvh_leaf_pack, 1), leaf_size(ctx->tune.bvh_leaf_max, 1)),
+                               ctx->tune.bvh_collapse == 0));
         SNK_TRY(launch_fill_triangles(ctx->d_prim_order.p, mi.num_triangles, ctx->d_pos.p, ctx->d_idx.p,
                                       mi.vertex_offset, mi.index_offset, ctx->d_tris.p + prim_base, st));
         mi.blas_root = node_base;
@@ -284,6 +287,7 @@ Status build_meshes(snk_pt_ctx* ctx) {
     }
     ctx->blas_nodes = node_base;
     ctx->total_tris = prim_base;
+    ctx->blas_leaf_single = leaf_size(ctx->tune.bvh_leaf_max, 1) == 1 && leaf_size(ctx->tune.bvh_leaf_pack, 1) <= 1;
     ctx->blas_sah = sah_w > 0 ? sah_sum / sah_w : 0.0;
     SNK_TRY(upload(ctx->d_meshes, ctx->h_meshes.data(), ctx->h_meshes.size(), st));
     SNK_TRY_CUDA(cudaStreamSynchronize(st));
@@ -453,6 +457,7 @@ Status build_instances(snk_pt_ctx* ctx) {
         ctx->tlas_meshes = meshes_now;
         ctx->tlas_updates_since_build = 0;
         ctx->tlas_refittable = true;
+        ctx->tlas_leaf_single = leaf_size(ctx->tune.tlas_leaf_max, 1) == 1;
         if (n <= (uint32_t)SMALL_BUILD_MAX) {
             // one launch, no host round trip; the node count stays on the device
             // (traversal bounds its node indices by the capacity, n + 1)
@@ -543,6 +548,7 @@ SceneDev scene_dev(snk_pt_ctx* ctx) {
     S.light_cdf = ctx->d_cdf.p;
     S.light_pmf = ctx->d_pmf.p;
     S.num_local_lights = ctx->n_local;
+    S.single_leaf = ctx->blas_leaf_single && ctx->tlas_leaf_single ? 1u : 0u;
     std::memcpy(&S.dir_light, &ctx->dir_light, sizeof(S.dir_light));
     S.error_word = ctx->d_err.p;
     S.num_blas_nodes = (uint32_t)ctx->blas_nodes;
@@ -1351,7 +1357,7 @@ int snk_pt_set_tuning(snk_pt_ctx* ctx, const snk_tuning* t) {
         t->bvh_leaf_max > LEAF_MAX_LIMIT || t->tlas_leaf_max > LEAF_MAX_LIMIT || t->bvh_leaf_pack > LEAF_MAX_LIMIT ||
         t->max_traversal_steps > MAX_TRAVERSAL_STEPS || t->stack_limit > (uint32_t)STACK_MAX ||
         t->shadow_blocks_per_sm > 64 || t->shadow_ray_chunk > 4096 || t->shadow_refill_idle > 32 ||
-        t->shadow_prim_bias > 64 || t->shadow_variant > 3 || t->reserved != 0)
+        t->shadow_prim_bias > 64 || t->shadow_variant > 3 || t->bvh_collapse > 1)
         return fail(ctx, SNK_ERR_INVALID_ARG, "set_tuning: knob out of range");
     ctx->tune = *t;
     return SNK_OK;

@@ -666,6 +666,84 @@ __device__ __forceinline__ void quant_child(const QuantFrame& F, float4 a4, floa
     }
 }
 
+// ---- SAH-optimal 8-wide collapse ------------------------------------------------
+// Dynamic programming over the binary tree (Ylitie, Karras, Laine, HPG 2017): for
+// every internal node x and every i in 1..8, D(x, i) is the least SAH cost of the
+// subtree of x represented by at most i children of a wide node.  A child is x
+// itself (a wide node of cost WIDE_CN A(x) plus the best distribution of x's
+// subtree over 8 children, or a leaf of WIDE_CT A(x) per primitive when x holds at
+// most leaf_pack primitives), or the children of a split of the i slots between
+// x's two binary children.  wide_split[x] packs the argmins in 4-bit fields: field
+// 0 the split of a wide node rooted at x (8 slots), field i - 1 (i = 2..8) the
+// choice for D(x, i): 0 keeps x as one child, k > 0 gives k slots to the left child
+// and i - k to the right one.
+constexpr float WIDE_CN = 1.0f;   // one 8-wide node test
+constexpr float WIDE_CT = 1.0f;   // one primitive test (0.3 and 0.6 gave the same trees on the test scenes)
+
+__device__ __forceinline__ void wide_costs(int c, int nl, const float4* node_lo, const float4* node_hi,
+                                           const float* wide_cost, float d[8]) {
+    if (c >= nl) {
+        const float v = WIDE_CT * half_area(node_lo[c], node_hi[c]);
+#pragma unroll
+        for (int i = 0; i < 8; i++) d[i] = v;
+    } else {
+        const float4* src = reinterpret_cast<const float4*>(wide_cost + 8 * (size_t)c);
+        const float4 a = __ldcg(src), b = __ldcg(src + 1);
+        d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w; d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
+    }
+}
+
+// bottom-up from leaf j (the second thread to arrive at a node completes it)
+__global__ void k_collapse_cost(int n, const int2* __restrict__ children, const int* __restrict__ parent, int* flags,
+                                const float4* __restrict__ node_lo, const float4* __restrict__ node_hi,
+                                const uint32_t* __restrict__ leaf_count, float* wide_cost, uint32_t* wide_split,
+                                uint32_t leaf_max, uint32_t leaf_pack) {
+    const int j = blockIdx.x * BLK + threadIdx.x;
+    if (j >= n || n == 1) return;
+    const int nl = n - 1;
+    int p = parent[nl + j];
+    while (p >= 0) {
+        __threadfence();
+        if (atomicAdd(&flags[p], 1) == 0) return;
+        __threadfence();
+        const int2 ch = children[p];
+        float a[8], b[8];
+        wide_costs(ch.x, nl, node_lo, node_hi, wide_cost, a);
+        wide_costs(ch.y, nl, node_lo, node_hi, wide_cost, b);
+        float e[9];
+        uint32_t ek[9];
+#pragma unroll
+        for (int i = 2; i <= 8; i++) {
+            float best = a[0] + b[i - 2];
+            uint32_t bk = 1;
+#pragma unroll
+            for (int k = 2; k < i; k++) {
+                const float c = a[k - 1] + b[i - k - 1];
+                if (c < best) { best = c; bk = (uint32_t)k; }
+            }
+            e[i] = best;
+            ek[i] = bk;
+        }
+        const float area = half_area(node_lo[p], node_hi[p]);
+        const uint32_t cnt = leaf_count[p];
+        const float d1 = cnt <= leaf_pack ? WIDE_CT * area * (float)cnt : WIDE_CN * area + e[8];
+        float d[8];
+        uint32_t split = ek[8];
+        d[0] = d1;
+#pragma unroll
+        for (int i = 2; i <= 8; i++) {
+            const bool open = cnt > leaf_max && e[i] < d1;   // subtrees of at most leaf_max primitives stay leaves
+            d[i - 1] = open ? e[i] : d1;
+            split |= (open ? ek[i] : 0u) << (4 * (i - 1));
+        }
+        float4* dst = reinterpret_cast<float4*>(wide_cost + 8 * (size_t)p);
+        dst[0] = make_float4(d[0], d[1], d[2], d[3]);
+        dst[1] = make_float4(d[4], d[5], d[6], d[7]);
+        wide_split[p] = split;
+        p = parent[p];
+    }
+}
+
 // One output node: task = (binary node, wide node slot).  counters: [1] tasks
 // out, [2] wide nodes, [3] primitive slots, [4] capacity error bits.
 __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, int n,
@@ -673,15 +751,36 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
                               const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
                               const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
                               uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area,
-                              uint32_t leaf_max, uint32_t leaf_pack) {
+                              uint32_t leaf_max, uint32_t leaf_pack, const uint32_t* __restrict__ wide_split) {
     int b = (int)task.x;
     uint32_t w = task.y;
     const int nl = n - 1;  // first leaf id
     int C[8];
     int nc;
     if (b >= nl) { C[0] = b; nc = 1; }
+    else if (wide_split) {
+        // the children chosen by the SAH-optimal distribution of b's subtree over 8 slots
+        int sn[8], ss[8], sp = 0;
+        const int2 ch = children[b];
+        const int k8 = (int)(wide_split[b] & 15u);
+        sn[sp] = ch.y; ss[sp++] = 8 - k8;
+        sn[sp] = ch.x; ss[sp++] = k8;
+        nc = 0;
+        while (sp > 0 && nc < 8) {
+            const int y = sn[--sp], slots = ss[sp];
+            const int k = (y >= nl || slots <= 1) ? 0 : (int)((wide_split[y] >> (4 * (slots - 1))) & 15u);
+            if (k == 0 || k >= slots || sp > 6) {
+                C[nc++] = y;
+            } else {
+                const int2 cy = children[y];
+                sn[sp] = cy.y; ss[sp++] = slots - k;
+                sn[sp] = cy.x; ss[sp++] = k;
+            }
+        }
+        if (sp > 0) atomicOr(&counters[4], 8u);   // more than 8 children (never with a consistent table)
+    }
     else { int2 ch = children[b]; C[0] = ch.x; C[1] = ch.y; nc = 2; }
-    while (nc < 8) {
+    while (!wide_split && nc < 8) {
         int best = -1;
         float best_a = -1.0f;
         for (int k = 0; k < nc; k++) {
@@ -807,11 +906,11 @@ __global__ void k_collapse(const uint2* __restrict__ tasks_in, uint32_t* counter
                            const float4* __restrict__ node_hi, const uint32_t* __restrict__ leaf_count,
                            const uint32_t* __restrict__ sorted, WideNode* nodes, uint32_t node_base,
                            uint32_t prim_base, uint32_t* prim_order, double* sah, float root_half_area,
-                           uint32_t leaf_max, uint32_t leaf_pack) {
+                           uint32_t leaf_max, uint32_t leaf_pack, const uint32_t* __restrict__ wide_split) {
     uint32_t ti = blockIdx.x * BLK + threadIdx.x;
     if (ti >= counters[0]) return;
     collapse_task(tasks_in[ti], counters, tasks_out, n, children, node_lo, node_hi, leaf_count, sorted, nodes,
-                  node_base, prim_base, prim_order, sah, root_half_area, leaf_max, leaf_pack);
+                  node_base, prim_base, prim_order, sah, root_half_area, leaf_max, leaf_pack, wide_split);
 }
 
 // ---- single-CTA agglomerative builder for small primitive sets -----------------
@@ -1620,9 +1719,22 @@ Status build_binary_tree(BuildScratch& sc, const float4* prim_lo, const float4* 
 
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t st,
-                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack) {
+                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack,
+                      bool sah_collapse) {
     const uint32_t* sorted = nullptr;
     SNK_TRY(build_binary_tree(sc, prim_lo, prim_hi, n, st, treelet_passes, leaf_max, leaf_pack, &sorted));
+    // SAH-optimal choice of each wide node's children (bottom-up over the final binary tree)
+    const uint32_t* wide_split = nullptr;
+    if (n > 1 && sah_collapse) {
+        SNK_TRY_CUDA(sc.wide_cost.reserve(8 * (size_t)(n - 1)));
+        SNK_TRY_CUDA(sc.wide_split.reserve(n - 1));
+        SNK_TRY_CUDA(cudaMemsetAsync(sc.flags.p, 0, sizeof(int) * n, st));
+        k_collapse_cost<<<grid_for(n), BLK, 0, st>>>((int)n, sc.children.p, sc.parent.p, sc.flags.p, sc.node_lo.p,
+                                                     sc.node_hi.p, sc.leaf_count.p, sc.wide_cost.p, sc.wide_split.p,
+                                                     leaf_max, leaf_pack);
+        SNK_TRY_CUDA(cudaGetLastError());
+        wide_split = sc.wide_split.p;
+    }
     float4 rlo, rhi;
     SNK_TRY_CUDA(cudaMemcpyAsync(&rlo, sc.node_lo.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
     SNK_TRY_CUDA(cudaMemcpyAsync(&rhi, sc.node_hi.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
@@ -1642,7 +1754,8 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
         if (level > 4096) return Status::Err(5, "build_wide_bvh: collapse did not terminate");
         k_collapse<<<grid_for(ntasks), BLK, 0, st>>>(tin, sc.counters.p, tout, (int)n, sc.children.p, sc.node_lo.p,
                                                      sc.node_hi.p, sc.leaf_count.p, sorted, nodes, node_base,
-                                                     prim_base, prim_order, sc.sah.p, rha, leaf_max, leaf_pack);
+                                                     prim_base, prim_order, sc.sah.p, rha, leaf_max, leaf_pack,
+                                                     wide_split);
         SNK_TRY_CUDA(cudaGetLastError());
         uint32_t ctr[5];
         SNK_TRY_CUDA(cudaMemcpyAsync(ctr, sc.counters.p, sizeof(ctr), cudaMemcpyDeviceToHost, st));

@@ -317,7 +317,7 @@ struct SceneDev {
     const float* light_cdf;
     const float* light_pmf;
     uint32_t num_local_lights;
-    uint32_t pad;
+    uint32_t single_leaf;       // non-zero when every leaf of both levels holds one primitive
     DirLightDev dir_light;
     unsigned int* error_word;   // device status: 0 ok, else SNK_ERR_LIMIT info
     uint32_t num_blas_nodes, num_tris, num_tlas_nodes, num_tlas_prims;   // bounds checked by traversal

@@ -78,6 +78,8 @@ struct BuildScratch {
     DBuf<uint32_t> sort_hist;     // per-tile digit counts of the multi-CTA radix sort
     DBuf<double> sah;             // SAH accumulator
     DBuf<uint32_t> level_tasks;   // task count per wide level (device-driven collapse)
+    DBuf<float> wide_cost;        // 8 per binary internal node: SAH cost of its subtree in 1..8 wide children
+    DBuf<uint32_t> wide_split;    // per binary internal node: the split of those children (4-bit fields)
     size_t cap = 0;
 };
 
@@ -93,7 +95,8 @@ struct BuildResult {
 // the primitive id stored in slot prim_base + k.
 Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                       uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, cudaStream_t stream,
-                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack);
+                      BuildResult* out, int treelet_passes, uint32_t leaf_max, uint32_t leaf_pack,
+                      bool sah_collapse = true);
 
 struct SmallBuildOut;
 // The same tree without host round trips (for per-frame rebuilds): the collapse

@@ -90,13 +90,13 @@ __device__ __forceinline__ float byte_m(uint32_t w, uint32_t k) {
 // with internal hit bit of slot s at position s ^ oct (ORDERED) or s; tgroup <- (prim_base,
 // primitive hits).
 // Near/far planes are swapped once per node by the ray octant; each plane costs a
-// byte permute and one FMA, and an integer compare with BOX_SLACK_ULPS of slack
+// byte permute and half a packed FMA, and an integer compare with BOX_SLACK_ULPS of slack
 // (on top of the per-axis widening below) keeps the test conservative.  The 8 box tests only
 // set one bit each; the internal-child bits are then moved into visiting order
 // with three conditional swaps (bit s -> s ^ oct) when the order matters (closest
 // hit; an any-hit ray stops at whichever occluder it meets first and skips the
 // swaps), and only the hit leaf slots are expanded into primitive bits.
-template <bool ORDERED>
+template <bool ORDERED, bool SINGLE>
 __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ nodes, uint32_t idx, const NodeRay& r,
                                                float tmin, float tmax, uint2& ngroup, uint2& tgroup) {
     const float4* np = reinterpret_cast<const float4*>(nodes + idx);
@@ -125,14 +125,24 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
     uint32_t nz[2] = {sz ? hz0 : lz0, sz ? hz1 : lz1}, fz[2] = {sz ? lz0 : hz0, sz ? lz1 : hz1};
     const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
     uint32_t hits = 0;   // bit s: the box of slot s is hit
+    // children s and s + 1 in one packed FMA per plane (sm_100 and later: two
+    // binary32 FMAs per instruction, each rounded as fmaf)
+    const float2 AX = make_float2(ax, ax), AY = make_float2(ay, ay), AZ = make_float2(az, az);
+    const float2 BNX = make_float2(bnx, bnx), BNY = make_float2(bny, bny), BNZ = make_float2(bnz, bnz);
+    const float2 BFX = make_float2(bfx, bfx), BFY = make_float2(bfy, bfy), BFZ = make_float2(bfz, bfz);
 #pragma unroll
-    for (int s = 0; s < 8; s++) {
+    for (int s = 0; s < 8; s += 2) {
         const int h = s >> 2, k = s & 3;
-        float tn = max3f(__fmaf_rn(byte_m(nx[h], k), ax, bnx), __fmaf_rn(byte_m(ny[h], k), ay, bny),
-                         fmaxf(__fmaf_rn(byte_m(nz[h], k), az, bnz), tmin));
-        float tf = min3f(__fmaf_rn(byte_m(fx[h], k), ax, bfx), __fmaf_rn(byte_m(fy[h], k), ay, bfy),
-                         fminf(__fmaf_rn(byte_m(fz[h], k), az, bfz), tmax));
-        hits |= (__float_as_int(tn) <= __float_as_int(tf) + BOX_SLACK_ULPS) ? (1u << s) : 0u;
+        const float2 tnx = __ffma2_rn(make_float2(byte_m(nx[h], k), byte_m(nx[h], k + 1)), AX, BNX);
+        const float2 tny = __ffma2_rn(make_float2(byte_m(ny[h], k), byte_m(ny[h], k + 1)), AY, BNY);
+        const float2 tnz = __ffma2_rn(make_float2(byte_m(nz[h], k), byte_m(nz[h], k + 1)), AZ, BNZ);
+        const float2 tfx = __ffma2_rn(make_float2(byte_m(fx[h], k), byte_m(fx[h], k + 1)), AX, BFX);
+        const float2 tfy = __ffma2_rn(make_float2(byte_m(fy[h], k), byte_m(fy[h], k + 1)), AY, BFY);
+        const float2 tfz = __ffma2_rn(make_float2(byte_m(fz[h], k), byte_m(fz[h], k + 1)), AZ, BFZ);
+        const float tn0 = max3f(tnx.x, tny.x, fmaxf(tnz.x, tmin)), tn1 = max3f(tnx.y, tny.y, fmaxf(tnz.y, tmin));
+        const float tf0 = min3f(tfx.x, tfy.x, fminf(tfz.x, tmax)), tf1 = min3f(tfx.y, tfy.y, fminf(tfz.y, tmax));
+        hits |= (__float_as_int(tn0) <= __float_as_int(tf0) + BOX_SLACK_ULPS) ? (1u << s) : 0u;
+        hits |= (__float_as_int(tn1) <= __float_as_int(tf1) + BOX_SLACK_ULPS) ? (2u << s) : 0u;
     }
     // internal children (imask bits) in visiting order: bit s moves to s ^ oct
     uint32_t x = hits & imask;
@@ -141,16 +151,26 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
         x = (r.oct & 2u) ? (((x & 0x33u) << 2) | ((x >> 2) & 0x33u)) : x;
         x = (r.oct & 4u) ? (((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu)) : x;
     }
-    // leaf children: (count << 5) | offset -> primitive bits; an empty slot (meta 0) adds none
-    uint32_t leaves = hits & ~imask, hit_prim = 0;
-    while (leaves) {
-        const uint32_t s = __ffs(leaves) - 1;
-        leaves &= leaves - 1u;
-        const uint32_t m = __byte_perm(meta0, meta1, s) & 0xFFu;
-        hit_prim |= bit_mask(m & 31u, m >> 5);
-    }
     ngroup = make_uint2(__float_as_uint(w1.x), (x << 24) | imask);
-    tgroup = make_uint2(__float_as_uint(w1.y), hit_prim);
+    if constexpr (SINGLE) {
+        // every leaf holds one primitive, stored in slot order: the leaf slots are
+        // those whose meta count bits are 1 (bit 5 of the byte), gathered from the
+        // four bytes of each meta word by one multiply; primitive groups are then
+        // (prim_base, hit leaf slots << 24 | leaf slots), like node groups
+        const uint32_t l0 = (meta0 >> 5) & 0x01010101u, l1 = (meta1 >> 5) & 0x01010101u;
+        const uint32_t leafmask = ((l0 * 0x10204080u) >> 28) | (((l1 * 0x10204080u) >> 28) << 4);
+        tgroup = make_uint2(__float_as_uint(w1.y), ((hits & leafmask) << 24) | leafmask);
+    } else {
+        // leaf children: (count << 5) | offset -> primitive bits; an empty slot (meta 0) adds none
+        uint32_t leaves = hits & ~imask, hit_prim = 0;
+        while (leaves) {
+            const uint32_t s = __ffs(leaves) - 1;
+            leaves &= leaves - 1u;
+            const uint32_t m = __byte_perm(meta0, meta1, s) & 0xFFu;
+            hit_prim |= bit_mask(m & 31u, m >> 5);
+        }
+        tgroup = make_uint2(__float_as_uint(w1.y), hit_prim);
+    }
 }
 
 struct TraceResult { float t, u, v; uint32_t inst, prim; bool hit; };
@@ -184,9 +204,13 @@ struct ShortStack {
 //                or at the instance level: enter that instance's BLAS)
 //   settle()     pop the stack until there is work again, leaving the BLAS
 //                when its part of the stack is used up; true when finished
-template <bool ANY, bool COUNT>
+// SINGLE: every leaf of both levels holds one primitive (SceneDev::single_leaf);
+// primitive groups are then (prim_base, hit leaf slots << 24 | leaf slots).  The
+// general form (primitive offset bits from the meta bytes) is valid for any tree.
+template <bool ANY, bool COUNT, bool SINGLE = false>
 struct Traverser {
     static constexpr bool ORD = !ANY;   // visit children front to back (closest hit only)
+    static constexpr uint32_t PTHR = SINGLE ? 0x00FFFFFFu : 0u;   // a primitive group is pending above this
     V3 o, d;             // world-space ray
     float tmin, tmax;
     NodeRay cr;          // ray of the current level (world or object space)
@@ -213,7 +237,7 @@ struct Traverser {
     }
 
     __device__ __forceinline__ bool has_node() const { return ngroup.y > 0x00FFFFFFu; }
-    __device__ __forceinline__ bool has_prim() const { return tgroup.y != 0u; }
+    __device__ __forceinline__ bool has_prim() const { return tgroup.y > PTHR; }
 
     __device__ __forceinline__ void fail(unsigned e) { err |= e; done = true; }
 
@@ -244,14 +268,21 @@ struct Traverser {
         }
         if (COUNT) ctr->nodes++;
         if (child >= (level ? S.num_blas_nodes : S.num_tlas_nodes)) { fail(ERR_BAD_INDEX); return; }
-        intersect_node<ORD>(level ? S.blas_nodes : S.tlas_nodes, child, cr, tmin, best_t, ngroup, tgroup);
+        intersect_node<ORD, SINGLE>(level ? S.blas_nodes : S.tlas_nodes, child, cr, tmin, best_t, ngroup, tgroup);
     }
 
     __device__ __forceinline__ void prim_step(const SceneDev& S, TraceCounters* ctr) {
         if (++steps > S.max_steps) { fail(ERR_STEP_LIMIT); return; }
-        uint32_t k = __ffs(tgroup.y) - 1;
-        tgroup.y &= tgroup.y - 1u;
-        uint32_t pidx = tgroup.x + k;
+        uint32_t pidx;
+        if constexpr (SINGLE) {   // the primitive's rank among the node's leaf slots
+            const uint32_t k = __ffs(tgroup.y >> 24) - 1;
+            tgroup.y &= ~(1u << (24 + k));
+            pidx = tgroup.x + __popc(tgroup.y & ((1u << k) - 1u));
+        } else {
+            const uint32_t k = __ffs(tgroup.y) - 1;
+            tgroup.y &= tgroup.y - 1u;
+            pidx = tgroup.x + k;
+        }
         if (level == 0) {
             if (pidx >= S.num_tlas_prims) { fail(ERR_BAD_INDEX); return; }
             uint32_t inst = __ldg(&S.tlas_prims[pidx]);

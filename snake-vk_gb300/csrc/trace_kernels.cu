@@ -89,7 +89,7 @@ struct RayFeed {
 };
 
 // closest hit of the rays queued for segment d
-template <bool COUNT, int MINB>
+template <bool COUNT, int MINB, bool SINGLE>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uint32_t d) {
     const Knobs kn(F.tune);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
     uint32_t* work = &F.counters[CNT_WORK_TRACE + d];
     const uint32_t lane = threadIdx.x & 31u;
     TraceCounters ctr{0ull, 0ull};
-    Traverser<false, COUNT> tv;
+    Traverser<false, COUNT, SINGLE> tv;
     uint2 spill[STACK_MAX - STACK_SH];
     RayFeed feed;
     feed.init();
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
 // contribution entry (shadow_entry); the visibility goes to that contribution's w
 // component, and k_accum_shadow adds the visible contributions in entry order
 // (the same order as the CPU oracle, so sums are bit-identical).
-template <bool COUNT, int MINB>
+template <bool COUNT, int MINB, bool SINGLE>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint32_t d) {
     const Knobs kn(F.tune_any);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint
     uint32_t* work = &F.counters[CNT_WORK_SHADOW + d];
     const uint32_t lane = threadIdx.x & 31u;
     TraceCounters ctr{0ull, 0ull};
-    Traverser<true, COUNT> tv;
+    Traverser<true, COUNT, SINGLE> tv;
     uint2 spill[STACK_MAX - STACK_SH];
     RayFeed feed;
     feed.init();
@@ -238,7 +238,7 @@ struct FilteredFeed {
 // 0 when something is; entries with tmax < 0 are empty (skipped, vis[i] not written:
 // the passes never read the result of a slot they did not record).
 // The ReSTIR passes queue their visibility rays here instead of tracing inline.
-template <int MINB>
+template <int MINB, bool SINGLE>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_visibility(SceneDev S, const float4* __restrict__ rays,
                                                                  uint32_t n, uint8_t* vis, uint32_t* work,
                                                                  TraceTuning tune) {
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_visibility(SceneDev S, con
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
     __shared__ uint32_t ring[TBLK / 32][64];
     const uint32_t lane = threadIdx.x & 31u;
-    Traverser<true, false> tv;
+    Traverser<true, false, SINGLE> tv;
     uint2 spill[STACK_MAX - STACK_SH];
     FilteredFeed feed;
     feed.init();
@@ -277,13 +277,13 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_visibility(SceneDev S, con
 }
 
 // generic trace of an array of rays (the snk_pt_trace_rays test hook)
-template <bool ANY>
+template <bool ANY, bool SINGLE>
 __global__ void __launch_bounds__(TBLK, 6) k_trace_rays(SceneDev S, const float4* __restrict__ rays, uint32_t n,
                                                      HitDev* hits, uint32_t* work, TraceTuning tune) {
     const Knobs kn(tune);
     __shared__ uint2 sh_stack[STACK_SH * TBLK];
     const uint32_t lane = threadIdx.x & 31u;
-    Traverser<ANY, false> tv;
+    Traverser<ANY, false, SINGLE> tv;
     uint2 spill[STACK_MAX - STACK_SH];
     RayFeed feed;
     feed.init();
@@ -324,29 +324,32 @@ __global__ void __launch_bounds__(TBLK, 6) k_trace_rays(SceneDev S, const float4
 }  // namespace
 
 // register budget variants: 0 -> at most 85 registers (6 blocks of 128 per SM),
-// 1 -> 64 registers (8 blocks), 2 -> unconstrained (4 blocks)
-template <bool COUNT>
+// 1 -> 64 registers (8 blocks), 2 -> unconstrained (4 blocks); each in the
+// single-primitive-leaf form when the scene's trees allow it
+template <bool COUNT, bool SINGLE>
 void launch_closest_variant(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s) {
-    if (F.tune.variant == 1) k_trace_closest<COUNT, 8><<<grid, TBLK, 0, s>>>(F, depth);
-    else if (F.tune.variant == 2) k_trace_closest<COUNT, 4><<<grid, TBLK, 0, s>>>(F, depth);
-    else k_trace_closest<COUNT, 6><<<grid, TBLK, 0, s>>>(F, depth);
+    if (F.tune.variant == 1) k_trace_closest<COUNT, 8, SINGLE><<<grid, TBLK, 0, s>>>(F, depth);
+    else if (F.tune.variant == 2) k_trace_closest<COUNT, 4, SINGLE><<<grid, TBLK, 0, s>>>(F, depth);
+    else k_trace_closest<COUNT, 6, SINGLE><<<grid, TBLK, 0, s>>>(F, depth);
 }
-template <bool COUNT>
+template <bool COUNT, bool SINGLE>
 void launch_shadow_variant(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s) {
-    if (F.tune_any.variant == 1) k_trace_shadow<COUNT, 8><<<grid, TBLK, 0, s>>>(F, depth);
-    else if (F.tune_any.variant == 2) k_trace_shadow<COUNT, 4><<<grid, TBLK, 0, s>>>(F, depth);
-    else k_trace_shadow<COUNT, 6><<<grid, TBLK, 0, s>>>(F, depth);
+    if (F.tune_any.variant == 1) k_trace_shadow<COUNT, 8, SINGLE><<<grid, TBLK, 0, s>>>(F, depth);
+    else if (F.tune_any.variant == 2) k_trace_shadow<COUNT, 4, SINGLE><<<grid, TBLK, 0, s>>>(F, depth);
+    else k_trace_shadow<COUNT, 6, SINGLE><<<grid, TBLK, 0, s>>>(F, depth);
 }
 
 cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s) {
-    if (count) launch_closest_variant<true>(F, depth, grid, s);
-    else launch_closest_variant<false>(F, depth, grid, s);
+    const bool single = F.S.single_leaf != 0u;
+    if (count) single ? launch_closest_variant<true, true>(F, depth, grid, s) : launch_closest_variant<true, false>(F, depth, grid, s);
+    else single ? launch_closest_variant<false, true>(F, depth, grid, s) : launch_closest_variant<false, false>(F, depth, grid, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s) {
-    if (count) launch_shadow_variant<true>(F, depth, grid, s);
-    else launch_shadow_variant<false>(F, depth, grid, s);
+    const bool single = F.S.single_leaf != 0u;
+    if (count) single ? launch_shadow_variant<true, true>(F, depth, grid, s) : launch_shadow_variant<true, false>(F, depth, grid, s);
+    else single ? launch_shadow_variant<false, true>(F, depth, grid, s) : launch_shadow_variant<false, false>(F, depth, grid, s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_accum_shadow<<<grid / 2 > 0 ? grid / 2 : 1, 256, 0, s>>>(F, depth);
@@ -355,16 +358,27 @@ cudaError_t launch_trace_shadow(const FrameParams& F, uint32_t depth, int grid, 
 
 cudaError_t launch_trace_visibility(const SceneDev& S, const float4* rays, uint32_t n, uint8_t* vis, uint32_t* work,
                                     int grid, const TraceTuning& tune, cudaStream_t s) {
-    if (tune.variant == 1) k_trace_visibility<8><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
-    else if (tune.variant == 2) k_trace_visibility<4><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
-    else k_trace_visibility<6><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+    if (S.single_leaf) {
+        if (tune.variant == 1) k_trace_visibility<8, true><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+        else if (tune.variant == 2) k_trace_visibility<4, true><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+        else k_trace_visibility<6, true><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+    } else {
+        if (tune.variant == 1) k_trace_visibility<8, false><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+        else if (tune.variant == 2) k_trace_visibility<4, false><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+        else k_trace_visibility<6, false><<<grid, TBLK, 0, s>>>(S, rays, n, vis, work, tune);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_rays(const SceneDev& S, const float4* rays, uint32_t n, HitDev* hits, bool any,
                               uint32_t* work, int grid, const TraceTuning& tune, cudaStream_t s) {
-    if (any) k_trace_rays<true><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
-    else k_trace_rays<false><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
+    if (S.single_leaf) {
+        if (any) k_trace_rays<true, true><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
+        else k_trace_rays<false, true><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
+    } else {
+        if (any) k_trace_rays<true, false><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
+        else k_trace_rays<false, false><<<grid, TBLK, 0, s>>>(S, rays, n, hits, work, tune);
+    }
     return cudaGetLastError();
 }
 

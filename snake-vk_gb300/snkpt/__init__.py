@@ -58,11 +58,11 @@ class Tuning(C.Structure):
                 ("bvh_leaf_pack", C.c_uint32), ("max_traversal_steps", C.c_uint32), ("stack_limit", C.c_uint32),
                 ("shadow_blocks_per_sm", C.c_uint32), ("shadow_ray_chunk", C.c_uint32),
                 ("shadow_refill_idle", C.c_uint32), ("shadow_prim_bias", C.c_uint32), ("shadow_variant", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("bvh_collapse", C.c_uint32)]
     KNOBS = ("trace_blocks_per_sm", "shade_blocks_per_sm", "ray_chunk", "refill_idle", "prim_bias", "trace_variant",
              "bvh_treelet_passes", "tlas_treelet_passes", "tlas_refit_interval", "bvh_leaf_max", "tlas_leaf_max",
              "bvh_leaf_pack", "max_traversal_steps", "stack_limit", "shadow_blocks_per_sm", "shadow_ray_chunk",
-             "shadow_refill_idle", "shadow_prim_bias", "shadow_variant")
+             "shadow_refill_idle", "shadow_prim_bias", "shadow_variant", "bvh_collapse")
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k in self.KNOBS}

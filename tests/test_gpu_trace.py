@@ -249,6 +249,42 @@ def test_treelet_restructuring_lowers_sah_and_keeps_hits(cuda, built_lib):
     assert full[0] < one[0] < plain[0], (plain[0], one[0], full[0])
     assert full[2] < plain[2], (plain[2], full[2])
     assert_hits_equal(full[1], O.OracleScene(sc).trace(rays), "restructured BVH vs oracle")
+    # the least-SAH choice of each wide node's children against the greedy one
+    # (open the largest child until 8): lower cost, identical hits
+    pt = snkpt.PathTracer(0)
+    pt.set_tuning({"bvh_collapse": 1})
+    pt.load_scene(sc)
+    greedy_hits = pt.trace_rays(rays)
+    greedy_sah = pt.stats()["blas_sah_cost"]
+    assert full[0] < greedy_sah, (full[0], greedy_sah)
+    assert_hits_equal(greedy_hits, full[1], "greedy vs least-SAH collapse")
+
+
+@pytest.mark.parametrize("knobs", [{"bvh_leaf_max": 2}, {"bvh_leaf_max": 1, "bvh_leaf_pack": 4},
+                                   {"tlas_leaf_max": 3}, {"bvh_leaf_max": 4, "tlas_leaf_max": 2}])
+def test_multi_primitive_leaves_keep_hits(cuda, built_lib, knobs):
+    """Leaves of several primitives (mesh or instance level) use the general
+    primitive groups in traversal; single-primitive leaves use the slot-mask form.
+    Hits, any-hit answers and a rendered frame must not depend on which."""
+    sc = scenes.config1(width=320, height=180)
+    rng = np.random.default_rng(23)
+    rays = np.concatenate([camera_rays(sc.views[0]), random_rays(sc, 100_000, rng)])
+    srays = shadow_rays(sc, 100_000, rng)
+    single = snkpt.PathTracer(0)
+    single.load_scene(sc)
+    multi = snkpt.PathTracer(0)
+    multi.set_tuning(knobs)
+    multi.load_scene(sc)
+    assert_hits_equal(multi.trace_rays(rays), single.trace_rays(rays), f"{knobs} vs single-primitive leaves")
+    assert np.array_equal(multi.trace_rays(srays, any_hit=True)["flags"], single.trace_rays(srays, any_hit=True)["flags"])
+    assert_hits_equal(multi.trace_rays(rays), O.OracleScene(sc).trace(rays), f"{knobs} vs oracle")
+    st = abi.settings(spp=1, max_depth=4, seed=9)
+    outs = [snkpt.alloc_outputs(320, 180, device=cuda) for _ in range(2)]
+    single.render([sc.views[0]], st, [outs[0]])
+    multi.render([sc.views[0]], st, [outs[1]])
+    single.synchronize(); multi.synchronize()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k].cpu().numpy(), outs[1][k].cpu().numpy()), k
 
 
 @pytest.mark.parametrize("cfg", [1, 2])
