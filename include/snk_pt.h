@@ -308,9 +308,10 @@ typedef struct snk_tuning {
     uint32_t shadow_refill_idle;    /* any-hit traversal: refill threshold (0: refill_idle) */
     uint32_t shadow_prim_bias;      /* any-hit traversal: primitive-step bias (0: prim_bias) */
     uint32_t shadow_variant;        /* any-hit traversal registers: 0 as trace_variant, k + 1 variant k */
-    uint32_t bvh_collapse;          /* how later mesh BVH builds pick each 8-wide node's children from
-                                       the binary tree: 0 the least-SAH choice (dynamic programming
-                                       over the tree), 1 greedily opening the largest child */
+    uint32_t bvh_collapse;          /* how BVH builds (later mesh BVHs, every instance BVH) pick each
+                                       8-wide node's children from the binary tree: 0 the least-SAH
+                                       choice (dynamic programming over the tree), 1 greedily opening
+                                       the largest child */
 } snk_tuning;
 
 #define SNK_TREELET_PASSES_NONE 0xFFFFFFFFu

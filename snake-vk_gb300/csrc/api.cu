@@ -464,7 +464,7 @@ Status build_instances(snk_pt_ctx* ctx) {
             SNK_TRY(build_wide_bvh_small(ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
                                          ctx->d_tlas_order.p, passes, ctx->d_small_out.p, ctx->d_err.p,
                                          ctx->d_tlas_box.p, ctx->d_tlas_depth.p, st,
-                                         leaf_size(ctx->tune.tlas_leaf_max, 1)));
+                                         leaf_size(ctx->tune.tlas_leaf_max, 1), ctx->tune.bvh_collapse == 0));
             SNK_TRY(launch_map_prims(ctx->d_tlas_order.p, ctx->d_inst_list.p, n, ctx->d_tlas_prims.p, st));
             ctx->tlas_nodes = n + 1;
             ctx->tlas_small = true;
@@ -477,7 +477,7 @@ Status build_instances(snk_pt_ctx* ctx) {
             SNK_TRY(build_wide_bvh_device(ctx->scratch, ctx->d_box_lo.p, ctx->d_box_hi.p, n, ctx->d_tlas.p, 0u, 0u,
                                           ctx->d_tlas_order.p, ctx->d_err.p, st, passes,
                                           leaf_size(ctx->tune.tlas_leaf_max, 1), leaf_size(ctx->tune.tlas_leaf_max, 1),
-                                          ctx->d_small_out.p, ctx->d_tlas_depth.p));
+                                          ctx->d_small_out.p, ctx->d_tlas_depth.p, ctx->tune.bvh_collapse == 0));
             ctx->tlas_nodes = n + 1;
             ctx->tlas_small = false;
             ctx->tlas_builds++;

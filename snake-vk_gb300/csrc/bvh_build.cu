@@ -680,68 +680,109 @@ __device__ __forceinline__ void quant_child(const QuantFrame& F, float4 a4, floa
 constexpr float WIDE_CN = 1.0f;   // one 8-wide node test
 constexpr float WIDE_CT = 1.0f;   // one primitive test (0.3 and 0.6 gave the same trees on the test scenes)
 
+template <bool G>
 __device__ __forceinline__ void wide_costs(int c, int nl, const float4* node_lo, const float4* node_hi,
                                            const float* wide_cost, float d[8]) {
     if (c >= nl) {
-        const float v = WIDE_CT * half_area(node_lo[c], node_hi[c]);
+        const float v = WIDE_CT * half_area(ldx<G>(&node_lo[c]), ldx<G>(&node_hi[c]));
 #pragma unroll
         for (int i = 0; i < 8; i++) d[i] = v;
     } else {
         const float4* src = reinterpret_cast<const float4*>(wide_cost + 8 * (size_t)c);
-        const float4 a = __ldcg(src), b = __ldcg(src + 1);
+        const float4 a = ldx<G>(src), b = ldx<G>(src + 1);
         d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w; d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
     }
 }
 
-// bottom-up from leaf j (the second thread to arrive at a node completes it)
+// D(p, 1..8) and wide_split[p] of internal node p from its two children's entries
+template <bool G>
+__device__ __forceinline__ void wide_cost_node(int p, int nl, const int2* children, const float4* node_lo,
+                                               const float4* node_hi, const uint32_t* leaf_count, float* wide_cost,
+                                               uint32_t* wide_split, uint32_t leaf_max, uint32_t leaf_pack) {
+    const int2 ch = ldx<G>(&children[p]);
+    float a[8], b[8];
+    wide_costs<G>(ch.x, nl, node_lo, node_hi, wide_cost, a);
+    wide_costs<G>(ch.y, nl, node_lo, node_hi, wide_cost, b);
+    float e[9];
+    uint32_t ek[9];
+#pragma unroll
+    for (int i = 2; i <= 8; i++) {
+        float best = a[0] + b[i - 2];
+        uint32_t bk = 1;
+#pragma unroll
+        for (int k = 2; k < i; k++) {
+            const float c = a[k - 1] + b[i - k - 1];
+            if (c < best) { best = c; bk = (uint32_t)k; }
+        }
+        e[i] = best;
+        ek[i] = bk;
+    }
+    const float area = half_area(ldx<G>(&node_lo[p]), ldx<G>(&node_hi[p]));
+    const uint32_t cnt = ldx<G>(&leaf_count[p]);
+    const float d1 = cnt <= leaf_pack ? WIDE_CT * area * (float)cnt : WIDE_CN * area + e[8];
+    float d[8];
+    uint32_t split = ek[8];
+    d[0] = d1;
+#pragma unroll
+    for (int i = 2; i <= 8; i++) {
+        const bool open = cnt > leaf_max && e[i] < d1;   // subtrees of at most leaf_max primitives stay leaves
+        d[i - 1] = open ? e[i] : d1;
+        split |= (open ? ek[i] : 0u) << (4 * (i - 1));
+    }
+    float4* dst = reinterpret_cast<float4*>(wide_cost + 8 * (size_t)p);
+    dst[0] = make_float4(d[0], d[1], d[2], d[3]);
+    dst[1] = make_float4(d[4], d[5], d[6], d[7]);
+    wide_split[p] = split;
+}
+
+// bottom-up from leaf j of n (the second thread to arrive at a node completes it)
+template <bool G>
+__device__ void wide_cost_climb(int j, int n, const int2* children, const int* parent, int* flags,
+                                const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count,
+                                float* wide_cost, uint32_t* wide_split, uint32_t leaf_max, uint32_t leaf_pack) {
+    if (n == 1) return;
+    const int nl = n - 1;
+    int p = parent[nl + j];
+    while (p >= 0) {
+        mem_fence<G>();
+        if (atomicAdd(&flags[p], 1) == 0) return;
+        mem_fence<G>();
+        wide_cost_node<G>(p, nl, children, node_lo, node_hi, leaf_count, wide_cost, wide_split, leaf_max, leaf_pack);
+        p = parent[p];
+    }
+}
+
 __global__ void k_collapse_cost(int n, const int2* __restrict__ children, const int* __restrict__ parent, int* flags,
                                 const float4* __restrict__ node_lo, const float4* __restrict__ node_hi,
                                 const uint32_t* __restrict__ leaf_count, float* wide_cost, uint32_t* wide_split,
                                 uint32_t leaf_max, uint32_t leaf_pack) {
     const int j = blockIdx.x * BLK + threadIdx.x;
-    if (j >= n || n == 1) return;
-    const int nl = n - 1;
-    int p = parent[nl + j];
-    while (p >= 0) {
-        __threadfence();
-        if (atomicAdd(&flags[p], 1) == 0) return;
-        __threadfence();
-        const int2 ch = children[p];
-        float a[8], b[8];
-        wide_costs(ch.x, nl, node_lo, node_hi, wide_cost, a);
-        wide_costs(ch.y, nl, node_lo, node_hi, wide_cost, b);
-        float e[9];
-        uint32_t ek[9];
-#pragma unroll
-        for (int i = 2; i <= 8; i++) {
-            float best = a[0] + b[i - 2];
-            uint32_t bk = 1;
-#pragma unroll
-            for (int k = 2; k < i; k++) {
-                const float c = a[k - 1] + b[i - k - 1];
-                if (c < best) { best = c; bk = (uint32_t)k; }
-            }
-            e[i] = best;
-            ek[i] = bk;
+    if (j < n)
+        wide_cost_climb<true>(j, n, children, parent, flags, node_lo, node_hi, leaf_count, wide_cost, wide_split,
+                              leaf_max, leaf_pack);
+}
+
+// the children of the wide node rooted at internal node b chosen by wide_split
+// (the least-SAH distribution of b's subtree over 8 slots); returns their number
+__device__ __forceinline__ int wide_children(int b, int nl, const int2* children, const uint32_t* wide_split,
+                                             int C[8]) {
+    int sn[8], ss[8], sp = 0, nc = 0;
+    const int2 ch = children[b];
+    const int k8 = (int)(wide_split[b] & 15u);
+    sn[sp] = ch.y; ss[sp++] = 8 - k8;
+    sn[sp] = ch.x; ss[sp++] = k8;
+    while (sp > 0 && nc < 8) {
+        const int y = sn[--sp], slots = ss[sp];
+        const int k = (y >= nl || slots <= 1) ? 0 : (int)((wide_split[y] >> (4 * (slots - 1))) & 15u);
+        if (k == 0 || k >= slots || sp > 6) {
+            C[nc++] = y;
+        } else {
+            const int2 cy = children[y];
+            sn[sp] = cy.y; ss[sp++] = slots - k;
+            sn[sp] = cy.x; ss[sp++] = k;
         }
-        const float area = half_area(node_lo[p], node_hi[p]);
-        const uint32_t cnt = leaf_count[p];
-        const float d1 = cnt <= leaf_pack ? WIDE_CT * area * (float)cnt : WIDE_CN * area + e[8];
-        float d[8];
-        uint32_t split = ek[8];
-        d[0] = d1;
-#pragma unroll
-        for (int i = 2; i <= 8; i++) {
-            const bool open = cnt > leaf_max && e[i] < d1;   // subtrees of at most leaf_max primitives stay leaves
-            d[i - 1] = open ? e[i] : d1;
-            split |= (open ? ek[i] : 0u) << (4 * (i - 1));
-        }
-        float4* dst = reinterpret_cast<float4*>(wide_cost + 8 * (size_t)p);
-        dst[0] = make_float4(d[0], d[1], d[2], d[3]);
-        dst[1] = make_float4(d[4], d[5], d[6], d[7]);
-        wide_split[p] = split;
-        p = parent[p];
     }
+    return sp > 0 ? -1 : nc;   // -1: more than 8 children (never with a consistent table)
 }
 
 // One output node: task = (binary node, wide node slot).  counters: [1] tasks
@@ -759,25 +800,8 @@ __device__ void collapse_task(uint2 task, uint32_t* counters, uint2* tasks_out, 
     int nc;
     if (b >= nl) { C[0] = b; nc = 1; }
     else if (wide_split) {
-        // the children chosen by the SAH-optimal distribution of b's subtree over 8 slots
-        int sn[8], ss[8], sp = 0;
-        const int2 ch = children[b];
-        const int k8 = (int)(wide_split[b] & 15u);
-        sn[sp] = ch.y; ss[sp++] = 8 - k8;
-        sn[sp] = ch.x; ss[sp++] = k8;
-        nc = 0;
-        while (sp > 0 && nc < 8) {
-            const int y = sn[--sp], slots = ss[sp];
-            const int k = (y >= nl || slots <= 1) ? 0 : (int)((wide_split[y] >> (4 * (slots - 1))) & 15u);
-            if (k == 0 || k >= slots || sp > 6) {
-                C[nc++] = y;
-            } else {
-                const int2 cy = children[y];
-                sn[sp] = cy.y; ss[sp++] = slots - k;
-                sn[sp] = cy.x; ss[sp++] = k;
-            }
-        }
-        if (sp > 0) atomicOr(&counters[4], 8u);   // more than 8 children (never with a consistent table)
+        nc = wide_children(b, nl, children, wide_split, C);
+        if (nc < 0) { atomicOr(&counters[4], 8u); return; }
     }
     else { int2 ch = children[b]; C[0] = ch.x; C[1] = ch.y; nc = 2; }
     while (!wide_split && nc < 8) {
@@ -945,7 +969,13 @@ struct SmallSmem {
     uint32_t counters[8];
     unsigned cb[6];
     double sah;
-    TreeletSmem tl[SMALL_THREADS / 32];
+    union {
+        TreeletSmem tl[SMALL_THREADS / 32];    // treelet passes
+        struct {                               // then the least-SAH collapse table
+            float wide_cost[8 * SMALL_BUILD_MAX];
+            uint32_t wide_split[SMALL_BUILD_MAX];
+        } dp;
+    };
     WideNode stage[SMALL_THREADS / 32];        // per-warp staging of collapsed nodes
 };
 static_assert(sizeof(SmallSmem) <= 227 * 1024, "single-CTA builder exceeds shared memory");
@@ -999,7 +1029,8 @@ __device__ void collapse_task_warp(uint2 task, uint32_t* counters, uint32_t* nex
                                    const int2* children,
                                    const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count,
                                    const uint32_t* sorted, WideNode* nodes, WideNode* stage, uint32_t node_base,
-                                   uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack) {
+                                   uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack,
+                                   const uint32_t* wide_split) {
     constexpr unsigned FULL = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const int b = (int)task.x;
@@ -1009,13 +1040,29 @@ __device__ void collapse_task_warp(uint2 task, uint32_t* counters, uint32_t* nex
     if (b >= nl) {
         nc = 1;
         if (lane == 0) c = b;
+    } else if (wide_split) {
+        // the least-SAH children (lane 0 expands the split table, lane k takes child k)
+        int C[8];
+        int m = 0;
+        if (lane == 0) m = wide_children(b, nl, children, wide_split, C);
+        m = __shfl_sync(FULL, m, 0);
+        if (m < 0) {
+            if (lane == 0) atomicOr(&counters[4], 8u);
+            return;
+        }
+        nc = m;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int v = __shfl_sync(FULL, (lane == 0 && k < m) ? C[k] : -1, 0);
+            if (lane == k) c = v;
+        }
     } else {
         const int2 ch = children[b];
         nc = 2;
         c = lane == 0 ? ch.x : (lane == 1 ? ch.y : -1);
     }
-    // open the largest internal candidate (more than leaf_max primitives) until 8 children
-    while (nc < 8) {
+    // greedy: open the largest internal candidate (more than leaf_max primitives) until 8 children
+    while (!wide_split && nc < 8) {
         const bool elig = lane < nc && c < nl && leaf_count[c] > leaf_max;
         const unsigned key = elig ? __float_as_uint(half_area(node_lo[c], node_hi[c])) + 1u : 0u;   // areas >= 0
         const unsigned mx = __reduce_max_sync(FULL, key);
@@ -1149,7 +1196,7 @@ __device__ void collapse_task_warp(uint2 task, uint32_t* counters, uint32_t* nex
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
 k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, int n, int passes, WideNode* nodes,
               uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, SmallBuildOut* out, unsigned* err_word,
-              float4* wide_box, uint32_t* wide_depth, uint32_t leaf_max) {
+              float4* wide_box, uint32_t* wide_depth, uint32_t leaf_max, bool sah_collapse) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmallSmem& S = *reinterpret_cast<SmallSmem*>(smem_raw);
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -1365,6 +1412,22 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
             __syncthreads();
         }
     }
+    // 5c. least-SAH choice of every wide node's children (bottom-up, in shared memory)
+    const bool dp = sah_collapse && n > 1 && S.counters[6] == 0u;
+    if (dp) {
+        if (tid == 0) S.parent[0] = -1;
+        if (tid < n - 1) {
+            const int2 ch = S.children[tid];
+            S.parent[ch.x] = tid;
+            S.parent[ch.y] = tid;
+        }
+        if (tid < n) S.flags[tid] = 0;
+        __syncthreads();
+        if (tid < n)
+            wide_cost_climb<false>(tid, n, S.children, S.parent, S.flags, S.node_lo, S.node_hi, S.leaf_count,
+                                   S.dp.wide_cost, S.dp.wide_split, leaf_max, leaf_max);
+        __syncthreads();
+    }
     // 6. collapse, level by level
     const float4 rlo = S.node_lo[0], rhi = S.node_hi[0];
     float rha = half_area(rlo, rhi);
@@ -1391,7 +1454,7 @@ k_build_small(const float4* __restrict__ plo, const float4* __restrict__ phi, in
             }
             collapse_task_warp(task, S.counters, &S.counters[1], S.tasks[cc ^ 1], n, S.children, S.node_lo, S.node_hi,
                                S.leaf_count, S.vals, nodes, &S.stage[tid >> 5], node_base, prim_base, prim_order,
-                               leaf_max, leaf_max);
+                               leaf_max, leaf_max, dp ? S.dp.wide_split : nullptr);
         }
         __syncthreads();
         if (tid == 0) { S.counters[0] = S.counters[1]; S.counters[1] = 0u; }
@@ -1443,7 +1506,7 @@ __global__ void __launch_bounds__(32 * LEVEL_WARPS) k_collapse_level(
     int level, uint2* tasks_a, uint2* tasks_b, uint32_t* level_tasks, uint32_t* counters, int n, const int2* children,
     const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count, const uint32_t* sorted, WideNode* nodes,
     uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, uint32_t leaf_max, uint32_t leaf_pack,
-    uint32_t* wide_depth) {
+    uint32_t* wide_depth, const uint32_t* wide_split) {
     __shared__ WideNode stage[LEVEL_WARPS];
     const uint32_t nin = min(level_tasks[level], (uint32_t)n);   // the task arrays hold n entries
     if (nin == 0 || counters[4] != 0u) return;
@@ -1454,7 +1517,8 @@ __global__ void __launch_bounds__(32 * LEVEL_WARPS) k_collapse_level(
         const uint2 task = tin[t];
         note_depth(wide_depth, task, node_base, n, level);
         collapse_task_warp(task, counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi, leaf_count,
-                           sorted, nodes, &stage[w], node_base, prim_base, prim_order, leaf_max, leaf_pack);
+                           sorted, nodes, &stage[w], node_base, prim_base, prim_order, leaf_max, leaf_pack,
+                           wide_split);
     }
 }
 
@@ -1462,7 +1526,8 @@ __global__ void __launch_bounds__(1024) k_collapse_finish(
     int first_level, uint2* tasks_a, uint2* tasks_b, uint32_t* level_tasks, uint32_t* counters, int n,
     const int2* children, const float4* node_lo, const float4* node_hi, const uint32_t* leaf_count,
     const uint32_t* sorted, WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
-    uint32_t leaf_max, uint32_t leaf_pack, unsigned* err_word, uint32_t* wide_depth, SmallBuildOut* out) {
+    uint32_t leaf_max, uint32_t leaf_pack, unsigned* err_word, uint32_t* wide_depth, SmallBuildOut* out,
+    const uint32_t* wide_split) {
     __shared__ WideNode stage[32];
     const uint32_t w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int level = first_level;
@@ -1476,7 +1541,7 @@ __global__ void __launch_bounds__(1024) k_collapse_finish(
             note_depth(wide_depth, task, node_base, n, level);
             collapse_task_warp(task, counters, &level_tasks[level + 1], tout, n, children, node_lo, node_hi,
                                leaf_count, sorted, nodes, &stage[w], node_base, prim_base, prim_order, leaf_max,
-                               leaf_pack);
+                               leaf_pack, wide_split);
         }
         __syncthreads();   // this level's child tasks and their count are complete
     }
@@ -1782,9 +1847,20 @@ Status build_wide_bvh(BuildScratch& sc, const float4* prim_lo, const float4* pri
 Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n,
                              WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
                              unsigned* err_word, cudaStream_t st, int treelet_passes, uint32_t leaf_max,
-                             uint32_t leaf_pack, SmallBuildOut* out, uint32_t* wide_depth) {
+                             uint32_t leaf_pack, SmallBuildOut* out, uint32_t* wide_depth, bool sah_collapse) {
     const uint32_t* sorted = nullptr;
     SNK_TRY(build_binary_tree(sc, prim_lo, prim_hi, n, st, treelet_passes, leaf_max, leaf_pack, &sorted));
+    const uint32_t* wide_split = nullptr;
+    if (n > 1 && sah_collapse) {
+        SNK_TRY_CUDA(sc.wide_cost.reserve(8 * (size_t)(n - 1)));
+        SNK_TRY_CUDA(sc.wide_split.reserve(n - 1));
+        SNK_TRY_CUDA(cudaMemsetAsync(sc.flags.p, 0, sizeof(int) * n, st));
+        k_collapse_cost<<<grid_for(n), BLK, 0, st>>>((int)n, sc.children.p, sc.parent.p, sc.flags.p, sc.node_lo.p,
+                                                     sc.node_hi.p, sc.leaf_count.p, sc.wide_cost.p, sc.wide_split.p,
+                                                     leaf_max, leaf_pack);
+        SNK_TRY_CUDA(cudaGetLastError());
+        wide_split = sc.wide_split.p;
+    }
     SNK_TRY_CUDA(sc.level_tasks.reserve(COLLAPSE_MAX_LEVELS + 1));
     k_collapse_init<<<1, 128, 0, st>>>(sc.tasks_a.p, sc.counters.p, sc.level_tasks.p, node_base);
     // enough warps for the widest level of a typical tree, at most 1024 blocks
@@ -1799,11 +1875,12 @@ Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const floa
         k_collapse_level<<<grid, 32 * LEVEL_WARPS, 0, st>>>(level, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
                                                             sc.counters.p, (int)n, sc.children.p, sc.node_lo.p,
                                                             sc.node_hi.p, sc.leaf_count.p, sorted, nodes, node_base,
-                                                            prim_base, prim_order, leaf_max, leaf_pack, wide_depth);
+                                                            prim_base, prim_order, leaf_max, leaf_pack, wide_depth,
+                                                            wide_split);
     k_collapse_finish<<<1, 1024, 0, st>>>(fast, sc.tasks_a.p, sc.tasks_b.p, sc.level_tasks.p,
                                           sc.counters.p, (int)n, sc.children.p, sc.node_lo.p, sc.node_hi.p,
                                           sc.leaf_count.p, sorted, nodes, node_base, prim_base, prim_order, leaf_max,
-                                          leaf_pack, err_word, wide_depth, out);
+                                          leaf_pack, err_word, wide_depth, out, wide_split);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }
@@ -1811,14 +1888,14 @@ Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const floa
 Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                             uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
                             SmallBuildOut* out, unsigned* err_word, float4* wide_box, uint32_t* wide_depth,
-                            cudaStream_t st, uint32_t leaf_max) {
+                            cudaStream_t st, uint32_t leaf_max, bool sah_collapse) {
     if (n == 0 || n > (uint32_t)SMALL_BUILD_MAX) return Status::Err(1, "build_wide_bvh_small: bad primitive count");
     if (leaf_max < 1 || leaf_max > LEAF_MAX_LIMIT) return Status::Err(1, "build_wide_bvh_small: leaf size out of range");
     SNK_TRY_CUDA(cudaFuncSetAttribute(k_build_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(SmallSmem)));
     k_build_small<<<1, SMALL_THREADS, sizeof(SmallSmem), st>>>(prim_lo, prim_hi, (int)n, treelet_passes, nodes,
                                                                 node_base, prim_base, prim_order, out, err_word,
-                                                                wide_box, wide_depth, leaf_max);
+                                                                wide_box, wide_depth, leaf_max, sah_collapse);
     SNK_TRY_CUDA(cudaGetLastError());
     return Status::Ok();
 }

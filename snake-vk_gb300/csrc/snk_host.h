@@ -107,7 +107,8 @@ struct SmallBuildOut;
 Status build_wide_bvh_device(BuildScratch& sc, const float4* prim_lo, const float4* prim_hi, uint32_t n,
                              WideNode* nodes, uint32_t node_base, uint32_t prim_base, uint32_t* prim_order,
                              unsigned* err_word, cudaStream_t stream, int treelet_passes, uint32_t leaf_max,
-                             uint32_t leaf_pack, SmallBuildOut* out = nullptr, uint32_t* wide_depth = nullptr);
+                             uint32_t leaf_pack, SmallBuildOut* out = nullptr, uint32_t* wide_depth = nullptr,
+                             bool sah_collapse = true);
 
 // Single-launch build for n <= SMALL_BUILD_MAX primitives (one CTA, shared
 // memory, no host synchronisation); same algorithm and output layout as
@@ -124,7 +125,7 @@ struct SmallBuildOut {
 Status build_wide_bvh_small(const float4* prim_lo, const float4* prim_hi, uint32_t n, WideNode* nodes,
                             uint32_t node_base, uint32_t prim_base, uint32_t* prim_order, int treelet_passes,
                             SmallBuildOut* out, unsigned* err_word, float4* wide_box, uint32_t* wide_depth,
-                            cudaStream_t stream, uint32_t leaf_max);
+                            cudaStream_t stream, uint32_t leaf_max, bool sah_collapse = true);
 // Refit of a tree made by build_wide_bvh_small or build_wide_bvh_device (with its
 // record and depths) for the same n primitives in new boxes (prim_order as that
 // build wrote it; wide_box: 2 x (n + 1) float4 of scratch that receives every
