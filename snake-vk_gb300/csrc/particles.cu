@@ -67,7 +67,7 @@ __device__ __noinline__ Contact contact_ray(const SceneDev& S, V3 o, V3 d, float
 
 __global__ void __launch_bounds__(PBLK) k_contact_rays(SceneDev S, const float4* __restrict__ rays, uint32_t n,
                                                        float timestep, ContactOut* out) {
-    __shared__ uint2 sh[STACK_SH * PBLK];
+    __shared__ uint2 sh[TRACE_SH_ROWS * PBLK];
     for (uint32_t i = blockIdx.x * PBLK + threadIdx.x; i < n; i += gridDim.x * PBLK) {
         const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
         store(out + i, contact_ray(S, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), a.w, b.w, timestep, sh));
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(PBLK) k_contact_rays(SceneDev S, const float4*
 
 __global__ void __launch_bounds__(PBLK) k_particle_probe(SceneDev S, const ParticleDev* __restrict__ P, uint32_t n,
                                                          float timestep, ContactOut* cand_out, float* gravity) {
-    __shared__ uint2 sh[STACK_SH * PBLK];
+    __shared__ uint2 sh[TRACE_SH_ROWS * PBLK];
     for (uint32_t i = blockIdx.x * PBLK + threadIdx.x; i < n; i += gridDim.x * PBLK) {
         const ParticleDev q = P[i];
         const V3 pos = v3(q.pr.x, q.pr.y, q.pr.z), vel = v3(q.vel.x, q.vel.y, q.vel.z);
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(PBLK) k_particle_probe(SceneDev S, const Parti
 __global__ void __launch_bounds__(PBLK) k_particle_constrain(SceneDev S, const ParticleDev* __restrict__ P,
                                                              const float* __restrict__ off, uint32_t n, float timestep,
                                                              float* out) {
-    __shared__ uint2 sh[STACK_SH * PBLK];
+    __shared__ uint2 sh[TRACE_SH_ROWS * PBLK];
     for (uint32_t i = blockIdx.x * PBLK + threadIdx.x; i < n; i += gridDim.x * PBLK) {
         const ParticleDev q = P[i];
         const V3 o = v3(off[3ull * i], off[3ull * i + 1], off[3ull * i + 2]);

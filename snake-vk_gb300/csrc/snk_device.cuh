@@ -291,6 +291,10 @@ struct DirLightDev { float dir[3]; uint32_t enabled; float colour[3]; float pad;
 // bound stops and sets a bit in the scene's error word.
 constexpr uint32_t MAX_TRAVERSAL_STEPS = 1u << 16;
 constexpr int STACK_SH = 8;
+// rows of a traversal kernel's shared array per thread: the STACK_SH stack
+// entries, then two rows that keep the world ray's reciprocal direction and
+// octant while the ray is inside an instance
+constexpr int TRACE_SH_ROWS = STACK_SH + 2;
 constexpr int STACK_MAX = 64;
 
 // device pointers of the whole scene, passed by value to kernels

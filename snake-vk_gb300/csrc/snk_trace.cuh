@@ -178,7 +178,9 @@ struct TraceResult { float t, u, v; uint32_t inst, prim; bool hit; };
 struct TraceCounters { unsigned long long nodes, tris; };
 
 // Short stack: entries [0, STACK_SH) live in shared memory at sh[k * nthreads + tid],
-// deeper entries in a local array; at most lim (<= STACK_MAX) entries.
+// deeper entries in a local array; at most lim (<= STACK_MAX) entries.  Rows
+// STACK_SH and STACK_SH + 1 of sh (TRACE_SH_ROWS rows in all) keep the world ray's
+// node-test reciprocals while the ray is in an instance.
 struct ShortStack {
     uint2* sh;
     uint2* spill;   // STACK_MAX - STACK_SH entries (a local array of the caller)
@@ -232,6 +234,7 @@ struct Traverser {
         level = 0; blas_sp = 0; cur_inst = 0; steps = 0; err = 0; done = false;
         st.sh = sh; st.spill = spill; st.tid = tid; st.nthreads = nthreads; st.sp = 0;
         st.lim = S.stack_max < STACK_MAX ? S.stack_max : STACK_MAX;
+        save_world();
         ngroup = S.tlas_root == INVALID ? make_uint2(0u, 0u) : make_uint2(S.tlas_root, (1u << (24 + (ORD ? cr.oct : 0u))) | 1u);
         tgroup = make_uint2(0u, 0u);
     }
@@ -241,10 +244,22 @@ struct Traverser {
 
     __device__ __forceinline__ void fail(unsigned e) { err |= e; done = true; }
 
+    // the world ray's node-test set-up, kept in shared memory while in an instance
+    __device__ __forceinline__ void save_world() {
+        st.sh[STACK_SH * st.nthreads + st.tid] = make_uint2(__float_as_uint(cr.idx), __float_as_uint(cr.idy));
+        st.sh[(STACK_SH + 1) * st.nthreads + st.tid] = make_uint2(__float_as_uint(cr.idz), cr.oct);
+    }
+    __device__ __forceinline__ void restore_world() {
+        const uint2 a = st.sh[STACK_SH * st.nthreads + st.tid], b = st.sh[(STACK_SH + 1) * st.nthreads + st.tid];
+        cr.ox = o.x; cr.oy = o.y; cr.oz = o.z;
+        cr.idx = __uint_as_float(a.x); cr.idy = __uint_as_float(a.y); cr.idz = __uint_as_float(b.x);
+        cr.oct = b.y;
+    }
+
     // Pops until a node or primitive group is pending; sets done when the ray is finished.
     __device__ __forceinline__ void settle() {
         while (!done && !has_node() && !has_prim()) {
-            if (level == 1 && st.sp == blas_sp) { level = 0; cr = make_node_ray(o, d); }
+            if (level == 1 && st.sp == blas_sp) { level = 0; restore_world(); }
             if (st.sp == 0) { done = true; return; }
             uint2 g = st.pop();
             if (g.x & PRIM_GROUP) tgroup = make_uint2(g.x & ~PRIM_GROUP, g.y);

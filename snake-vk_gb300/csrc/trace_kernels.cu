@@ -92,7 +92,7 @@ struct RayFeed {
 template <bool COUNT, int MINB, bool SINGLE>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uint32_t d) {
     const Knobs kn(F.tune);
-    __shared__ uint2 sh_stack[STACK_SH * TBLK];
+    __shared__ uint2 sh_stack[TRACE_SH_ROWS * TBLK];
     const uint32_t n = F.counters[CNT_QUEUE + d];
     const float4* rays = F.rays[d & 1u];
     uint32_t* work = &F.counters[CNT_WORK_TRACE + d];
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
 template <bool COUNT, int MINB, bool SINGLE>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_shadow(FrameParams F, uint32_t d) {
     const Knobs kn(F.tune_any);
-    __shared__ uint2 sh_stack[STACK_SH * TBLK];
+    __shared__ uint2 sh_stack[TRACE_SH_ROWS * TBLK];
     const uint32_t n0 = F.counters[CNT_SHADOW_Q + 2 * d], n = n0 + F.counters[CNT_SHADOW_Q + 2 * d + 1];
     uint32_t* work = &F.counters[CNT_WORK_SHADOW + d];
     const uint32_t lane = threadIdx.x & 31u;
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_visibility(SceneDev S, con
                                                                  uint32_t n, uint8_t* vis, uint32_t* work,
                                                                  TraceTuning tune) {
     const Knobs kn(tune);
-    __shared__ uint2 sh_stack[STACK_SH * TBLK];
+    __shared__ uint2 sh_stack[TRACE_SH_ROWS * TBLK];
     __shared__ uint32_t ring[TBLK / 32][64];
     const uint32_t lane = threadIdx.x & 31u;
     Traverser<true, false, SINGLE> tv;
@@ -281,7 +281,7 @@ template <bool ANY, bool SINGLE>
 __global__ void __launch_bounds__(TBLK, 6) k_trace_rays(SceneDev S, const float4* __restrict__ rays, uint32_t n,
                                                      HitDev* hits, uint32_t* work, TraceTuning tune) {
     const Knobs kn(tune);
-    __shared__ uint2 sh_stack[STACK_SH * TBLK];
+    __shared__ uint2 sh_stack[TRACE_SH_ROWS * TBLK];
     const uint32_t lane = threadIdx.x & 31u;
     Traverser<ANY, false, SINGLE> tv;
     uint2 spill[STACK_MAX - STACK_SH];
