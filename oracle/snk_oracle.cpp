@@ -295,9 +295,9 @@ static inline WRay wray_setup(V3 o, V3 d, float tmin, float tmax) {
     int ky = kx + 1; if (ky == 3) ky = 0;
     if (r.d[kz] < 0.0f) std::swap(kx, ky);
     r.kx = kx; r.ky = ky; r.kz = kz;
-    r.Sx = r.d[kx] / r.d[kz];
-    r.Sy = r.d[ky] / r.d[kz];
-    r.Sz = 1.0f / r.d[kz];
+    r.Sz = 1.0f / r.d[kz];           // shear constants rounded as d[kx] * (1 / d[kz])
+    r.Sx = r.d[kx] * r.Sz;
+    r.Sy = r.d[ky] * r.Sz;
     r.tmin = tmin; r.tmax = tmax;
     return r;
 }

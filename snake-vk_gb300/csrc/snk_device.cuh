@@ -351,9 +351,18 @@ SNK_HD WRay wray_setup(V3 o, V3 dv) {
     float dx = kx == 0 ? d[0] : (kx == 1 ? d[1] : d[2]);
     float dy = ky == 0 ? d[0] : (ky == 1 ? d[1] : d[2]);
     float dz = kz == 0 ? d[0] : (kz == 1 ? d[1] : d[2]);
-    r.Sx = dx / dz;
-    r.Sy = dy / dz;
+    // one division: the shear constants are dx / dz and dy / dz rounded as
+    // dx * (1 / dz) (any per-ray constants keep the test watertight; the CPU
+    // oracle rounds them the same way)
+#ifdef __CUDA_ARCH__
+    r.Sz = __fdiv_rn(1.0f, dz);
+    r.Sx = __fmul_rn(dx, r.Sz);
+    r.Sy = __fmul_rn(dy, r.Sz);
+#else
     r.Sz = 1.0f / dz;
+    r.Sx = dx * r.Sz;
+    r.Sy = dy * r.Sz;
+#endif
     return r;
 }
 SNK_HD float sel3(const float* a, int k) { return k == 0 ? a[0] : (k == 1 ? a[1] : a[2]); }

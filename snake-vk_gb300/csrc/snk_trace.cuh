@@ -216,7 +216,7 @@ struct Traverser {
     V3 o, d;             // world-space ray
     float tmin, tmax;
     NodeRay cr;          // ray of the current level (world or object space)
-    WRay tr;             // object-space watertight set-up (valid in a BLAS)
+    WRay tr;             // object-space watertight set-up (in a BLAS, once kx >= 0)
     float best_t, best_u, best_v;
     uint32_t best_inst, best_prim;
     uint2 ngroup, tgroup;
@@ -315,7 +315,9 @@ struct Traverser {
             V3 oo = xform_point_rn(inv, o);
             V3 od = xform_dir_rn(inv, d);
             cr = make_node_ray(oo, od);
-            tr = wray_setup(oo, od);
+            // the watertight set-up waits for the instance's first triangle test (many
+            // instances are left without one); until then its shear slots hold the direction
+            tr.kx = -1; tr.Sx = od.x; tr.Sy = od.y; tr.Sz = od.z;
             blas_sp = st.sp;
             level = 1;
             cur_inst = inst;
@@ -324,6 +326,7 @@ struct Traverser {
         } else {
             if (pidx >= S.num_tris) { fail(ERR_BAD_INDEX); return; }
             if (COUNT) ctr->tris++;
+            if (tr.kx < 0) tr = wray_setup(v3(cr.ox, cr.oy, cr.oz), v3(tr.Sx, tr.Sy, tr.Sz));
             const float4* tp = reinterpret_cast<const float4*>(S.tris + pidx);
             float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
             float va[3] = {a.x, a.y, a.z}, vb[3] = {b.x, b.y, b.z}, vc[3] = {c.x, c.y, c.z};
