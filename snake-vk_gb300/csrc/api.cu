@@ -1267,7 +1267,8 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
                 });
             };
             // (the first shading pass wrote the G-buffer and the surface records)
-            cudaError_t e = pass(1, 0, q1, q3);
+            cudaError_t e = pass(1, -1, q1, q3);   // the RIS candidates
+            if (e == cudaSuccess) e = pass(1, 0, q1, q3);
             if (e == cudaSuccess) e = visibility(K1, ctx->rq_vis_a.p, 0);
             if (e == cudaSuccess) e = pass(1, 1, q1, q3);
             if (e == cudaSuccess) e = pass(2, 0, q2, q3);

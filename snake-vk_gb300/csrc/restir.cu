@@ -11,8 +11,9 @@
 //   ComputeAndWriteSpatialReservoirReuse :470-506
 //   CalculateRadianceFromReservoirs .... :508-528, main :530-570
 // dispatched by RT::RecordRenderCmdBuf (Core/src/rendering/Raytracing.cpp:250-263)
-// as two full-screen launches with a barrier between them; here: the
-// initial+temporal kernel and the spatial+shading kernel.  The G-buffer (the reference's raster G-buffer pass, read at :534-555) comes
+// as two full-screen launches with a barrier between them; here: the initial
+// candidates (RIS) kernel, the visibility+temporal kernel and the spatial+shading
+// kernel.  The G-buffer (the reference's raster G-buffer pass, read at :534-555) comes
 // from the wavefront: camera rays through pixel centres traced by the persistent
 // closest-hit kernel, whose first shading pass writes the G-buffer outputs and the
 // surface records these passes read.  In the mode that adds path-traced indirect
@@ -438,6 +439,84 @@ __device__ __forceinline__ void flush_rays(uint32_t n, uint32_t* ctr) {
 // WriteInitialReservoirs: initial RIS + temporal reuse
 // RIS/temporal and spatial passes: 8 resident blocks per SM (64 registers); their
 // light and reservoir loads are latency bound and the extra warps outweigh the spills
+// initial candidates (RayGen.rgen:296-357): resampled importance sampling of
+// 32 point-light and 32 emissive-triangle candidates per surface pixel into the
+// pixel's reservoir, with the candidates' target values and the random stream
+// position after them (what k_restir_initial continues from).  A kernel of its
+// own: it holds no visibility queue or reuse state, so the candidate loops keep
+// their values in registers.
+__global__ void __launch_bounds__(RBLK, 8) k_restir_ris(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs) {
+    const ViewDev& V = F.views[vi];
+    const SceneDev& S = F.S;
+    const uint32_t W = V.v.width, H = V.v.height, n = W * H;
+    // surface pixels are gathered 32 at a time from each warp's pixels (per-warp ring)
+    __shared__ uint32_t ring[RBLK / 32][64];
+    uint32_t* hq = ring[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t head = 0, cnt = 0;
+    for (uint32_t base = blockIdx.x * RBLK + (threadIdx.x & ~31u);; base += gridDim.x * RBLK) {
+        const bool more = base < n;
+        if (more) {
+            const uint32_t o = base + lane;
+            const bool surf = o < n && R.g_pos[o].w == 1.0f;
+            const unsigned sm = __ballot_sync(0xFFFFFFFFu, surf);
+            if (surf) hq[(head + cnt + (uint32_t)__popc(sm & ((1u << lane) - 1u))) & 63u] = o;
+            cnt += (uint32_t)__popc(sm);
+            __syncwarp();
+        }
+        while (cnt >= 32u || (!more && cnt > 0u)) {
+            const uint32_t take = cnt < 32u ? cnt : 32u;
+            const bool have = lane < take;
+            const uint32_t o = have ? hq[(head + lane) & 63u] : 0u;
+            head = (head + take) & 63u;
+            cnt -= take;
+            __syncwarp();
+            if (!have) continue;
+            const float4 gp = R.g_pos[o], gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
+            const Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), v3(gn.x, gn.y, gn.z), v3(ga.x, ga.y, ga.z), ga.w, gm.x);
+            Pcg rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000001u, rs.seed);
+            Reservoir Rr = res_init();
+            float phat_pl = 0.0f, phat_em = 0.0f;
+            const uint32_t npl = S.num_point_lights;
+            if (npl > 0) {
+                for (uint32_t i = 0; i < rs.candidates; i++) {
+                    uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
+                    if (idx > npl - 1) idx = npl - 1;
+                    float p_hat = length(calc_pointlight(S.point_lights[idx], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
+                                                         sh.albedo));
+                    float w = p_hat / (1.0f / (float)npl);
+                    if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
+                }
+            }
+            const uint32_t nem = S.num_emissive_instances;
+            if (nem > 0) {
+                for (uint32_t i = 0; i < rs.candidates; i++) {
+                    uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
+                    if (k > nem - 1) k = nem - 1;
+                    const EmissiveRec* E = S.emissive_recs + k;
+                    const uint32_t inst = E->inst, ntri = E->ntri;
+                    uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
+                    if (tri > ntri - 1) tri = ntri - 1;
+                    float bu = pcg_float(rng), bv = pcg_float(rng);
+                    if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
+                    float area;
+                    V3 rad = rec_candidate(S, E, tri, bu, bv, sh, &area);
+                    float p_hat = length(rad);
+                    float pdf = 1.0f / ((float)(nem * ntri) * area);
+                    float w = p_hat / pdf;
+                    if (update_em(Rr, inst, tri, bu, bv, w, rng)) phat_em = p_hat;
+                }
+            }
+            res_store(R.temporal, o, Rr);
+            R.ris[2ull * o] = make_float4(phat_pl, phat_em, 0.0f, 0.0f);
+            R.ris[2ull * o + 1] =
+                make_float4(__uint_as_float((uint32_t)rng.state), __uint_as_float((uint32_t)(rng.state >> 32)),
+                            __uint_as_float((uint32_t)rng.inc), __uint_as_float((uint32_t)(rng.inc >> 32)));
+        }
+        if (!more) break;
+    }
+}
+
 __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
                                                         RestirQueue q, int phase) {
     const ViewDev& V = F.views[vi];
@@ -487,55 +566,13 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
             float4 gn = R.g_normal[o], ga = R.g_albedo[o], gm = R.g_misc[o];
             V3 nrm = v3(gn.x, gn.y, gn.z);
             Shade sh = shade_of(V.v, v3(gp.x, gp.y, gp.z), nrm, v3(ga.x, ga.y, ga.z), ga.w, gm.x);
+            // the RIS result of k_restir_ris: reservoir, target values and stream position
+            Reservoir Rr = res_load(R.temporal, o);
+            const float4 ra = R.ris[2ull * o], rb = R.ris[2ull * o + 1];
+            const float phat_pl = ra.x, phat_em = ra.y;
             Pcg rng;
-            Reservoir Rr;
-            float phat_pl = 0.0f, phat_em = 0.0f;
-            if (!record) {
-                // the RIS result of the recording run: reservoir, target values and stream position
-                Rr = res_load(R.temporal, o);
-                const float4 a = R.ris[2ull * o], b = R.ris[2ull * o + 1];
-                phat_pl = a.x; phat_em = a.y;
-                rng.state = ((uint64_t)__float_as_uint(b.y) << 32) | __float_as_uint(b.x);
-                rng.inc = ((uint64_t)__float_as_uint(b.w) << 32) | __float_as_uint(b.z);
-            } else {
-                rng = pcg_stream(V.pixel_offset + o, rs.frame_index, 0x80000001u, rs.seed);
-                Rr = res_init();
-                const uint32_t npl = S.num_point_lights;
-                if (npl > 0) {
-                    for (uint32_t i = 0; i < rs.candidates; i++) {
-                        uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
-                        if (idx > npl - 1) idx = npl - 1;
-                        float p_hat = length(calc_pointlight(S.point_lights[idx], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
-                                                             sh.albedo));
-                        float w = p_hat / (1.0f / (float)npl);
-                        if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
-                    }
-                }
-                const uint32_t nem = S.num_emissive_instances;
-                if (nem > 0) {
-                    for (uint32_t i = 0; i < rs.candidates; i++) {
-                        uint32_t k = (uint32_t)(pcg_float(rng) * (float)nem);
-                        if (k > nem - 1) k = nem - 1;
-                        const EmissiveRec* E = S.emissive_recs + k;
-                        const uint32_t inst = E->inst, ntri = E->ntri;
-                        uint32_t tri = (uint32_t)(pcg_float(rng) * (float)ntri);
-                        if (tri > ntri - 1) tri = ntri - 1;
-                        float bu = pcg_float(rng), bv = pcg_float(rng);
-                        if (bu + bv >= 1.0f) { bu = 1.0f - bu; bv = 1.0f - bv; }
-                        float area;
-                        V3 rad = rec_candidate(S, E, tri, bu, bv, sh, &area);
-                        float p_hat = length(rad);
-                        float pdf = 1.0f / ((float)(nem * ntri) * area);
-                        float w = p_hat / pdf;
-                        if (update_em(Rr, inst, tri, bu, bv, w, rng)) phat_em = p_hat;
-                    }
-                }
-                res_store(R.temporal, o, Rr);
-                R.ris[2ull * o] = make_float4(phat_pl, phat_em, 0.0f, 0.0f);
-                R.ris[2ull * o + 1] =
-                    make_float4(__uint_as_float((uint32_t)rng.state), __uint_as_float((uint32_t)(rng.state >> 32)),
-                                __uint_as_float((uint32_t)rng.inc), __uint_as_float((uint32_t)(rng.inc >> 32)));
-            }
+            rng.state = ((uint64_t)__float_as_uint(rb.y) << 32) | __float_as_uint(rb.x);
+            rng.inc = ((uint64_t)__float_as_uint(rb.w) << 32) | __float_as_uint(rb.z);
             if (Rr.pl_idx != INVALID) {
                 V3 lp = load3(S.point_lights[Rr.pl_idx].pos);
                 float dist = length(sub(lp, sh.biased));
@@ -784,7 +821,8 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
 cudaError_t launch_restir_stage(int stage, int phase, const FrameParams& F, uint32_t vi, const RestirView& R,
                                 const RestirSettings& rs, const RestirQueue& q, const RestirQueue& qs, int grid,
                                 cudaStream_t s) {
-    if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, phase);
+    if (stage == 1 && phase < 0) k_restir_ris<<<grid, RBLK, 0, s>>>(F, vi, R, rs);
+    else if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, phase);
     else if (stage == 2) k_restir_spatial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs, phase);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
