@@ -292,9 +292,9 @@ struct DirLightDev { float dir[3]; uint32_t enabled; float colour[3]; float pad;
 constexpr uint32_t MAX_TRAVERSAL_STEPS = 1u << 16;
 constexpr int STACK_SH = 8;
 // rows of a traversal kernel's shared array per thread: the STACK_SH stack
-// entries, then two rows that keep the world ray's reciprocal direction and
-// octant while the ray is inside an instance
-constexpr int TRACE_SH_ROWS = STACK_SH + 2;
+// entries, then five rows that keep the world ray (origin, direction,
+// reciprocal direction and octant) while it is traced
+constexpr int TRACE_SH_ROWS = STACK_SH + 5;
 constexpr int STACK_MAX = 64;
 
 // device pointers of the whole scene, passed by value to kernels
@@ -332,14 +332,14 @@ struct SceneDev {
 // --------------------------------------------------------------------------
 // watertight ray/triangle test
 // --------------------------------------------------------------------------
+// The per-ray set-up: the axis permutation packed as kx | ky << 2 | kz << 4 (k) and
+// the shear constants; the ray origin is passed to the test separately.
 struct WRay {
-    float o[3];
-    int kx, ky, kz;
+    uint32_t k;
     float Sx, Sy, Sz;
 };
-SNK_HD WRay wray_setup(V3 o, V3 dv) {
+SNK_HD WRay wray_setup(V3 dv) {
     WRay r;
-    r.o[0] = o.x; r.o[1] = o.y; r.o[2] = o.z;
     float d[3] = {dv.x, dv.y, dv.z};
     int kz = 0;
     if (fabsf(d[1]) > fabsf(d[0])) kz = 1;
@@ -347,7 +347,7 @@ SNK_HD WRay wray_setup(V3 o, V3 dv) {
     int kx = kz + 1; if (kx == 3) kx = 0;
     int ky = kx + 1; if (ky == 3) ky = 0;
     if (d[kz] < 0.0f) { int t = kx; kx = ky; ky = t; }
-    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4);
     float dx = kx == 0 ? d[0] : (kx == 1 ? d[1] : d[2]);
     float dy = ky == 0 ? d[0] : (ky == 1 ? d[1] : d[2]);
     float dz = kz == 0 ? d[0] : (kz == 1 ? d[1] : d[2]);
@@ -368,8 +368,8 @@ SNK_HD WRay wray_setup(V3 o, V3 dv) {
 SNK_HD float sel3(const float* a, int k) { return k == 0 ? a[0] : (k == 1 ? a[1] : a[2]); }
 // Returns true for a hit with tmin < t < tmax; exact binary32 arithmetic via
 // _rn intrinsics on the device (so the result does not depend on --fmad).
-SNK_HD bool intersect_tri(const WRay& r, const float* v0, const float* v1, const float* v2, float tmin, float tmax,
-                          float* t_out, float* b1_out, float* b2_out) {
+SNK_HD bool intersect_tri(const WRay& r, V3 org, const float* v0, const float* v1, const float* v2, float tmin,
+                          float tmax, float* t_out, float* b1_out, float* b2_out) {
 #ifdef __CUDA_ARCH__
 #define SNK_SUB __fsub_rn
 #define SNK_MUL __fmul_rn
@@ -381,12 +381,13 @@ SNK_HD bool intersect_tri(const WRay& r, const float* v0, const float* v1, const
 #define SNK_ADD(a, b) ((a) + (b))
 #define SNK_DIV(a, b) ((a) / (b))
 #endif
-    float A[3] = {SNK_SUB(v0[0], r.o[0]), SNK_SUB(v0[1], r.o[1]), SNK_SUB(v0[2], r.o[2])};
-    float B[3] = {SNK_SUB(v1[0], r.o[0]), SNK_SUB(v1[1], r.o[1]), SNK_SUB(v1[2], r.o[2])};
-    float C[3] = {SNK_SUB(v2[0], r.o[0]), SNK_SUB(v2[1], r.o[1]), SNK_SUB(v2[2], r.o[2])};
-    float Akx = sel3(A, r.kx), Aky = sel3(A, r.ky), Akz = sel3(A, r.kz);
-    float Bkx = sel3(B, r.kx), Bky = sel3(B, r.ky), Bkz = sel3(B, r.kz);
-    float Ckx = sel3(C, r.kx), Cky = sel3(C, r.ky), Ckz = sel3(C, r.kz);
+    float A[3] = {SNK_SUB(v0[0], org.x), SNK_SUB(v0[1], org.y), SNK_SUB(v0[2], org.z)};
+    float B[3] = {SNK_SUB(v1[0], org.x), SNK_SUB(v1[1], org.y), SNK_SUB(v1[2], org.z)};
+    float C[3] = {SNK_SUB(v2[0], org.x), SNK_SUB(v2[1], org.y), SNK_SUB(v2[2], org.z)};
+    const int kx = (int)(r.k & 3u), ky = (int)((r.k >> 2) & 3u), kz = (int)(r.k >> 4);
+    float Akx = sel3(A, kx), Aky = sel3(A, ky), Akz = sel3(A, kz);
+    float Bkx = sel3(B, kx), Bky = sel3(B, ky), Bkz = sel3(B, kz);
+    float Ckx = sel3(C, kx), Cky = sel3(C, ky), Ckz = sel3(C, kz);
     float Ax = SNK_SUB(Akx, SNK_MUL(r.Sx, Akz)), Ay = SNK_SUB(Aky, SNK_MUL(r.Sy, Akz));
     float Bx = SNK_SUB(Bkx, SNK_MUL(r.Sx, Bkz)), By = SNK_SUB(Bky, SNK_MUL(r.Sy, Bkz));
     float Cx = SNK_SUB(Ckx, SNK_MUL(r.Sx, Ckz)), Cy = SNK_SUB(Cky, SNK_MUL(r.Sy, Ckz));

@@ -179,8 +179,7 @@ struct TraceCounters { unsigned long long nodes, tris; };
 
 // Short stack: entries [0, STACK_SH) live in shared memory at sh[k * nthreads + tid],
 // deeper entries in a local array; at most lim (<= STACK_MAX) entries.  Rows
-// STACK_SH and STACK_SH + 1 of sh (TRACE_SH_ROWS rows in all) keep the world ray's
-// node-test reciprocals while the ray is in an instance.
+// STACK_SH .. STACK_SH + 4 of sh (TRACE_SH_ROWS rows in all) keep the world ray.
 struct ShortStack {
     uint2* sh;
     uint2* spill;   // STACK_MAX - STACK_SH entries (a local array of the caller)
@@ -213,10 +212,9 @@ template <bool ANY, bool COUNT, bool SINGLE = false>
 struct Traverser {
     static constexpr bool ORD = !ANY;   // visit children front to back (closest hit only)
     static constexpr uint32_t PTHR = SINGLE ? 0x00FFFFFFu : 0u;   // a primitive group is pending above this
-    V3 o, d;             // world-space ray
-    float tmin, tmax;
+    float tmin, tmax;    // (the world-space ray itself is kept in shared memory: save_world)
     NodeRay cr;          // ray of the current level (world or object space)
-    WRay tr;             // object-space watertight set-up (in a BLAS, once kx >= 0)
+    WRay tr;             // object-space watertight set-up (in a BLAS, once k != INVALID)
     float best_t, best_u, best_v;
     uint32_t best_inst, best_prim;
     uint2 ngroup, tgroup;
@@ -228,13 +226,13 @@ struct Traverser {
 
     __device__ __forceinline__ void init(const SceneDev& S, V3 o_, V3 d_, float tmin_, float tmax_, uint2* sh,
                                          uint2* spill, uint32_t tid, uint32_t nthreads) {
-        o = o_; d = d_; tmin = fmaxf(tmin_, 0.0f); tmax = tmax_;
-        cr = make_node_ray(o, d);
+        tmin = fmaxf(tmin_, 0.0f); tmax = tmax_;
+        cr = make_node_ray(o_, d_);
         best_t = tmax; best_u = 0.0f; best_v = 0.0f; best_inst = INVALID; best_prim = INVALID;
         level = 0; blas_sp = 0; cur_inst = 0; steps = 0; err = 0; done = false;
         st.sh = sh; st.spill = spill; st.tid = tid; st.nthreads = nthreads; st.sp = 0;
         st.lim = S.stack_max < STACK_MAX ? S.stack_max : STACK_MAX;
-        save_world();
+        save_world(d_);
         ngroup = S.tlas_root == INVALID ? make_uint2(0u, 0u) : make_uint2(S.tlas_root, (1u << (24 + (ORD ? cr.oct : 0u))) | 1u);
         tgroup = make_uint2(0u, 0u);
     }
@@ -244,16 +242,27 @@ struct Traverser {
 
     __device__ __forceinline__ void fail(unsigned e) { err |= e; done = true; }
 
-    // the world ray's node-test set-up, kept in shared memory while in an instance
-    __device__ __forceinline__ void save_world() {
-        st.sh[STACK_SH * st.nthreads + st.tid] = make_uint2(__float_as_uint(cr.idx), __float_as_uint(cr.idy));
-        st.sh[(STACK_SH + 1) * st.nthreads + st.tid] = make_uint2(__float_as_uint(cr.idz), cr.oct);
+    // the world ray (origin, direction) and its node-test set-up, kept in shared
+    // memory rows STACK_SH .. STACK_SH + 4 of this thread: read when the ray enters an
+    // instance and when it leaves one
+    __device__ __forceinline__ uint2& row(int k) const { return st.sh[(STACK_SH + k) * st.nthreads + st.tid]; }
+    __device__ __forceinline__ void save_world(V3 d) {
+        row(0) = make_uint2(__float_as_uint(cr.idx), __float_as_uint(cr.idy));
+        row(1) = make_uint2(__float_as_uint(cr.idz), cr.oct);
+        row(2) = make_uint2(__float_as_uint(cr.ox), __float_as_uint(cr.oy));
+        row(3) = make_uint2(__float_as_uint(cr.oz), __float_as_uint(d.x));
+        row(4) = make_uint2(__float_as_uint(d.y), __float_as_uint(d.z));
     }
     __device__ __forceinline__ void restore_world() {
-        const uint2 a = st.sh[STACK_SH * st.nthreads + st.tid], b = st.sh[(STACK_SH + 1) * st.nthreads + st.tid];
-        cr.ox = o.x; cr.oy = o.y; cr.oz = o.z;
+        const uint2 a = row(0), b = row(1), c = row(2), e = row(3);
+        cr.ox = __uint_as_float(c.x); cr.oy = __uint_as_float(c.y); cr.oz = __uint_as_float(e.x);
         cr.idx = __uint_as_float(a.x); cr.idy = __uint_as_float(a.y); cr.idz = __uint_as_float(b.x);
         cr.oct = b.y;
+    }
+    __device__ __forceinline__ void world_ray(V3& o, V3& d) const {
+        const uint2 c = row(2), e = row(3), f = row(4);
+        o = v3(__uint_as_float(c.x), __uint_as_float(c.y), __uint_as_float(e.x));
+        d = v3(__uint_as_float(e.y), __uint_as_float(f.x), __uint_as_float(f.y));
     }
 
     // Pops until a node or primitive group is pending; sets done when the ray is finished.
@@ -312,12 +321,14 @@ struct Traverser {
             float4 r0 = __ldg(ip), r1 = __ldg(ip + 1), r2 = __ldg(ip + 2);
             uint32_t root = __ldg(reinterpret_cast<const uint32_t*>(ip + 3));
             float inv[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+            V3 o, d;
+            world_ray(o, d);
             V3 oo = xform_point_rn(inv, o);
             V3 od = xform_dir_rn(inv, d);
             cr = make_node_ray(oo, od);
             // the watertight set-up waits for the instance's first triangle test (many
             // instances are left without one); until then its shear slots hold the direction
-            tr.kx = -1; tr.Sx = od.x; tr.Sy = od.y; tr.Sz = od.z;
+            tr.k = INVALID; tr.Sx = od.x; tr.Sy = od.y; tr.Sz = od.z;
             blas_sp = st.sp;
             level = 1;
             cur_inst = inst;
@@ -326,12 +337,12 @@ struct Traverser {
         } else {
             if (pidx >= S.num_tris) { fail(ERR_BAD_INDEX); return; }
             if (COUNT) ctr->tris++;
-            if (tr.kx < 0) tr = wray_setup(v3(cr.ox, cr.oy, cr.oz), v3(tr.Sx, tr.Sy, tr.Sz));
+            if (tr.k == INVALID) tr = wray_setup(v3(tr.Sx, tr.Sy, tr.Sz));
             const float4* tp = reinterpret_cast<const float4*>(S.tris + pidx);
             float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
             float va[3] = {a.x, a.y, a.z}, vb[3] = {b.x, b.y, b.z}, vc[3] = {c.x, c.y, c.z};
             float t, b1, b2;
-            if (intersect_tri(tr, va, vb, vc, tmin, tmax, &t, &b1, &b2)) {
+            if (intersect_tri(tr, v3(cr.ox, cr.oy, cr.oz), va, vb, vc, tmin, tmax, &t, &b1, &b2)) {
                 uint32_t prim = __float_as_uint(a.w);
                 bool better = best_inst == INVALID || t < best_t ||
                               (t == best_t && (cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)));
