@@ -105,6 +105,7 @@ __device__ __forceinline__ void write_gbuffer_miss(const ViewDev& V, uint32_t o)
 // time, so the surface shading runs with full warps even when most rays of a
 // bounce leave the scene.  Every output is indexed by queue entry or path, so
 // the order in which entries are shaded does not change any result.
+template <bool CACHE, bool FIRST>   // the MLP cache is on; FIRST (camera rays: G-buffer, emission)
 __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
     __shared__ uint32_t ring[BLK / 32][64];
     const uint32_t cur = d & 1u, nxt = cur ^ 1u;
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 if (!hit) {   // no shadow rays: zero contributions
                     F.shadow_contrib[shadow_entry(F, i, 0)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     F.shadow_contrib[shadow_entry(F, i, 1)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (d == 0) {
+                    if (FIRST) {
                         uint32_t gpix, s, vi, x, y;
                         const bool train = decode_path(F, F.path_ids[cur][i], &gpix, &s, &vi, &x, &y);
                         if (s == 0 && !train) {
@@ -166,8 +167,8 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 V3 rd = v3(rd4.x, rd4.y, rd4.z);
                 HitDev h = F.hits[i];
                 Pcg rng = pcg_stream(gpix, s, d, frame_seed(F));
-                if (d == 0) { pcg_next(rng); pcg_next(rng); }
-                const bool gbuf = d == 0 && s == 0 && !train;
+                if (FIRST) { pcg_next(rng); pcg_next(rng); }
+                const bool gbuf = FIRST && s == 0 && !train;
                 {   // a hit (misses ended in the first pass)
                     Surface sf = surface_at(S, h.inst, h.prim, h.u, h.v, rd);
                     if (gbuf) {
@@ -176,23 +177,23 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         if (V.rs_pos) write_restir_surface(V, o, sf, mo);
                     }
                     // indirect mode: ReSTIR DI shades the primary vertex (no emission, no NEE here)
-                    const bool direct = !(F.indirect && d == 0);
+                    const bool direct = !(F.indirect && FIRST);
                     float u_sel = pcg_float(rng), u1 = pcg_float(rng), u2 = pcg_float(rng);
                     float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
                     float u_lobe = pcg_float(rng);
                     float4 b4 = F.beta[p];
                     V3 beta = v3(b4.x, b4.y, b4.z);
                     bool to_cache = false;
-                    if (F.cache) {
+                    if (CACHE) {
                         // path spread (Mueller et al. 2021): a0 = t^2 / (4 pi cos) at the primary
                         // vertex; later vertices add sqrt(t^2 / (pdf cos)); the path is handed
                         // to the cache once spread^2 > c a0
                         float2 sp = F.spread[p];
                         const float cosv = fmax_(fabsf(dot(sf.n, rd)), 1e-6f);
-                        if (d == 0) sp = make_float2((h.t * h.t) / ((4.0f * PI) * cosv), 0.0f);
+                        if (FIRST) sp = make_float2((h.t * h.t) / ((4.0f * PI) * cosv), 0.0f);
                         else sp.y = sp.y + sqrtf((h.t * h.t) / (fmax_(b4.w, 1e-6f) * cosv));
                         F.spread[p] = sp;
-                        to_cache = !train && d >= 1 && !(sf.flags & MAT_EMISSIVE) && (sp.y * sp.y > F.spread_c * sp.x);
+                        to_cache = !train && !FIRST && !(sf.flags & MAT_EMISSIVE) && (sp.y * sp.y > F.spread_c * sp.x);
                         if (train && d < TRAIN_V && !(sf.flags & MAT_EMISSIVE)) {
                             const uint32_t slot = (p - F.n_render) * TRAIN_V + d;
                             float4* r = F.train_rec + 4ull * slot;
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                         qb = make_float4(beta.x, beta.y, beta.z, 0.0f);
                         query = true;
                     } else if (sf.flags & MAT_EMISSIVE) {
-                        if (d == 0 && direct) {
+                        if (FIRST && direct) {
                             float4 l4 = F.L[p];
                             V3 Lp = add(v3(l4.x, l4.y, l4.z), cmul(beta, sf.albedo));
                             F.L[p] = make_float4(Lp.x, Lp.y, Lp.z, 0.0f);
@@ -296,7 +297,7 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 F.shadow_rays[2 * e] = make_float4(so.x, so.y, so.z, __uint_as_float((uint32_t)shadow_entry(F, i, 1)));
                 F.shadow_rays[2 * e + 1] = sd1;
             }
-            if (F.cache) {
+            if (CACHE) {
                 const unsigned qm = __ballot_sync(full, query);
                 uint32_t qbase = 0;
                 if (lane == 0 && qm) qbase = atomicAdd(&F.counters[CNT_CACHE_QUERIES], (uint32_t)__popc(qm));
@@ -373,7 +374,14 @@ cudaError_t launch_generate(const FrameParams& F, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 cudaError_t launch_shade(const FrameParams& F, uint32_t depth, int grid, cudaStream_t s) {
-    k_shade<<<grid, BLK, 0, s>>>(F, depth);
+    const bool cache = F.cache != 0, first = depth == 0;
+    if (cache) {
+        if (first) k_shade<true, true><<<grid, BLK, 0, s>>>(F, depth);
+        else k_shade<true, false><<<grid, BLK, 0, s>>>(F, depth);
+    } else {
+        if (first) k_shade<false, true><<<grid, BLK, 0, s>>>(F, depth);
+        else k_shade<false, false><<<grid, BLK, 0, s>>>(F, depth);
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_resolve(const FrameParams& F, int grid, cudaStream_t s) {
