@@ -517,8 +517,10 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_ris(FrameParams F, uint32_t 
     }
 }
 
+template <int PHASE>
 __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
-                                                        RestirQueue q, int phase) {
+                                                        RestirQueue q) {
+    constexpr int phase = PHASE;
     const ViewDev& V = F.views[vi];
     const SceneDev& S = F.S;
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
@@ -642,8 +644,10 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint3
 // phase 0: record q (sun ray, combine rays); phase 1: replay q, write the spatial
 // reservoirs, record qs (final shading rays); phase 2: replay q's sun ray and qs,
 // write radiance, the FP64 accumulator and the next frame's history normals.
+template <int PHASE>
 __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
-                                                        RestirQueue q, RestirQueue qs, int phase) {
+                                                        RestirQueue q, RestirQueue qs) {
+    constexpr int phase = PHASE;
     const ViewDev& V = F.views[vi];
     const SceneDev& S = F.S;
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
@@ -821,9 +825,13 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_spatial(FrameParams F, uint3
 cudaError_t launch_restir_stage(int stage, int phase, const FrameParams& F, uint32_t vi, const RestirView& R,
                                 const RestirSettings& rs, const RestirQueue& q, const RestirQueue& qs, int grid,
                                 cudaStream_t s) {
+    // (one kernel per phase: each keeps only its own phase's paths)
     if (stage == 1 && phase < 0) k_restir_ris<<<grid, RBLK, 0, s>>>(F, vi, R, rs);
-    else if (stage == 1) k_restir_initial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, phase);
-    else if (stage == 2) k_restir_spatial<<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs, phase);
+    else if (stage == 1 && phase == 0) k_restir_initial<0><<<grid, RBLK, 0, s>>>(F, vi, R, rs, q);
+    else if (stage == 1 && phase == 1) k_restir_initial<1><<<grid, RBLK, 0, s>>>(F, vi, R, rs, q);
+    else if (stage == 2 && phase == 0) k_restir_spatial<0><<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs);
+    else if (stage == 2 && phase == 1) k_restir_spatial<1><<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs);
+    else if (stage == 2 && phase == 2) k_restir_spatial<2><<<grid, RBLK, 0, s>>>(F, vi, R, rs, q, qs);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
