@@ -132,7 +132,7 @@ __device__ __forceinline__ void ctx_close(Ctx& c) {
 
 // 1 when the segment is unoccluded (recording: always 1, the value is not used
 // for anything the replay would see differently)
-__device__ __noinline__ float shadow_test(Ctx& c, V3 o, V3 d, float tmax) {
+__device__ __forceinline__ float shadow_test(Ctx& c, V3 o, V3 d, float tmax) {
     if (c.k >= c.cap) { c.overflow = true; return 0.0f; }
     const size_t slot = c.base + (size_t)c.k++ * c.stride;
     if (c.rays) {
@@ -154,7 +154,7 @@ __device__ __forceinline__ float memo_answer(Ctx& c, uint32_t code) {
 
 // shadow test toward point light idx at its full distance (minus == false) or at
 // distance - 0.001, reusing an identical earlier test of this pixel
-__device__ __noinline__ float shadow_test_pl(Ctx& c, uint32_t idx, bool minus, V3 o, V3 d, float tmax) {
+__device__ __forceinline__ float shadow_test_pl(Ctx& c, uint32_t idx, bool minus, V3 o, V3 d, float tmax) {
     Memo* m = c.m;
     if (m) {
         if (!minus && m->pla_idx == idx) return memo_answer(c, m->pla_code);
@@ -173,7 +173,7 @@ __device__ __noinline__ float shadow_test_pl(Ctx& c, uint32_t idx, bool minus, V
 }
 
 // shadow test toward an emissive sample, reusing an identical earlier test of this pixel
-__device__ __noinline__ float shadow_test_em(Ctx& c, uint4 key, V3 o, V3 d, float tmax) {
+__device__ __forceinline__ float shadow_test_em(Ctx& c, uint4 key, V3 o, V3 d, float tmax) {
     Memo* m = c.m;
     if (m)
         for (uint32_t j = 0; j < m->n_em; j++) {
@@ -313,7 +313,7 @@ __device__ __forceinline__ V3 emitted_at(const SceneDev& S, uint32_t inst, V3 p,
 // The unshadowed radiance of sample (bu, bv) of the triangle and, when asked
 // for, the triangle's world-space area (det(mat3) x object area), from one fetch
 // of its vertices (the sample's normal is not needed: no shadow ray is aimed)
-__device__ __noinline__ V3 tri_candidate(const SceneDev& S, uint32_t inst, uint32_t tri, float bu, float bv,
+__device__ __forceinline__ V3 tri_candidate(const SceneDev& S, uint32_t inst, uint32_t tri, float bu, float bv,
                                          const Shade& sh, float* area) {
     const InstShade& I = S.inst_shade[inst];
     const MeshInfo& M = S.meshes[I.mesh_id];
@@ -350,7 +350,7 @@ __device__ __noinline__ V3 rec_candidate(const SceneDev& S, const EmissiveRec* E
               ((em.z * sh.albedo.z) * brdf.z) / d2);
 }
 
-__device__ __noinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, const Shade& sh,
+__device__ __forceinline__ V3 tri_radiance(Ctx& c, uint32_t inst, uint32_t tri, float bu, float bv, const Shade& sh,
                                         bool shadow, V3* unshadowed = nullptr) {
     const SceneDev& S = *c.S;
     V3 p, pn;
@@ -378,7 +378,7 @@ struct ComboSlots {
     bool fill, use;
 };
 
-__device__ __noinline__ void combine(Ctx& c, Reservoir& cur, const Reservoir& nb, float& phat_pl, float& phat_em,
+__device__ __forceinline__ void combine(Ctx& c, Reservoir& cur, const Reservoir& nb, float& phat_pl, float& phat_em,
                                      const Shade& sh, Pcg& rng, ComboSlots& cs) {
     const SceneDev& S = *c.S;
     float4* slot = (cs.p && cs.j < cs.cap) ? cs.p + cs.j * cs.stride : nullptr;
@@ -436,9 +436,12 @@ __device__ __forceinline__ void flush_rays(uint32_t n, uint32_t* ctr) {
     if ((threadIdx.x & 31u) == 0 && n) atomicAdd(ctr, n);
 }
 
-// WriteInitialReservoirs: initial RIS + temporal reuse
-// RIS/temporal and spatial passes: 8 resident blocks per SM (64 registers); their
-// light and reservoir loads are latency bound and the extra warps outweigh the spills
+// The reservoir passes run 8 resident blocks per SM (64 registers): their light
+// and reservoir loads are latency bound and the extra warps outweigh the spills.
+// Their helpers (visibility tests, combines, triangle radiance) are inlined: a call
+// would keep the per-pixel context, memo and shading state it takes by reference
+// in local memory (a kilobyte per thread, which L1 cannot hold for 32 warps).
+
 // initial candidates (RayGen.rgen:296-357): resampled importance sampling of
 // 32 point-light and 32 emissive-triangle candidates per surface pixel into the
 // pixel's reservoir, with the candidates' target values and the random stream
@@ -451,6 +454,9 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_ris(FrameParams F, uint32_t 
     const uint32_t W = V.v.width, H = V.v.height, n = W * H;
     // surface pixels are gathered 32 at a time from each warp's pixels (per-warp ring)
     __shared__ uint32_t ring[RBLK / 32][64];
+    // the point lights' target values of each thread's pixel (scenes of up to 16 lights)
+    constexpr uint32_t RIS_PL_TABLE = 16;
+    __shared__ float pl_table[RIS_PL_TABLE * RBLK];
     uint32_t* hq = ring[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t head = 0, cnt = 0;
@@ -478,7 +484,21 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_ris(FrameParams F, uint32_t 
             Reservoir Rr = res_init();
             float phat_pl = 0.0f, phat_em = 0.0f;
             const uint32_t npl = S.num_point_lights;
-            if (npl > 0) {
+            if (npl > 0 && npl <= RIS_PL_TABLE && npl < rs.candidates) {
+                // every light's target value once, then the candidates look theirs up (the
+                // same values: the target is a function of the light and the surface)
+                float* ph = pl_table + threadIdx.x;
+                for (uint32_t l = 0; l < npl; l++)
+                    ph[l * RBLK] = length(calc_pointlight(S.point_lights[l], sh.v, sh.f0, sh.ro, sh.n, sh.rough, sh.metal,
+                                                          sh.albedo));
+                for (uint32_t i = 0; i < rs.candidates; i++) {
+                    uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
+                    if (idx > npl - 1) idx = npl - 1;
+                    const float p_hat = ph[idx * RBLK];
+                    float w = p_hat / (1.0f / (float)npl);
+                    if (update_pl(Rr, idx, w, rng)) phat_pl = p_hat;
+                }
+            } else if (npl > 0) {
                 for (uint32_t i = 0; i < rs.candidates; i++) {
                     uint32_t idx = (uint32_t)(pcg_float(rng) * (float)npl);
                     if (idx > npl - 1) idx = npl - 1;
@@ -517,6 +537,9 @@ __global__ void __launch_bounds__(RBLK, 8) k_restir_ris(FrameParams F, uint32_t 
     }
 }
 
+// WriteInitialReservoirs after the candidates of k_restir_ris: the visibility of
+// the RIS samples, then temporal reuse; phase 0 records the visibility rays,
+// phase 1 replays their results and writes the temporal reservoirs
 template <int PHASE>
 __global__ void __launch_bounds__(RBLK, 8) k_restir_initial(FrameParams F, uint32_t vi, RestirView R, RestirSettings rs,
                                                         RestirQueue q) {
