@@ -681,8 +681,10 @@ def run_ours(args):
             line["cpu_baseline"] = cpu_baseline(sc, view, settings(1, 0))
         line["taa"] = taa_bench(snkpt, dev, stream)
         line["particles"] = particle_bench(pt, abi, sc, dev)
-        line["restir"] = restir_bench(snkpt, abi, scenes, dev, stream, tuning)
-        line["restir_pt"] = restir_bench(snkpt, abi, scenes, dev, stream, tuning, mode=abi.MODE_RESTIR_PT)
+        # (the ReSTIR frames use the default launch knobs: the autotuned ones are the
+        # path-tracing frame's, and its visibility queues trace best at the defaults)
+        line["restir"] = restir_bench(snkpt, abi, scenes, dev, stream, None)
+        line["restir_pt"] = restir_bench(snkpt, abi, scenes, dev, stream, None, mode=abi.MODE_RESTIR_PT)
         line["bvh_build"] = bvh_bench(snkpt, scenes, dev, stream)
         if not args.no_batched:
             line["batched_views"] = batched_views(snkpt, abi, scenes, dev, stream, tuning)

@@ -1062,6 +1062,11 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
 
     {
         if (!path_like) F.indirect = 1;   // ReSTIR shades the primary vertex
+        // (host outputs keep the resolve pass: its coalesced writes to page-locked host
+        // memory beat the scattered writes of paths as they end)
+        bool host_out = false;
+        for (uint32_t v = 0; v < num_views; v++) host_out = host_out || outputs[v].memory == SNK_MEM_HOST;
+        F.early_resolve = (path_like && !cache && spp == 1u && !host_out) ? 1u : 0u;
         if (restir_pt) {
             if (ctx->indirect.reserve(n_pixels) != cudaSuccess)
                 return fail(ctx, SNK_ERR_OUT_OF_MEMORY, "render: indirect light buffer");
@@ -1173,7 +1178,7 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
                 return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
             });
         }
-        if (e == cudaSuccess && !restir_di)
+        if (e == cudaSuccess && !restir_di && !F.early_resolve)
             e = staged(ctx, profile, SNK_STAGE_RESOLVE, [&] { return launch_resolve(F, g8, st); });
         if (cache && e == cudaSuccess) {
             e = staged(ctx, profile, SNK_STAGE_CACHE_SAMPLES, [&] { return launch_make_samples(F, g8, st); });

@@ -135,6 +135,8 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                             if (V.rs_pos) write_restir_miss(V, y * V.v.width + x);
                         }
                     }
+                    // the path ends here (after the G-buffer above has decoded its id)
+                    if (F.early_resolve) F.path_ids[cur][i] |= 0x80000000u;
                 }
             }
             const unsigned hm = __ballot_sync(0xFFFFFFFFu, hit);
@@ -286,6 +288,8 @@ __global__ void __launch_bounds__(BLK, 4) k_shade(FrameParams F, uint32_t d) {
                 F.rays[nxt][2ull * j] = nr0;
                 F.rays[nxt][2ull * j + 1] = nr1;
                 F.path_ids[nxt][j] = p;
+            } else if (have && F.early_resolve) {
+                F.path_ids[cur][i] = p | 0x80000000u;   // the path ends in this segment
             }
             if (sv0) {   // (the origin's w carries the bits of the contribution entry)
                 const size_t e = b0 + (uint32_t)__popc(m0 & lt);

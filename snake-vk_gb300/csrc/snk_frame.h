@@ -69,6 +69,11 @@ struct FrameParams {
     // instead of the views' radiance outputs
     uint32_t indirect;
     float4* indirect_out;
+    // one sample per pixel and no cache or indirect mode: a path's radiance is final
+    // once the segment it ends in has added its shadow-ray contributions, so
+    // k_shade marks the queue entries whose path ends (bit 31 of the path id) and
+    // k_accum_shadow writes those pixels' outputs; no resolve pass follows
+    uint32_t early_resolve;
     // per-frame values in device memory (seed, frame, accumulate), read by the kernels
     // instead of the fields above when set, so that a captured frame replays for new
     // values of them

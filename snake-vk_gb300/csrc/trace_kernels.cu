@@ -10,6 +10,7 @@
 // local spill.
 #include "snk_frame.h"
 #include "snk_trace.cuh"
+#include "snk_shade.cuh"
 
 namespace snk {
 namespace {
@@ -187,11 +188,35 @@ __global__ void __launch_bounds__(256) k_accum_shadow(FrameParams F, uint32_t d)
     const uint32_t* pids = F.path_ids[d & 1u];
     for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
         float4 c0 = F.shadow_contrib[shadow_entry(F, i, 0)], c1 = F.shadow_contrib[shadow_entry(F, i, 1)];
-        if (c0.w == 0.0f && c1.w == 0.0f) continue;
-        uint32_t p = pids[i];
+        const bool add = c0.w != 0.0f || c1.w != 0.0f;
+        uint32_t p = 0;
+        bool fin = false;   // (early resolve) the path ends in this segment
+        if (F.early_resolve) {
+            const uint32_t raw = pids[i];
+            p = raw & 0x7FFFFFFFu;
+            fin = (raw >> 31) != 0u;
+        } else {
+            if (!add) continue;
+            p = pids[i];
+        }
+        if (!add && !fin) continue;
         float4 l = F.L[p];
         if (c0.w != 0.0f) l = make_float4(l.x + c0.x, l.y + c0.y, l.z + c0.z, 0.0f);
         if (c1.w != 0.0f) l = make_float4(l.x + c1.x, l.y + c1.y, l.z + c1.z, 0.0f);
+        if (fin) {   // the pixel's outputs, as the resolve pass writes them for one sample
+            const uint32_t vi = find_view(F.views, F.nviews, p);   // (one sample: path p is pixel p)
+            const ViewDev& V = F.views[vi];
+            const uint32_t o = p - V.pixel_offset;
+            const float4 r = make_float4(l.x, l.y, l.z, 1.0f);
+            if (V.radiance) V.radiance[o] = r;
+            if (vi == 0 && frame_accumulate(F)) {
+                double2 a0 = F.accum[2ull * o], a1 = F.accum[2ull * o + 1];
+                a0.x += (double)r.x; a0.y += (double)r.y; a1.x += (double)r.z; a1.y += 1.0;
+                F.accum[2ull * o] = a0;
+                F.accum[2ull * o + 1] = a1;
+            }
+            continue;
+        }
         F.L[p] = l;
         if (F.cache && p >= F.n_render) {   // radiance gathered at this vertex of a training path
             const uint32_t slot = (p - F.n_render) * TRAIN_V + (d < TRAIN_V - 1 ? d : TRAIN_V - 1);

@@ -142,9 +142,12 @@ def test_path_multi_view_batch(cuda, built_lib, spp):
         base += int(v["width"]) * int(v["height"])
 
 
-def test_host_outputs_match_device_outputs(cuda, built_lib):
+@pytest.mark.parametrize("spp", [1, 2])
+def test_host_outputs_match_device_outputs(cuda, built_lib, spp):
+    """Device outputs of one-sample frames are written as each path ends (no resolve
+    pass); host outputs, and frames of several samples, by the resolve pass."""
     sc = scenes.config0(width=128, height=128)
-    st = abi.settings(spp=2, max_depth=4)
+    st = abi.settings(spp=spp, max_depth=4)
     pt = snkpt.PathTracer(0)
     pt.load_scene(sc)
     g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
@@ -164,6 +167,26 @@ def test_host_outputs_match_device_outputs(cuda, built_lib):
     for k in g:
         h = pinned[k].view(np.uint32) if k in ("mat_flags", "inst_id", "prim_id") else pinned[k]
         assert np.array_equal(g[k], h), ("pinned", k)
+
+
+def test_fp64_accumulator_device_outputs(cuda, built_lib):
+    """The FP64 accumulator gets the same sums whether the frame's outputs are on the
+    device (pixels written as their paths end) or on the host (resolve pass)."""
+    import torch
+    sc = scenes.config1(width=160, height=90)
+    sums = []
+    for device in (True, False):
+        pt = snkpt.PathTracer(0)
+        pt.load_scene(sc)
+        for f in range(3):
+            flags = abi.RENDER_ACCUMULATE_F64 | (abi.RENDER_RESET_ACCUM if f == 0 else 0)
+            st = abi.settings(spp=1, max_depth=4, seed=30 + f, flags=flags)
+            out = snkpt.alloc_outputs(160, 90, device=cuda if device else None, names=("radiance",))
+            pt.render([sc.views[0]], st, [out])
+        pt.synchronize()
+        sums.append(pt.read_accumulator(160, 90))
+    assert sums[0][1] == sums[1][1] == 3
+    assert np.array_equal(sums[0][0], sums[1][0])
 
 
 def test_fp64_accumulator(cuda, built_lib):
