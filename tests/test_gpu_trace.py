@@ -261,11 +261,13 @@ def test_treelet_restructuring_lowers_sah_and_keeps_hits(cuda, built_lib):
 
 
 @pytest.mark.parametrize("knobs", [{"bvh_leaf_max": 2}, {"bvh_leaf_max": 1, "bvh_leaf_pack": 4},
-                                   {"tlas_leaf_max": 3}, {"bvh_leaf_max": 4, "tlas_leaf_max": 2}])
+                                   {"tlas_leaf_max": 3}, {"bvh_leaf_max": 4, "tlas_leaf_max": 2},
+                                   {"bvh_collapse": 1}, {"bvh_collapse": 1, "tlas_leaf_max": 2}])
 def test_multi_primitive_leaves_keep_hits(cuda, built_lib, knobs):
     """Leaves of several primitives (mesh or instance level) use the general
     primitive groups in traversal; single-primitive leaves use the slot-mask form.
-    Hits, any-hit answers and a rendered frame must not depend on which."""
+    The greedy collapse (bvh_collapse 1) makes other trees of either kind.  Hits,
+    any-hit answers and a rendered frame must not depend on any of it."""
     sc = scenes.config1(width=320, height=180)
     rng = np.random.default_rng(23)
     rays = np.concatenate([camera_rays(sc.views[0]), random_rays(sc, 100_000, rng)])
