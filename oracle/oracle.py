@@ -55,6 +55,7 @@ def lib():
         L.snko_build.argtypes = [vp]
         L.snko_trace.argtypes = [vp, vp, u32, u32, vp, u32, u64p]
         L.snko_render_path.argtypes = [vp, vp, vp, vp, u32, u32, vp, u32, u64p]
+        L.snko_render_path_cache.argtypes = [vp, vp, vp, u32, vp, vp, vp, u32]
         L.snko_restir_state_create.restype = vp
         L.snko_restir_state_create.argtypes = [u32, u32]
         L.snko_restir_state_destroy.argtypes = [vp]
@@ -204,6 +205,23 @@ class OracleScene:
                                     C.byref(os_), nthreads or threads(), ctr.ctypes.data_as(C.POINTER(C.c_uint64)))
         assert rc == 0, rc
         return out
+
+
+    def render_path_cache(self, view, settings, pixel_base: int = 0, nthreads: int | None = None) -> dict:
+        """One-sample paths with the radiance-cache mode's termination (settings'
+        cache_spread, 0 = 0.01): the radiance gathered before each path ends, and
+        the query record (16 floats) and throughput (rgb, 1) of each path that ends
+        in the cache (zeros otherwise)."""
+        view = np.ascontiguousarray(np.asarray(view, abi.VIEW_DTYPE).reshape(1))
+        st = np.ascontiguousarray(np.asarray(settings, abi.SETTINGS_DTYPE).reshape(1))
+        n = int(view["width"][0] * view["height"][0])
+        rad = np.zeros((n, 4), np.float32)
+        qrec = np.zeros((n, 16), np.float32)
+        qbeta = np.zeros((n, 4), np.float32)
+        rc = lib().snko_render_path_cache(self._h, _p(view), _p(st), pixel_base, rad.ctypes.data, qrec.ctypes.data,
+                                          qbeta.ctypes.data, nthreads or threads())
+        assert rc == 0, rc
+        return {"radiance": rad, "qrec": qrec, "qbeta": qbeta}
 
 
 class OracleRestir:

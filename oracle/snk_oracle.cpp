@@ -899,11 +899,26 @@ static inline bool sample_continuation(const Surface& s, V3 v, V3 f0, float u_lo
     return true;
 }
 
+// A path handed to the radiance cache: its query record (position, roughness,
+// outgoing direction, metallic, shading normal, 0, albedo, 0) and throughput.
+struct CacheQuery {
+    bool valid = false;
+    float rec[16];
+    V3 beta;
+};
+
 // indirect: the path carries only the light that reaches the primary vertex
 // indirectly (the ReSTIR + indirect mode): no emission and no NEE at the primary
 // vertex, which the ReSTIR passes shade; its random numbers are drawn all the same.
+// spread_c > 0: the radiance-cache mode's termination (the path spread heuristic of
+// Mueller et al. 2021, as the shading kernel restates it): a0 = t^2 / (4 pi cos) at
+// the primary vertex, later vertices add sqrt(t^2 / (pdf cos)) with the pdf of the
+// direction that reached them; a non-emissive vertex after the first ends the path
+// in the cache once spread^2 > c a0 (no NEE there), recorded in *q.
 static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uint32_t pixel_key, uint32_t sample,
-                     const Settings& st, GSample* g, Counters* ctr, bool indirect = false) {
+                     const Settings& st, GSample* g, Counters* ctr, bool indirect = false, float spread_c = 0.0f,
+                     CacheQuery* q = nullptr) {
+    float a0 = 0.0f, acc = 0.0f, prev_pdf = 0.0f;
     Pcg rng = pcg_stream(pixel_key, sample, 0, st.seed);
     float j1 = pcg_float(rng), j2 = pcg_float(rng);
     float jx = sample == 0 ? 0.5f : j1, jy = sample == 0 ? 0.5f : j2;
@@ -926,6 +941,25 @@ static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uin
         float u_rr = pcg_float(rng), u_d1 = pcg_float(rng), u_d2 = pcg_float(rng);
         float u_lobe = pcg_float(rng);
         const bool direct = !(indirect && d == 0);
+        if (spread_c > 0.0f) {
+            const float cosv = fmaxf_(std::fabs(dot(s.n, rd)), 1e-6f);
+            if (d == 0) {
+                a0 = (h.t * h.t) / ((4.0f * PI) * cosv);
+                acc = 0.0f;
+            } else {
+                acc = acc + std::sqrt((h.t * h.t) / (fmaxf_(prev_pdf, 1e-6f) * cosv));
+            }
+            if (d >= 1 && !(s.flags & MAT_EMISSIVE) && acc * acc > spread_c * a0) {
+                if (q) {
+                    const float r[16] = {s.pos.x, s.pos.y, s.pos.z, s.roughness, -rd.x, -rd.y, -rd.z, s.metallic,
+                                         s.n.x, s.n.y, s.n.z, 0.0f, s.albedo.x, s.albedo.y, s.albedo.z, 0.0f};
+                    std::memcpy(q->rec, r, sizeof(r));
+                    q->beta = beta;
+                    q->valid = true;
+                }
+                return L;
+            }
+        }
         if (s.flags & MAT_EMISSIVE) {
             if (d == 0 && direct) L = add(L, cmul(beta, s.albedo));
             break;
@@ -956,6 +990,7 @@ static V3 trace_path(const Scene& S, const View& vw, uint32_t x, uint32_t y, uin
         float pdf;
         if (!sample_continuation(s, v, f0, u_lobe, u_d1, u_d2, &wi, &w, &pdf)) break;
         beta = cmul(beta, w);
+        prev_pdf = pdf;
         ro = xb;
         rd = wi;
         tmin = EXT_TMIN;
@@ -1418,6 +1453,36 @@ int snko_render_path(void* sp, const View* vw, const Settings* st, const uint32_
     });
     if (counters)
         for (auto& c : ctr) { counters[0] += c.camera; counters[1] += c.extension; counters[2] += c.shadow; counters[3] += c.nodes; counters[4] += c.tris; }
+    return 0;
+}
+
+// One-sample path tracing of one view in the radiance-cache mode's form: the
+// radiance the paths gather before they end (radiance, 4 floats per pixel) and,
+// for the paths that end in the cache, their query record (qrec, 16 floats) and
+// throughput (qbeta: rgb, 1; 0 in the fourth float when the path ended otherwise).
+int snko_render_path_cache(void* sp, const View* vw, const Settings* st, uint32_t pixel_base, float* radiance,
+                           float* qrec, float* qbeta, uint32_t nthreads) {
+    Scene& S = *(Scene*)sp;
+    if (!S.built) return 4;
+    if (st->spp != 1) return 1;
+    const float spread_c = st->cache_spread > 0.0f ? st->cache_spread : 0.01f;
+    const uint32_t W = vw->width, n = W * vw->height;
+    parallel_for(n, nthreads, 64, [&](uint32_t b, uint32_t e, uint32_t) {
+        for (uint32_t p = b; p < e; p++) {
+            CacheQuery q;
+            const V3 L = trace_path(S, *vw, p % W, p / W, pixel_base + p, 0, *st, nullptr, nullptr, false, spread_c, &q);
+            float* r = radiance + 4 * (size_t)p;
+            r[0] = L.x; r[1] = L.y; r[2] = L.z; r[3] = 1.0f;
+            float* qb = qbeta + 4 * (size_t)p;
+            if (q.valid) {
+                std::memcpy(qrec + 16 * (size_t)p, q.rec, sizeof(q.rec));
+                qb[0] = q.beta.x; qb[1] = q.beta.y; qb[2] = q.beta.z; qb[3] = 1.0f;
+            } else {
+                std::memset(qrec + 16 * (size_t)p, 0, 16 * sizeof(float));
+                qb[0] = qb[1] = qb[2] = qb[3] = 0.0f;
+            }
+        }
+    });
     return 0;
 }
 

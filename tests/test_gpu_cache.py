@@ -36,6 +36,37 @@ def test_cache_mode_without_termination_matches_plain(cuda, built_lib):
     assert s["cache_queries"] == 0 and s["cache_samples"] == 16384 * 4
 
 
+@pytest.mark.parametrize("cfg", [1, 4])
+def test_cache_termination_matches_oracle(cuda, built_lib, cfg):
+    """Cache-mode frames with termination against the oracle: which paths end in
+    the cache, where, with what throughput, and the radiance they gathered before
+    must equal the oracle's restatement of the spread heuristic.  With a zero
+    network the image is exactly the truncated one; with the network of a cache
+    reset, each ended path adds throughput x max(network(record), 0), the network
+    evaluated on the oracle's query records by the same inference kernel."""
+    import oracle as O
+    sc = scenes.config1(width=320, height=180) if cfg == 1 else scenes.config4(width=320, height=180, frames=1)
+    view = sc.views[0]
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    st = abi.settings(mode=abi.MODE_PATH_CACHE, spp=1, max_depth=6, seed=21, cache_lr=-1.0)   # no update
+    ref = O.OracleScene(sc).render_path_cache(view, st)
+    q = ref["qbeta"][:, 3] > 0
+    assert 0.02 < q.mean() < 0.9, q.mean()   # the heuristic really ends paths here
+    pt.cache_set_weights(np.zeros(snkpt.CACHE_NUM_WEIGHTS, np.float32))
+    g = frame(pt, view, st, cuda)["radiance"]
+    assert np.array_equal(g, ref["radiance"]), "truncated radiance"
+    assert pt.stats()["cache_queries"] == int(q.sum())
+    pt.cache_reset(5)
+    g = frame(pt, view, st, cuda)["radiance"].astype(np.float64)
+    y = pt.cache_infer(ref["qrec"][q]).astype(np.float64)
+    expect = ref["radiance"][:, :3].astype(np.float64)
+    expect[q] += ref["qbeta"][q, :3].astype(np.float64) * np.maximum(y, 0.0)
+    err = np.abs(g[:, :3] - expect) / np.maximum(np.abs(expect), 1e-3)
+    assert float(err.max()) <= 1e-4, float(err.max())
+    assert float(np.abs(g[q, :3] - ref["radiance"][q, :3]).max()) > 0.0   # the network added something
+
+
 def test_cache_learns_what_truncation_loses(cuda, built_lib):
     """Against an FP64-accumulated converged image: the trained cache must recover
     most of the energy that the same cache-truncated paths lose without it."""

@@ -182,6 +182,27 @@ def test_oracle_render_thread_independent():
     assert np.array_equal(c["radiance"], a["radiance"][px])
 
 
+def test_oracle_cache_termination():
+    """The oracle's cache-mode paths: without termination (a huge threshold) they
+    are the plain paths; with it, a path that ends in the cache has gathered no
+    more than its plain continuation (the same random numbers up to its end), the
+    others are unchanged, and every query record is a unit direction and normal."""
+    sc = scenes.config1(width=64, height=36)
+    osc = O.OracleScene(sc)
+    plain = osc.render_path(sc.views[0], abi.settings(spp=1, max_depth=6, seed=3))["radiance"]
+    none = osc.render_path_cache(sc.views[0], abi.settings(spp=1, max_depth=6, seed=3, cache_spread=1e30))
+    assert not none["qbeta"].any()
+    assert np.array_equal(none["radiance"], plain)
+    c = osc.render_path_cache(sc.views[0], abi.settings(spp=1, max_depth=6, seed=3))
+    q = c["qbeta"][:, 3] > 0
+    assert 0.02 < q.mean() < 0.9
+    assert np.array_equal(c["radiance"][~q], plain[~q])
+    assert (c["radiance"][q, :3] <= plain[q, :3] * (1 + 1e-6) + 1e-12).all()
+    assert np.allclose(np.linalg.norm(c["qrec"][q, 4:7], axis=1), 1.0, atol=1e-4)
+    assert np.allclose(np.linalg.norm(c["qrec"][q, 8:11], axis=1), 1.0, atol=1e-4)
+    assert (c["qbeta"][q, :3] >= 0).all()
+
+
 def test_oracle_restir_frames():
     sc = scenes.config2(width=48, height=27, frames=3)
     osc = O.OracleScene(sc)
