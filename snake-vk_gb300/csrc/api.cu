@@ -120,6 +120,11 @@ struct snk_pt_ctx {
     DBuf<ViewDev> d_views;
     std::map<uint64_t, DBuf<unsigned char>> staging;
     uint32_t* h_counters = nullptr;          // pinned copy of the last frame's counters
+    // pinned copies, made at the end of each render, of the device error word and
+    // the instance BVH's build record (read by snk_pt_get_stats without a copy)
+    unsigned* h_err = nullptr;
+    SmallBuildOut* h_small = nullptr;
+    bool aux_pending = false;
     unsigned long long* h_trav = nullptr;    // pinned copy of traversal counters
     bool counters_pending = false;
     uint32_t last_mode = 0, last_depth = 0, last_count_nodes = 0;
@@ -695,6 +700,8 @@ int snk_pt_create(const snk_pt_config* config, snk_pt_ctx** out_ctx) {
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
     if (cudaMallocHost(&ctx->h_counters, CNT_TOTAL * sizeof(uint32_t)) != cudaSuccess ||
         cudaMallocHost(&ctx->h_trav, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_err, sizeof(unsigned)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_small, sizeof(SmallBuildOut)) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         ctx->d_err.reserve(1) != cudaSuccess || cudaMemset(ctx->d_err.p, 0, sizeof(unsigned)) != cudaSuccess) {
         snk_pt_destroy(ctx);
@@ -702,6 +709,8 @@ int snk_pt_create(const snk_pt_config* config, snk_pt_ctx** out_ctx) {
     }
     std::memset(ctx->h_counters, 0, CNT_TOTAL * sizeof(uint32_t));
     std::memset(ctx->h_trav, 0, 4 * sizeof(unsigned long long));
+    *ctx->h_err = 0;
+    std::memset(ctx->h_small, 0, sizeof(SmallBuildOut));
     *out_ctx = ctx;
     return SNK_OK;
 }
@@ -712,6 +721,8 @@ int snk_pt_destroy(snk_pt_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     if (ctx->h_trav) cudaFreeHost(ctx->h_trav);
+    if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
@@ -1290,7 +1301,11 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
     ctx->timing_pending = true;
     cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, CNT_TOTAL * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(ctx->h_trav, ctx->trav.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(ctx->h_err, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (ctx->tlas_refittable && ctx->tlas_root != INVALID && ctx->d_small_out.p)
+        cudaMemcpyAsync(ctx->h_small, ctx->d_small_out.p, sizeof(SmallBuildOut), cudaMemcpyDeviceToHost, st);
     ctx->counters_pending = true;
+    ctx->aux_pending = true;
     ctx->last_mode = rs.mode;
     ctx->last_depth = max_depth;
     ctx->last_paths = n_paths;
@@ -1727,6 +1742,10 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     if (!ctx || !out) return SNK_ERR_INVALID_ARG;
     std::memset(out, 0, sizeof(*out));
     cudaSetDevice(ctx->device);
+    // the first call after a frame reads the error word and build record that the
+    // frame copied at its end (later calls read them from the device)
+    const bool aux = ctx->aux_pending && ctx->counters_pending;
+    ctx->aux_pending = false;
     if (ctx->counters_pending || ctx->timing_pending) {
         if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, SNK_ERR_CUDA, "get_stats: sync");
         if (ctx->timing_pending) {
@@ -1794,10 +1813,14 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     }
     uint64_t tlas_nodes = ctx->tlas_nodes;
     if (ctx->tlas_refittable && ctx->tlas_root != INVALID && ctx->d_small_out.p) {
-        SmallBuildOut r{};
-        if (cudaMemcpyAsync(&r, ctx->d_small_out.p, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
-            cudaStreamSynchronize(ctx->stream) == cudaSuccess)
-            tlas_nodes = r.num_nodes;
+        if (aux) {
+            tlas_nodes = ctx->h_small->num_nodes;
+        } else {
+            SmallBuildOut r{};
+            if (cudaMemcpyAsync(&r, ctx->d_small_out.p, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream) == cudaSuccess &&
+                cudaStreamSynchronize(ctx->stream) == cudaSuccess)
+                tlas_nodes = r.num_nodes;
+        }
     }
     out->wide_nodes = ctx->blas_nodes + tlas_nodes;
     out->triangles = ctx->total_tris;
@@ -1805,7 +1828,8 @@ int snk_pt_get_stats(const snk_pt_ctx* cctx, snk_pt_stats* out) {
     out->blas_sah_cost = ctx->blas_sah;
     out->last_render_ms = ctx->last_ms;
     unsigned e = 0;
-    if (ctx->d_err.p) cudaMemcpy(&e, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (aux) e = *ctx->h_err;
+    else if (ctx->d_err.p) cudaMemcpy(&e, ctx->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost);
     out->device_error = e;
     out->instance_bvh_refits = (uint32_t)ctx->tlas_refits;
     out->graph_launches = ctx->graph_launches;

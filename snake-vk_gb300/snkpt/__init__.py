@@ -459,9 +459,9 @@ class PathTracer:
     def stats(self) -> dict:
         s = np.zeros(1, abi.STATS_DTYPE)
         self._check(lib().snk_pt_get_stats(self._h, s.ctypes.data))
-        d = {k: s[k][0].item() for k in abi.STATS_DTYPE.names if k not in ("stage_ms", "stage_launches")}
-        d["stage_ms"] = dict(zip(abi.STAGES, s["stage_ms"][0].tolist()))
-        d["stage_launches"] = dict(zip(abi.STAGES, s["stage_launches"][0].tolist()))
+        d = dict(zip(abi.STATS_DTYPE.names, s[0].tolist()))   # (one conversion of the whole record)
+        d["stage_ms"] = dict(zip(abi.STAGES, np.asarray(d["stage_ms"]).tolist()))
+        d["stage_launches"] = dict(zip(abi.STAGES, np.asarray(d["stage_launches"]).tolist()))
         return d
 
     def read_accumulator(self, width: int, height: int):
