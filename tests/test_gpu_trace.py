@@ -289,6 +289,52 @@ def test_multi_primitive_leaves_keep_hits(cuda, built_lib, knobs):
         assert np.array_equal(outs[0][k].cpu().numpy(), outs[1][k].cpu().numpy()), k
 
 
+def _small_meshes():
+    """Meshes of 1, 2, 4 and 8 triangles (mesh BVHs of one wide node, whose
+    children are all leaves when leaves hold one triangle) and the 12-triangle
+    cube (a root with an internal child)."""
+    tri = scenes.Mesh(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), None, np.array([[0, 1, 2]], np.uint32))
+    tet = scenes.Mesh(np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], np.float32), None,
+                      np.array([[0, 1, 2], [0, 3, 1], [0, 2, 3], [1, 3, 2]], np.uint32))
+    octa = scenes.Mesh(np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32),
+                       None, np.array([[0, 2, 4], [2, 1, 4], [1, 3, 4], [3, 0, 4], [2, 0, 5], [1, 2, 5], [3, 1, 5],
+                                       [0, 3, 5]], np.uint32))
+    return [tri, scenes.quad_mesh(), tet, octa, scenes.cube_mesh()]
+
+
+@pytest.mark.parametrize("knobs", [{}, {"tlas_leaf_max": 2}, {"bvh_leaf_max": 2}])
+def test_small_meshes_bit_exact(cuda, built_lib, knobs):
+    """600 instances of meshes of 1 to 12 triangles, most of them a single wide
+    node: single-primitive leaves in both levels (slot-mask primitive groups),
+    multi-primitive instance leaves, multi-primitive mesh leaves.  Closest hits
+    and any-hit answers equal the oracle's in all three."""
+    rng = np.random.default_rng(41)
+    rows = []
+    for k in range(600):
+        R = scenes.random_rotation(rng)
+        s = rng.uniform(0.2, 2.0, 3)
+        rows.append((scenes.affine(R, tuple(s), tuple(rng.uniform(-20.0, 20.0, 3))), k % 5, 0))
+    sc = scenes.Scene(_small_meshes(), scenes.make_instances(rows),
+                      scenes.make_materials([((0.5, 0.5, 0.5), 0.5, 0.0, 0)]), scenes.no_dir_light(),
+                      scenes.point_lights([]), [], "small meshes")
+    pt = snkpt.PathTracer(0)
+    if knobs:
+        pt.set_tuning(knobs)
+    pt.load_scene(sc)
+    osc = O.OracleScene(sc)
+    rays = random_rays(sc, 300_000, rng)
+    h = pt.trace_rays(rays)
+    assert_hits_equal(h, osc.trace(rays), f"small meshes {knobs}")
+    assert (h["flags"] == 1).mean() > 0.2
+    hit_mesh = np.array([r[1] for r in rows])[h["inst"][h["flags"] == 1]]
+    assert len(np.unique(hit_mesh)) == 5
+    srays = shadow_rays(sc, 200_000, rng)
+    a = pt.trace_rays(srays, any_hit=True)
+    assert np.array_equal(a["flags"], osc.trace(srays, any_hit=True)["flags"])
+    assert 0.02 < a["flags"].mean() < 0.98
+    pt.synchronize()
+
+
 @pytest.mark.parametrize("cfg", [1, 2])
 def test_instance_bvh_refit_keeps_hits(cuda, built_lib, cfg):
     """Refitting the instance BVH (tlas_refit_interval) while instances move must
