@@ -52,9 +52,27 @@ __device__ __forceinline__ bool decode_path(const FrameParams& F, uint32_t p, ui
     return train;
 }
 
+// Path of camera-ray queue entry q: the pixels of a view whose sides are multiples
+// of 8 and 4 are queued in 8 x 4 tiles (row-major tiles, row-major pixels within
+// a tile), so a warp's 32 rays cover a compact patch of the image; other views,
+// and the training paths of the radiance cache, in path order.
+__device__ __forceinline__ uint32_t queue_path(const FrameParams& F, uint32_t q) {
+    if (F.cache && q >= F.n_render) return q;
+    const uint32_t g = q / F.spp, s = q - g * F.spp;
+    const ViewDev& V = F.views[find_view(F.views, F.nviews, g)];
+    const uint32_t W = V.v.width, H = V.v.height;
+    uint32_t r = g - V.pixel_offset;
+    if ((W & 7u) == 0 && (H & 3u) == 0) {
+        const uint32_t t = r >> 5, w = r & 31u, tiles_x = W >> 3;
+        r = ((t / tiles_x) * 4u + (w >> 3)) * W + (t % tiles_x) * 8u + (w & 7u);
+    }
+    return (V.pixel_offset + r) * F.spp + s;
+}
+
 __global__ void __launch_bounds__(BLK) k_generate(FrameParams F) {
     if (blockIdx.x == 0 && threadIdx.x == 0) F.counters[CNT_QUEUE + 0] = F.n_paths;
-    for (uint32_t p = blockIdx.x * BLK + threadIdx.x; p < F.n_paths; p += gridDim.x * BLK) {
+    for (uint32_t q = blockIdx.x * BLK + threadIdx.x; q < F.n_paths; q += gridDim.x * BLK) {
+        const uint32_t p = queue_path(F, q);
         uint32_t gpix, s, vi, x, y;
         decode_path(F, p, &gpix, &s, &vi, &x, &y);
         const ViewDev& V = F.views[vi];
@@ -62,9 +80,9 @@ __global__ void __launch_bounds__(BLK) k_generate(FrameParams F) {
         float j1 = pcg_float(rng), j2 = pcg_float(rng);
         float jx = s == 0 ? 0.5f : j1, jy = s == 0 ? 0.5f : j2;
         V3 d = camera_dir(V.v, x, y, jx, jy);
-        F.rays[0][2ull * p] = make_float4(V.v.pos[0], V.v.pos[1], V.v.pos[2], 0.0f);
-        F.rays[0][2ull * p + 1] = make_float4(d.x, d.y, d.z, T_FAR);
-        F.path_ids[0][p] = p;
+        F.rays[0][2ull * q] = make_float4(V.v.pos[0], V.v.pos[1], V.v.pos[2], 0.0f);
+        F.rays[0][2ull * q + 1] = make_float4(d.x, d.y, d.z, T_FAR);
+        F.path_ids[0][q] = p;
         F.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         F.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (F.cache) F.spread[p] = make_float2(0.0f, 0.0f);

@@ -86,22 +86,14 @@ __device__ __forceinline__ float byte_m(uint32_t w, uint32_t k) {
     return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (k << 4)));
 }
 
-// Tests the 8 children of node idx.  ngroup <- (child_base, internal hits << 24 | imask)
-// with internal hit bit of slot s at position s ^ oct (ORDERED) or s; tgroup <- (prim_base,
-// primitive hits).
+// Box tests of the 8 children of a node (words w0, w2, w3, w4) against ray r on
+// [tmin, tmax]: bit s of the result is set when the box of slot s is hit.
 // Near/far planes are swapped once per node by the ray octant; each plane costs a
 // byte permute and half a packed FMA, and an integer compare with BOX_SLACK_ULPS of slack
-// (on top of the per-axis widening below) keeps the test conservative.  The 8 box tests only
-// set one bit each; the internal-child bits are then moved into visiting order
-// with three conditional swaps (bit s -> s ^ oct) when the order matters (closest
-// hit; an any-hit ray stops at whichever occluder it meets first and skips the
-// swaps), and only the hit leaf slots are expanded into primitive bits.
-template <bool ORDERED, bool SINGLE>
-__device__ __forceinline__ void intersect_node(const WideNode* __restrict__ nodes, uint32_t idx, const NodeRay& r,
-                                               float tmin, float tmax, uint2& ngroup, uint2& tgroup) {
-    const float4* np = reinterpret_cast<const float4*>(nodes + idx);
-    float4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-    uint32_t e = __float_as_uint(w0.w);
+// (on top of the per-axis widening below) keeps the test conservative.
+__device__ __forceinline__ uint32_t box_hits(const float4& w0, const float4& w2, const float4& w3, const float4& w4,
+                                             const NodeRay& r, float tmin, float tmax) {
+    const uint32_t e = __float_as_uint(w0.w);
     // per axis A = 2^15 x (grid step) / d, B = (p - o) / d - A rounded once; a plane
     // byte q decodes as x = 1 + q 2^-15 (one byte permute), so t = fma(x, A, B).
     // B's rounding (at most |A| 2^-24) is covered with room to spare by moving the
@@ -109,7 +101,6 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
     const float ax = __uint_as_float(((e & 0xFFu) + 15u) << 23) * r.idx;
     const float ay = __uint_as_float((((e >> 8) & 0xFFu) + 15u) << 23) * r.idy;
     const float az = __uint_as_float((((e >> 16) & 0xFFu) + 15u) << 23) * r.idz;
-    uint32_t imask = e >> 24;
     const float bx = __fmaf_rn(w0.x - r.ox, r.idx, -ax), by = __fmaf_rn(w0.y - r.oy, r.idy, -ay),
                 bz = __fmaf_rn(w0.z - r.oz, r.idz, -az);
     const float mx = fabsf(ax) * 4.76837158e-7f, my = fabsf(ay) * 4.76837158e-7f, mz = fabsf(az) * 4.76837158e-7f;
@@ -123,7 +114,6 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
     uint32_t nx[2] = {sx ? hx0 : lx0, sx ? hx1 : lx1}, fx[2] = {sx ? lx0 : hx0, sx ? lx1 : hx1};
     uint32_t ny[2] = {sy ? hy0 : ly0, sy ? hy1 : ly1}, fy[2] = {sy ? ly0 : hy0, sy ? ly1 : hy1};
     uint32_t nz[2] = {sz ? hz0 : lz0, sz ? hz1 : lz1}, fz[2] = {sz ? lz0 : hz0, sz ? lz1 : hz1};
-    const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
     uint32_t hits = 0;   // bit s: the box of slot s is hit
     // children s and s + 1 in one packed FMA per plane (sm_100 and later: two
     // binary32 FMAs per instruction, each rounded as fmaf)
@@ -144,21 +134,47 @@ __device__ __forceinline__ void intersect_node(const WideNode* __restrict__ node
         hits |= (__float_as_int(tn0) <= __float_as_int(tf0) + BOX_SLACK_ULPS) ? (1u << s) : 0u;
         hits |= (__float_as_int(tn1) <= __float_as_int(tf1) + BOX_SLACK_ULPS) ? (2u << s) : 0u;
     }
+    return hits;
+}
+
+// Leaf slots of a single-primitive-leaf node (meta count bits 1: bit 5 of each
+// byte), gathered from the four bytes of each meta word by one multiply.
+__device__ __forceinline__ uint32_t leaf_slots(uint32_t meta0, uint32_t meta1) {
+    const uint32_t l0 = (meta0 >> 5) & 0x01010101u, l1 = (meta1 >> 5) & 0x01010101u;
+    return ((l0 * 0x10204080u) >> 28) | (((l1 * 0x10204080u) >> 28) << 4);
+}
+
+// Child bits in visiting order for octant oct: bit s moves to s ^ oct (three
+// conditional swaps).
+__device__ __forceinline__ uint32_t visit_order(uint32_t x, uint32_t oct) {
+    x = (oct & 1u) ? (((x & 0x55u) << 1) | ((x >> 1) & 0x55u)) : x;
+    x = (oct & 2u) ? (((x & 0x33u) << 2) | ((x >> 2) & 0x33u)) : x;
+    x = (oct & 4u) ? (((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu)) : x;
+    return x;
+}
+
+// Tests the 8 children of node idx.  ngroup <- (child_base, internal hits << 24 | imask)
+// with internal hit bit of slot s at position s ^ oct (ORDERED) or s; tgroup <- (prim_base,
+// primitive hits).  The internal-child bits are moved into visiting order with three
+// conditional swaps (bit s -> s ^ oct) when the order matters (closest hit; an any-hit
+// ray stops at whichever occluder it meets first and skips the swaps), and only the
+// hit leaf slots are expanded into primitive bits.
+template <bool ORDERED, bool SINGLE>
+__device__ __forceinline__ void intersect_node(const WideNode* __restrict__ nodes, uint32_t idx, const NodeRay& r,
+                                               float tmin, float tmax, uint2& ngroup, uint2& tgroup) {
+    const float4* np = reinterpret_cast<const float4*>(nodes + idx);
+    float4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    const uint32_t imask = __float_as_uint(w0.w) >> 24;
+    const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
+    const uint32_t hits = box_hits(w0, w2, w3, w4, r, tmin, tmax);
     // internal children (imask bits) in visiting order: bit s moves to s ^ oct
     uint32_t x = hits & imask;
-    if (ORDERED) {
-        x = (r.oct & 1u) ? (((x & 0x55u) << 1) | ((x >> 1) & 0x55u)) : x;
-        x = (r.oct & 2u) ? (((x & 0x33u) << 2) | ((x >> 2) & 0x33u)) : x;
-        x = (r.oct & 4u) ? (((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu)) : x;
-    }
+    if (ORDERED) x = visit_order(x, r.oct);
     ngroup = make_uint2(__float_as_uint(w1.x), (x << 24) | imask);
     if constexpr (SINGLE) {
-        // every leaf holds one primitive, stored in slot order: the leaf slots are
-        // those whose meta count bits are 1 (bit 5 of the byte), gathered from the
-        // four bytes of each meta word by one multiply; primitive groups are then
+        // every leaf holds one primitive, stored in slot order; primitive groups are
         // (prim_base, hit leaf slots << 24 | leaf slots), like node groups
-        const uint32_t l0 = (meta0 >> 5) & 0x01010101u, l1 = (meta1 >> 5) & 0x01010101u;
-        const uint32_t leafmask = ((l0 * 0x10204080u) >> 28) | (((l1 * 0x10204080u) >> 28) << 4);
+        const uint32_t leafmask = leaf_slots(meta0, meta1);
         tgroup = make_uint2(__float_as_uint(w1.y), ((hits & leafmask) << 24) | leafmask);
     } else {
         // leaf children: (count << 5) | offset -> primitive bits; an empty slot (meta 0) adds none
@@ -361,6 +377,225 @@ struct Traverser {
         res.t = -1.0f; res.u = 0.0f; res.v = 0.0f; res.inst = INVALID; res.prim = INVALID;
         if (err) {
             if (S.error_word) atomicOr(S.error_word, err);
+            return false;
+        }
+        if (best_inst != INVALID) {
+            res.hit = true; res.t = best_t; res.inst = best_inst; res.prim = best_prim; res.u = best_u; res.v = best_v;
+        }
+        return res.hit;
+    }
+};
+
+// ---- warp packets ------------------------------------------------------------
+// Traversal of up to 32 coherent rays (one per lane) by the whole warp together,
+// for queues whose neighbouring entries are neighbouring pixels (camera rays).
+// Node groups and instance groups are uniform over the warp and carry the mask of
+// the lanes whose rays hit one of their boxes: every node is tested by all lanes
+// against their own rays (lanes outside the mask count no hits), and the children
+// hit by any lane form the next group, visited in the order of the octant of the
+// group's first lane.  A mesh node's hit triangles stay per lane and are tested
+// before anything else, each lane its own, in as many rounds as the lane with the
+// most.  Hits equal the per-ray traversal's: boxes only cull, and the closest hit
+// is the minimum over the tested triangles in the same (t, instance, triangle)
+// order.  The group stack is one array of PSTACK entries (base, bits, lane mask)
+// per warp in shared memory; every lane writes the same values, so each lane
+// reads back what it wrote itself.  Each lane's world ray and its node-test set-up
+// wait in shared-memory rows while the lane's ray is in an instance.  For single-primitive-leaf trees only.  A
+// packet that runs past its stack or past 32x the per-ray step cap reports the
+// same error bits as a ray would (all its rays then miss).
+constexpr int PSTACK = 2 * STACK_MAX;
+
+template <bool ANY, int NT>
+struct PacketTraverser {
+    static constexpr bool ORD = !ANY;
+    static constexpr uint32_t FULL = 0xFFFFFFFFu;
+    // per lane
+    float tmin, tmax;
+    uint2* rows;             // this thread's 5 shared-memory rows (stride NT): the world ray and its set-up
+    NodeRay cr;              // node-test set-up of the current level's ray
+    WRay tr;                 // object-space watertight set-up (in a mesh, once k != INVALID)
+    float best_t, best_u, best_v;
+    uint32_t best_inst, best_prim;
+    uint32_t tbits;          // hit leaf slots of the current mesh node this lane still has to test
+    // uniform over the warp
+    uint4* stk;
+    uint2 ngroup, tgroup;    // node group; instance group (leaves of the instance BVH)
+    uint32_t nmask, tmask, live, lane_bit;
+    uint32_t tri_base, tri_leaves;   // prim_base and leaf slots of the mesh node tbits refers to
+    uint32_t woct, coct;     // visiting octant of the world level and of the current level
+    int level, sp, blas_sp;
+    uint32_t cur_inst, steps, step_limit;
+    unsigned err;
+
+    __device__ __forceinline__ uint2& row(int k) const { return rows[k * NT]; }
+    __device__ __forceinline__ void restore_world() {
+        const uint2 a = row(0), b = row(1), c = row(2), e = row(3);
+        cr.ox = __uint_as_float(c.x); cr.oy = __uint_as_float(c.y); cr.oz = __uint_as_float(e.x);
+        cr.idx = __uint_as_float(a.x); cr.idy = __uint_as_float(a.y); cr.idz = __uint_as_float(b.x);
+        cr.oct = b.y;
+    }
+
+    __device__ __forceinline__ void init(const SceneDev& S, V3 o, V3 d, float tmin_, float tmax_, bool active,
+                                         uint4* stack, uint2* world_rows) {
+        tmin = fmaxf(tmin_, 0.0f); tmax = tmax_;
+        cr = make_node_ray(o, d);
+        rows = world_rows;
+        row(0) = make_uint2(__float_as_uint(cr.idx), __float_as_uint(cr.idy));
+        row(1) = make_uint2(__float_as_uint(cr.idz), cr.oct);
+        row(2) = make_uint2(__float_as_uint(o.x), __float_as_uint(o.y));
+        row(3) = make_uint2(__float_as_uint(o.z), __float_as_uint(d.x));
+        row(4) = make_uint2(__float_as_uint(d.y), __float_as_uint(d.z));
+        tr.k = INVALID; tr.Sx = 0.0f; tr.Sy = 0.0f; tr.Sz = 0.0f;
+        best_t = tmax; best_u = 0.0f; best_v = 0.0f; best_inst = INVALID; best_prim = INVALID;
+        tbits = 0;
+        stk = stack;
+        lane_bit = 1u << (threadIdx.x & 31u);
+        live = __ballot_sync(FULL, active);
+        woct = live ? __shfl_sync(FULL, cr.oct, __ffs(live) - 1) : 0u;
+        coct = woct;
+        level = 0; sp = 0; blas_sp = 0; cur_inst = 0; steps = 0; err = 0; tri_base = 0; tri_leaves = 0;
+        step_limit = S.max_steps < 0x07FFFFFFu ? 32u * S.max_steps : 0xFFFFFFFFu;
+        ngroup = (S.tlas_root == INVALID || !live) ? make_uint2(0u, 0u)
+                                                   : make_uint2(S.tlas_root, (1u << (24 + (ORD ? woct : 0u))) | 1u);
+        nmask = live;
+        tgroup = make_uint2(0u, 0u);
+        tmask = 0;
+    }
+
+    __device__ __forceinline__ bool push(uint32_t x, uint32_t y, uint32_t mask) {
+        if (sp >= PSTACK) { err |= ERR_STACK_OVERFLOW; return false; }
+        stk[sp++] = make_uint4(x, y, mask, 0u);
+        return true;
+    }
+
+    // one internal child of the node group, tested by every lane
+    __device__ __forceinline__ void node_step(const SceneDev& S) {
+        const uint32_t k = __ffs(ngroup.y >> 24) - 1;
+        ngroup.y &= ~(1u << (24 + k));
+        const uint32_t m = nmask & live;
+        if (m == 0) { ngroup.y &= 0x00FFFFFFu; return; }   // the group's rays are all finished
+        const uint32_t slot = ORD ? k ^ coct : k;
+        const uint32_t child = ngroup.x + __popc(ngroup.y & ((1u << slot) - 1u) & 0xFFu);
+        if (tgroup.y > 0x00FFFFFFu) {
+            if (!push(tgroup.x | PRIM_GROUP, tgroup.y, tmask)) return;
+            tgroup = make_uint2(0u, 0u);
+        }
+        if (ngroup.y > 0x00FFFFFFu && !push(ngroup.x, ngroup.y, nmask)) return;
+        if (child >= (level ? S.num_blas_nodes : S.num_tlas_nodes)) { err |= ERR_BAD_INDEX; return; }
+        const float4* np = reinterpret_cast<const float4*>((level ? S.blas_nodes : S.tlas_nodes) + child);
+        const float4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
+                     w4 = __ldg(np + 4);
+        uint32_t hits = box_hits(w0, w2, w3, w4, cr, tmin, best_t);
+        if (!(m & lane_bit)) hits = 0;
+        const uint32_t imask = __float_as_uint(w0.w) >> 24;
+        const uint32_t leaves = leaf_slots(__float_as_uint(w1.z), __float_as_uint(w1.w));
+        const uint32_t hi = hits & imask, hl = hits & leaves;
+        const uint32_t ui = __reduce_or_sync(FULL, hi);
+        nmask = __ballot_sync(FULL, hi != 0u);
+        ngroup = make_uint2(__float_as_uint(w1.x), ((ORD ? visit_order(ui, coct) : ui) << 24) | imask);
+        if (level == 0) {
+            const uint32_t ul = __reduce_or_sync(FULL, hl);
+            tmask = __ballot_sync(FULL, hl != 0u);
+            tgroup = make_uint2(__float_as_uint(w1.y), (ul << 24) | leaves);
+        } else {
+            tbits = hl;
+            tri_base = __float_as_uint(w1.y);
+            tri_leaves = leaves;
+        }
+    }
+
+    // enter the next instance of the instance group (the lanes that hit its leaf box)
+    __device__ __forceinline__ void inst_step(const SceneDev& S) {
+        const uint32_t k = __ffs(tgroup.y >> 24) - 1;
+        tgroup.y &= ~(1u << (24 + k));
+        const uint32_t m = tmask & live;
+        if (m == 0) { tgroup.y &= 0x00FFFFFFu; return; }
+        const uint32_t pidx = tgroup.x + __popc(tgroup.y & ((1u << k) - 1u));
+        if (pidx >= S.num_tlas_prims) { err |= ERR_BAD_INDEX; return; }
+        const uint32_t inst = __ldg(&S.tlas_prims[pidx]);
+        if (inst >= S.num_instances) { err |= ERR_BAD_INDEX; return; }
+        if (tgroup.y > 0x00FFFFFFu && !push(tgroup.x | PRIM_GROUP, tgroup.y, tmask)) return;
+        if (ngroup.y > 0x00FFFFFFu && !push(ngroup.x, ngroup.y, nmask)) return;
+        const float4* ip = reinterpret_cast<const float4*>(S.inst_trace + inst);
+        const float4 r0 = __ldg(ip), r1 = __ldg(ip + 1), r2 = __ldg(ip + 2);
+        const uint32_t root = __ldg(reinterpret_cast<const uint32_t*>(ip + 3));
+        if (m & lane_bit) {
+            const float inv[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+            const uint2 c = row(2), e = row(3), f = row(4);
+            const V3 wo = v3(__uint_as_float(c.x), __uint_as_float(c.y), __uint_as_float(e.x));
+            const V3 wd = v3(__uint_as_float(e.y), __uint_as_float(f.x), __uint_as_float(f.y));
+            const V3 oo = xform_point_rn(inv, wo);
+            const V3 od = xform_dir_rn(inv, wd);
+            cr = make_node_ray(oo, od);
+            // (the watertight set-up waits for the instance's first triangle test)
+            tr.k = INVALID; tr.Sx = od.x; tr.Sy = od.y; tr.Sz = od.z;
+        }
+        coct = __shfl_sync(FULL, cr.oct, __ffs(m) - 1);
+        blas_sp = sp;
+        level = 1;
+        cur_inst = inst;
+        ngroup = make_uint2(root, (1u << (24 + (ORD ? coct : 0u))) | 1u);
+        nmask = m;
+        tgroup = make_uint2(0u, 0u);
+        tmask = 0;
+    }
+
+    // every lane with a hit leaf slot left tests its next triangle
+    __device__ __forceinline__ void tri_step(const SceneDev& S) {
+        bool found = false;
+        unsigned e = 0;
+        if (tbits) {
+            const uint32_t k = __ffs(tbits) - 1;
+            tbits &= tbits - 1u;
+            const uint32_t pidx = tri_base + __popc(tri_leaves & ((1u << k) - 1u));
+            if (pidx >= S.num_tris) {
+                e = ERR_BAD_INDEX;
+            } else {
+                if (tr.k == INVALID) tr = wray_setup(v3(tr.Sx, tr.Sy, tr.Sz));
+                const float4* tp = reinterpret_cast<const float4*>(S.tris + pidx);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                const float va[3] = {a.x, a.y, a.z}, vb[3] = {b.x, b.y, b.z}, vc[3] = {c.x, c.y, c.z};
+                float t, b1, b2;
+                if (intersect_tri(tr, v3(cr.ox, cr.oy, cr.oz), va, vb, vc, tmin, tmax, &t, &b1, &b2)) {
+                    const uint32_t prim = __float_as_uint(a.w);
+                    const bool better = best_inst == INVALID || t < best_t ||
+                                        (t == best_t && (cur_inst < best_inst || (cur_inst == best_inst && prim < best_prim)));
+                    if (ANY || better) {
+                        best_t = t; best_inst = cur_inst; best_prim = prim; best_u = b1; best_v = b2;
+                    }
+                    found = true;
+                }
+            }
+        }
+        err |= __reduce_or_sync(FULL, e);
+        if (ANY) {
+            const uint32_t f = __ballot_sync(FULL, found);
+            live &= ~f;
+            if (f & lane_bit) tbits = 0;
+        }
+    }
+
+    __device__ __forceinline__ void run(const SceneDev& S) {
+        for (;;) {
+            if (err || live == 0) return;
+            if (++steps > step_limit) { err |= ERR_STEP_LIMIT; return; }
+            if (level == 1 && __any_sync(FULL, tbits != 0u)) { tri_step(S); continue; }
+            if (tgroup.y > 0x00FFFFFFu) { inst_step(S); continue; }
+            if (ngroup.y > 0x00FFFFFFu) { node_step(S); continue; }
+            if (level == 1 && sp == blas_sp) { level = 0; restore_world(); coct = woct; }
+            if (sp == 0) return;
+            const uint4 g = stk[--sp];
+            if (g.x & PRIM_GROUP) { tgroup = make_uint2(g.x & ~PRIM_GROUP, g.y); tmask = g.z; }
+            else { ngroup = make_uint2(g.x, g.y); nmask = g.z; }
+        }
+    }
+
+    // this lane's result; an error of the packet is reported once and read as a miss
+    __device__ __forceinline__ bool finish(const SceneDev& S, TraceResult& res) {
+        res.hit = false;
+        res.t = -1.0f; res.u = 0.0f; res.v = 0.0f; res.inst = INVALID; res.prim = INVALID;
+        if (err) {
+            if (S.error_word && (threadIdx.x & 31u) == 0) atomicOr(S.error_word, err);
             return false;
         }
         if (best_inst != INVALID) {

@@ -135,6 +135,41 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
     flush_counts<COUNT>(ctr, F.trav_counters);
 }
 
+// closest hits of segment d's rays in warp packets of 32 consecutive queue entries
+// (the camera segment: 32 neighbouring pixels of a row per warp)
+template <int MINB>
+__global__ void __launch_bounds__(TBLK, MINB) k_trace_packet(FrameParams F, uint32_t d) {
+    __shared__ uint4 sh_pstack[(TBLK / 32) * PSTACK];
+    __shared__ uint2 sh_world[5 * TBLK];
+    const uint32_t n = F.counters[CNT_QUEUE + d];
+    const float4* rays = F.rays[d & 1u];
+    uint32_t* work = &F.counters[CNT_WORK_TRACE + d];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint4* stack = sh_pstack + (threadIdx.x >> 5) * PSTACK;
+    for (;;) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(work, 32u);
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (b >= n) break;
+        const uint32_t i = b + lane;
+        const bool active = i < n;
+        float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c = a;
+        if (active) { a = __ldg(rays + 2ull * i); c = __ldg(rays + 2ull * i + 1); }
+        PacketTraverser<false, TBLK> tv;
+        tv.init(F.S, v3(a.x, a.y, a.z), v3(c.x, c.y, c.z), a.w, c.w, active, stack, sh_world + threadIdx.x);
+        tv.run(F.S);
+        TraceResult r;
+        tv.finish(F.S, r);
+        if (active) {
+            HitDev h;
+            h.t = r.t; h.inst = r.inst; h.prim = r.prim; h.u = r.u; h.v = r.v; h.flags = r.hit ? 1u : 0u;
+            uint2* dst = reinterpret_cast<uint2*>(F.hits + i);
+            const uint2* src = reinterpret_cast<const uint2*>(&h);
+            dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2];
+        }
+    }
+}
+
 // shadow rays of segment d: the compacted queue's n0 directional-light rays, then
 // its n1 local-light rays (from n_paths on).  A ray's origin w holds its
 // contribution entry (shadow_entry); the visibility goes to that contribution's w
@@ -366,6 +401,12 @@ void launch_shadow_variant(const FrameParams& F, uint32_t depth, int grid, cudaS
 
 cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s) {
     const bool single = F.S.single_leaf != 0u;
+    // camera rays (segment 0) in warp packets, unless the bounds were lowered (their
+    // limits are per ray) or the launch counts traversal work
+    if (depth == 0 && single && !count && F.S.max_steps == MAX_TRAVERSAL_STEPS && F.S.stack_max >= STACK_MAX) {
+        k_trace_packet<6><<<grid, TBLK, 0, s>>>(F, depth);
+        return cudaGetLastError();
+    }
     if (count) single ? launch_closest_variant<true, true>(F, depth, grid, s) : launch_closest_variant<true, false>(F, depth, grid, s);
     else single ? launch_closest_variant<false, true>(F, depth, grid, s) : launch_closest_variant<false, false>(F, depth, grid, s);
     return cudaGetLastError();
