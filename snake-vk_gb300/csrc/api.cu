@@ -1171,6 +1171,7 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
                 if (e == cudaSuccess)
                     e = staged(ctx, profile, SNK_STAGE_TRACE_SHADOW,
                                [&] { return launch_trace_shadow(F, d, gany, count_nodes, side); }, side);
+                ctx->stage_launches[SNK_STAGE_TRACE_SHADOW]++;   // (its second kernel: the accumulation)
                 if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join[d], side);
             }
             if (e == cudaSuccess && d + 1 < max_depth)
@@ -1206,6 +1207,7 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
                                               ctx->d_err.p, st);
                     return s.ok() ? cudaSuccess : cudaErrorLaunchFailure;
                 });
+                ctx->stage_launches[SNK_STAGE_CACHE_TRAIN]++;   // (its second kernel: the Adam step)
             }
         }
         }   // (!replay)
@@ -1900,7 +1902,7 @@ void ctx_note_render(snk_pt_ctx* ctx, uint32_t mode, uint32_t depth, uint64_t pa
     ctx->stage_launches[SNK_STAGE_GENERATE] = 1;
     ctx->stage_launches[SNK_STAGE_TRACE_CLOSEST] = depth;
     ctx->stage_launches[SNK_STAGE_SHADE] = depth;
-    ctx->stage_launches[SNK_STAGE_TRACE_SHADOW] = depth;
+    ctx->stage_launches[SNK_STAGE_TRACE_SHADOW] = 2 * depth;   // the shadow rays and their accumulation
     ctx->stage_launches[SNK_STAGE_RESOLVE] = 1;
 }
 
