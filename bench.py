@@ -592,7 +592,10 @@ def run_ours(args):
     # hits of segment d + 1 on a second stream), so the unit is the frame's
     # traversal: the algorithmic bytes of all its closest-hit and shadow rays over
     # the time during which a traversal launch runs (the union of their spans,
-    # stage "trace_any", from CUDA events on the streams the kernels run on)
+    # stage "trace_any", from CUDA events on the streams the kernels run on).  The
+    # per-ray node and triangle counts are each ray's own traversal (the counting
+    # frame traces ray by ray), also for the camera rays, which the timed frames
+    # trace in warp packets.
     peak, peak_kind = measured_peaks()
     c_rays = cnt["rays_camera"] + cnt["rays_extension"]
     s_rays = cnt["rays_shadow"]
@@ -603,7 +606,8 @@ def run_ours(args):
     trav_s = stage_ms["trace_any"] / 1e3
     achieved = trav_bytes / trav_s / 1e9
     traffic = profile_traffic()
-    roofline = {"bound": "hbm", "kernel": "k_trace_closest + k_trace_shadow (one traversal core, overlapped)",
+    roofline = {"bound": "hbm", "kernel": "k_trace_packet (camera rays) + k_trace_closest + k_trace_shadow "
+                                                 "(one traversal core, overlapped)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": traffic, "traffic_source": os.path.relpath(PROFILE_SUMMARY, ROOT) if traffic else None,
                 "bytes_per_closest_ray": b_closest, "bytes_per_shadow_ray": b_shadow,

@@ -1026,6 +1026,11 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
     F.seed = restir_pt ? rs.seed + 0x9E3779B9u * rs.frame_index : rs.seed;
     F.n_paths = n_paths;
     F.n_pixels = (uint32_t)n_pixels;
+    F.packet_primary = 1u;
+    for (uint32_t v = 0; v < num_views; v++) {
+        const uint32_t w = views[v].width, h = views[v].height;
+        if ((w & 7u) || (h & 3u) || (uint64_t)w * h < PACKET_MIN_PIXELS) F.packet_primary = 0u;
+    }
     F.tune = trace_tuning(ctx);
     F.tune_any = any_tuning(ctx);
     const bool count_nodes = (rs.flags & SNK_RENDER_COUNT_NODES) != 0;

@@ -10,6 +10,7 @@ constexpr uint32_t MAX_DEPTH = 16;
 constexpr uint32_t MAX_VIEWS = 64;
 
 // counters (uint32) of one frame, zeroed at frame start
+constexpr uint64_t PACKET_MIN_PIXELS = 1280ull * 720ull;   // smallest view traced in warp packets
 constexpr uint32_t CNT_QUEUE = 0;         // [d]: rays queued for segment d
 constexpr uint32_t CNT_WORK_TRACE = 16;   // [d]: work fetch of the closest-hit pass of segment d
 constexpr uint32_t CNT_WORK_SHADOW = 32;  // [d]: work fetch of the shadow pass of segment d
@@ -74,6 +75,11 @@ struct FrameParams {
     // k_shade marks the queue entries whose path ends (bit 31 of the path id) and
     // k_accum_shadow writes those pixels' outputs; no resolve pass follows
     uint32_t early_resolve;
+    // every view's sides are multiples of 8 and 4 and it has at least
+    // PACKET_MIN_PIXELS pixels: the camera rays are queued in 8 x 4 pixel tiles and
+    // traced in warp packets (neighbouring pixels of smaller images are too far
+    // apart in the scene for a packet's rays to share their nodes)
+    uint32_t packet_primary;
     // per-frame values in device memory (seed, frame, accumulate), read by the kernels
     // instead of the fields above when set, so that a captured frame replays for new
     // values of them

@@ -126,6 +126,45 @@ def test_path_config1_1080p_sampled_pixels_and_determinism(cuda, built_lib):
     _compare(sub, r, "config 1 1080p (20k sampled pixels)")
 
 
+def test_path_config1_720p_camera_packets_full_frame(cuda, built_lib):
+    """A 1280x720 view (the smallest size whose camera rays are queued in 8x4
+    tiles and traced in warp packets): the whole frame equals the oracle's."""
+    sc = scenes.config1(width=1280, height=720)
+    st = abi.settings(spp=1, max_depth=4, rr_depth=3, seed=6)
+    pt = snkpt.PathTracer(0)
+    pt.load_scene(sc)
+    g = _gpu_frame(pt, [sc.views[0]], st, cuda)[0]
+    _compare(g, O.OracleScene(sc).render_path(sc.views[0], st), "config 1 720p")
+
+
+@pytest.mark.parametrize("case", ["config1 path", "config2 path spp2", "config2 restir", "two views"])
+def test_camera_packets_match_ray_by_ray(cuda, built_lib, case):
+    """Camera rays traced in warp packets (views of at least 1280x720) give every
+    output bit for bit as when each ray is traced by itself (a lowered step cap
+    turns the packets off): path frames with 1 and 2 samples per pixel, a ReSTIR
+    DI frame's G-buffer and shading, and a batch of two views."""
+    cfg = 1 if case.startswith("config1") or case == "two views" else 2
+    sc = scenes.config1(width=1280, height=720) if cfg == 1 else scenes.config2(width=1280, height=720, frames=2)
+    views = [sc.views[0]] if case != "two views" else \
+        [sc.views[0], scenes.look_at_view((20.0, 12.0, 5.0), (60.0, 0.0, 70.0), 50.0, 1280, 720)]
+    if case == "config2 restir":
+        st = abi.settings(mode=abi.MODE_RESTIR_DI, frame_index=0, seed=2)
+    else:
+        st = abi.settings(spp=2 if "spp2" in case else 1, max_depth=4, rr_depth=3, seed=8)
+    outs = []
+    for knobs in ({}, {"max_traversal_steps": 65535}):
+        pt = snkpt.PathTracer(0)
+        if knobs:
+            pt.set_tuning(knobs)
+        pt.load_scene(sc)
+        outs.append(_gpu_frame(pt, views, st, cuda))
+        del pt
+    for v in range(len(views)):
+        for k in outs[0][v]:
+            assert np.array_equal(outs[0][v][k], outs[1][v][k]), f"{case}: view {v} '{k}' differs"
+    assert (outs[0][0]["inst_id"] != 0xFFFFFFFF).mean() > 0.3
+
+
 @pytest.mark.parametrize("spp", [1, 3])
 def test_path_multi_view_batch(cuda, built_lib, spp):
     res = [(160, 90), (96, 54), (200, 120)]
