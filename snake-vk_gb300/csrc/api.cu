@@ -1029,7 +1029,7 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
     F.packet_primary = 1u;
     for (uint32_t v = 0; v < num_views; v++) {
         const uint32_t w = views[v].width, h = views[v].height;
-        if ((w & 7u) || (h & 3u) || (uint64_t)w * h < PACKET_MIN_PIXELS) F.packet_primary = 0u;
+        if (w % PACKET_TILE_W || h % PACKET_TILE_H || (uint64_t)w * h < PACKET_MIN_PIXELS) F.packet_primary = 0u;
     }
     F.tune = trace_tuning(ctx);
     F.tune_any = any_tuning(ctx);

@@ -53,15 +53,16 @@ __device__ __forceinline__ bool decode_path(const FrameParams& F, uint32_t p, ui
 }
 
 // Path of camera-ray queue entry q: for warp packets (F.packet_primary) the pixels
-// of each view are queued in 8 x 4 tiles (row-major tiles, row-major pixels within
-// a tile), so a warp's 32 rays cover a compact patch of the image; otherwise, and
-// for the training paths of the radiance cache, in path order.
+// of each view are queued in PACKET_TILE_W x PACKET_TILE_H tiles (row-major tiles,
+// row-major pixels within a tile), so a warp's 32 rays cover a compact patch of the
+// image; otherwise, and for the training paths of the radiance cache, in path order.
 __device__ __forceinline__ uint32_t queue_path(const FrameParams& F, uint32_t q) {
     if (!F.packet_primary || (F.cache && q >= F.n_render)) return q;
     const uint32_t g = q / F.spp, s = q - g * F.spp;
     const ViewDev& V = F.views[find_view(F.views, F.nviews, g)];
-    const uint32_t r = g - V.pixel_offset, t = r >> 5, w = r & 31u, tiles_x = V.v.width >> 3;
-    const uint32_t x = (t % tiles_x) * 8u + (w & 7u), y = (t / tiles_x) * 4u + (w >> 3);
+    const uint32_t r = g - V.pixel_offset, t = r >> 5, w = r & 31u, tiles_x = V.v.width / PACKET_TILE_W;
+    const uint32_t x = (t % tiles_x) * PACKET_TILE_W + w % PACKET_TILE_W,
+                   y = (t / tiles_x) * PACKET_TILE_H + w / PACKET_TILE_W;
     return (V.pixel_offset + y * V.v.width + x) * F.spp + s;
 }
 

@@ -11,6 +11,8 @@ constexpr uint32_t MAX_VIEWS = 64;
 
 // counters (uint32) of one frame, zeroed at frame start
 constexpr uint64_t PACKET_MIN_PIXELS = 1280ull * 720ull;   // smallest view traced in warp packets
+// camera-ray tile of one warp packet (16 x 2 and 4 x 8 tiles were slower at 1080p)
+constexpr uint32_t PACKET_TILE_W = 8, PACKET_TILE_H = 4;
 constexpr uint32_t CNT_QUEUE = 0;         // [d]: rays queued for segment d
 constexpr uint32_t CNT_WORK_TRACE = 16;   // [d]: work fetch of the closest-hit pass of segment d
 constexpr uint32_t CNT_WORK_SHADOW = 32;  // [d]: work fetch of the shadow pass of segment d
