@@ -21,7 +21,9 @@
 // index xor the ray octant, which the builder makes approximately front to back;
 // any-hit rays visit them in slot order.  Leaves of the instance BVH hold instance ids: on reaching one
 // the ray is transformed into object space and the BLAS root is entered; when
-// the stack unwinds to the entry depth, the world ray is restored.
+// the stack unwinds to the entry depth, the world ray is restored.  Coherent rays
+// (the camera rays of large views) can instead be traced 32 at a time by a whole
+// warp (PacketTraverser, below), with the same results.
 #pragma once
 #include "snk_device.cuh"
 

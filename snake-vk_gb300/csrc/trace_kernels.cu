@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(TBLK, MINB) k_trace_closest(FrameParams F, uin
 }
 
 // closest hits of segment d's rays in warp packets of 32 consecutive queue entries
-// (the camera segment: 32 neighbouring pixels of a row per warp)
+// (the camera segment: the 32 pixels of one 8 x 4 tile per warp)
 template <int MINB>
 __global__ void __launch_bounds__(TBLK, MINB) k_trace_packet(FrameParams F, uint32_t d) {
     __shared__ uint4 sh_pstack[(TBLK / 32) * PSTACK];
