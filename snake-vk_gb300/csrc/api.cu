@@ -1026,7 +1026,10 @@ int render_impl(snk_pt_ctx* ctx, const snk_view* views, uint32_t num_views, cons
     F.seed = restir_pt ? rs.seed + 0x9E3779B9u * rs.frame_index : rs.seed;
     F.n_paths = n_paths;
     F.n_pixels = (uint32_t)n_pixels;
-    F.packet_primary = 1u;
+    // camera packets: every view large, single-primitive leaves, the default
+    // traversal bounds (their limits are per ray) and no counting of traversal work
+    F.packet_primary = F.S.single_leaf && !(rs.flags & SNK_RENDER_COUNT_NODES) &&
+                       F.S.max_steps == MAX_TRAVERSAL_STEPS && F.S.stack_max >= STACK_MAX;
     for (uint32_t v = 0; v < num_views; v++) {
         const uint32_t w = views[v].width, h = views[v].height;
         if (w % PACKET_TILE_W || h % PACKET_TILE_H || (uint64_t)w * h < PACKET_MIN_PIXELS) F.packet_primary = 0u;

@@ -77,10 +77,12 @@ struct FrameParams {
     // k_shade marks the queue entries whose path ends (bit 31 of the path id) and
     // k_accum_shadow writes those pixels' outputs; no resolve pass follows
     uint32_t early_resolve;
-    // every view's sides are multiples of 8 and 4 and it has at least
-    // PACKET_MIN_PIXELS pixels: the camera rays are queued in 8 x 4 pixel tiles and
-    // traced in warp packets (neighbouring pixels of smaller images are too far
-    // apart in the scene for a packet's rays to share their nodes)
+    // every view's sides are multiples of the tile's and it has at least
+    // PACKET_MIN_PIXELS pixels (neighbouring pixels of smaller images are too far
+    // apart in the scene for a packet's rays to share their nodes), both trees have
+    // single-primitive leaves, the traversal bounds are the defaults (their limits
+    // are per ray) and the frame does not count traversal work: the camera rays are
+    // queued in PACKET_TILE_W x PACKET_TILE_H pixel tiles and traced in warp packets
     uint32_t packet_primary;
     // per-frame values in device memory (seed, frame, accumulate), read by the kernels
     // instead of the fields above when set, so that a captured frame replays for new

@@ -401,10 +401,9 @@ void launch_shadow_variant(const FrameParams& F, uint32_t depth, int grid, cudaS
 
 cudaError_t launch_trace_closest(const FrameParams& F, uint32_t depth, int grid, bool count, cudaStream_t s) {
     const bool single = F.S.single_leaf != 0u;
-    // camera rays (segment 0) of large views in warp packets, unless the bounds were
-    // lowered (their limits are per ray) or the launch counts traversal work
-    if (depth == 0 && F.packet_primary && single && !count && F.S.max_steps == MAX_TRAVERSAL_STEPS &&
-        F.S.stack_max >= STACK_MAX) {
+    // camera rays (segment 0) in warp packets when the frame allows them
+    // (FrameParams::packet_primary; a counting launch always traces ray by ray)
+    if (depth == 0 && F.packet_primary && !count) {
         k_trace_packet<6><<<grid, TBLK, 0, s>>>(F, depth);
         return cudaGetLastError();
     }
