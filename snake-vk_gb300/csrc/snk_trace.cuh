@@ -401,10 +401,11 @@ struct Traverser {
 // is the minimum over the tested triangles in the same (t, instance, triangle)
 // order.  The group stack is one array of PSTACK entries (base, bits, lane mask)
 // per warp in shared memory; every lane writes the same values, so each lane
-// reads back what it wrote itself.  Each lane's world ray and its node-test set-up
-// wait in shared-memory rows while the lane's ray is in an instance.  For single-primitive-leaf trees only.  A
-// packet that runs past its stack or past 32x the per-ray step cap reports the
-// same error bits as a ray would (all its rays then miss).
+// reads back what it wrote itself.  Each lane's world ray and its node-test
+// set-up wait in shared-memory rows while the lane's ray is in an instance.  For
+// single-primitive-leaf trees only.  A packet that runs past its stack or past
+// 32x the per-ray step cap reports the same error bits as a ray would (all its
+// rays then miss).
 constexpr int PSTACK = 2 * STACK_MAX;
 
 template <bool ANY, int NT>
